@@ -1,0 +1,149 @@
+/*
+ * wmom.h -- C ABI of the GB300 thin-wire Method-of-Moments fill-and-solve library
+ * (libwmom.so).  Plain pointers and sizes only; every call returns a wmom_status
+ * and nothing throws across this boundary.
+ *
+ * Reference interfaces each entry point replaces (paths inside the reference
+ * project; REF = "wersja referencyjna", GPU = "wersja gpu"):
+ *
+ *   wmom_topology_from_geo   geoinp() + config()/configwire()
+ *                            REF/Configuration.h:10-19, REF/Configuration.cpp:5-520
+ *   wmom_ka                  wave number from a float MHz frequency, REF/Wire_MoM.cu:338-340
+ *   wmom_plan_create/destroy the per-call cudaMalloc + H2D geometry upload of
+ *                            zmatrix_gpu(), REF/Wire_MoM.cu:4075-4107 (done once here)
+ *   wmom_fill                zmatrix() REF/Zmatrix.h:7-9 and zmatrix_gpu()
+ *                            REF/Wire_MoM.h:49-51, into device memory, many
+ *                            frequencies per call
+ *   wmom_zgetrf / wmom_zgetrs
+ *                            LAPACKE_zgetrf / LAPACKE_zgetrs, REF/Wire_MoM.cu:372,382
+ *                            (and cublasZgetrfBatched / cublasZgetrsBatched,
+ *                            GPU/Wire_MoM.cu:468,477), on device buffers
+ *   wmom_zgesv_like          the LAPACKE_zgetrf + LAPACKE_zgetrs pair on host buffers,
+ *                            REF/Wire_MoM.cu:364-389
+ *   wmom_excitation          delta-gap excitation vector, REF/Wire_MoM.cu:301-309
+ *   wmom_solve_sweep         the per-frequency loop body of main()/CalculateByFreq(),
+ *                            REF/Wire_MoM.cu:335-400, GPU/Wire_MoM.cu:331-413,
+ *                            batched over frequencies on one GPU
+ *
+ * Conventions.  Complex numbers are interleaved (re, im) doubles (the layout of
+ * cuDoubleComplex / MKL_Complex16).  Matrices are column-major, Z[m + n*ld] with
+ * m the observation (test) function and n the source function, as the reference
+ * stores them.  Index arrays use the reference's layout: 0-based storage holding
+ * 1-based numbers, second columns at offset nsmax.  `stream` arguments are
+ * cudaStream_t values passed as void* (NULL = the legacy default stream).
+ */
+#ifndef WMOM_H
+#define WMOM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum wmom_status {
+  WMOM_OK = 0,
+  WMOM_ERR_ARG = 1,           /* invalid argument: null pointer, size or mode out of range */
+  WMOM_ERR_CUDA = 2,          /* a CUDA runtime/driver call failed */
+  WMOM_ERR_SINGULAR = 3,      /* exactly zero pivot (LAPACK info > 0) */
+  WMOM_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+  WMOM_ERR_NOMEM = 5,         /* device allocation failed or the HBM budget is exceeded */
+  WMOM_ERR_NOT_CONVERGED = 6, /* iterative refinement missed its tolerance */
+  WMOM_ERR_GEOMETRY = 7,      /* bad .geo input or a topology limit exceeded */
+  WMOM_ERR_UNSUPPORTED = 8    /* no device of the required architecture */
+} wmom_status;
+
+/* Topology arrays as configwire() leaves them (Configuration.cpp:485-514).  The
+ * caller owns every array: x, y, z, rad, ipc hold nsmax entries; ips, ise, isp,
+ * iwe hold 2*nsmax. */
+typedef struct wmom_topology {
+  int nsmax;
+  int npnt, npls, nseg, nw; /* out: points, basis functions (unknowns), segments, wires */
+  float *x, *y, *z, *rad;
+  int *ipc, *ips, *ise, *isp, *iwe;
+} wmom_topology;
+
+/* Parses the text of a .geo file and builds the topology.  ienv 1 = free space,
+ * 2 = PEC ground at z = 0 (image wires).  `listing` (optional) receives the text
+ * the reference writes to configwire.txt; errbuf (optional) a message. */
+wmom_status wmom_topology_from_geo(const char* geo_text, int ienv, int nsmax, int nwmax,
+                                   wmom_topology* topo, char* listing, size_t listing_cap,
+                                   char* errbuf, size_t errcap);
+
+/* k = 2*pi / (c / f * 1e-6) with f in MHz as a float and c = 2.99792448e8. */
+double wmom_ka(float freq_mhz);
+
+/* ---------------------------------------------------------------- plans ---- */
+/* A plan holds one geometry resident on the current CUDA device: per-basis source
+ * and observation tables derived once (in FP64, from the float geometry) and
+ * uploaded once.  Plans are independent; distinct plans may be used from
+ * different host threads. */
+typedef struct wmom_plan_s* wmom_plan;
+
+wmom_status wmom_plan_create(const float* x, const float* y, const float* z, const float* rad,
+                             const int* ipc, const int* ips, const int* ise, int nsmax, int npls,
+                             int ienv, float sgnx, float sgny, float sgnz, float sgnenv,
+                             wmom_plan* out);
+wmom_status wmom_plan_destroy(wmom_plan plan);
+int wmom_plan_npls(wmom_plan plan);
+
+/* Fills nk impedance matrices, one per wave number ka[i] (host array), in FP64.
+ * Matrix i starts at z_dev + i*zstride complex elements; ldz >= npls.  The
+ * j*eta0/(4*pi*k) scale of zmatrix() is included. */
+wmom_status wmom_fill(wmom_plan plan, const double* ka, int nk, void* z_dev, long long ldz,
+                      long long zstride, void* stream);
+
+/* ------------------------------------------------------------ FP64 LU ---- */
+/* In-place LU with partial pivoting of an n x n complex128 device matrix
+ * (LAPACK zgetrf semantics: pivot = first row of largest |re|+|im|, ipiv 1-based,
+ * L unit lower, U upper).  ipiv_dev: n ints on the device.  *info receives the
+ * LAPACK info (0, or the 1-based column of the first exactly-zero pivot, which
+ * also returns WMOM_ERR_SINGULAR).  Synchronises `stream`. */
+wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream);
+
+/* Solves A x = b with the factors from wmom_zgetrf for nrhs right-hand sides held
+ * column-major in b_dev (ldb >= n); b_dev is overwritten with x. */
+wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const int* ipiv_dev,
+                        void* b_dev, long long ldb, void* stream);
+
+/* Host-buffer drop-in for LAPACKE_zgetrf + LAPACKE_zgetrs with one right-hand
+ * side: z (n*n, overwritten by the factors), v (n), i_out (n), ipiv (n, 1-based). */
+wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, int* ipiv,
+                            int* info);
+
+/* ----------------------------------------------------------- solver ---- */
+typedef enum wmom_mode {
+  WMOM_MODE_FP64 = 0, /* plain form: FP64 fill, FP64 LU, FP64 solves */
+  WMOM_MODE_MIXED = 1 /* precision form: FP64 fill, complex-FP32 tensor-core LU, FP64
+                         iterative refinement, FP64 LU fallback when refinement stalls */
+} wmom_mode;
+
+/* Per-frequency result record. */
+typedef struct wmom_report {
+  double rel_residual;  /* ||V - Z I||_2 / ||V||_2 of the returned currents (FP64) */
+  int iterations;       /* refinement steps taken (0 for WMOM_MODE_FP64) */
+  int fell_back;        /* 1 if the FP64 LU was used after refinement stalled */
+  int info;             /* LAPACK-style info of the factorisation that produced I */
+  int status;           /* wmom_status of this frequency */
+} wmom_report;
+
+/* Delta-gap excitation: V = 0 except V[ngap-1] = ampl*(cos + j sin)(pi*phas/180). */
+wmom_status wmom_excitation(int npls, int ngap, float ampl, float phas_deg, double* v);
+
+/* Fills, factors and solves one (geometry, frequency) system per frequency, all
+ * frequencies batched on the device.  currents: nfreq*npls complex (host, may be
+ * NULL); zin: nfreq complex input impedances V[ngap-1]/I[ngap-1] (host, may be
+ * NULL); reports: nfreq records (may be NULL).  tol is the relative residual the
+ * mixed mode refines to (<= 0 selects 1e-12). */
+wmom_status wmom_solve_sweep(wmom_plan plan, const float* freq_mhz, int nfreq, int ngap,
+                             float ampl, float phas_deg, int mode, double tol, double* currents,
+                             double* zin, wmom_report* reports, void* stream);
+
+/* Human-readable name of a status code. */
+const char* wmom_status_string(wmom_status s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WMOM_H */

@@ -1,0 +1,65 @@
+"""Build recipe for the oracle libraries (test infrastructure only).
+
+* oracle/liboracle.so  -- the C restatement in oracle/wmom_oracle.c (always built).
+* oracle/_ref/libwmomref.so -- the reference's own Configuration.cpp, Zmatrix.cpp and
+  Complex.cpp, compiled UNMODIFIED where they lie in the reference checkout, plus
+  oracle/ref_harness.cpp.  Built only when that checkout is present (it is not on
+  the GPU machine); outputs go to oracle/_ref/ only.
+
+Both use -ffp-contract=off so no multiply-add is fused, which keeps x86-64 and
+aarch64 builds bit-identical to each other.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.environ.get("WMOM_REFERENCE_DIR", "/root/reference/wersja referencyjna")
+CUDA_INC = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/include"
+
+PORT_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libwmomref.so")
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_port(force=False):
+    src = os.path.join(HERE, "wmom_oracle.c")
+    if not force and _newer(PORT_SO, [src]):
+        return PORT_SO
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", PORT_SO, src, "-lm"]
+    subprocess.check_call(cmd)
+    return PORT_SO
+
+
+def reference_available():
+    return all(os.path.exists(os.path.join(REF_DIR, f)) for f in ("Zmatrix.cpp", "Configuration.cpp", "Complex.cpp"))
+
+
+def build_ref(force=False):
+    if not reference_available():
+        return None
+    srcs = [os.path.join(REF_DIR, f) for f in ("Configuration.cpp", "Zmatrix.cpp", "Complex.cpp")]
+    srcs.append(os.path.join(HERE, "ref_harness.cpp"))
+    if not force and _newer(REF_SO, srcs):
+        return REF_SO
+    os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-fpermissive",
+           "-I", REF_DIR, "-I", CUDA_INC, "-o", REF_SO] + srcs
+    subprocess.check_call(cmd)
+    return REF_SO
+
+
+def main():
+    print(build_port(force="--force" in sys.argv))
+    print(build_ref(force="--force" in sys.argv))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,181 @@
+"""CPU oracle of the thin-wire MoM fill-and-solve path -- TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs
+as the checker; never by the product library.
+
+* fill(): the C restatement of the reference's zmatrix() (oracle/wmom_oracle.c,
+  after "wersja referencyjna/Zmatrix.cpp":27-770), optionally threaded over rows
+  (entries are independent, so the result does not depend on the thread count).
+* lu_solve(): LAPACK zgetrf + zgetrs, the routines the reference calls through
+  LAPACKE ("wersja referencyjna/Wire_MoM.cu":372,382).  The reference linked Intel
+  MKL (unversioned); here the system LAPACK that scipy ships is used (OpenBLAS on
+  aarch64; in the build container torch's MKL 2024.2 is used instead when
+  available, see lapack_backend()).  zgetf2()/zgetrs() restate the unblocked
+  algorithm in C for small pinning cases.
+* ref_*(): the reference's own Configuration.cpp/Zmatrix.cpp compiled unmodified
+  (oracle/_ref/libwmomref.so), present only where the reference checkout exists.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libwmomref.so")
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+
+_port = None
+_ref = None
+
+
+def _load_port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            from . import build as _b
+            _b.build_port()
+        _port = ctypes.CDLL(PORT_SO)
+        _port.oracle_zmatrix.restype = None
+        _port.oracle_zmatrix.argtypes = [_dp, _fp, _fp, _fp, _ip, _ip, _ip, _fp, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, ctypes.c_int]
+        _port.oracle_ka.restype = ctypes.c_double
+        _port.oracle_ka.argtypes = [ctypes.c_float]
+        _port.oracle_zgetf2.restype = ctypes.c_int
+        _port.oracle_zgetf2.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip]
+        _port.oracle_zgetrs.restype = None
+        _port.oracle_zgetrs.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _dp]
+    return _port
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        _ref = ctypes.CDLL(REF_SO)
+        _ref.ref_nsmax.restype = ctypes.c_int
+        _ref.ref_load_geometry.restype = ctypes.c_int
+        _ref.ref_load_geometry.argtypes = [ctypes.c_char_p, ctypes.c_int, _ip, _fp, _fp, _fp, _fp, _ip, _ip, _ip,
+                                           _ip, _ip]
+        _ref.ref_zmatrix.restype = None
+        _ref.ref_zmatrix.argtypes = [_dp, _fp, _fp, _fp, _ip, _ip, _ip, _fp, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float]
+    return _ref
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def ka(freq_mhz):
+    return _load_port().oracle_ka(float(np.float32(freq_mhz)))
+
+
+def fill(g, freq_mhz, ienv=1, sgn=(1.0, 1.0, 1.0, 1.0), threads=1):
+    """Z (npls x npls complex128, Fortran order = the reference's column-major cz).
+    g: mapping with x, y, z, rad, ipc, ips, ise (reference layout), nsmax, npls."""
+    lib = _load_port()
+    n = int(g["npls"])
+    z = np.zeros((n, n), np.complex128, order="F")
+    lib.oracle_zmatrix(z.ctypes.data_as(_dp), _p(g["x"], _fp), _p(g["y"], _fp), _p(g["z"], _fp),
+                       _p(g["ipc"], _ip), _p(g["ips"], _ip), _p(g["ise"], _ip), _p(g["rad"], _fp), n,
+                       ka(freq_mhz), int(g["nsmax"]), ienv, sgn[0], sgn[1], sgn[2], sgn[3], threads)
+    return z
+
+
+def zgetf2(a):
+    """Unblocked LU (zgetf2 semantics) of a copy of a; returns (lu, ipiv 1-based, info)."""
+    lib = _load_port()
+    lu = np.array(a, np.complex128, order="F", copy=True)
+    n = lu.shape[0]
+    ipiv = np.zeros(n, np.int32)
+    info = lib.oracle_zgetf2(n, lu.ctypes.data_as(_dp), n, _p(ipiv, _ip))
+    return lu, ipiv, info
+
+
+def zgetrs(lu, ipiv, b):
+    lib = _load_port()
+    x = np.array(b, np.complex128, copy=True)
+    n = lu.shape[0]
+    lu = np.asfortranarray(lu)
+    lib.oracle_zgetrs(n, lu.ctypes.data_as(_dp), n, _p(np.ascontiguousarray(ipiv, np.int32), _ip),
+                      x.ctypes.data_as(_dp))
+    return x
+
+
+def lapack_backend():
+    return "scipy"
+
+
+def lu_solve(z, v):
+    """I = Z^-1 V with LAPACK zgetrf + zgetrs (partial pivoting).  Returns (I, info)."""
+    from scipy.linalg import lapack
+    lu, piv, info = lapack.zgetrf(np.asfortranarray(z), overwrite_a=0)
+    if info < 0:
+        raise ValueError("zgetrf argument error")
+    x, info2 = lapack.zgetrs(lu, piv, np.asarray(v, np.complex128))
+    return x, info
+
+
+def zin(v, i, ngap):
+    return complex(v[ngap - 1]) / complex(i[ngap - 1])
+
+
+def excitation(npls, ngap, ampl=1.0, phas=0.0):
+    v = np.zeros(npls, np.complex128)
+    arg = np.pi * float(np.float32(phas)) / 180.0
+    a = abs(float(np.float32(ampl)))
+    v[ngap - 1] = complex(a * np.cos(arg), a * np.sin(arg))
+    return v
+
+
+def solve(g, freq_mhz, ngap, ampl=1.0, phas=0.0, ienv=1, sgn=(1.0, 1.0, 1.0, 1.0), threads=1):
+    """One frequency of the reference driver: fill, LU, solve, Z_in.  Returns (I, zin, Z)."""
+    z = fill(g, freq_mhz, ienv, sgn, threads)
+    v = excitation(int(g["npls"]), ngap, ampl, phas)
+    i, _ = lu_solve(z, v)
+    return i, zin(v, i, ngap), z
+
+
+# ------------------------------------------------------------ reference ----
+def ref_geometry(geo_text, ienv=1, workdir=None):
+    """Runs the reference's geoinp()+config() on geo_text; returns the topology arrays
+    and the configwire.txt text it wrote."""
+    import tempfile
+    lib = _load_ref()
+    nsmax = lib.ref_nsmax()
+    d = workdir or tempfile.mkdtemp(prefix="wmomref_")
+    with open(os.path.join(d, "dipol.geo"), "w") as f:
+        f.write(geo_text)
+    counts = np.zeros(3, np.int32)
+    out = dict(x=np.zeros(nsmax, np.float32), y=np.zeros(nsmax, np.float32), z=np.zeros(nsmax, np.float32),
+               rad=np.zeros(nsmax, np.float32), ipc=np.zeros(nsmax, np.int32), ips=np.zeros(2 * nsmax, np.int32),
+               ise=np.zeros(2 * nsmax, np.int32), isp=np.zeros(2 * nsmax, np.int32),
+               iwe=np.zeros(2 * nsmax, np.int32))
+    rc = lib.ref_load_geometry(d.encode(), ienv, _p(counts, _ip), _p(out["x"], _fp), _p(out["y"], _fp),
+                               _p(out["z"], _fp), _p(out["rad"], _fp), _p(out["ipc"], _ip), _p(out["ips"], _ip),
+                               _p(out["ise"], _ip), _p(out["isp"], _ip), _p(out["iwe"], _ip))
+    if rc != 0:
+        raise RuntimeError(f"ref_load_geometry failed ({rc})")
+    out.update(npnt=int(counts[0]), npls=int(counts[1]), nseg=int(counts[2]), nsmax=nsmax)
+    with open(os.path.join(d, "configwire.txt")) as f:
+        out["listing"] = f.read()
+    return out
+
+
+def ref_fill(g, freq_mhz, ienv=1, sgn=(1.0, 1.0, 1.0, 1.0)):
+    lib = _load_ref()
+    n = int(g["npls"])
+    z = np.zeros((n, n), np.complex128, order="F")
+    lib.ref_zmatrix(z.ctypes.data_as(_dp), _p(g["x"], _fp), _p(g["y"], _fp), _p(g["z"], _fp), _p(g["ipc"], _ip),
+                    _p(g["ips"], _ip), _p(g["ise"], _ip), _p(g["rad"], _fp), n, ka(freq_mhz), int(g["nsmax"]),
+                    ienv, sgn[0], sgn[1], sgn[2], sgn[3])
+    return z

@@ -1,0 +1,259 @@
+"""wmom -- GB300-native thin-wire Method-of-Moments fill-and-solve.
+
+Host-side Python mirror of the reference's fill-and-solve path ("Praca magisterska",
+``wersja referencyjna``): the same ``.geo`` / ``freq.txt`` inputs, the same
+``configwire`` topology arrays, the same ``zmatrix`` fill and LAPACK-style LU
+semantics, and the per-frequency input impedance and currents.  Every numeric
+step runs in libwmom.so (hand-written sm_103a CUDA behind a C ABI, include/wmom.h);
+this module only marshals arguments.  There is no CPU fallback: if the library is
+missing, importing this package raises.
+
+The package directory name contains a hyphen, so import it with
+``importlib.import_module("praca-magisterska_gb300")``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import geometry  # noqa: F401  (workload generators)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libwmom.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        "libwmom.so is not built; run praca-magisterska_gb300/build.py (or __graft_entry__.build()) first")
+
+_lib = ctypes.CDLL(LIB_PATH)
+
+WMOM_OK = 0
+STATUS_NAMES = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "singular matrix (zero pivot)",
+    4: "device-side wait timed out", 5: "out of device memory",
+    6: "iterative refinement did not converge", 7: "invalid geometry", 8: "unsupported device",
+}
+MODE_FP64 = 0
+MODE_MIXED = 1
+NSMAX = 30480   # array capacity of the reference driver (Wire_MoM.cu:44)
+NWMAX = 10000
+
+
+class WmomError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)} (status {status})")
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+
+class _Topology(ctypes.Structure):
+    _fields_ = [("nsmax", ctypes.c_int), ("npnt", ctypes.c_int), ("npls", ctypes.c_int),
+                ("nseg", ctypes.c_int), ("nw", ctypes.c_int),
+                ("x", _fp), ("y", _fp), ("z", _fp), ("rad", _fp),
+                ("ipc", _ip), ("ips", _ip), ("ise", _ip), ("isp", _ip), ("iwe", _ip)]
+
+
+class _Report(ctypes.Structure):
+    _fields_ = [("rel_residual", ctypes.c_double), ("iterations", ctypes.c_int),
+                ("fell_back", ctypes.c_int), ("info", ctypes.c_int), ("status", ctypes.c_int)]
+
+
+def _sig(name, res, args):
+    f = getattr(_lib, name)
+    f.restype = res
+    f.argtypes = args
+    return f
+
+
+_topology_from_geo = _sig("wmom_topology_from_geo", ctypes.c_int,
+                          [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Topology),
+                           ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t])
+_ka = _sig("wmom_ka", ctypes.c_double, [ctypes.c_float])
+_plan_create = _sig("wmom_plan_create", ctypes.c_int,
+                    [_fp, _fp, _fp, _fp, _ip, _ip, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                     ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.POINTER(_vp)])
+_plan_destroy = _sig("wmom_plan_destroy", ctypes.c_int, [_vp])
+_plan_npls = _sig("wmom_plan_npls", ctypes.c_int, [_vp])
+_fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
+_zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
+_zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
+               [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_longlong, _vp, _vp, ctypes.c_longlong, _vp])
+_zgesv_like = _sig("wmom_zgesv_like", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _ip, _ip])
+_excitation = _sig("wmom_excitation", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, _dp])
+_solve_sweep = _sig("wmom_solve_sweep", ctypes.c_int,
+                    [_vp, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
+                     ctypes.c_double, _dp, _dp, ctypes.POINTER(_Report), _vp])
+_status_string = _sig("wmom_status_string", ctypes.c_char_p, [ctypes.c_int])
+
+
+def _check(st, what):
+    if st != WMOM_OK:
+        raise WmomError(st, what)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+def library_symbols():
+    """Names of the C-ABI entry points this module binds."""
+    return ["wmom_topology_from_geo", "wmom_ka", "wmom_plan_create", "wmom_plan_destroy", "wmom_plan_npls",
+            "wmom_fill", "wmom_zgetrf", "wmom_zgetrs", "wmom_zgesv_like", "wmom_excitation",
+            "wmom_solve_sweep", "wmom_status_string"]
+
+
+# ----------------------------------------------------------------- geometry ----
+class Topology:
+    """Reference topology arrays (configwire layout: 0-based storage, 1-based values,
+    second columns at offset nsmax) built from the text of a .geo file."""
+
+    def __init__(self, geo_text, ienv=1, nsmax=NSMAX, nwmax=NWMAX):
+        self.nsmax = nsmax
+        self.ienv = ienv
+        self.x = np.zeros(nsmax, np.float32)
+        self.y = np.zeros(nsmax, np.float32)
+        self.z = np.zeros(nsmax, np.float32)
+        self.rad = np.zeros(nsmax, np.float32)
+        self.ipc = np.zeros(nsmax, np.int32)
+        self.ips = np.zeros(2 * nsmax, np.int32)
+        self.ise = np.zeros(2 * nsmax, np.int32)
+        self.isp = np.zeros(2 * nsmax, np.int32)
+        self.iwe = np.zeros(2 * nsmax, np.int32)
+        t = _Topology(nsmax, 0, 0, 0, 0, _ptr(self.x, _fp), _ptr(self.y, _fp), _ptr(self.z, _fp),
+                      _ptr(self.rad, _fp), _ptr(self.ipc, _ip), _ptr(self.ips, _ip), _ptr(self.ise, _ip),
+                      _ptr(self.isp, _ip), _ptr(self.iwe, _ip))
+        cap = 1 << 24
+        listing = ctypes.create_string_buffer(cap)
+        err = ctypes.create_string_buffer(512)
+        st = _topology_from_geo(geo_text.encode(), ienv, nsmax, nwmax, ctypes.byref(t), listing, cap, err, 512)
+        if st != WMOM_OK:
+            raise WmomError(st, "wmom_topology_from_geo: " + err.value.decode(errors="replace"))
+        self.npnt, self.npls, self.nseg, self.nw = t.npnt, t.npls, t.nseg, t.nw
+        self.listing = listing.value.decode()
+        if ienv == 1:
+            self.sgn = (1.0, 1.0, 1.0, 1.0)
+        else:  # PEC ground at z = 0 (Wire_MoM.cu:107-122)
+            self.sgn = (1.0, 1.0, -1.0, -1.0)
+
+    @classmethod
+    def from_file(cls, path, **kw):
+        with open(path) as f:
+            return cls(f.read(), **kw)
+
+    def arrays(self):
+        return dict(x=self.x, y=self.y, z=self.z, rad=self.rad, ipc=self.ipc, ips=self.ips, ise=self.ise,
+                    nsmax=self.nsmax, npls=self.npls)
+
+
+def ka(freq_mhz):
+    """Wave number of a float32 MHz frequency (Wire_MoM.cu:338-340)."""
+    return _ka(float(np.float32(freq_mhz)))
+
+
+def read_freq_file(text):
+    """freq.txt: a count, then that many frequencies in MHz, read as float32
+    (Wire_MoM.cu:254-265)."""
+    tok = text.split()
+    n = int(tok[0])
+    return np.array([np.float32(t) for t in tok[1:1 + n]], np.float32)
+
+
+def excitation(npls, ngap, ampl=1.0, phas=0.0):
+    v = np.zeros(npls, np.complex128)
+    _check(_excitation(npls, ngap, ampl, phas, _ptr(v.view(np.float64), _dp)), "wmom_excitation")
+    return v
+
+
+# --------------------------------------------------------------------- plan ----
+class Plan:
+    """One geometry resident on the current CUDA device."""
+
+    def __init__(self, topo):
+        self.topo = topo
+        h = _vp()
+        sg = topo.sgn
+        st = _plan_create(_ptr(topo.x, _fp), _ptr(topo.y, _fp), _ptr(topo.z, _fp), _ptr(topo.rad, _fp),
+                          _ptr(topo.ipc, _ip), _ptr(topo.ips, _ip), _ptr(topo.ise, _ip), topo.nsmax, topo.npls,
+                          topo.ienv, sg[0], sg[1], sg[2], sg[3], ctypes.byref(h))
+        _check(st, "wmom_plan_create")
+        self._h = h
+        self.npls = topo.npls
+
+    def close(self):
+        if self._h:
+            _plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fill_device(self, kas, z_ptr, ldz, zstride, stream=0):
+        kas = np.ascontiguousarray(kas, np.float64)
+        _check(_fill(self._h, _ptr(kas, _dp), len(kas), z_ptr, ldz, zstride, stream), "wmom_fill")
+
+    def fill(self, freqs_mhz):
+        """Impedance matrices for float32 MHz frequencies, as a complex128 torch tensor
+        on the device of shape (nfreq, npls, npls) whose [k].T is the reference's
+        column-major cz (element [k, n, m] = Z[m, n])."""
+        import torch
+        freqs = np.atleast_1d(np.asarray(freqs_mhz, np.float32))
+        n = self.npls
+        z = torch.empty((len(freqs), n, n), dtype=torch.complex128, device="cuda")
+        kas = np.array([ka(f) for f in freqs], np.float64)
+        self.fill_device(kas, z.data_ptr(), n, n * n, torch.cuda.current_stream().cuda_stream)
+        return z
+
+    def solve(self, freqs_mhz, ngap, ampl=1.0, phas=0.0, mode=MODE_FP64, tol=1e-12, currents=True, stream=0):
+        """Fill, factor and solve per frequency.  Returns (currents (nfreq, npls) complex128
+        or None, zin (nfreq,) complex128, reports list of dicts)."""
+        freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
+        nf = len(freqs)
+        cur = np.zeros((nf, self.npls), np.complex128) if currents else None
+        zin = np.zeros(nf, np.complex128)
+        reps = (_Report * nf)()
+        st = _solve_sweep(self._h, _ptr(freqs, _fp), nf, ngap, ampl, phas, mode, tol,
+                          _ptr(cur.view(np.float64), _dp) if cur is not None else None,
+                          _ptr(zin.view(np.float64), _dp), reps, stream)
+        if st not in (WMOM_OK, 3):
+            raise WmomError(st, "wmom_solve_sweep")
+        reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
+                        info=r.info, status=r.status) for r in reps]
+        return cur, zin, reports
+
+
+# ----------------------------------------------------------------- LAPACK-ish ----
+def zgetrf_device(a_ptr, n, lda, ipiv_ptr, stream=0):
+    info = ctypes.c_int(0)
+    st = _zgetrf(n, a_ptr, lda, ipiv_ptr, ctypes.byref(info), stream)
+    if st not in (WMOM_OK, 3):
+        raise WmomError(st, "wmom_zgetrf")
+    return info.value
+
+
+def zgetrs_device(n, nrhs, a_ptr, lda, ipiv_ptr, b_ptr, ldb, stream=0):
+    _check(_zgetrs(n, nrhs, a_ptr, lda, ipiv_ptr, b_ptr, ldb, stream), "wmom_zgetrs")
+
+
+def zgesv_like(Z, V):
+    """Host-buffer drop-in for LAPACKE_zgetrf + zgetrs: Z (n, n) complex128 in the
+    reference's column-major layout (a Fortran-ordered array), V (n,).  Returns
+    (I, LU, ipiv, info)."""
+    n = Z.shape[0]
+    lu = np.array(Z, dtype=np.complex128, order="F", copy=True)
+    v = np.ascontiguousarray(V, np.complex128)
+    i_out = np.zeros(n, np.complex128)
+    ipiv = np.zeros(n, np.int32)
+    info = ctypes.c_int(0)
+    st = _zgesv_like(n, lu.ctypes.data_as(_dp), _ptr(v.view(np.float64), _dp), _ptr(i_out.view(np.float64), _dp),
+                     _ptr(ipiv, _ip), ctypes.byref(info))
+    if st not in (WMOM_OK, 3):
+        raise WmomError(st, "wmom_zgesv_like")
+    return i_out, lu, ipiv, info.value

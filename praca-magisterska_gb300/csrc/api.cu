@@ -1,0 +1,342 @@
+// api.cu -- the C ABI of libwmom (include/wmom.h): plans, fill, LU, solves and the
+// batched frequency-sweep solver with the FP64 (plain) and mixed-precision
+// (FP32 tensor-core LU + FP64 iterative refinement) forms.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "lu_common.cuh"
+#include "lu_internal.h"
+#include "solve_internal.h"
+#include "wmom_internal.h"
+
+wmom_status wmom_fail_cuda(cudaError_t e, const char* what) {
+  if (std::getenv("WMOM_VERBOSE")) std::fprintf(stderr, "wmom: %s failed: %s\n", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return WMOM_ERR_NOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+    return WMOM_ERR_UNSUPPORTED;
+  return WMOM_ERR_CUDA;
+}
+
+namespace wmom {
+
+// ---------------------------------------------------------- workspace ----
+cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max) {
+  *ws = LuWorkspace{};
+  const size_t stage = lu_workspace_bytes(16);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, stage);
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(p, 0, stage);
+  if (e != cudaSuccess) return e;
+  ws->barrier = reinterpret_cast<GridBarrier*>(p);
+  ws->stage = reinterpret_cast<char*>(p) + 256;
+  e = cudaMalloc(&ws->perm, sizeof(int) * (size_t)std::max(nmax, 1));
+  if (e != cudaSuccess) return e;
+  ws->perm_cap = nmax;
+  ws->rhs_bytes = sizeof(double2) * (size_t)std::max(nmax, 1) * (size_t)std::max(nrhs_max, 1);
+  e = cudaMalloc(&ws->rhs, ws->rhs_bytes);
+  return e;
+}
+
+void lu_workspace_destroy(LuWorkspace* ws) {
+  if (ws->barrier) cudaFree(ws->barrier);
+  if (ws->perm) cudaFree(ws->perm);
+  if (ws->rhs) cudaFree(ws->rhs);
+  *ws = LuWorkspace{};
+}
+
+cudaError_t lu_workspace_reset_barrier(LuWorkspace* ws, cudaStream_t s) {
+  return cudaMemsetAsync(ws->barrier, 0, sizeof(GridBarrier), s);
+}
+
+// Returns 0 when the last factorisation finished its waits; *info = first zero pivot.
+int lu_workspace_read_status(LuWorkspace* ws, int* info, cudaStream_t s) {
+  GridBarrier h{};
+  cudaMemcpyAsync(&h, ws->barrier, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  if (info) *info = h.info;
+  return h.err;
+}
+
+namespace {
+
+// A lazily created workspace per device for the stateless LAPACK-style entry points.
+struct DefaultWs {
+  std::mutex mu;
+  std::vector<LuWorkspace> ws;
+  std::vector<int> cap_n, cap_rhs;
+};
+DefaultWs& default_ws() {
+  static DefaultWs* d = new DefaultWs();
+  return *d;
+}
+
+cudaError_t get_default_ws(int n, int nrhs, LuWorkspace** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  DefaultWs& d = default_ws();
+  if ((int)d.ws.size() <= dev) {
+    d.ws.resize(dev + 1);
+    d.cap_n.resize(dev + 1, 0);
+    d.cap_rhs.resize(dev + 1, 0);
+  }
+  if (d.cap_n[dev] < n || d.cap_rhs[dev] < nrhs) {
+    if (d.cap_n[dev] > 0) {
+      cudaDeviceSynchronize();
+      lu_workspace_destroy(&d.ws[dev]);
+    }
+    const int cn = std::max(n, d.cap_n[dev]);
+    const int cr = std::max(nrhs, d.cap_rhs[dev]);
+    e = lu_workspace_create(&d.ws[dev], cn, cr);
+    if (e != cudaSuccess) {
+      d.cap_n[dev] = 0;
+      return e;
+    }
+    d.cap_n[dev] = cn;
+    d.cap_rhs[dev] = cr;
+  }
+  *out = &d.ws[dev];
+  return cudaSuccess;
+}
+
+struct FreqParamsH {
+  double ka, ka2, cq;
+};
+
+FreqParamsH freq_params(double ka) {
+  const double pi = std::acos(-1.0);
+  const double eta0 = 120. * pi;
+  return FreqParamsH{ka, ka * ka, eta0 / (4.0 * pi * ka)};
+}
+
+}  // namespace
+}  // namespace wmom
+
+using namespace wmom;
+
+struct wmom_plan_s {
+  Plan p;
+  std::mutex mu;
+  FreqParamsH* d_fp = nullptr;
+  int fp_cap = 0;
+  LuWorkspace ws{};
+  int ws_n = 0;
+};
+
+extern "C" {
+
+const char* wmom_status_string(wmom_status s) {
+  switch (s) {
+    case WMOM_OK: return "ok";
+    case WMOM_ERR_ARG: return "invalid argument";
+    case WMOM_ERR_CUDA: return "CUDA error";
+    case WMOM_ERR_SINGULAR: return "singular matrix (zero pivot)";
+    case WMOM_ERR_TIMEOUT: return "device-side wait timed out";
+    case WMOM_ERR_NOMEM: return "out of device memory";
+    case WMOM_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+    case WMOM_ERR_GEOMETRY: return "invalid geometry";
+    case WMOM_ERR_UNSUPPORTED: return "unsupported device";
+  }
+  return "unknown";
+}
+
+double wmom_ka(float freq_mhz) { return ka_from_mhz(freq_mhz); }
+
+wmom_status wmom_excitation(int npls, int ngap, float ampl, float phas_deg, double* v) {
+  if (npls <= 0 || !v || ngap < 1 || ngap > npls) return WMOM_ERR_ARG;
+  const double pi = std::acos(-1.);
+  std::memset(v, 0, sizeof(double) * 2 * (size_t)npls);
+  const double arg = pi * phas_deg / 180.;
+  const double a = std::fabs((double)ampl);
+  // (a, 0) * (cos, sin), as Z_MUL does it (REF/Wire_MoM.cu:307-309)
+  const double c = std::cos(arg), s = std::sin(arg);
+  v[2 * (ngap - 1)] = a * c - 0.0 * s;
+  v[2 * (ngap - 1) + 1] = a * s + 0.0 * c;
+  return WMOM_OK;
+}
+
+wmom_status wmom_plan_create(const float* x, const float* y, const float* z, const float* rad,
+                             const int* ipc, const int* ips, const int* ise, int nsmax, int npls,
+                             int ienv, float sgnx, float sgny, float sgnz, float sgnenv,
+                             wmom_plan* out) {
+  if (!out) return WMOM_ERR_ARG;
+  *out = nullptr;
+  if (!x || !y || !z || !rad || !ipc || !ips || !ise || nsmax <= 0 || npls <= 0 || npls > nsmax ||
+      (ienv != 1 && ienv != 2))
+    return WMOM_ERR_ARG;
+  wmom_plan_s* h = new (std::nothrow) wmom_plan_s();
+  if (!h) return WMOM_ERR_NOMEM;
+  Plan& p = h->p;
+  p.npls = npls;
+  p.nsmax = nsmax;
+  p.ienv = ienv;
+  p.sgnx = sgnx;
+  p.sgny = sgny;
+  p.sgnz = sgnz;
+  p.sgnenv = sgnenv;
+  int st = plan_build_tables(&p, x, y, z, rad, ipc, ips, ise);
+  if (st != WMOM_OK) {
+    delete h;
+    return (wmom_status)st;
+  }
+  cudaError_t e = cudaGetDevice(&p.device);
+  if (e == cudaSuccess) e = cudaMalloc(&p.d_obs, sizeof(ObsHalf) * p.h_obs.size());
+  if (e == cudaSuccess) e = cudaMalloc(&p.d_src, sizeof(SrcHalf) * p.h_src.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p.d_obs, p.h_obs.data(), sizeof(ObsHalf) * p.h_obs.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p.d_src, p.h_src.data(), sizeof(SrcHalf) * p.h_src.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (p.d_obs) cudaFree(p.d_obs);
+    if (p.d_src) cudaFree(p.d_src);
+    delete h;
+    return wmom_fail_cuda(e, "plan upload");
+  }
+  *out = h;
+  return WMOM_OK;
+}
+
+wmom_status wmom_plan_destroy(wmom_plan h) {
+  if (!h) return WMOM_ERR_ARG;
+  cudaDeviceSynchronize();
+  if (h->p.d_obs) cudaFree(h->p.d_obs);
+  if (h->p.d_src) cudaFree(h->p.d_src);
+  if (h->d_fp) cudaFree(h->d_fp);
+  if (h->ws_n) lu_workspace_destroy(&h->ws);
+  delete h;
+  return WMOM_OK;
+}
+
+int wmom_plan_npls(wmom_plan h) { return h ? h->p.npls : -1; }
+
+wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long long ldz,
+                      long long zstride, void* stream) {
+  if (!h || !ka || nk <= 0 || !z_dev || ldz < h->p.npls || (nk > 1 && zstride < ldz * h->p.npls))
+    return WMOM_ERR_ARG;
+  for (int i = 0; i < nk; ++i)
+    if (!(ka[i] > 0.0) || !std::isfinite(ka[i])) return WMOM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (h->fp_cap < nk) {
+    if (h->d_fp) {
+      cudaStreamSynchronize(s);
+      cudaFree(h->d_fp);
+      h->d_fp = nullptr;
+    }
+    WMOM_CUDA_TRY(cudaMalloc(&h->d_fp, sizeof(FreqParamsH) * nk));
+    h->fp_cap = nk;
+  }
+  std::vector<FreqParamsH> fp(nk);
+  for (int i = 0; i < nk; ++i) fp[i] = freq_params(ka[i]);
+  WMOM_CUDA_TRY(cudaMemcpyAsync(h->d_fp, fp.data(), sizeof(FreqParamsH) * nk, cudaMemcpyHostToDevice, s));
+  WMOM_CUDA_TRY(launch_fill(h->p, reinterpret_cast<const double*>(h->d_fp), nk,
+                            reinterpret_cast<double2*>(z_dev), ldz, zstride, s));
+  // the parameter upload is from pageable memory: finish before the vector dies
+  WMOM_CUDA_TRY(cudaStreamSynchronize(s));
+  return WMOM_OK;
+}
+
+wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream) {
+  if (n <= 0 || !a_dev || lda < n || !ipiv_dev) return WMOM_ERR_ARG;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(default_ws().mu);
+  LuWorkspace* ws = nullptr;
+  WMOM_CUDA_TRY(get_default_ws(n, 1, &ws));
+  WMOM_CUDA_TRY(lu_workspace_reset_barrier(ws, s));
+  WMOM_CUDA_TRY(lu_factor_t<double2>(reinterpret_cast<double2*>(a_dev), lda, n, ipiv_dev, ws, s, nullptr));
+  int inf = 0;
+  const int err = lu_workspace_read_status(ws, &inf, s);
+  WMOM_CUDA_TRY(cudaGetLastError());
+  if (info) *info = inf;
+  if (err) return WMOM_ERR_TIMEOUT;
+  return inf ? WMOM_ERR_SINGULAR : WMOM_OK;
+}
+
+wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const int* ipiv_dev,
+                        void* b_dev, long long ldb, void* stream) {
+  if (n <= 0 || nrhs <= 0 || !a_dev || lda < n || !ipiv_dev || !b_dev || ldb < n) return WMOM_ERR_ARG;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(default_ws().mu);
+  LuWorkspace* ws = nullptr;
+  WMOM_CUDA_TRY(get_default_ws(n, nrhs, &ws));
+  WMOM_CUDA_TRY(lu_solve_t<double2>(reinterpret_cast<const double2*>(a_dev), lda, n, ipiv_dev,
+                                    reinterpret_cast<double2*>(b_dev), ldb, nrhs, ws, s));
+  WMOM_CUDA_TRY(cudaStreamSynchronize(s));
+  return WMOM_OK;
+}
+
+wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, int* ipiv, int* info) {
+  if (n <= 0 || !z || !v || !i_out || !ipiv) return WMOM_ERR_ARG;
+  double2* dz = nullptr;
+  double2* db = nullptr;
+  int* dp = nullptr;
+  wmom_status st = WMOM_OK;
+  int inf = 0;
+  cudaError_t e = cudaMalloc(&dz, sizeof(double2) * (size_t)n * n);
+  if (e == cudaSuccess) e = cudaMalloc(&db, sizeof(double2) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(int) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpy(dz, z, sizeof(double2) * (size_t)n * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db, v, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    st = wmom_fail_cuda(e, "zgesv_like upload");
+  } else {
+    st = wmom_zgetrf(n, dz, n, dp, &inf, nullptr);
+    if (st == WMOM_OK || st == WMOM_ERR_SINGULAR) {
+      const wmom_status st2 = wmom_zgetrs(n, 1, dz, n, dp, db, n, nullptr);
+      if (st == WMOM_OK) st = st2;
+      e = cudaMemcpy(z, dz, sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(i_out, db, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(ipiv, dp, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess && st == WMOM_OK) st = wmom_fail_cuda(e, "zgesv_like download");
+    }
+  }
+  if (info) *info = inf;
+  if (dz) cudaFree(dz);
+  if (db) cudaFree(db);
+  if (dp) cudaFree(dp);
+  return st;
+}
+
+wmom_status wmom_solve_sweep(wmom_plan h, const float* freq_mhz, int nfreq, int ngap, float ampl,
+                             float phas_deg, int mode, double tol, double* currents, double* zin,
+                             wmom_report* reports, void* stream) {
+  if (!h || !freq_mhz || nfreq <= 0 || ngap < 1 || ngap > h->p.npls ||
+      (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED))
+    return WMOM_ERR_ARG;
+  for (int i = 0; i < nfreq; ++i)
+    if (!(freq_mhz[i] > 0.f) || !std::isfinite(freq_mhz[i])) return WMOM_ERR_ARG;
+  SweepArgs a;
+  a.plan = &h->p;
+  a.freq_mhz = freq_mhz;
+  a.nfreq = nfreq;
+  a.ngap = ngap;
+  a.ampl = ampl;
+  a.phas_deg = phas_deg;
+  a.mode = mode;
+  a.tol = tol > 0 ? tol : 1e-12;
+  a.currents = currents;
+  a.zin = zin;
+  a.reports = reports;
+  a.stream = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (h->ws_n < h->p.npls) {
+    if (h->ws_n) lu_workspace_destroy(&h->ws);
+    h->ws_n = 0;
+    WMOM_CUDA_TRY(lu_workspace_create(&h->ws, h->p.npls, 1));
+    h->ws_n = h->p.npls;
+  }
+  a.ws = &h->ws;
+  return run_sweep(a);
+}
+
+}  // extern "C"

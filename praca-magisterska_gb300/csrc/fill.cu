@@ -1,0 +1,253 @@
+// fill.cu -- FP64 impedance-matrix fill on the GPU.
+//
+// Computes Z[m, n] of the reference's thin-wire formulation
+// ("wersja referencyjna/Zmatrix.cpp":27-770, the same math as the reference's GPU
+// kernels wim_gpu_cknn_* / wim_gpu_ckmn_* in "wersja referencyjna/Wire_MoM.cu":454-4049)
+// in ONE kernel launch per batch of frequencies, writing every entry exactly once
+// (the reference makes six read-modify-write passes over Z per frequency).
+//
+// Per entry: two observation points (midpoints of S_m+ and S_m-), two source
+// half-segments (S_n+ rising ramp, S_n- falling ramp).  Regular pairs use the
+// reference's 2-point Gauss rule of exp(-jkR)/R with R = sqrt(a^2 + |r_m - r'|^2);
+// identical segments use its two 4-point rules of the regularised kernel plus the
+// analytic log term; both the ramped (vector potential) and the plain (scalar
+// potential) integrals come from the same kernel evaluations.  The geometric
+// arithmetic is done with explicitly rounded operations in the reference's order,
+// so that the float-derived coordinates give the same doubles as the CPU code.
+#include <cuda_runtime.h>
+
+#include "wmom_internal.h"
+
+namespace wmom {
+namespace {
+
+constexpr double kGl2C = 0.288675134594812882;  // 1/(2*sqrt(3))
+constexpr double kGl4C1 = 0.43056815579702629;
+constexpr double kGl4W1 = 0.17392742256872693;
+constexpr double kGl4C2 = 0.16999052179242813;
+constexpr double kGl4W2 = 0.32607257743127307;
+
+struct Cx {
+  double re, im;
+};
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// Complete elliptic integral K, Hastings polynomial-log approximation with the
+// reference's coefficients (Zmatrix.cpp:738-747; Abramowitz & Stegun 17.3.34).
+__device__ double ell_k(double bet) {
+  const double a0 = 1.38629436112, a1 = 0.09666344259, a2 = 0.03590092383,
+               a3 = 0.03742563713, a4 = 0.01451196212;
+  const double b0 = 0.5, b1 = 0.12498593597, b2 = 0.06880248576, b3 = 0.03328355346,
+               b4 = 0.00441787012;
+  double m1 = sub(1.0, mul(bet, bet));
+  double a = add(a0, mul(a1, m1)), b = add(b0, mul(b1, m1));
+  double m2 = 0.0, m3 = 0.0;
+  if (m1 >= 1.0e-18) {
+    m2 = mul(m1, m1);
+    a = add(a, mul(a2, m2));
+    b = add(b, mul(b2, m2));
+  }
+  if (m1 >= 1.0e-12) {
+    m3 = mul(m2, m1);
+    a = add(a, mul(a3, m3));
+    b = add(b, mul(b3, m3));
+  }
+  if (m1 >= 1.0e-9) {
+    double m4 = mul(m3, m1);
+    a = add(a, mul(a4, m4));
+    b = add(b, mul(b4, m4));
+  }
+  return sub(a, mul(b, log(m1)));
+}
+
+// Regular source half: returns the ramped integral A and the plain integral P.
+__device__ void regular_half(const double rm[3], const double rs[3], const double dc[3],
+                             double dl, double an, double ka, bool falling, Cx* A, Cx* P) {
+  const double a = mul(0.5, dl);
+  const double c = mul(kGl2C, dl);
+  const double an2 = mul(an, an);
+  Cx sa = {0.0, 0.0}, sp = {0.0, 0.0};
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    const double s = g == 0 ? add(a, c) : sub(a, c);
+    const double dx = sub(sub(rm[0], rs[0]), mul(s, dc[0]));
+    const double dy = sub(sub(rm[1], rs[1]), mul(s, dc[1]));
+    const double dz = sub(sub(rm[2], rs[2]), mul(s, dc[2]));
+    const double r = sqrt(add(add(add(an2, mul(dx, dx)), mul(dy, dy)), mul(dz, dz)));
+    double sn, cs;
+    sincos(mul(ka, r), &sn, &cs);
+    const double gre = __ddiv_rn(cs, r), gim = __ddiv_rn(-sn, r);
+    const double w = falling ? __ddiv_rn(sub(dl, s), dl) : __ddiv_rn(s, dl);
+    sa.re = add(sa.re, mul(w, gre));
+    sa.im = add(sa.im, mul(w, gim));
+    sp.re = add(sp.re, gre);
+    sp.im = add(sp.im, gim);
+  }
+  const double h = mul(dl, 0.5);
+  A->re = mul(sa.re, h);
+  A->im = mul(sa.im, h);
+  P->re = mul(sp.re, h);
+  P->im = mul(sp.im, h);
+}
+
+// Regularised self kernel bracket (Zmatrix.cpp:695-709) at parameter s.
+__device__ Cx self_bracket(double s, double ka, double dl, double an) {
+  const double pi = 3.141592653589793;  // acos(-1.0)
+  const double r = sub(mul(0.5, dl), s);
+  const double rr = sqrt(add(mul(an, an), mul(r, r)));
+  double sn, cs;
+  sincos(mul(ka, rr), &sn, &cs);
+  const double ere = __ddiv_rn(sub(cs, 1.0), rr), eim = __ddiv_rn(-sn, rr);
+  const double bet = __ddiv_rn(add(an, an), sqrt(add(mul(mul(4.0, an), an), mul(r, r))));
+  const double stat =
+      __ddiv_rn(add(mul(bet, ell_k(bet)), log(fabs(__ddiv_rn(r, mul(8.0, an))))), mul(pi, an));
+  return Cx{add(ere, stat), eim};
+}
+
+// Self source half: two 4-point Gauss rules on [0, dl/2] and [dl/2, dl] plus the
+// analytic term (Zmatrix.cpp:277-323).
+__device__ void self_half(double dl, double an, double ka, bool falling, Cx* A, Cx* P) {
+  const double pi = 3.141592653589793;
+  const double dlh = mul(0.5, dl);
+  Cx ta = {0.0, 0.0}, tp = {0.0, 0.0};
+#pragma unroll 1
+  for (int part = 0; part < 2; ++part) {
+    const double lo = part == 0 ? 0.0 : dlh, hi = part == 0 ? dlh : dl;
+    const double a = mul(0.5, add(lo, hi)), b = sub(hi, lo);
+    Cx qa[2], qp[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const double c = mul(q == 0 ? kGl4C1 : kGl4C2, b);
+      const double s1 = add(a, c), s2 = sub(a, c);
+      const Cx v1 = self_bracket(s1, ka, dl, an), v2 = self_bracket(s2, ka, dl, an);
+      const double w1 = falling ? __ddiv_rn(sub(dl, s1), dl) : __ddiv_rn(s1, dl);
+      const double w2 = falling ? __ddiv_rn(sub(dl, s2), dl) : __ddiv_rn(s2, dl);
+      const double wq = q == 0 ? kGl4W1 : kGl4W2;
+      qa[q].re = mul(add(mul(w1, v1.re), mul(w2, v2.re)), wq);
+      qa[q].im = mul(add(mul(w1, v1.im), mul(w2, v2.im)), wq);
+      qp[q].re = mul(add(v1.re, v2.re), wq);
+      qp[q].im = mul(add(v1.im, v2.im), wq);
+    }
+    const double pa_re = mul(add(qa[0].re, qa[1].re), b), pa_im = mul(add(qa[0].im, qa[1].im), b);
+    const double pp_re = mul(add(qp[0].re, qp[1].re), b), pp_im = mul(add(qp[0].im, qp[1].im), b);
+    ta.re = part == 0 ? pa_re : add(ta.re, pa_re);
+    ta.im = part == 0 ? pa_im : add(ta.im, pa_im);
+    tp.re = part == 0 ? pp_re : add(tp.re, pp_re);
+    tp.im = part == 0 ? pp_im : add(tp.im, pp_im);
+  }
+  const double lg = add(1.0, log(__ddiv_rn(mul(16.0, an), dl)));
+  const double res3 = __ddiv_rn(mul(dl, lg), mul(pi, an));
+  const double res12 = __ddiv_rn(mul(mul(0.5, dl), lg), mul(pi, an));
+  A->re = add(ta.re, res12);
+  A->im = ta.im;
+  P->re = add(tp.re, res3);
+  P->im = tp.im;
+}
+
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+  return add(add(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2]));
+}
+
+struct FreqParams {
+  double ka, ka2, cq;  // k, k^2, eta0/(4*pi*k)
+};
+
+// One thread per entry: blockIdx.x*blockDim.x + threadIdx.x = row m (observation),
+// blockIdx.y = column n (source), blockIdx.z = frequency.  Consecutive threads write
+// consecutive rows of one column: coalesced 16-byte complex stores.
+__global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restrict__ obs,
+                                                         const SrcHalf* __restrict__ src, int npls,
+                                                         const FreqParams* __restrict__ fp,
+                                                         double2* __restrict__ Z, long long ldz,
+                                                         long long zstride, int ienv,
+                                                         float sgnenv) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = blockIdx.y;
+  const int k = blockIdx.z;
+  if (m >= npls) return;
+  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+  const double senv = (double)sgnenv;
+  double acc_re = 0.0, acc_im = 0.0;
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    const ObsHalf o = obs[2 * m + h];
+    double av_re = 0.0, av_im = 0.0, sv_re = 0.0, sv_im = 0.0;
+#pragma unroll 1
+    for (int sgm = 0; sgm < 2; ++sgm) {
+      const SrcHalf sh = src[2 * n + sgm];
+      const bool falling = sgm == 1;
+      const bool same = (sh.nl == o.ml && sh.nr == o.mr) || (sh.nl == o.mr && sh.nr == o.ml);
+      Cx A, P;
+      if (same)
+        self_half(sh.dl, sh.an, ka, falling, &A, &P);
+      else
+        regular_half(o.rm, sh.rs, sh.dc, sh.dl, sh.an, ka, falling, &A, &P);
+      const double t = dot3(sh.dc, o.lm);
+      av_re = add(av_re, mul(A.re, t));
+      av_im = add(av_im, mul(A.im, t));
+      Cx Ai, Pi;
+      if (ienv == 2) {
+        if (same && o.on_ground)
+          self_half(sh.dl, sh.an, ka, falling, &Ai, &Pi);
+        else
+          regular_half(o.rm, sh.rs_img, sh.dc_img, sh.dl, sh.an, ka, falling, &Ai, &Pi);
+        const double ti = mul(dot3(sh.dc_img, o.lm), senv);
+        av_re = add(av_re, mul(Ai.re, ti));
+        av_im = add(av_im, mul(Ai.im, ti));
+      }
+      // scalar potential: + P(S_n+)/dl - P(S_n-)/dl
+      const double pre = __ddiv_rn(P.re, sh.dl), pim = __ddiv_rn(P.im, sh.dl);
+      if (!falling) {
+        sv_re = add(sv_re, pre);
+        sv_im = add(sv_im, pim);
+      } else {
+        sv_re = sub(sv_re, pre);
+        sv_im = sub(sv_im, pim);
+      }
+      if (ienv == 2) {
+        const double f = __ddiv_rn(senv, sh.dl);
+        const double qre = mul(Pi.re, f), qim = mul(Pi.im, f);
+        if (!falling) {
+          sv_re = add(sv_re, qre);
+          sv_im = add(sv_im, qim);
+        } else {
+          sv_re = sub(sv_re, qre);
+          sv_im = sub(sv_im, qim);
+        }
+      }
+    }
+    double c_re = mul(av_re, ka2), c_im = mul(av_im, ka2);
+    if (h == 0) {
+      c_re = sub(c_re, sv_re);
+      c_im = sub(c_im, sv_im);
+    } else {
+      c_re = add(c_re, sv_re);
+      c_im = add(c_im, sv_im);
+    }
+    acc_re = add(acc_re, c_re);
+    acc_im = add(acc_im, c_im);
+  }
+  // times j*cq
+  double2 out;
+  out.x = -mul(cq, acc_im);
+  out.y = mul(cq, acc_re);
+  Z[(size_t)k * zstride + (size_t)n * ldz + m] = out;
+}
+
+}  // namespace
+
+cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, long long ldz,
+                        long long zstride, cudaStream_t stream) {
+  if (nk <= 0 || p.npls <= 0) return cudaSuccess;
+  dim3 block(128);
+  dim3 grid((p.npls + 127) / 128, p.npls, nk);
+  fill_entry_kernel<<<grid, block, 0, stream>>>(p.d_obs, p.d_src, p.npls,
+                                                reinterpret_cast<const FreqParams*>(d_fp), z, ldz,
+                                                zstride, p.ienv, p.sgnenv);
+  return cudaGetLastError();
+}
+
+}  // namespace wmom

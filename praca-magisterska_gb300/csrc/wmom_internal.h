@@ -1,0 +1,94 @@
+// wmom_internal.h -- shared declarations of libwmom's translation units.
+#pragma once
+
+#include <cstdint>
+#include <istream>
+#include <string>
+#include <vector>
+
+#include "../../include/wmom.h"
+
+#if defined(__CUDACC__) || defined(WMOM_WITH_CUDA_RUNTIME)
+#include <cuda_runtime.h>
+#endif
+
+namespace wmom {
+
+// ---------------------------------------------------------------- geometry ----
+struct GeoInput {
+  int nnod = 0, nw = 0, nt = 0;
+  std::vector<float> xnod, ynod, znod;  // 1-based, nnod+1
+  std::vector<int> iwn;                 // 1-based: [1..nw] first node, [nw+1..2nw] second
+  std::vector<float> wrad;              // 1-based
+  std::vector<int> nsw;                 // 1-based segment counts
+  std::vector<int> iwt;                 // patch triplets (read and ignored, as the reference)
+};
+
+struct Topology {
+  int npnt = 0, npls = 0, nseg = 0;
+  float *x, *y, *z, *rad;
+  int *ipc, *ips, *ise, *isp, *iwe;
+};
+
+int geo_parse(std::istream& in, int nnmax, int nwmax, int ntmax, GeoInput* g, std::string* err);
+int build_topology(const GeoInput& gin, int nsmax, int nwmax, int ienv, Topology* out,
+                   std::string* listing, std::string* err);
+
+// --------------------------------------------------------- fill tables ----
+// Observation half of a test function m (h = 0: point on S_m+, h = 1: on S_m-).
+// All values are the reference's double expressions of the float geometry
+// (Zmatrix.cpp:69-84 and 154-165).
+struct ObsHalf {
+  double rm[3];  // observation point (segment midpoint)
+  double lm[3];  // test vector: h=0 -> r_p - r_m, h=1 -> r_m - r_p
+  int ml, mr;    // node numbers of the observation segment (self-term test)
+  int on_ground; // both nodes at z < 1e-6 (image self-term test)
+  int pad;
+};
+
+// Source half of a basis function n (s = 0: S_n+ with rising ramp s/dl from its
+// first node to the centre, s = 1: S_n- with falling ramp from the centre).
+// (Zmatrix.cpp:252-276 and 466-490.)
+struct SrcHalf {
+  double rs[3];  // start of the parametrisation
+  double dc[3];  // unit vector
+  double dl;     // length
+  double an;     // wire radius
+  double rs_img[3];  // mirrored start (PEC ground image), rs * sgn
+  double dc_img[3];  // mirrored unit vector
+  int nl, nr;        // node numbers of the source segment
+};
+
+// ------------------------------------------------------------------ plan ----
+struct Plan {
+  int device = 0;
+  int npls = 0, nsmax = 0, ienv = 1;
+  float sgnx = 1.f, sgny = 1.f, sgnz = 1.f, sgnenv = 1.f;
+  std::vector<ObsHalf> h_obs;  // 2*npls
+  std::vector<SrcHalf> h_src;  // 2*npls
+  ObsHalf* d_obs = nullptr;
+  SrcHalf* d_src = nullptr;
+};
+
+int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, const float* rad,
+                      const int* ipc, const int* ips, const int* ise);
+
+double ka_from_mhz(float f);
+
+}  // namespace wmom
+
+#if defined(__CUDACC__) || defined(WMOM_WITH_CUDA_RUNTIME)
+namespace wmom {
+// Fill launcher (fill.cu).
+cudaError_t launch_fill(const Plan& p, const double* d_ka, int nk, double2* z, long long ldz,
+                        long long zstride, cudaStream_t stream);
+}  // namespace wmom
+
+#define WMOM_CUDA_TRY(call)                                   \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return wmom_fail_cuda(_e, #call);  \
+  } while (0)
+
+wmom_status wmom_fail_cuda(cudaError_t e, const char* what);
+#endif
