@@ -111,6 +111,13 @@ wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const
 wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, int* ipiv,
                             int* info);
 
+/* The precision form's trailing update on the tensor cores: C -= A * B for complex
+ * FP32 (float2) column-major device matrices, C m x n, A m x k, B k x n, computed
+ * as 3xTF32 tcgen05 products with FP32 accumulation.  No reference counterpart
+ * (the reference never factors in reduced precision); exposed for testing. */
+wmom_status wmom_cgemm_sub_tc(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
+                              long long ldb, void* c_dev, long long ldc, void* stream);
+
 /* ----------------------------------------------------------- solver ---- */
 typedef enum wmom_mode {
   WMOM_MODE_FP64 = 0, /* plain form: FP64 fill, FP64 LU, FP64 solves */

@@ -10,7 +10,7 @@ Both use -ffp-contract=off so no multiply-add is fused, which keeps x86-64 and
 aarch64 builds bit-identical to each other.
 """
 import os
-import shutil
+import platform
 import subprocess
 import sys
 
@@ -29,12 +29,23 @@ def _newer(target, sources):
     return all(os.path.getmtime(s) <= t for s in sources)
 
 
+def _arch_ok(lib):
+    stamp = lib + ".arch"
+    return os.path.exists(stamp) and open(stamp).read().strip() == platform.machine()
+
+
+def _stamp(lib):
+    with open(lib + ".arch", "w") as f:
+        f.write(platform.machine())
+
+
 def build_port(force=False):
     src = os.path.join(HERE, "wmom_oracle.c")
-    if not force and _newer(PORT_SO, [src]):
+    if not force and _newer(PORT_SO, [src]) and _arch_ok(PORT_SO):
         return PORT_SO
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", PORT_SO, src, "-lm"]
     subprocess.check_call(cmd)
+    _stamp(PORT_SO)
     return PORT_SO
 
 
@@ -47,12 +58,13 @@ def build_ref(force=False):
         return None
     srcs = [os.path.join(REF_DIR, f) for f in ("Configuration.cpp", "Zmatrix.cpp", "Complex.cpp")]
     srcs.append(os.path.join(HERE, "ref_harness.cpp"))
-    if not force and _newer(REF_SO, srcs):
+    if not force and _newer(REF_SO, srcs) and _arch_ok(REF_SO):
         return REF_SO
     os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
     cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-fpermissive",
            "-I", REF_DIR, "-I", CUDA_INC, "-o", REF_SO] + srcs
     subprocess.check_call(cmd)
+    _stamp(REF_SO)
     return REF_SO
 
 

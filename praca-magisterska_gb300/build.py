@@ -9,6 +9,7 @@ WMOM_ERR_UNSUPPORTED / WMOM_ERR_CUDA).
 """
 import concurrent.futures as cf
 import os
+import platform
 import subprocess
 import sys
 
@@ -59,15 +60,21 @@ def _compile(src):
 
 def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "ARCH")
+    machine = platform.machine()
+    if not os.path.exists(stamp) or open(stamp).read().strip() != machine:
+        force = True  # objects from another host architecture
     if force:
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))
     srcs = CPP_SOURCES + CU_SOURCES
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
-    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         subprocess.check_call(cmd)
+    with open(stamp, "w") as f:
+        f.write(machine)
     return LIB
 
 

@@ -75,6 +75,23 @@ __global__ void __launch_bounds__(1024) sumsq_kernel(const double2* __restrict__
   if (threadIdx.x == 0) *out = sh[0];
 }
 
+__global__ void __launch_bounds__(1024) sumsq_f32_kernel(const float2* __restrict__ x, int n, double scale,
+                                                         double* out) {
+  __shared__ double sh[1024];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += 1024) {
+    const double a = (double)x[i].x * scale, b = (double)x[i].y * scale;
+    acc = fma(a, a, fma(b, b, acc));
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
 __global__ void convert_matrix_kernel(const double2* __restrict__ src, long long lds, float2* __restrict__ dst,
                                       long long ldd, int rows, int cols) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -163,6 +180,8 @@ struct DevBuf {
 struct Scalars {
   double vnorm2;
   double rnorm2;
+  double dnorm2;  // last refinement correction
+  double xnorm2;  // solution before that correction
 };
 
 }  // namespace
@@ -265,7 +284,7 @@ wmom_status run_sweep(const SweepArgs& a) {
         SWEEP_TRY(convert_matrix_64_to_32(Zk, n, z32.as<float2>(), n, n, n, s));
         SWEEP_TRY(lu_workspace_reset_barrier(a.ws, s));
         SWEEP_TRY(lu_factor_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), a.ws, s, hook32));
-        const int err = lu_workspace_read_status(a.ws, &info, s);
+        const int err = lu_workspace_read_status(a.ws, &info, s) | (hook32 ? tc::read_and_clear_error() : 0);
         SWEEP_TRY(cudaGetLastError());
         if (err) return WMOM_ERR_TIMEOUT;
         bool fallback = info != 0;
@@ -288,7 +307,11 @@ wmom_status run_sweep(const SweepArgs& a) {
               fallback = true;
               break;
             }
-            if (rel <= a.tol) break;
+            // converged: the residual target is met, or the last correction no longer
+            // changes the solution at FP64 resolution (ill-conditioned systems whose
+            // FP64 residual floor lies above the target)
+            const double corr = it > 0 ? std::sqrt(hs.dnorm2 / hs.xnorm2) : HUGE_VAL;
+            if (rel <= a.tol || corr <= 0x1p-48) break;
             if (rel > 0.5 * prev) {
               if (++stall >= 2) {
                 fallback = true;
@@ -307,6 +330,8 @@ wmom_status run_sweep(const SweepArgs& a) {
             const double scale = rn > 0 ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
             SWEEP_TRY(convert_vec_64_to_32(r64.as<double2>(), d32.as<float2>(), n, scale, s));
             SWEEP_TRY(lu_solve_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), d32.as<float2>(), n, 1, a.ws, s));
+            sumsq_f32_kernel<<<1, 1024, 0, s>>>(d32.as<float2>(), n, 1.0 / scale, &sc.as<Scalars>()->dnorm2);
+            SWEEP_TRY(sumsq_fp64(x64.as<double2>(), n, &sc.as<Scalars>()->xnorm2, s));
             SWEEP_TRY(accumulate_vec_32_to_64(x64.as<double2>(), d32.as<float2>(), n, 1.0 / scale, s));
           }
         }

@@ -39,5 +39,8 @@ cudaError_t accumulate_vec_32_to_64(double2* x, const float2* d, int n, double s
 // FP32 trailing-update GEMM on the tensor cores (lu_tc.cu); nullptr when the
 // device has no tcgen05 path, in which case the SIMT GEMM is used.
 GemmHook<float2> tc_gemm_hook();
+namespace tc {
+int read_and_clear_error();  // 1 if a tensor-core GEMM wait timed out since the last call
+}
 
 }  // namespace wmom

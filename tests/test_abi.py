@@ -1,0 +1,65 @@
+"""The C-ABI library loads without a GPU and exports every entry point the public
+headers declare (no compute call is made here)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HDR = os.path.join(ROOT, "include", "wmom.h")
+LIB = os.path.join(ROOT, "praca-magisterska_gb300", "libwmom.so")
+
+
+def _declared():
+    text = open(HDR).read()
+    return sorted(set(re.findall(r"\b(wmom_[a-z0-9_]+)\s*\(", text)))
+
+
+def _exports():
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.strip()}
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for must in ("wmom_plan_create", "wmom_fill", "wmom_zgetrf", "wmom_zgetrs", "wmom_zgesv_like",
+                 "wmom_solve_sweep", "wmom_topology_from_geo"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(wmom):
+    exp = _exports()
+    missing = [n for n in _declared() if n not in exp]
+    assert not missing, missing
+    lib = ctypes.CDLL(LIB)
+    for n in _declared():
+        getattr(lib, n)
+
+
+def test_dropin_cxx_symbols_have_reference_mangling(wmom):
+    # the reference's own declarations mangle to these names (g++ Itanium ABI)
+    exp = _exports()
+    for sym in ("_Z7zmatrixP7double2PfS1_S1_PiS2_S2_S1_idiiffff",
+                "_Z11zmatrix_gpuP7double2PfS1_S1_S1_PiS2_S2_idiiffff",
+                "_Z6geoinpiiiRiPfS0_S0_S_PiS0_S1_S_S1_"):
+        assert sym in exp, sym
+    assert any(s.startswith("_Z6configRi") for s in exp)
+    assert any(s.startswith("_Z10configwireRi") for s in exp)
+
+
+def test_status_strings(wmom):
+    for code, name in wmom.STATUS_NAMES.items():
+        assert wmom._status_string(code).decode() == name
+
+
+def test_no_device_calls_fail_cleanly_without_gpu(wmom):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("has a GPU")
+    topo = wmom.Topology(wmom.geometry.dipole(1.0, 1e-3, 16))
+    with pytest.raises(wmom.WmomError) as e:
+        wmom.Plan(topo)
+    assert e.value.status in (2, 8)

@@ -1,0 +1,71 @@
+"""GPU fill (libwmom, fill.cu) against the oracle fill and the reference's own
+zmatrix() output (fixtures), entry by entry."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+# Per column, |Z_gpu - Z_ref| <= TOL * max|Z_ref column|: the two differ only in the
+# last-bit rounding of the device sin/cos against the host libm.
+TOL = 1e-13
+
+
+def _gpu_fill(wmom, topo, freqs):
+    plan = wmom.Plan(topo)
+    z = plan.fill(freqs)
+    out = [z[k].T.cpu().numpy() for k in range(len(freqs))]
+    plan.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ["dipole64", "grid5_ns3", "bent_ground", "mixed_junctions", "dipole25m_lowf"])
+def test_fill_matches_reference_fixture(cuda, wmom, name):
+    d = np.load(os.path.join(GOLDEN, f"zfill_{name}.npz"))
+    topo = wmom.Topology(str(d["geo"]), ienv=int(d["ienv"]))
+    (z,) = _gpu_fill(wmom, topo, [float(d["freq"])])
+    zr = d["z"]
+    err = np.max(np.abs(z - zr) / np.max(np.abs(zr), axis=0))
+    assert err < TOL, err
+
+
+@pytest.mark.parametrize("geo,freqs", [
+    ("dipole", [0.01, 1.0, 150.0, 1200.0]),
+    ("grid", [0.001, 0.1, 10.0, 30.0]),
+    ("random", [0.01, 3.0, 10.0]),
+])
+def test_fill_matches_oracle_batched(cuda, wmom, orc, geo, freqs):
+    g = wmom.geometry
+    text = {"dipole": g.dipole(1.0, 1e-3, 300), "grid": g.grid(7, 1.0, 1.0, 5e-3, None, 3),
+            "random": g.random_wires(600, seed=11)}[geo]
+    topo = wmom.Topology(text)
+    zs = _gpu_fill(wmom, topo, freqs)
+    for f, z in zip(freqs, zs):
+        zr = orc.fill(topo.arrays(), f, threads=os.cpu_count() or 1)
+        err = np.max(np.abs(z - zr) / np.max(np.abs(zr), axis=0))
+        assert err < TOL, (f, err)
+
+
+def test_fill_batch_invariance(cuda, wmom):
+    # a matrix is bit-identical whether filled alone or inside a batch
+    topo = wmom.Topology(wmom.geometry.random_wires(400, seed=5))
+    freqs = [0.01, 0.5, 7.0, 10.0]
+    batch = _gpu_fill(wmom, topo, freqs)
+    for f, zb in zip(freqs, batch):
+        (za,) = _gpu_fill(wmom, topo, [f])
+        assert np.array_equal(za, zb)
+
+
+def test_fill_rejects_bad_arguments(cuda, wmom):
+    topo = wmom.Topology(wmom.geometry.dipole(1.0, 1e-3, 32))
+    plan = wmom.Plan(topo)
+    import torch
+    z = torch.empty((1, 31, 31), dtype=torch.complex128, device="cuda")
+    with pytest.raises(wmom.WmomError):
+        plan.fill_device(np.array([-1.0]), z.data_ptr(), 31, 31 * 31)
+    with pytest.raises(wmom.WmomError):
+        plan.fill_device(np.array([1.0]), z.data_ptr(), 30, 31 * 31)
+    plan.close()

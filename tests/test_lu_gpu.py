@@ -1,0 +1,80 @@
+"""FP64 LU with partial pivoting and the triangular solves (lu.cu) against LAPACK
+semantics: the same pivot sequence as zgetf2 on matrices without ties, factors and
+solutions within rounding, zero-pivot info, the host-buffer zgesv drop-in."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+
+
+def _lu_device(cuda, wmom, a):
+    n = a.shape[0]
+    at = cuda.from_numpy(np.ascontiguousarray(a.T)).to("cuda")  # column-major storage of a
+    ipiv = cuda.zeros(n, dtype=cuda.int32, device="cuda")
+    info = wmom.zgetrf_device(at.data_ptr(), n, n, ipiv.data_ptr())
+    cuda.cuda.synchronize()
+    return at, ipiv, info
+
+
+@pytest.mark.parametrize("n", [1, 3, 63, 64, 65, 130, 257, 700])
+def test_lu_pivots_and_factors_match_zgetf2(cuda, wmom, orc, n):
+    a = _rand(n, n)
+    at, ipiv, info = _lu_device(cuda, wmom, a)
+    lu = at.cpu().numpy().T
+    lu_r, ipiv_r, info_r = orc.zgetf2(a)
+    assert info == info_r == 0
+    assert np.array_equal(ipiv.cpu().numpy(), ipiv_r)
+    assert np.max(np.abs(lu - lu_r)) <= 1e-11 * max(1.0, np.max(np.abs(lu_r)))
+
+
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (100, 1), (200, 3), (513, 2)])
+def test_solve_matches_lapack(cuda, wmom, n, nrhs):
+    from scipy.linalg import lapack
+    a = _rand(n, 100 + n)
+    b = np.random.default_rng(1).normal(size=(n, nrhs)) + 0j
+    at, ipiv, info = _lu_device(cuda, wmom, a)
+    bt = cuda.from_numpy(np.ascontiguousarray(b.T)).to("cuda")
+    wmom.zgetrs_device(n, nrhs, at.data_ptr(), n, ipiv.data_ptr(), bt.data_ptr(), n)
+    x = bt.cpu().numpy().T
+    lu, piv, _ = lapack.zgetrf(np.asfortranarray(a))
+    xr, _ = lapack.zgetrs(lu, piv, b)
+    assert np.max(np.abs(x - xr)) <= 1e-10 * np.max(np.abs(xr))
+
+
+def test_zero_pivot_reports_info(cuda, wmom, orc):
+    a = np.zeros((80, 80), np.complex128)
+    a[np.arange(80), np.arange(80)] = 1.0
+    a[:, 40] = 0.0
+    at, ipiv, info = _lu_device(cuda, wmom, a)
+    _, _, info_r = orc.zgetf2(a)
+    assert info == info_r == 41
+
+
+def test_zgesv_like_dropin(cuda, wmom):
+    n = 150
+    a = _rand(n, 3)
+    v = np.zeros(n, np.complex128)
+    v[9] = 1.0
+    i, lu, ipiv, info = wmom.zgesv_like(a, v)
+    assert info == 0
+    assert np.linalg.norm(a @ i - v) < 1e-11 * np.linalg.norm(a) * np.linalg.norm(i)
+    from scipy.linalg import lapack
+    lu_r, piv_r, _ = lapack.zgetrf(np.asfortranarray(a))
+    assert np.array_equal(ipiv, piv_r + 1)
+
+
+def test_large_lu_residual(cuda, wmom):
+    n = 2000
+    a = _rand(n, 77)
+    at, ipiv, info = _lu_device(cuda, wmom, a)
+    b = np.ones((n, 1), np.complex128)
+    bt = cuda.from_numpy(np.ascontiguousarray(b.T)).to("cuda")
+    wmom.zgetrs_device(n, 1, at.data_ptr(), n, ipiv.data_ptr(), bt.data_ptr(), n)
+    x = bt.cpu().numpy().T
+    r = np.linalg.norm(a @ x - b) / (np.linalg.norm(a, 1) * np.linalg.norm(x, 1))
+    assert r < 1e-14

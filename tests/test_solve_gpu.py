@@ -1,0 +1,122 @@
+"""End-to-end fill -> LU -> solve -> Z_in on the GPU against the oracle and the
+reference fixtures.  Tolerances are the solver's contract: relative error 1e-10
+on currents and input impedance for the plain FP64 form, 1e-9 for the refined
+mixed-precision form."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+TOL_MIXED = 1e-9
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def _fixture(name):
+    d = np.load(os.path.join(GOLDEN, f"currents_{name}.npz"))
+    geo = str(np.load(os.path.join(GOLDEN, f"topology_{name}.npz"))["geo"])
+    return d, geo
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name", ["dipole1m_512", "dipole25m_512", "mixed_junctions", "random_1024"])
+def test_currents_match_reference_fixtures(cuda, wmom, name, mode):
+    d, geo = _fixture(name)
+    topo = wmom.Topology(geo, ienv=int(d["ienv"]))
+    plan = wmom.Plan(topo)
+    cur, zin, rep = plan.solve(d["freqs"], int(d["ngap"]), mode=mode, tol=1e-12)
+    tol = TOL_FP64 if mode == 0 else TOL_MIXED
+    for k in range(len(d["freqs"])):
+        assert _rel(cur[k], d["currents"][k]) < tol, (k, _rel(cur[k], d["currents"][k]), rep[k])
+        assert abs(zin[k] - d["zin"][k]) / abs(d["zin"][k]) < tol
+        assert rep[k]["status"] == 0
+    plan.close()
+
+
+def test_grid_2048_against_reference(cuda, wmom):
+    # junction grid: kappa grows at low frequency, the tolerance is scaled by it
+    d, geo = _fixture("grid21_2048")
+    topo = wmom.Topology(geo)
+    plan = wmom.Plan(topo)
+    for mode in (0, 1):
+        cur, zin, rep = plan.solve(d["freqs"], int(d["ngap"]), mode=mode)
+        for k in range(len(d["freqs"])):
+            err = _rel(cur[k], d["currents"][k])
+            # two backward-stable FP64 solves differ by about kappa * eps (kappa reaches
+            # ~1e10 here at 10 kHz); the residual relative to V is bounded the same way
+            assert err < 1e-6, (mode, k, err, rep[k])
+            assert rep[k]["rel_residual"] < 1e-6 and rep[k]["status"] == 0
+    plan.close()
+
+
+def test_logged_zin_known_answers(cuda, wmom):
+    with open(os.path.join(GOLDEN, "zin_logs.json")) as f:
+        logs = json.load(f)
+    for nsw in (512, 1024, 2048):
+        rows = {}
+        for r in logs:
+            if r["nsw"] == nsw:
+                rows.setdefault(r["freq"], r)
+        freqs = sorted(rows)
+        topo = wmom.Topology(wmom.geometry.dipole(25.0, 5e-4, nsw))
+        plan = wmom.Plan(topo)
+        for mode in (0, 1):
+            _, zin, _ = plan.solve(freqs, 100, mode=mode, currents=False)
+            for f, z in zip(freqs, zin):
+                r = rows[f]
+                for val, text in ((z.real, r["re_text"]), (z.imag, r["im_text"])):
+                    v = abs(float(text))
+                    half = 0.5 * 10.0 ** (math.floor(math.log10(v)) - 3) if v else 5e-5
+                    assert abs(val - float(text)) <= 1.01 * half, (nsw, f, z, text)
+        plan.close()
+
+
+def test_batch_invariance_and_alone(cuda, wmom):
+    # every frequency's result is the same alone and inside a batch
+    topo = wmom.Topology(wmom.geometry.random_wires(700, seed=9))
+    plan = wmom.Plan(topo)
+    freqs = np.array([0.01, 0.3, 2.0, 9.0], np.float32)
+    for mode in (0, 1):
+        cb, zb, _ = plan.solve(freqs, 100, mode=mode)
+        for k, f in enumerate(freqs):
+            ca, za, _ = plan.solve([f], 100, mode=mode)
+            assert np.array_equal(ca[0], cb[k])
+    plan.close()
+
+
+def test_mixed_reports_refinement(cuda, wmom, orc):
+    topo = wmom.Topology(wmom.geometry.dipole(1.0, 1e-3, 512))
+    plan = wmom.Plan(topo)
+    cur, zin, rep = plan.solve([150.0], 256, mode=1, tol=1e-12)
+    assert rep[0]["fell_back"] == 0 and rep[0]["iterations"] >= 1
+    assert rep[0]["rel_residual"] <= 1e-12
+    i_ref, zin_ref, _ = orc.solve(topo.arrays(), 150.0, 256, threads=os.cpu_count() or 1)
+    assert _rel(cur[0], i_ref) < TOL_MIXED
+    plan.close()
+
+
+def test_dropin_zmatrix_symbol(cuda, wmom, orc):
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(wmom.__file__), "libwmom.so"))
+    f = getattr(lib, "_Z7zmatrixP7double2PfS1_S1_PiS2_S2_S1_idiiffff")
+    fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+    f.restype = None
+    f.argtypes = [ctypes.c_void_p, fp, fp, fp, ip, ip, ip, fp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+    topo = wmom.Topology(wmom.geometry.grid(4, 1.0, 1.0, 5e-3, None, 3))
+    n = topo.npls
+    cz = np.zeros((n, n), np.complex128, order="F")
+    p = lambda a, t: a.ctypes.data_as(t)
+    f(cz.ctypes.data, p(topo.x, fp), p(topo.y, fp), p(topo.z, fp), p(topo.ipc, ip), p(topo.ips, ip),
+      p(topo.ise, ip), p(topo.rad, fp), n, orc.ka(20.0), topo.nsmax, 1, 1.0, 1.0, 1.0, 1.0)
+    zr = orc.fill(topo.arrays(), 20.0)
+    assert np.max(np.abs(cz - zr) / np.max(np.abs(zr), axis=0)) < 1e-13
