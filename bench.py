@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Frequency-solves/s of the thin-wire MoM fill-and-solve path on GB300.
+
+Workload (one "step"): the plain-FP64-sweep configuration at N = 8192 unknowns -- a
+seeded random straight-wire structure (wires 0.5-5 m, radius 1-10 mm, endpoints in a
+20 m cube, segments <= lambda/10 at 10 MHz) -- with its 12 frequencies log-spaced
+10 kHz - 10 MHz: for every frequency the Z fill, the LU, the solve and Z_in.  Every
+step solves all 12 (geometry, frequency) systems with the precision form (FP64 fill,
+complex-FP32 tensor-core LU, FP64 iterative refinement to a relative residual of
+1e-12, FP64 LU fallback when refinement stalls).  The plain FP64 form is timed on
+the same workload beside it (2 of the 12 frequencies) and both answers are compared.
+
+    value  device throughput: geometry resident on the GPU before the timed region
+    e2e    through the C ABI with host buffers: geometry tables uploaded (plan
+           creation) and currents copied back inside the timed region
+
+--impl reference times the reference's CPU path (its fill restated in C, threaded
+over rows, plus LAPACK zgetrf/zgetrs) on the host cores instead, one frequency of the
+same workload per step.
+
+Multi-GPU: frequencies are independent, so N GPUs run N replicas of the step (weak
+scaling, no collective in the data path); value = all ranks' solves / max time.
+"""
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 8192
+SEED = 20261203
+METRIC = "freq-solves/s and p50/p99 latency: mixed+refine vs FP64 LU at rel err <=1e-10"
+UNIT = "freq-solves/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.path = tempfile.mktemp(prefix="wmom_clocks_", suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx = float(p[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        except OSError:
+            pass
+        os.unlink(self.path) if os.path.exists(self.path) else None
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(n):
+    w = importlib.import_module("praca-magisterska_gb300")
+    topo = w.Topology(w.geometry.random_wires(n, seed=SEED))
+    freqs = w.geometry.sweep_freqs()
+    ngap = n // 2
+    return w, topo, freqs, ngap
+
+
+def cpu_solve_once(topo, freq, ngap, threads):
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    i, zin, _ = orc.solve(topo.arrays(), float(freq), ngap, threads=threads)
+    return time.perf_counter() - t0, i, zin
+
+
+def run_reference(args):
+    """The reference's CPU path (oracle port: fill threaded over rows + LAPACK)."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build_port()
+    w, topo, freqs, ngap = workload(args.n)
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
+    k = 0
+    for _ in range(args.warmup):
+        cpu_solve_once(topo, freqs[k % len(freqs)], ngap, threads)
+        k += 1
+    t = 0.0
+    for _ in range(args.steps):
+        dt, _, _ = cpu_solve_once(topo, freqs[k % len(freqs)], ngap, threads)
+        t += dt
+        k += 1
+    value = args.steps / t
+    sample = (f"one frequency per step of the {len(freqs)}-frequency sweep (cycling), full N={topo.npls} "
+              "fill + zgetrf + zgetrs")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"random-wire sweep, N={topo.npls}, 12 frequencies 10 kHz-10 MHz",
+                       "unknowns": topo.npls, "frequencies": len(freqs), "seed": SEED},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_wmom(args):
+    import numpy as np
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w, topo, freqs, ngap = workload(args.n)
+    n = topo.npls
+    nf = len(freqs)
+    plan = w.Plan(topo)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up
+    for _ in range(args.warmup):
+        plan.solve(freqs, ngap, mode=w.MODE_MIXED, currents=False)
+    torch.cuda.synchronize()
+
+    # timed region: K steps of the mixed + refinement sweep, device-resident geometry
+    w.stats_reset()
+    w.stats_enable(True)
+    reports = []
+    step_ms = []
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _, zin, rep = plan.solve(freqs, ngap, mode=w.MODE_MIXED, currents=False)
+            step_ms.append(1e3 * (time.perf_counter() - t0))
+            reports.extend(rep)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+    w.stats_enable(False)
+    st = w.stats_read()
+    clocks = clk.summary()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    value = ws * nf * args.steps / (ms / 1e3)
+
+    # end to end through the C ABI: geometry upload + solves + currents to host
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        p2 = w.Plan(topo)
+        cur, zin_e2e, rep_e2e = p2.solve(freqs, ngap, mode=w.MODE_MIXED, currents=True)
+        up = p2.upload_bytes
+        p2.close()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = ws * nf * e2e_steps / e2e_s
+    iters = sum(r["iterations"] for r in rep_e2e)
+    h2d = up + 4 * nf + 3 * 8 * nf + 16 * n          # tables, frequencies, k params, excitation
+    d2h = 16 * n * nf + 32 * (iters + nf) + 16 * nf  # currents, residual norms, factor status
+
+    # plain FP64 form on the same systems (2 of the 12 frequencies) + agreement check
+    fsub = np.array([freqs[0], freqs[-1]], np.float32) if args.fp64_freqs == 2 else freqs[:args.fp64_freqs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cur64, zin64, rep64 = plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=True)
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - t0
+    fp64_value = len(fsub) / fp64_s
+    idx = [int(np.argmin(np.abs(freqs - f))) for f in fsub]
+    rel = [float(np.linalg.norm(cur[i] - cur64[j]) / np.linalg.norm(cur64[j])) for j, i in enumerate(idx)]
+
+    # roofline of the dominant kernel class (device time inside the timed region)
+    peaks, peak_src = _peaks()
+    dom = max(st, key=lambda c: st[c]["ms"])
+    d = st[dom]
+    avg_ms = d["ms"] / max(d["timed"], 1)
+    work_per_launch = d["work"] / max(d["timed"], 1)
+    if dom == "tc_gemm":
+        achieved = work_per_launch / (avg_ms / 1e3) / 1e12
+        roof = {"kernel": "cgemm_sub_tc_kernel", "bound": "tensor", "unit": "TFLOP/s",
+                "peak": peaks["bf16_tflops"], "peak_source": f"{peak_src} bf16 (TF32 nominal is half of it)"}
+    elif dom == "residual":
+        achieved = work_per_launch / (avg_ms / 1e3) / 1e9
+        roof = {"kernel": "gemv_partial_kernel", "bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"],
+                "peak_source": peak_src}
+    else:
+        achieved = work_per_launch / (avg_ms / 1e3) / 1e12
+        roof = {"kernel": {"fill": "fill_entry_kernel", "panel": "panel_kernel"}.get(dom, dom), "bound": "fp64",
+                "unit": "TFLOP/s", "peak": args.fp64_peak,
+                "peak_source": "FP64 FMA pipe, measured (profiles/fp64_pipe_probe.md)"}
+    roof.update({"achieved": achieved, "frac": achieved / roof["peak"], "traffic": None,
+                 "avg_launch_ms": avg_ms, "launches": d["timed"],
+                 "share_of_device_time": d["ms"] / max(sum(v["ms"] for v in st.values()), 1e-9)})
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128 fill/residual, c64 tensor-core LU", "data": "synthetic (seeded random wires)",
+        "config": {"workload": f"random-wire sweep, N={n}, 12 frequencies 10 kHz-10 MHz, mixed+refine",
+                   "unknowns": n, "frequencies": nf, "seed": SEED, "ngap": ngap, "refine_tol": 1e-12,
+                   "l2": "inputs larger than L2 (each Z is %.2f GB)" % (16 * n * n / 1e9)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(v["launches"] for v in st.values())),
+        "roofline": roof,
+        "fp64_path": {"value": fp64_value, "unit": UNIT, "frequencies": len(fsub),
+                      "speedup_mixed_over_fp64": value / ws / fp64_value},
+        "accuracy": {"max_rel_err_mixed_vs_fp64": max(rel),
+                     "max_rel_residual": max(r["rel_residual"] for r in reports),
+                     "fallbacks": sum(r["fell_back"] for r in reports),
+                     "max_refinement_steps": max(r["iterations"] for r in reports)},
+        "latency_ms": {"p50_sweep": statistics.median(step_ms), "p99_sweep": sorted(step_ms)[-1]},
+        "kernel_ms": {k: round(v["ms"], 3) for k, v in st.items()},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import build as ob
+        ob.build_port()
+        threads = os.cpu_count() or 1
+        dt, i_cpu, zin_cpu = cpu_solve_once(topo, freqs[-1], ngap, threads)
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 of the 12 frequencies ({freqs[-1]:.4g} MHz), full N={n} fill + "
+                                          "zgetrf + zgetrs"}
+        j = fsub.tolist().index(freqs[-1]) if freqs[-1] in fsub else None
+        if j is not None:
+            line["accuracy"]["rel_err_fp64_vs_cpu_oracle"] = float(
+                np.linalg.norm(cur64[j] - i_cpu) / np.linalg.norm(i_cpu))
+            line["accuracy"]["rel_err_mixed_vs_cpu_oracle"] = float(
+                np.linalg.norm(cur[nf - 1] - i_cpu) / np.linalg.norm(i_cpu))
+    plan.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="wmom", choices=["wmom", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--fp64-freqs", type=int, default=2)
+    ap.add_argument("--fp64-peak", type=float, default=1.2, help="FP64 pipe TFLOP/s (measured)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_wmom(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -86,6 +86,12 @@ wmom_status wmom_plan_create(const float* x, const float* y, const float* z, con
                              wmom_plan* out);
 wmom_status wmom_plan_destroy(wmom_plan plan);
 int wmom_plan_npls(wmom_plan plan);
+/* Bytes of per-geometry tables the plan uploaded to the device. */
+long long wmom_plan_upload_bytes(wmom_plan plan);
+/* 1 when the plan fills with the pair-tiled kernel (free space), 0 when with the
+ * per-entry kernel (PEC ground image terms).  Setting WMOM_FILL_ENTRY=1 in the
+ * environment forces the per-entry kernel. */
+int wmom_plan_fill_variant(wmom_plan plan);
 
 /* Fills nk impedance matrices, one per wave number ka[i] (host array), in FP64.
  * Matrix i starts at z_dev + i*zstride complex elements; ldz >= npls.  The
@@ -148,6 +154,20 @@ wmom_status wmom_solve_sweep(wmom_plan plan, const float* freq_mhz, int nfreq, i
 
 /* Human-readable name of a status code. */
 const char* wmom_status_string(wmom_status s);
+
+/* ------------------------------------------------------- instrumentation ---- */
+/* Launch counters per kernel class are always kept.  With timing enabled every
+ * launch is also bracketed by CUDA events on its own stream.  Classes, in order:
+ * 0 fill, 1 panel, 2 tensor-core GEMM, 3 SIMT GEMM, 4 triangular solves,
+ * 5 row interchanges, 6 FP64 residual, 7 other.  wmom_stats_read fills up to n
+ * entries of each array (any may be NULL) and returns the number of classes;
+ * ms = summed device time, launches = launches issued, timed = launches timed,
+ * work = algorithmic flops (bytes for the residual) of the timed launches.  The
+ * reference's equivalent is its Timer / "GPU time.dat" (REF/Wire_MoM.cu:8-26,
+ * 4085-4175). */
+void wmom_stats_enable(int on);
+void wmom_stats_reset(void);
+int wmom_stats_read(double* ms, long long* launches, long long* timed, double* work, int n);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,8 @@ _plan_create = _sig("wmom_plan_create", ctypes.c_int,
                      ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.POINTER(_vp)])
 _plan_destroy = _sig("wmom_plan_destroy", ctypes.c_int, [_vp])
 _plan_npls = _sig("wmom_plan_npls", ctypes.c_int, [_vp])
+_plan_upload_bytes = _sig("wmom_plan_upload_bytes", ctypes.c_longlong, [_vp])
+_plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
 _zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
 _zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
@@ -89,6 +91,32 @@ _solve_sweep = _sig("wmom_solve_sweep", ctypes.c_int,
                     [_vp, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
                      ctypes.c_double, _dp, _dp, ctypes.POINTER(_Report), _vp])
 _status_string = _sig("wmom_status_string", ctypes.c_char_p, [ctypes.c_int])
+_stats_enable = _sig("wmom_stats_enable", None, [ctypes.c_int])
+_stats_reset = _sig("wmom_stats_reset", None, [])
+_stats_read = _sig("wmom_stats_read", ctypes.c_int,
+                   [_dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _dp, ctypes.c_int])
+
+STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc"]
+
+
+def stats_enable(on=True):
+    """Bracket every library kernel launch with CUDA events on its stream."""
+    _stats_enable(1 if on else 0)
+
+
+def stats_reset():
+    _stats_reset()
+
+
+def stats_read():
+    """{class: dict(ms, launches, timed, work)} since the last reset."""
+    n = len(STAT_CLASSES)
+    ms = (ctypes.c_double * n)()
+    la = (ctypes.c_longlong * n)()
+    ti = (ctypes.c_longlong * n)()
+    wk = (ctypes.c_double * n)()
+    _stats_read(ms, la, ti, wk, n)
+    return {c: dict(ms=ms[i], launches=la[i], timed=ti[i], work=wk[i]) for i, c in enumerate(STAT_CLASSES)}
 
 
 def _check(st, what):
@@ -104,7 +132,7 @@ def library_symbols():
     """Names of the C-ABI entry points this module binds."""
     return ["wmom_topology_from_geo", "wmom_ka", "wmom_plan_create", "wmom_plan_destroy", "wmom_plan_npls",
             "wmom_fill", "wmom_zgetrf", "wmom_zgetrs", "wmom_zgesv_like", "wmom_excitation",
-            "wmom_solve_sweep", "wmom_status_string"]
+            "wmom_solve_sweep", "wmom_status_string", "wmom_stats_enable", "wmom_stats_reset", "wmom_stats_read"]
 
 
 # ----------------------------------------------------------------- geometry ----
@@ -183,6 +211,8 @@ class Plan:
         _check(st, "wmom_plan_create")
         self._h = h
         self.npls = topo.npls
+        self.upload_bytes = int(_plan_upload_bytes(h))
+        self.fill_variant = "pair" if _plan_fill_variant(h) == 1 else "entry"
 
     def close(self):
         if self._h:

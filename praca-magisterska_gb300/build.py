@@ -22,8 +22,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CPP_SOURCES = ["topology.cpp", "plan.cpp", "dropin.cpp"]
-CU_SOURCES = ["fill.cu", "lu.cu", "solve.cu", "api.cu", "lu_tc.cu"]
-HEADERS = ["wmom_internal.h", "lu_common.cuh", "lu_internal.h", "solve_internal.h"]
+CU_SOURCES = ["fill.cu", "lu.cu", "solve.cu", "api.cu", "lu_tc.cu", "stats.cu"]
+HEADERS = ["wmom_internal.h", "lu_common.cuh", "lu_internal.h", "solve_internal.h", "stats.h"]
 
 
 def _deps():

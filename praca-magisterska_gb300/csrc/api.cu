@@ -129,6 +129,7 @@ struct wmom_plan_s {
   int fp_cap = 0;
   LuWorkspace ws{};
   int ws_n = 0;
+  size_t tile_bytes = 0;
 };
 
 extern "C" {
@@ -194,9 +195,38 @@ wmom_status wmom_plan_create(const float* x, const float* y, const float* z, con
     e = cudaMemcpy(p.d_obs, p.h_obs.data(), sizeof(ObsHalf) * p.h_obs.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(p.d_src, p.h_src.data(), sizeof(SrcHalf) * p.h_src.size(), cudaMemcpyHostToDevice);
+  // pair-tiled fill tables (free space)
+  plan_build_pair_tiles(&p, x, y, z, rad, ipc, ips, ise);
+  if (e == cudaSuccess && p.pt.ok) {
+    const PairTiles& t = p.pt;
+    std::vector<int> ints;
+    ints.insert(ints.end(), t.rt_off.begin(), t.rt_off.end());
+    p.off_rt_ids = (int)ints.size();
+    ints.insert(ints.end(), t.rt_ids.begin(), t.rt_ids.end());
+    p.off_ct_off = (int)ints.size();
+    ints.insert(ints.end(), t.ct_off.begin(), t.ct_off.end());
+    p.off_ct_ids = (int)ints.size();
+    ints.insert(ints.end(), t.ct_ids.begin(), t.ct_ids.end());
+    p.off_row_local = (int)ints.size();
+    ints.insert(ints.end(), t.row_local.begin(), t.row_local.end());
+    p.off_col_local = (int)ints.size();
+    ints.insert(ints.end(), t.col_local.begin(), t.col_local.end());
+    e = cudaMalloc(&p.d_oi, sizeof(ObsInst) * t.obs.size());
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_si, sizeof(SrcInst) * t.src.size());
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_tiles, sizeof(int) * ints.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p.d_oi, t.obs.data(), sizeof(ObsInst) * t.obs.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p.d_si, t.src.data(), sizeof(SrcInst) * t.src.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p.d_tiles, ints.data(), sizeof(int) * ints.size(), cudaMemcpyHostToDevice);
+    h->tile_bytes = sizeof(ObsInst) * t.obs.size() + sizeof(SrcInst) * t.src.size() + sizeof(int) * ints.size();
+  }
   if (e != cudaSuccess) {
     if (p.d_obs) cudaFree(p.d_obs);
     if (p.d_src) cudaFree(p.d_src);
+    if (p.d_oi) cudaFree(p.d_oi);
+    if (p.d_si) cudaFree(p.d_si);
+    if (p.d_tiles) cudaFree(p.d_tiles);
     delete h;
     return wmom_fail_cuda(e, "plan upload");
   }
@@ -209,6 +239,9 @@ wmom_status wmom_plan_destroy(wmom_plan h) {
   cudaDeviceSynchronize();
   if (h->p.d_obs) cudaFree(h->p.d_obs);
   if (h->p.d_src) cudaFree(h->p.d_src);
+  if (h->p.d_oi) cudaFree(h->p.d_oi);
+  if (h->p.d_si) cudaFree(h->p.d_si);
+  if (h->p.d_tiles) cudaFree(h->p.d_tiles);
   if (h->d_fp) cudaFree(h->d_fp);
   if (h->ws_n) lu_workspace_destroy(&h->ws);
   delete h;
@@ -216,6 +249,13 @@ wmom_status wmom_plan_destroy(wmom_plan h) {
 }
 
 int wmom_plan_npls(wmom_plan h) { return h ? h->p.npls : -1; }
+
+int wmom_plan_fill_variant(wmom_plan h) { return h ? (h->p.pt.ok ? 1 : 0) : -1; }
+
+long long wmom_plan_upload_bytes(wmom_plan h) {
+  if (!h) return -1;
+  return (long long)(sizeof(ObsHalf) * h->p.h_obs.size() + sizeof(SrcHalf) * h->p.h_src.size() + h->tile_bytes);
+}
 
 wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long long ldz,
                       long long zstride, void* stream) {

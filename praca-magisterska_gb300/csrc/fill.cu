@@ -16,6 +16,9 @@
 // so that the float-derived coordinates give the same doubles as the CPU code.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
+#include "stats.h"
 #include "wmom_internal.h"
 
 namespace wmom {
@@ -237,13 +240,199 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
   Z[(size_t)k * zstride + (size_t)n * ldz + m] = out;
 }
 
+// ------------------------------------------------------------------------
+// Pair-tiled fill.  One CTA per 32 x 32 tile of Z (and per frequency): phase A
+// evaluates every distinct (observation instance, source instance) pair of the tile
+// once -- the rising-ramp, falling-ramp and plain integrals, the first two already
+// multiplied by the test-vector projection and the last divided by the segment
+// length -- into shared memory; phase B assembles each entry from four pair values
+// in the reference's order of operations.  Each pair is the same arithmetic as in
+// fill_entry_kernel, so both kernels produce the same matrix.
+// ------------------------------------------------------------------------
+struct PairVal {
+  double2 wu, wd, ph;
+};
+
+__device__ void self_pair(double dl, double an, double ka, Cx* Au, Cx* Ad, Cx* P) {
+  const double pi = 3.141592653589793;
+  const double dlh = mul(0.5, dl);
+  Cx tu = {0.0, 0.0}, td = {0.0, 0.0}, tp = {0.0, 0.0};
+#pragma unroll 1
+  for (int part = 0; part < 2; ++part) {
+    const double lo = part == 0 ? 0.0 : dlh, hi = part == 0 ? dlh : dl;
+    const double a = mul(0.5, add(lo, hi)), b = sub(hi, lo);
+    Cx qu[2], qd[2], qp[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const double c = mul(q == 0 ? kGl4C1 : kGl4C2, b);
+      const double s1 = add(a, c), s2 = sub(a, c);
+      const Cx v1 = self_bracket(s1, ka, dl, an), v2 = self_bracket(s2, ka, dl, an);
+      const double u1 = __ddiv_rn(s1, dl), u2 = __ddiv_rn(s2, dl);
+      const double d1 = __ddiv_rn(sub(dl, s1), dl), d2 = __ddiv_rn(sub(dl, s2), dl);
+      const double wq = q == 0 ? kGl4W1 : kGl4W2;
+      qu[q].re = mul(add(mul(u1, v1.re), mul(u2, v2.re)), wq);
+      qu[q].im = mul(add(mul(u1, v1.im), mul(u2, v2.im)), wq);
+      qd[q].re = mul(add(mul(d1, v1.re), mul(d2, v2.re)), wq);
+      qd[q].im = mul(add(mul(d1, v1.im), mul(d2, v2.im)), wq);
+      qp[q].re = mul(add(v1.re, v2.re), wq);
+      qp[q].im = mul(add(v1.im, v2.im), wq);
+    }
+    const Cx pu = {mul(add(qu[0].re, qu[1].re), b), mul(add(qu[0].im, qu[1].im), b)};
+    const Cx pd = {mul(add(qd[0].re, qd[1].re), b), mul(add(qd[0].im, qd[1].im), b)};
+    const Cx pp = {mul(add(qp[0].re, qp[1].re), b), mul(add(qp[0].im, qp[1].im), b)};
+    if (part == 0) {
+      tu = pu;
+      td = pd;
+      tp = pp;
+    } else {
+      tu = Cx{add(tu.re, pu.re), add(tu.im, pu.im)};
+      td = Cx{add(td.re, pd.re), add(td.im, pd.im)};
+      tp = Cx{add(tp.re, pp.re), add(tp.im, pp.im)};
+    }
+  }
+  const double lg = add(1.0, log(__ddiv_rn(mul(16.0, an), dl)));
+  const double res3 = __ddiv_rn(mul(dl, lg), mul(pi, an));
+  const double res12 = __ddiv_rn(mul(mul(0.5, dl), lg), mul(pi, an));
+  *Au = Cx{add(tu.re, res12), tu.im};
+  *Ad = Cx{add(td.re, res12), td.im};
+  *P = Cx{add(tp.re, res3), tp.im};
+}
+
+__global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restrict__ oinst,
+                                                        const SrcInst* __restrict__ sinst,
+                                                        const int* __restrict__ tiles, int off_rt_ids,
+                                                        int off_ct_off, int off_ct_ids, int off_row_local,
+                                                        int off_col_local, int npls, int max_o, int max_q,
+                                                        const FreqParams* __restrict__ fp,
+                                                        double2* __restrict__ Z, long long ldz,
+                                                        long long zstride) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  ObsInst* so = reinterpret_cast<ObsInst*>(sm);
+  SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
+  const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
+  PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
+  const int* rt_off = tiles;
+  const int* rt_ids = tiles + off_rt_ids;
+  const int* ct_off = tiles + off_ct_off;
+  const int* ct_ids = tiles + off_ct_ids;
+  const int* row_local = tiles + off_row_local;
+  const int* col_local = tiles + off_col_local;
+
+  const int tr = blockIdx.x, tc = blockIdx.y, k = blockIdx.z;
+  const int tid = threadIdx.x;
+  const int o0 = rt_off[tr], nO = rt_off[tr + 1] - o0;
+  const int q0 = ct_off[tc], nQ = ct_off[tc + 1] - q0;
+  for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[rt_ids[o0 + i]];
+  for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[ct_ids[q0 + i]];
+  __syncthreads();
+  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+
+  // phase A: distinct pairs of the tile
+  for (int p = tid; p < nO * nQ; p += blockDim.x) {
+    const int o = p / nQ, q = p - o * nQ;
+    const ObsInst& O = so[o];
+    const SrcInst& S = sq[q];
+    const bool same = (S.nl == O.ml && S.nr == O.mr) || (S.nl == O.mr && S.nr == O.ml);
+    Cx Au, Ad, P;
+    if (!same) {
+      const double an2 = mul(S.an, S.an);
+      Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const double s = S.s[g];
+        const double dx = sub(sub(O.rm[0], S.rs[0]), mul(s, S.dc[0]));
+        const double dy = sub(sub(O.rm[1], S.rs[1]), mul(s, S.dc[1]));
+        const double dz = sub(sub(O.rm[2], S.rs[2]), mul(s, S.dc[2]));
+        const double r = sqrt(add(add(add(an2, mul(dx, dx)), mul(dy, dy)), mul(dz, dz)));
+        double sn, cs;
+        sincos(mul(ka, r), &sn, &cs);
+        const double gre = __ddiv_rn(cs, r), gim = __ddiv_rn(-sn, r);
+        su.re = add(su.re, mul(S.w_up[g], gre));
+        su.im = add(su.im, mul(S.w_up[g], gim));
+        sd.re = add(sd.re, mul(S.w_dn[g], gre));
+        sd.im = add(sd.im, mul(S.w_dn[g], gim));
+        sp.re = add(sp.re, gre);
+        sp.im = add(sp.im, gim);
+      }
+      const double h = mul(S.dl, 0.5);
+      Au = Cx{mul(su.re, h), mul(su.im, h)};
+      Ad = Cx{mul(sd.re, h), mul(sd.im, h)};
+      P = Cx{mul(sp.re, h), mul(sp.im, h)};
+    } else {
+      self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
+    }
+    const double t = dot3(S.dc, O.u);
+    PairVal v;
+    v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
+    v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
+    v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
+    pt[p] = v;
+  }
+  __syncthreads();
+
+  // phase B: entries of the tile (consecutive threads = consecutive rows)
+  for (int e = tid; e < kPairTile * kPairTile; e += blockDim.x) {
+    const int r = e % kPairTile, c = e / kPairTile;
+    const int m = tr * kPairTile + r, n = tc * kPairTile + c;
+    if (m >= npls || n >= npls) continue;
+    const int c0 = col_local[2 * n], c1 = col_local[2 * n + 1];
+    double acc_re = 0.0, acc_im = 0.0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rl = row_local[2 * m + h];
+      const int o = rl & 0x3FFFFFFF;
+      const PairVal& pu = pt[o * nQ + c0];
+      const PairVal& pd = pt[o * nQ + c1];
+      double av_re = add(pu.wu.x, pd.wd.x), av_im = add(pu.wu.y, pd.wd.y);
+      if (rl >> 30) {
+        av_re = -av_re;
+        av_im = -av_im;
+      }
+      const double sv_re = sub(pu.ph.x, pd.ph.x), sv_im = sub(pu.ph.y, pd.ph.y);
+      double c_re = mul(av_re, ka2), c_im = mul(av_im, ka2);
+      if (h == 0) {
+        c_re = sub(c_re, sv_re);
+        c_im = sub(c_im, sv_im);
+      } else {
+        c_re = add(c_re, sv_re);
+        c_im = add(c_im, sv_im);
+      }
+      acc_re = add(acc_re, c_re);
+      acc_im = add(acc_im, c_im);
+    }
+    double2 out;
+    out.x = -mul(cq, acc_im);
+    out.y = mul(cq, acc_re);
+    Z[(size_t)k * zstride + (size_t)n * ldz + m] = out;
+  }
+}
+
+size_t pair_smem_bytes(const PairTiles& t) {
+  const size_t head = ((size_t)t.max_o * sizeof(ObsInst) + (size_t)t.max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
+  return head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
+}
+
 }  // namespace
 
 cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream) {
   if (nk <= 0 || p.npls <= 0) return cudaSuccess;
+  const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
+  if (p.pt.ok && p.d_tiles && !(force_entry && force_entry[0] == '1')) {
+    const size_t smem = pair_smem_bytes(p.pt);
+    cudaError_t e = cudaFuncSetAttribute(fill_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(p.pt.n_tiles, p.pt.n_tiles, nk);
+    stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
+    fill_pair_kernel<<<grid, 256, smem, stream>>>(p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off,
+                                                  p.off_ct_ids, p.off_row_local, p.off_col_local, p.npls,
+                                                  p.pt.max_o, p.pt.max_q, reinterpret_cast<const FreqParams*>(d_fp),
+                                                  z, ldz, zstride);
+    return cudaGetLastError();
+  }
   dim3 block(128);
   dim3 grid((p.npls + 127) / 128, p.npls, nk);
+  stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
   fill_entry_kernel<<<grid, block, 0, stream>>>(p.d_obs, p.d_src, p.npls,
                                                 reinterpret_cast<const FreqParams*>(d_fp), z, ldz,
                                                 zstride, p.ienv, p.sgnenv);

@@ -28,6 +28,7 @@
 
 #include "lu_common.cuh"
 #include "lu_internal.h"
+#include "stats.h"
 #include "wmom_internal.h"
 
 namespace wmom {
@@ -486,11 +487,15 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     int np = n, j0p = j0, nbp = nb, rpcp = rpc;
     int* ipivp = ipiv;
     void* args[] = {&Ap, &ldap, &np, &j0p, &nbp, &rpcp, &ipivp, &st, &gb};
-    e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P), dim3(NT), args, smem, s);
+    {
+      stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)nb * nb / 2.0);
+      e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P), dim3(NT), args, smem, s);
+    }
     if (e != cudaSuccess) return e;
     // interchanges on the other columns
     const int other = n - nb;
     if (other > 0) {
+      stats::Scope sc(stats::kLaswp, s, 2.0 * nb * other * sizeof(C));
       laswp_kernel<C><<<(other + 127) / 128, 128, 0, s>>>(A, lda, n, j0, j0 + nb, j0, nb, ipiv);
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
@@ -505,12 +510,16 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       e = cudaFuncSetAttribute(trsm_kernel<C, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tsmem);
       if (e != cudaSuccess) return e;
-      trsm_kernel<C, false><<<(rest + kTrsmCols - 1) / kTrsmCols, 256, tsmem, s>>>(A11, lda, A12, lda, nb, rest);
+      {
+        stats::Scope sc(stats::kTrsm, s, 4.0 * nb * (double)nb * rest);
+        trsm_kernel<C, false><<<(rest + kTrsmCols - 1) / kTrsmCols, 256, tsmem, s>>>(A11, lda, A12, lda, nb, rest);
+      }
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       if (gemm_hook) {
         e = gemm_hook(A21, lda, A12, lda, A22, lda, rest, rest, nb, s);
       } else {
+        stats::Scope sc(stats::kGemm, s, 8.0 * rest * (double)rest * nb);
         dim3 grid((rest + kGemmBM - 1) / kGemmBM, (rest + kGemmBN - 1) / kGemmBN);
         gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A21, lda, A12, lda, A22, lda, rest, rest, nb);
         e = cudaGetLastError();
@@ -531,6 +540,7 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
   e = cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(n * sizeof(int)));
   if (e != cudaSuccess) return e;
+  stats::count(stats::kMisc, 2);
   pivots_to_perm_kernel<<<1, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm);
   C* tmp = reinterpret_cast<C*>(ws->rhs);
   if ((size_t)n * nrhs * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
@@ -544,6 +554,8 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
   e = cudaFuncSetAttribute(trsm_kernel<C, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
   if (e != cudaSuccess) return e;
   // forward: L unit lower
+  const int nblocks = (n + NB - 1) / NB;
+  stats::Scope sc(stats::kTrsm, s, 8.0 * n * (double)n * nrhs, 4 * nblocks - 2);
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int kb = std::min(NB, n - k0);
     const size_t sm = ((size_t)kb * kb + (size_t)kb * kTrsmCols) * sizeof(C);

@@ -32,6 +32,7 @@
 
 #include "lu_common.cuh"
 #include "solve_internal.h"
+#include "stats.h"
 
 namespace wmom {
 namespace tc {
@@ -71,10 +72,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait on an mbarrier phase; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase; false on timeout or when another CTA of the
+// launch has already recorded one (err != 0).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const int* err) {
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
+    if (*reinterpret_cast<const volatile int*>(err)) return false;
     if (global_ns() - t0 > kWaitNs) return false;
   }
   return true;
@@ -199,13 +202,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t tmem = tmem_base;
 
   if (tid == 0) {
-    bool ok = true;
+    bool ok = *reinterpret_cast<const volatile int*>(err) == 0;
     int issued_last = -1;
+    int tma_pending = -1;  // chunk whose copies were issued but not yet seen complete
     for (int c = 0; c < nchunks && ok; ++c) {
       const int s = c % STAGES;
       const uint32_t full = smem_u32(&bars[s]);
       const uint32_t done = smem_u32(&bars[STAGES + s]);
-      if (c >= STAGES) ok = mbar_wait(done, ((c - STAGES) / STAGES) & 1);
+      if (c >= STAGES) ok = mbar_wait(done, ((c - STAGES) / STAGES) & 1, err);
       if (!ok) break;
       unsigned char* st = base + s * STAGE_BYTES;
       const uint32_t a_hi = smem_u32(st), a_lo = a_hi + A_BYTES;
@@ -215,8 +219,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       tma_load_2d(a_lo, &mapAlo, c * KC, m0, full);
       tma_load_2d(b_hi, &mapBhi, c * KC, j0, full);
       tma_load_2d(b_lo, &mapBlo, c * KC, j0, full);
-      ok = mbar_wait(full, (c / STAGES) & 1);
+      tma_pending = c;
+      ok = mbar_wait(full, (c / STAGES) & 1, err);
       if (!ok) break;
+      tma_pending = -1;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // tail terms first, head product last
       const uint32_t as[3] = {a_lo, a_hi, a_hi};
@@ -231,11 +237,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     if (ok && issued_last >= 0) {
       const int s = issued_last % STAGES;
-      ok = mbar_wait(smem_u32(&bars[STAGES + s]), (issued_last / STAGES) & 1);
+      ok = mbar_wait(smem_u32(&bars[STAGES + s]), (issued_last / STAGES) & 1, err);
     }
     if (!ok) {
       s_fail = 1;
       atomicExch(err, 1);
+      // before leaving, give this CTA's own copies and MMAs in flight a bounded
+      // chance to land, so nothing writes shared memory or TMEM after release
+      const int zero = 0;
+      if (tma_pending >= 0) mbar_wait(smem_u32(&bars[tma_pending % STAGES]), (tma_pending / STAGES) & 1, &zero);
+      if (issued_last >= 0)
+        mbar_wait(smem_u32(&bars[STAGES + issued_last % STAGES]), (issued_last / STAGES) & 1, &zero);
     }
   }
   __syncthreads();
@@ -366,6 +378,7 @@ cudaError_t cgemm_sub_tc(const float2* A, long long lda, const float2* B, long l
   float* alo = ahi + a_pl;
   float* bhi = alo + a_pl;
   float* blo = bhi + b_pl;
+  stats::count(stats::kMisc, 2);
   pack_a_kernel<<<dim3((M + 127) / 128, K2p / 2), 128, 0, s>>>(A, lda, M, K, K2p, ahi, alo);
   pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo);
   CUtensorMap mah, mal, mbh, mbl;
@@ -379,6 +392,7 @@ cudaError_t cgemm_sub_tc(const float2* A, long long lda, const float2* B, long l
     attr_set = true;
   }
   dim3 grid((M + BM - 1) / BM, (2 * N + BN - 1) / BN);
+  stats::Scope sc(stats::kTcGemm, s, 8.0 * M * (double)N * K);
   cgemm_sub_tc_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / KC, w->err);
   return cudaGetLastError();
 }

@@ -93,3 +93,156 @@ int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, c
 }
 
 }  // namespace wmom
+
+// ----------------------------------------------------------------------------
+// Pair-tiled fill tables.  Neighbouring basis functions share segments, so the
+// (observation point, source half-segment) integrals of one tile of 32 x 32 entries
+// involve only ~33 x 33 distinct pairs instead of 4 x 32 x 32.  This builds the
+// distinct instances and, per tile, the list of them and every half's position in
+// that list.  The per-entry values it feeds are the same expressions as above.
+// Free space only; the image terms of a PEC ground use the per-entry fill.
+// ----------------------------------------------------------------------------
+#include <array>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+namespace wmom {
+
+void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float* z, const float* rad,
+                           const int* ipc, const int* ips, const int* ise) {
+  PairTiles& t = p->pt;
+  t = PairTiles{};
+  if (p->ienv != 1) return;
+  const int npls = p->npls, nsmax = p->nsmax;
+  const double kGl2C = 0.288675134594812882;
+  auto node = [&](int k, double r[3]) {
+    r[0] = (double)x[k - 1];
+    r[1] = (double)y[k - 1];
+    r[2] = (double)z[k - 1];
+  };
+  std::map<std::array<int, 4>, int> okey;
+  std::map<std::tuple<int, int, int, int, uint32_t>, int> qkey;
+  std::vector<int> obs_of(2 * (size_t)npls), neg_of(2 * (size_t)npls), src_of(2 * (size_t)npls);
+  for (int b = 0; b < npls; ++b) {
+    const int np = std::abs(ipc[b]);
+    const int s1 = ips[b], s2 = ips[b + nsmax];
+    for (int h = 0; h < 2; ++h) {
+      const int ms = h == 0 ? s1 : s2;
+      const int ml = ise[ms - 1], mr = ise[ms + nsmax - 1];
+      const int other = h == 0 ? ise[s1 - 1] : ise[s2 + nsmax - 1];
+      const int lo = std::min(np, other), hi = std::max(np, other);
+      const std::array<int, 4> key{ml, mr, lo, hi};
+      auto it = okey.find(key);
+      int id;
+      const ObsHalf& oh = p->h_obs[2 * (size_t)b + h];
+      if (it == okey.end()) {
+        ObsInst oi{};
+        double rh[3];
+        node(hi, rh);
+        for (int k = 0; k < 3; ++k) {
+          oi.rm[k] = oh.rm[k];
+          oi.u[k] = rh[k] - oi.rm[k];
+        }
+        oi.ml = ml;
+        oi.mr = mr;
+        oi.on_ground = oh.on_ground;
+        id = (int)t.obs.size();
+        t.obs.push_back(oi);
+        okey.emplace(key, id);
+      } else {
+        id = it->second;
+      }
+      const ObsInst& oi = t.obs[id];
+      // the observation point and the test vector must be the instance's, bit for bit
+      bool pos = true, neg = true;
+      for (int k = 0; k < 3; ++k) {
+        if (oi.rm[k] != oh.rm[k]) return;
+        pos = pos && (oh.lm[k] == oi.u[k]);
+        neg = neg && (oh.lm[k] == -oi.u[k]);
+      }
+      if (!pos && !neg) return;
+      obs_of[2 * (size_t)b + h] = id;
+      neg_of[2 * (size_t)b + h] = pos ? 0 : 1;
+    }
+    for (int sg = 0; sg < 2; ++sg) {
+      const SrcHalf& sh = p->h_src[2 * (size_t)b + sg];
+      const int seg = sg == 0 ? s1 : s2;
+      const int a = sg == 0 ? ise[s1 - 1] : np;
+      const int e = sg == 0 ? np : ise[s2 + nsmax - 1];
+      uint32_t rbits;
+      std::memcpy(&rbits, &rad[seg - 1], 4);
+      const auto key = std::make_tuple(a, e, sh.nl, sh.nr, rbits);
+      auto it = qkey.find(key);
+      int id;
+      if (it == qkey.end()) {
+        SrcInst si{};
+        for (int k = 0; k < 3; ++k) {
+          si.rs[k] = sh.rs[k];
+          si.dc[k] = sh.dc[k];
+        }
+        si.dl = sh.dl;
+        si.an = sh.an;
+        const double aa = 0.5 * (0.0 + sh.dl), bb = sh.dl - 0.0, cc = kGl2C * bb;
+        si.s[0] = aa + cc;
+        si.s[1] = aa - cc;
+        for (int g = 0; g < 2; ++g) {
+          si.w_up[g] = si.s[g] / sh.dl;
+          si.w_dn[g] = (sh.dl - si.s[g]) / sh.dl;
+        }
+        si.nl = sh.nl;
+        si.nr = sh.nr;
+        id = (int)t.src.size();
+        t.src.push_back(si);
+        qkey.emplace(key, id);
+      } else {
+        id = it->second;
+      }
+      src_of[2 * (size_t)b + sg] = id;
+    }
+  }
+  const int T = t.tile;
+  t.n_tiles = (npls + T - 1) / T;
+  t.row_local.assign(2 * (size_t)npls, 0);
+  t.col_local.assign(2 * (size_t)npls, 0);
+  t.rt_off.assign(t.n_tiles + 1, 0);
+  t.ct_off.assign(t.n_tiles + 1, 0);
+  for (int tile = 0; tile < t.n_tiles; ++tile) {
+    std::map<int, int> lo, lq;
+    const int b0 = tile * T, b1 = std::min(npls, b0 + T);
+    for (int b = b0; b < b1; ++b)
+      for (int h = 0; h < 2; ++h) {
+        const int o = obs_of[2 * (size_t)b + h];
+        auto it = lo.find(o);
+        int l;
+        if (it == lo.end()) {
+          l = (int)lo.size();
+          lo.emplace(o, l);
+          t.rt_ids.push_back(o);
+        } else {
+          l = it->second;
+        }
+        t.row_local[2 * (size_t)b + h] = l | (neg_of[2 * (size_t)b + h] ? (1 << 30) : 0);
+        const int q = src_of[2 * (size_t)b + h];
+        auto iq = lq.find(q);
+        int m;
+        if (iq == lq.end()) {
+          m = (int)lq.size();
+          lq.emplace(q, m);
+          t.ct_ids.push_back(q);
+        } else {
+          m = iq->second;
+        }
+        t.col_local[2 * (size_t)b + h] = m;
+      }
+    t.rt_off[tile + 1] = (int)t.rt_ids.size();
+    t.ct_off[tile + 1] = (int)t.ct_ids.size();
+    t.max_o = std::max(t.max_o, (int)lo.size());
+    t.max_q = std::max(t.max_q, (int)lq.size());
+  }
+  const size_t smem = (size_t)t.max_o * sizeof(ObsInst) + (size_t)t.max_q * sizeof(SrcInst) +
+                      (size_t)t.max_o * t.max_q * 48;
+  t.ok = smem <= 200 * 1024;
+}
+
+}  // namespace wmom

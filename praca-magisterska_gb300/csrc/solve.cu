@@ -18,6 +18,7 @@
 
 #include "lu_common.cuh"
 #include "solve_internal.h"
+#include "stats.h"
 
 namespace wmom {
 
@@ -125,6 +126,7 @@ __global__ void widen_vec_kernel(const float2* __restrict__ d, double2* __restri
 cudaError_t residual_fp64(const double2* Z, long long ldz, const double2* x, const double2* v, int n,
                           double2* r, double2* partial, cudaStream_t s) {
   const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
+  stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n, 2);
   gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks), kGemvRows, 0, s>>>(Z, ldz, x, n,
                                                                                            partial);
   residual_finish_kernel<<<(n + 255) / 256, 256, 0, s>>>(v, partial, nchunks, n, r);
@@ -132,22 +134,26 @@ cudaError_t residual_fp64(const double2* Z, long long ldz, const double2* x, con
 }
 
 cudaError_t sumsq_fp64(const double2* x, int n, double* out, cudaStream_t s) {
+  stats::count(stats::kMisc);
   sumsq_kernel<<<1, 1024, 0, s>>>(x, n, out);
   return cudaGetLastError();
 }
 
 cudaError_t convert_matrix_64_to_32(const double2* src, long long lds, float2* dst, long long ldd, int rows,
                                     int cols, cudaStream_t s) {
+  stats::Scope sc(stats::kMisc, s, 24.0 * rows * (double)cols);
   convert_matrix_kernel<<<dim3((rows + 255) / 256, cols), 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
   return cudaGetLastError();
 }
 
 cudaError_t convert_vec_64_to_32(const double2* src, float2* dst, int n, double scale, cudaStream_t s) {
+  stats::count(stats::kMisc);
   convert_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n, scale);
   return cudaGetLastError();
 }
 
 cudaError_t accumulate_vec_32_to_64(double2* x, const float2* d, int n, double scale, cudaStream_t s) {
+  stats::count(stats::kMisc);
   accumulate_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(x, d, n, scale);
   return cudaGetLastError();
 }
@@ -292,6 +298,7 @@ wmom_status run_sweep(const SweepArgs& a) {
           // initial solve in FP32
           SWEEP_TRY(convert_vec_64_to_32(v64.as<double2>(), d32.as<float2>(), n, 1.0, s));
           SWEEP_TRY(lu_solve_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), d32.as<float2>(), n, 1, a.ws, s));
+          stats::count(stats::kMisc);
           widen_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(d32.as<float2>(), x64.as<double2>(), n);
           SWEEP_TRY(cudaGetLastError());
           double prev = HUGE_VAL;
@@ -330,6 +337,7 @@ wmom_status run_sweep(const SweepArgs& a) {
             const double scale = rn > 0 ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
             SWEEP_TRY(convert_vec_64_to_32(r64.as<double2>(), d32.as<float2>(), n, scale, s));
             SWEEP_TRY(lu_solve_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), d32.as<float2>(), n, 1, a.ws, s));
+            stats::count(stats::kMisc);
             sumsq_f32_kernel<<<1, 1024, 0, s>>>(d32.as<float2>(), n, 1.0 / scale, &sc.as<Scalars>()->dnorm2);
             SWEEP_TRY(sumsq_fp64(x64.as<double2>(), n, &sc.as<Scalars>()->xnorm2, s));
             SWEEP_TRY(accumulate_vec_32_to_64(x64.as<double2>(), d32.as<float2>(), n, 1.0 / scale, s));

@@ -59,6 +59,43 @@ struct SrcHalf {
   int nl, nr;        // node numbers of the source segment
 };
 
+// Unique observation point of the pair-tiled fill: the midpoint of one observation
+// segment and u = r_hi - r_m (r_hi = the segment node with the larger number);
+// every test half-vector l_m of the reference is exactly +u or -u.
+struct ObsInst {
+  double rm[3];
+  double u[3];
+  int ml, mr, on_ground, pad;
+};
+
+// Unique source half-segment (start node, end node, segment): start, unit vector,
+// length, radius, the two Gauss abscissae and both ramps evaluated at them.
+struct SrcInst {
+  double rs[3];
+  double dc[3];
+  double dl, an;
+  double s[2];
+  double w_up[2];  // s / dl        (rising ramp of S_n+)
+  double w_dn[2];  // (dl - s) / dl (falling ramp of S_n-)
+  int nl, nr;
+};
+
+// Basis-function tiles of the pair-tiled fill: for each tile of kPairTile test
+// (source) functions, the list of distinct observation (source) instances its
+// halves use, and for every half its index in that list.
+constexpr int kPairTile = 32;
+struct PairTiles {
+  bool ok = false;
+  int tile = kPairTile;
+  int n_tiles = 0;
+  int max_o = 0, max_q = 0;
+  std::vector<ObsInst> obs;
+  std::vector<SrcInst> src;
+  std::vector<int> rt_off, rt_ids, ct_off, ct_ids;
+  std::vector<int> row_local;  // 2*npls: local obs index, bit 30 set when l_m = -u
+  std::vector<int> col_local;  // 2*npls: local source index
+};
+
 // ------------------------------------------------------------------ plan ----
 struct Plan {
   int device = 0;
@@ -68,10 +105,18 @@ struct Plan {
   std::vector<SrcHalf> h_src;  // 2*npls
   ObsHalf* d_obs = nullptr;
   SrcHalf* d_src = nullptr;
+  // pair-tiled fill (free space)
+  PairTiles pt;
+  ObsInst* d_oi = nullptr;
+  SrcInst* d_si = nullptr;
+  int* d_tiles = nullptr;  // rt_off | rt_ids | ct_off | ct_ids | row_local | col_local
+  int off_rt_ids = 0, off_ct_off = 0, off_ct_ids = 0, off_row_local = 0, off_col_local = 0;
 };
 
 int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, const float* rad,
                       const int* ipc, const int* ips, const int* ise);
+void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float* z, const float* rad,
+                           const int* ipc, const int* ips, const int* ise);
 
 double ka_from_mhz(float f);
 

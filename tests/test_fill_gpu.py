@@ -69,3 +69,32 @@ def test_fill_rejects_bad_arguments(cuda, wmom):
     with pytest.raises(wmom.WmomError):
         plan.fill_device(np.array([1.0]), z.data_ptr(), 30, 31 * 31)
     plan.close()
+
+
+@pytest.mark.parametrize("geo", ["dipole", "grid", "random", "junctions"])
+def test_pair_tiled_fill_equals_per_entry_fill(cuda, wmom, geo):
+    # the pair-tiled kernel evaluates each distinct (observation, source) pair once and
+    # assembles entries from them; it must reproduce the per-entry kernel exactly
+    g = wmom.geometry
+    text = {"dipole": g.dipole(1.0, 1e-3, 200), "grid": g.grid(6, 1.0, 1.0, 5e-3, None, 3),
+            "random": g.random_wires(500, seed=2),
+            "junctions": str(np.load(os.path.join(GOLDEN, "topology_mixed_junctions.npz"))["geo"])}[geo]
+    topo = wmom.Topology(text)
+    freqs = [0.01, 2.0, 30.0]
+    plan = wmom.Plan(topo)
+    assert plan.fill_variant == "pair"
+    zp = plan.fill(freqs).cpu().numpy()
+    os.environ["WMOM_FILL_ENTRY"] = "1"
+    try:
+        ze = plan.fill(freqs).cpu().numpy()
+    finally:
+        del os.environ["WMOM_FILL_ENTRY"]
+    plan.close()
+    assert np.array_equal(zp, ze)
+
+
+def test_ground_plane_uses_per_entry_fill(cuda, wmom):
+    d = np.load(os.path.join(GOLDEN, "topology_bent_ground.npz"))
+    plan = wmom.Plan(wmom.Topology(str(d["geo"]), ienv=2))
+    assert plan.fill_variant == "entry"
+    plan.close()
