@@ -112,6 +112,21 @@ wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* i
 wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const int* ipiv_dev,
                         void* b_dev, long long ldb, void* stream);
 
+/* FP64 LU that allocates no device memory.  No counterpart in the reference (which
+ * allocates per call): for callers that cannot call cudaMalloc -- applications that
+ * hand the library device buffers from their own pool and forbid other allocations,
+ * or serving processes that must not pay cudaMalloc's device-wide synchronisation
+ * once running.  Same arguments and results as wmom_zgetrf; the factorisation's
+ * scratch lives in a fixed 576 KiB __device__ array inside the library, held by every
+ * GPU that loads the library until exit.  n above WMOM_NOALLOC_MAX_N returns
+ * WMOM_ERR_ARG.  The first call on a device looks up the array's device address
+ * (once per device); make that first call before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be serialised
+ * by the caller. */
+#define WMOM_NOALLOC_MAX_N 20480
+wmom_status wmom_zgetrf_noalloc(int n, void* a_dev, long long lda, int* ipiv_dev, int* info,
+                                void* stream);
+
 /* Host-buffer drop-in for LAPACKE_zgetrf + LAPACKE_zgetrs with one right-hand
  * side: z (n*n, overwritten by the factors), v (n), i_out (n), ipiv (n, 1-based). */
 wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, int* ipiv,
