@@ -110,10 +110,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def workload(n):
+WORKLOADS = {
+    "sweep": "random-wire sweep, N={n}, {nf} frequencies 10 kHz-10 MHz",
+    "precision": "20x20 m wire grid (1 m pitch, a = 5 mm), N={n}, {nf} frequencies 10 kHz-10 MHz",
+    "batching": "20x20 m wire grid, N={n}, {nf} frequencies 1 kHz-30 MHz",
+}
+
+
+def workload(n, kind="sweep", nfreq=None):
     w = importlib.import_module("praca-magisterska_gb300")
-    topo = w.Topology(w.geometry.random_wires(n, seed=SEED))
-    freqs = w.geometry.sweep_freqs()
+    if kind == "sweep":
+        topo = w.Topology(w.geometry.random_wires(n, seed=SEED))
+        freqs = w.geometry.sweep_freqs()
+    elif kind == "precision":
+        topo = w.Topology(w.geometry.precision_grid(n))
+        freqs = w.geometry.sweep_freqs()
+    elif kind == "batching":
+        topo = w.Topology(w.geometry.precision_grid(n))
+        freqs = w.geometry.log_freqs(0.001, 30.0, 256)
+    else:
+        raise ValueError(kind)
+    if nfreq and nfreq < len(freqs):
+        # evenly spaced subset of the sweep (small cases for the profiler)
+        import numpy as np
+        freqs = freqs[np.unique(np.linspace(0, len(freqs) - 1, nfreq).round().astype(int))]
     ngap = n // 2
     return w, topo, freqs, ngap
 
@@ -132,7 +152,7 @@ def run_reference(args):
         return
     from oracle import build as ob
     ob.build_port()
-    w, topo, freqs, ngap = workload(args.n)
+    w, topo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
     k = 0
@@ -150,7 +170,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": f"random-wire sweep, N={topo.npls}, 12 frequencies 10 kHz-10 MHz",
+            "config": {"workload": WORKLOADS[args.workload].format(n=topo.npls, nf=len(freqs)),
                        "unknowns": topo.npls, "frequencies": len(freqs), "seed": SEED},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -165,7 +185,7 @@ def run_wmom(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    w, topo, freqs, ngap = workload(args.n)
+    w, topo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
     n = topo.npls
     nf = len(freqs)
     plan = w.Plan(topo)
@@ -189,8 +209,8 @@ def run_wmom(args):
     torch.cuda.synchronize()
 
     # timed region: K steps of the mixed + refinement sweep, device-resident geometry
+    # timed region: K steps, device-resident geometry, nothing instrumented
     w.stats_reset()
-    w.stats_enable(True)
     reports = []
     step_ms = []
     with ClockSampler(local) as clk:
@@ -207,11 +227,22 @@ def run_wmom(args):
         e1.record()
         torch.cuda.synchronize()
         barrier()
-    w.stats_enable(False)
-    st = w.stats_read()
+    launches = w.stats_read()
     clocks = clk.summary()
     ms = max_over_ranks(e0.elapsed_time(e1))
     value = ws * nf * args.steps / (ms / 1e3)
+
+    # instrumented pass of one step: every library launch bracketed by CUDA events on
+    # its stream (factorisations launched directly, not as a replayed graph, so each
+    # kernel is timed); the roofline below comes from these per-launch times
+    os.environ["WMOM_NO_GRAPHS"] = "1"
+    w.stats_reset()
+    w.stats_enable(True)
+    plan.solve(freqs, ngap, mode=w.MODE_MIXED, currents=False)
+    torch.cuda.synchronize()
+    w.stats_enable(False)
+    st = w.stats_read()
+    del os.environ["WMOM_NO_GRAPHS"]
 
     # end to end through the C ABI: geometry upload + solves + currents to host
     e2e_steps = max(1, min(args.steps, 3))
@@ -241,8 +272,9 @@ def run_wmom(args):
     idx = [int(np.argmin(np.abs(freqs - f))) for f in fsub]
     rel = [float(np.linalg.norm(cur[i] - cur64[j]) / np.linalg.norm(cur64[j])) for j, i in enumerate(idx)]
 
-    # roofline of the dominant kernel class (device time inside the timed region)
+    # roofline of the dominant kernel class (per-launch device time from the instrumented step)
     peaks, peak_src = _peaks()
+    fp64_peak = w.probe_fp64_tflops()
     dom = max(st, key=lambda c: st[c]["ms"])
     d = st[dom]
     avg_ms = d["ms"] / max(d["timed"], 1)
@@ -257,9 +289,10 @@ def run_wmom(args):
                 "peak_source": peak_src}
     else:
         achieved = work_per_launch / (avg_ms / 1e3) / 1e12
-        roof = {"kernel": {"fill": "fill_entry_kernel", "panel": "panel_kernel"}.get(dom, dom), "bound": "fp64",
-                "unit": "TFLOP/s", "peak": args.fp64_peak,
-                "peak_source": "FP64 FMA pipe, measured (profiles/fp64_pipe_probe.md)"}
+        roof = {"kernel": {"fill": "fill_pair_kernel", "panel": "panel_kernel"}.get(dom, dom), "bound": "fp64",
+                "unit": "TFLOP/s", "peak": fp64_peak,
+                "peak_source": "FP64 FMA pipe, measured in this run by wmom_probe_fp64_tflops "
+                               "(MEASURED_PEAKS.json has no FP64 figure)"}
     roof.update({"achieved": achieved, "frac": achieved / roof["peak"], "traffic": None,
                  "avg_launch_ms": avg_ms, "launches": d["timed"],
                  "share_of_device_time": d["ms"] / max(sum(v["ms"] for v in st.values()), 1e-9)})
@@ -268,20 +301,22 @@ def run_wmom(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 fill/residual, c64 tensor-core LU", "data": "synthetic (seeded random wires)",
-        "config": {"workload": f"random-wire sweep, N={n}, 12 frequencies 10 kHz-10 MHz, mixed+refine",
+        "config": {"workload": WORKLOADS[args.workload].format(n=n, nf=nf) + ", mixed+refine",
                    "unknowns": n, "frequencies": nf, "seed": SEED, "ngap": ngap, "refine_tol": 1e-12,
                    "l2": "inputs larger than L2 (each Z is %.2f GB)" % (16 * n * n / 1e9)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(sum(v["launches"] for v in st.values())),
+        "gpu_launches": int(sum(v["launches"] for v in launches.values())),
         "roofline": roof,
         "fp64_path": {"value": fp64_value, "unit": UNIT, "frequencies": len(fsub),
                       "speedup_mixed_over_fp64": value / ws / fp64_value},
         "accuracy": {"max_rel_err_mixed_vs_fp64": max(rel),
                      "max_rel_residual": max(r["rel_residual"] for r in reports),
                      "fallbacks": sum(r["fell_back"] for r in reports),
+                     "krylov_refined": sum(1 for r in reports if r.get("krylov_steps", 0) > 0),
+                     "max_krylov_steps": max(r.get("krylov_steps", 0) for r in reports),
                      "max_refinement_steps": max(r["iterations"] for r in reports)},
         "latency_ms": {"p50_sweep": statistics.median(step_ms), "p99_sweep": sorted(step_ms)[-1]},
-        "kernel_ms": {k: round(v["ms"], 3) for k, v in st.items()},
+        "kernel_ms_one_instrumented_step": {k: round(v["ms"], 3) for k, v in st.items()},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -306,6 +341,57 @@ def run_wmom(args):
         dist.destroy_process_group()
 
 
+def run_serving(args):
+    """Serving configuration: Poisson request stream over a pool of seeded random-wire
+    geometries (N uniform in [nmin, nmax]), 1-16 frequencies per request drawn
+    log-uniformly from 64 values in 1 kHz - 30 MHz, 30% of the requests repeat an
+    earlier (geometry, frequencies) with a new gap/amplitude (resident factors).
+    Reports p50/p99 latency, throughput and goodput for each offered rate."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    w = importlib.import_module("praca-magisterska_gb300")
+    serve = importlib.import_module("praca-magisterska_gb300.serve")
+    rng = np.random.default_rng(SEED)
+    pool = [w.geometry.random_wires(int(rng.integers(args.serve_nmin, args.serve_nmax + 1)), seed=SEED + i)
+            for i in range(args.serve_geometries)]
+    grid = w.geometry.log_freqs(0.001, 30.0, 64)
+    results = []
+    for rate in args.serve_rates:
+        warm = serve.Server(workers=1)  # warm-up: CUDA context, kernels, batch-width tuner
+        warm.submit(serve.Request(pool[0], grid[:2], 1, currents=False)).result()
+        warm.close()
+        srv = serve.Server(workers=2)
+        t_end = time.perf_counter() + args.serve_seconds
+        history, futs = [], []
+        t = time.perf_counter()
+        while t < t_end:
+            if history and rng.random() < 0.3:
+                gi, fr = history[int(rng.integers(len(history)))]
+            else:
+                gi = int(rng.integers(len(pool)))
+                fr = np.sort(rng.choice(grid, size=int(rng.integers(1, 17)), replace=False))
+                history.append((gi, fr))
+            ngap = int(rng.integers(1, 200))
+            futs.append(srv.submit(serve.Request(pool[gi], fr, ngap, float(rng.uniform(0.5, 2.0)), currents=False)))
+            t += rng.exponential(1.0 / rate)
+            time.sleep(max(0.0, t - time.perf_counter()))
+        for f in futs:
+            f.result()
+        st = srv.stats()
+        srv.close()
+        st.update(offered_req_per_s=rate, submitted=len(futs))
+        results.append(st)
+    line = {"metric": "serving: p50/p99 latency and freq-solves/s under a Poisson request stream",
+            "unit": "freq-solves/s", "value": max(r["solves_per_s"] for r in results), "higher_is_better": True,
+            "n_gpus": 1, "data": "synthetic (seeded random wires)",
+            "config": {"workload": f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}], 1-16 "
+                                   "frequencies in 1 kHz-30 MHz, 30% repeat excitations",
+                       "geometries": args.serve_geometries, "seconds_per_rate": args.serve_seconds},
+            "rates": results}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -313,13 +399,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wmom", choices=["wmom", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS) + ["serving"])
     ap.add_argument("--fp64-freqs", type=int, default=2)
-    ap.add_argument("--fp64-peak", type=float, default=1.2, help="FP64 pipe TFLOP/s (measured)")
+    ap.add_argument("--nfreq", type=int, default=None,
+                    help="use an evenly spaced subset of the workload's frequencies (profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[2.0, 5.0, 10.0])
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-nmin", type=int, default=512)
+    ap.add_argument("--serve-nmax", type=int, default=6144)
+    ap.add_argument("--serve-geometries", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "serving":
+        run_serving(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_wmom(args)

@@ -153,7 +153,15 @@ typedef struct wmom_report {
   int fell_back;        /* 1 if the FP64 LU was used after refinement stalled */
   int info;             /* LAPACK-style info of the factorisation that produced I */
   int status;           /* wmom_status of this frequency */
+  int krylov_steps;     /* GMRES steps of the Krylov refinement (0 when plain refinement
+                           converged or for WMOM_MODE_FP64) */
 } wmom_report;
+
+/* Lumped series loads for the sweeps of this plan: Z[k-1, k-1] += r_ohm + j*2*pi*f*l_uh
+ * with f in MHz (the reference's addloads block, REF/Wire_MoM.cu:346-363, where the
+ * indices were hard-wired to one geometry).  idx is 1-based; nloads = 0 clears. */
+wmom_status wmom_plan_set_loads(wmom_plan plan, int nloads, const int* idx, const double* r_ohm,
+                                const double* l_uh);
 
 /* Delta-gap excitation: V = 0 except V[ngap-1] = ampl*(cos + j sin)(pi*phas/180). */
 wmom_status wmom_excitation(int npls, int ngap, float ampl, float phas_deg, double* v);
@@ -167,8 +175,30 @@ wmom_status wmom_solve_sweep(wmom_plan plan, const float* freq_mhz, int nfreq, i
                              float ampl, float phas_deg, int mode, double tol, double* currents,
                              double* zin, wmom_report* reports, void* stream);
 
+/* --------------------------------------------------- resident factors ---- */
+/* Fills and factors one plan's matrices for nfreq frequencies and keeps Z (FP64) and
+ * its factors resident on the device, so that new excitations of the same (geometry,
+ * frequency) -- another gap, amplitude or phase -- only run the solves.  The
+ * reference refills and refactors for every run (REF/Wire_MoM.cu:335-400).  Device
+ * memory: nfreq * (16 + 8) * npls^2 bytes (mixed) or nfreq * 32 * npls^2 (FP64). */
+typedef struct wmom_factors_s* wmom_factors;
+
+wmom_status wmom_factor(wmom_plan plan, const float* freq_mhz, int nfreq, int mode, wmom_factors* out,
+                        void* stream);
+/* Solves frequencies [first, first+count) of the set for one excitation; the result
+ * arrays are indexed from 0 (= frequency `first`). */
+wmom_status wmom_factors_solve(wmom_factors f, int first, int count, int ngap, float ampl, float phas_deg,
+                               double tol, double* currents, double* zin, wmom_report* reports, void* stream);
+long long wmom_factors_device_bytes(wmom_factors f);
+wmom_status wmom_factors_destroy(wmom_factors f);
+
 /* Human-readable name of a status code. */
 const char* wmom_status_string(wmom_status s);
+
+/* The CUDA call that last failed on the calling thread and CUDA's message for it
+ * ("" if none); valid until that thread's next failing call.  No reference
+ * counterpart (the reference printed CUDA errors and exited). */
+const char* wmom_last_error(void);
 
 /* ------------------------------------------------------- instrumentation ---- */
 /* Launch counters per kernel class are always kept.  With timing enabled every
@@ -183,6 +213,18 @@ const char* wmom_status_string(wmom_status s);
 void wmom_stats_enable(int on);
 void wmom_stats_reset(void);
 int wmom_stats_read(double* ms, long long* launches, long long* timed, double* work, int n);
+
+/* Measures this device's FP64 fused multiply-add throughput (TFLOP/s, 2 flop per
+ * FMA) with a short bounded kernel of independent FMA chains, best of a few launch
+ * shapes.  It is the denominator of the FP64-bound rooflines (fill, panel, SIMT
+ * GEMM).  No reference counterpart. */
+wmom_status wmom_probe_fp64_tflops(double* tflops);
+
+/* Diagnostic: for n device doubles x[i] writes d_out[4i..4i+3] = the fill's
+ * table-driven (sin, cos)(x[i]) followed by CUDA's sincos() of the same argument,
+ * so that tests can bound the difference.  Synchronises `stream`.  No reference
+ * counterpart. */
+wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -40,9 +40,11 @@ NWMAX = 10000
 
 
 class WmomError(RuntimeError):
-    def __init__(self, status, what=""):
+    def __init__(self, status, what="", detail=""):
         self.status = status
-        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)} (status {status})")
+        self.detail = detail
+        msg = f"{what}: {STATUS_NAMES.get(status, status)} (status {status})"
+        super().__init__(msg + (f" [{detail}]" if detail else ""))
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -60,7 +62,8 @@ class _Topology(ctypes.Structure):
 
 class _Report(ctypes.Structure):
     _fields_ = [("rel_residual", ctypes.c_double), ("iterations", ctypes.c_int),
-                ("fell_back", ctypes.c_int), ("info", ctypes.c_int), ("status", ctypes.c_int)]
+                ("fell_back", ctypes.c_int), ("info", ctypes.c_int), ("status", ctypes.c_int),
+                ("krylov_steps", ctypes.c_int)]
 
 
 def _sig(name, res, args):
@@ -81,6 +84,7 @@ _plan_destroy = _sig("wmom_plan_destroy", ctypes.c_int, [_vp])
 _plan_npls = _sig("wmom_plan_npls", ctypes.c_int, [_vp])
 _plan_upload_bytes = _sig("wmom_plan_upload_bytes", ctypes.c_longlong, [_vp])
 _plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
+_plan_set_loads = _sig("wmom_plan_set_loads", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
 _zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
 _zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
@@ -91,10 +95,20 @@ _solve_sweep = _sig("wmom_solve_sweep", ctypes.c_int,
                     [_vp, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
                      ctypes.c_double, _dp, _dp, ctypes.POINTER(_Report), _vp])
 _status_string = _sig("wmom_status_string", ctypes.c_char_p, [ctypes.c_int])
+_last_error = _sig("wmom_last_error", ctypes.c_char_p, [])
+_factor = _sig("wmom_factor", ctypes.c_int, [_vp, _fp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp), _vp])
+_factors_solve = _sig("wmom_factors_solve", ctypes.c_int,
+                      [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_double,
+                       _dp, _dp, ctypes.POINTER(_Report), _vp])
+_factors_bytes = _sig("wmom_factors_device_bytes", ctypes.c_longlong, [_vp])
+_factors_destroy = _sig("wmom_factors_destroy", ctypes.c_int, [_vp])
 _stats_enable = _sig("wmom_stats_enable", None, [ctypes.c_int])
 _stats_reset = _sig("wmom_stats_reset", None, [])
 _stats_read = _sig("wmom_stats_read", ctypes.c_int,
                    [_dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _dp, ctypes.c_int])
+
+_probe_fp64 = _sig("wmom_probe_fp64_tflops", ctypes.c_int, [_dp])
+_diag_sincos = _sig("wmom_diag_sincos", ctypes.c_int, [_vp, ctypes.c_longlong, _vp, _vp])
 
 STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc"]
 
@@ -119,9 +133,28 @@ def stats_read():
     return {c: dict(ms=ms[i], launches=la[i], timed=ti[i], work=wk[i]) for i, c in enumerate(STAT_CLASSES)}
 
 
+def probe_fp64_tflops():
+    """FP64 FMA throughput of the current device in TFLOP/s (short bounded kernel)."""
+    v = ctypes.c_double(0.0)
+    _check(_probe_fp64(ctypes.byref(v)), "wmom_probe_fp64_tflops")
+    return v.value
+
+
+def diag_sincos(x):
+    """(sin, cos, sin_ref, cos_ref) of a CUDA float64 tensor: the fill's table-driven
+    sin/cos and CUDA's sincos() of the same arguments."""
+    import torch
+    x = x.contiguous()
+    out = torch.empty((x.numel(), 4), dtype=torch.float64, device=x.device)
+    _check(_diag_sincos(x.data_ptr(), x.numel(), out.data_ptr(), torch.cuda.current_stream().cuda_stream),
+           "wmom_diag_sincos")
+    return out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+
+
 def _check(st, what):
     if st != WMOM_OK:
-        raise WmomError(st, what)
+        detail = _last_error().decode(errors="replace") if st == 2 else ""  # WMOM_ERR_CUDA
+        raise WmomError(st, what, detail)
 
 
 def _ptr(a, t):
@@ -225,6 +258,15 @@ class Plan:
         except Exception:
             pass
 
+    def set_loads(self, loads):
+        """Lumped series loads [(basis index 1-based, R ohm, L uH), ...] added to the
+        diagonal of Z in every sweep of this plan (empty list clears)."""
+        n = len(loads)
+        idx = np.array([l[0] for l in loads], np.int32)
+        r = np.array([l[1] for l in loads], np.float64)
+        lh = np.array([l[2] for l in loads], np.float64)
+        _check(_plan_set_loads(self._h, n, _ptr(idx, _ip), _ptr(r, _dp), _ptr(lh, _dp)), "wmom_plan_set_loads")
+
     def fill_device(self, kas, z_ptr, ldz, zstride, stream=0):
         kas = np.ascontiguousarray(kas, np.float64)
         _check(_fill(self._h, _ptr(kas, _dp), len(kas), z_ptr, ldz, zstride, stream), "wmom_fill")
@@ -255,8 +297,48 @@ class Plan:
         if st not in (WMOM_OK, 3):
             raise WmomError(st, "wmom_solve_sweep")
         reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
-                        info=r.info, status=r.status) for r in reps]
+                        info=r.info, status=r.status, krylov_steps=r.krylov_steps) for r in reps]
         return cur, zin, reports
+
+
+class Factors:
+    """Z and its LU factors for a list of frequencies of one plan, resident on the
+    device: new excitations of those (geometry, frequency) pairs only run solves."""
+
+    def __init__(self, plan, freqs_mhz, mode=MODE_MIXED, stream=0):
+        self.plan = plan  # keeps the plan alive
+        self.freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
+        self.mode = mode
+        h = _vp()
+        _check(_factor(plan._h, _ptr(self.freqs, _fp), len(self.freqs), mode, ctypes.byref(h), stream), "wmom_factor")
+        self._h = h
+        self.device_bytes = int(_factors_bytes(h))
+
+    def solve(self, ngap, ampl=1.0, phas=0.0, first=0, count=None, tol=1e-12, currents=True, stream=0):
+        count = len(self.freqs) - first if count is None else count
+        n = self.plan.npls
+        cur = np.zeros((count, n), np.complex128) if currents else None
+        zin = np.zeros(count, np.complex128)
+        reps = (_Report * count)()
+        st = _factors_solve(self._h, first, count, ngap, ampl, phas, tol,
+                            _ptr(cur.view(np.float64), _dp) if cur is not None else None,
+                            _ptr(zin.view(np.float64), _dp), reps, stream)
+        if st not in (WMOM_OK, 3):
+            raise WmomError(st, "wmom_factors_solve")
+        reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
+                        info=r.info, status=r.status, krylov_steps=r.krylov_steps) for r in reps]
+        return cur, zin, reports
+
+    def close(self):
+        if self._h:
+            _factors_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ----------------------------------------------------------------- LAPACK-ish ----

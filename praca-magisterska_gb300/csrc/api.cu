@@ -9,6 +9,8 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <set>
+#include <utility>
 #include <vector>
 
 #include "lu_common.cuh"
@@ -16,8 +18,13 @@
 #include "solve_internal.h"
 #include "wmom_internal.h"
 
+namespace {
+thread_local char g_last_error[256] = "";
+}
+
 wmom_status wmom_fail_cuda(cudaError_t e, const char* what) {
-  if (std::getenv("WMOM_VERBOSE")) std::fprintf(stderr, "wmom: %s failed: %s\n", what, cudaGetErrorString(e));
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s failed: %s", what, cudaGetErrorString(e));
+  if (std::getenv("WMOM_VERBOSE")) std::fprintf(stderr, "wmom: %s\n", g_last_error);
   if (e == cudaErrorMemoryAllocation) return WMOM_ERR_NOMEM;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
     return WMOM_ERR_UNSUPPORTED;
@@ -26,43 +33,87 @@ wmom_status wmom_fail_cuda(cudaError_t e, const char* what) {
 
 namespace wmom {
 
+cudaError_t allow_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> raised;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  if (raised.count({dev, func})) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa{};
+  e = cudaFuncGetAttributes(&fa, func);
+  if (e != cudaSuccess) return e;
+  const int cap = optin - (int)fa.sharedSizeBytes;  // static shared memory counts against it
+  if (bytes > (size_t)std::max(cap, 0)) return cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  if (e != cudaSuccess) return e;
+  raised.insert({dev, func});
+  return cudaSuccess;
+}
+
 // ---------------------------------------------------------- workspace ----
-cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max) {
+cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch) {
   *ws = LuWorkspace{};
-  const size_t stage = lu_workspace_bytes(16);
+  max_batch = std::max(max_batch, 1);
+  const size_t off = lu_stage_offset(max_batch);
+  const size_t bytes = off + lu_stage_bytes(max_batch);
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, stage);
+  cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) return e;
-  e = cudaMemset(p, 0, stage);
+  e = cudaMemset(p, 0, bytes);
   if (e != cudaSuccess) return e;
+  ws->max_batch = max_batch;
   ws->barrier = reinterpret_cast<GridBarrier*>(p);
-  ws->stage = reinterpret_cast<char*>(p) + 256;
-  e = cudaMalloc(&ws->perm, sizeof(int) * (size_t)std::max(nmax, 1));
+  ws->stage = reinterpret_cast<char*>(p) + off;
+  e = cudaMalloc(&ws->perm, sizeof(int) * (size_t)std::max(nmax, 1) * max_batch);
   if (e != cudaSuccess) return e;
   ws->perm_cap = nmax;
-  ws->rhs_bytes = sizeof(double2) * (size_t)std::max(nmax, 1) * (size_t)std::max(nrhs_max, 1);
+  ws->rhs_bytes =
+      sizeof(double2) * (size_t)std::max(nmax, 1) * (size_t)std::max(std::max(nrhs_max, 1), max_batch);
   e = cudaMalloc(&ws->rhs, ws->rhs_bytes);
-  return e;
+  if (e != cudaSuccess) return e;
+  ws->flag_cap = (std::max(nmax, 1) + 63) / 64 + 1;
+  const size_t fbytes = sizeof(int) * ((size_t)ws->flag_cap * max_batch + max_batch);
+  e = cudaMalloc(&ws->flags, fbytes);
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(ws->flags, 0, fbytes);
+  if (e != cudaSuccess) return e;
+  ws->ticket = reinterpret_cast<unsigned int*>(ws->flags + (size_t)ws->flag_cap * max_batch);
+  ws->epoch = 0;
+  e = cudaMalloc(&ws->tc_err, sizeof(int));
+  if (e != cudaSuccess) return e;
+  return cudaMemset(ws->tc_err, 0, sizeof(int));
 }
 
 void lu_workspace_destroy(LuWorkspace* ws) {
   if (ws->barrier) cudaFree(ws->barrier);
   if (ws->perm) cudaFree(ws->perm);
   if (ws->rhs) cudaFree(ws->rhs);
+  if (ws->flags) cudaFree(ws->flags);
+  if (ws->tc_buf) cudaFree(ws->tc_buf);
+  if (ws->tc_err) cudaFree(ws->tc_err);
   *ws = LuWorkspace{};
 }
 
 cudaError_t lu_workspace_reset_barrier(LuWorkspace* ws, cudaStream_t s) {
-  return cudaMemsetAsync(ws->barrier, 0, sizeof(GridBarrier), s);
+  return cudaMemsetAsync(ws->barrier, 0, sizeof(GridBarrier) * ws->max_batch, s);
 }
 
-// Returns 0 when the last factorisation finished its waits; *info = first zero pivot.
-int lu_workspace_read_status(LuWorkspace* ws, int* info, cudaStream_t s) {
-  GridBarrier h{};
-  cudaMemcpyAsync(&h, ws->barrier, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s);
+// Returns 0 when the last factorisation finished its waits; info[b] = first zero pivot.
+int lu_workspace_read_status(LuWorkspace* ws, int* info, cudaStream_t s, int batch) {
+  std::vector<GridBarrier> h(std::max(batch, 1));
+  cudaMemcpyAsync(h.data(), ws->barrier, sizeof(GridBarrier) * h.size(), cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
-  if (info) *info = h.info;
-  return h.err;
+  int err = 0;
+  for (size_t b = 0; b < h.size(); ++b) {
+    if (info) info[b] = h[b].info;
+    err |= h[b].err;
+  }
+  return err;
 }
 
 namespace {
@@ -133,6 +184,8 @@ struct wmom_plan_s {
 };
 
 extern "C" {
+
+const char* wmom_last_error(void) { return g_last_error; }
 
 const char* wmom_status_string(wmom_status s) {
   switch (s) {
@@ -251,6 +304,19 @@ wmom_status wmom_plan_destroy(wmom_plan h) {
 int wmom_plan_npls(wmom_plan h) { return h ? h->p.npls : -1; }
 
 int wmom_plan_fill_variant(wmom_plan h) { return h ? (h->p.pt.ok ? 1 : 0) : -1; }
+
+wmom_status wmom_plan_set_loads(wmom_plan h, int nloads, const int* idx, const double* r_ohm,
+                                const double* l_uh) {
+  if (!h || nloads < 0 || (nloads > 0 && (!idx || !r_ohm || !l_uh))) return WMOM_ERR_ARG;
+  for (int i = 0; i < nloads; ++i)
+    if (idx[i] < 1 || idx[i] > h->p.npls || !std::isfinite(r_ohm[i]) || !std::isfinite(l_uh[i]))
+      return WMOM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->p.load_idx.assign(idx, idx + nloads);
+  h->p.load_r.assign(r_ohm, r_ohm + nloads);
+  h->p.load_l_uh.assign(l_uh, l_uh + nloads);
+  return WMOM_OK;
+}
 
 long long wmom_plan_upload_bytes(wmom_plan h) {
   if (!h) return -1;
@@ -372,11 +438,86 @@ wmom_status wmom_solve_sweep(wmom_plan h, const float* freq_mhz, int nfreq, int 
   if (h->ws_n < h->p.npls) {
     if (h->ws_n) lu_workspace_destroy(&h->ws);
     h->ws_n = 0;
-    WMOM_CUDA_TRY(lu_workspace_create(&h->ws, h->p.npls, 1));
+    WMOM_CUDA_TRY(lu_workspace_create(&h->ws, h->p.npls, 1, kMaxLuBatch));
     h->ws_n = h->p.npls;
   }
   a.ws = &h->ws;
   return run_sweep(a);
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------- resident factors ----
+struct wmom_factors_s {
+  wmom::FactorSet fs;
+  wmom::LuWorkspace ws{};
+  wmom_plan plan = nullptr;
+  size_t bytes = 0;
+  std::mutex mu;
+};
+
+extern "C" {
+
+wmom_status wmom_factor(wmom_plan h, const float* freq_mhz, int nfreq, int mode, wmom_factors* out, void* stream) {
+  if (!out) return WMOM_ERR_ARG;
+  *out = nullptr;
+  if (!h || !freq_mhz || nfreq <= 0 || (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED)) return WMOM_ERR_ARG;
+  for (int i = 0; i < nfreq; ++i)
+    if (!(freq_mhz[i] > 0.f) || !std::isfinite(freq_mhz[i])) return WMOM_ERR_ARG;
+  const int n = h->p.npls;
+  const size_t nn = (size_t)n * n;
+  const size_t need = (size_t)nfreq * nn * (sizeof(double2) + (mode == WMOM_MODE_MIXED ? sizeof(float2) : sizeof(double2)));
+  size_t fr = 0, tot = 0;
+  WMOM_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+  if (need > fr) return WMOM_ERR_NOMEM;
+  wmom_factors_s* f = new (std::nothrow) wmom_factors_s();
+  if (!f) return WMOM_ERR_NOMEM;
+  cudaError_t e = lu_workspace_create(&f->ws, n, 1, kMaxLuBatch);
+  if (e != cudaSuccess) {
+    lu_workspace_destroy(&f->ws);
+    delete f;
+    return wmom_fail_cuda(e, "factor workspace");
+  }
+  f->plan = h;
+  f->fs.plan = &h->p;
+  f->fs.mode = mode;
+  f->fs.freq.assign(freq_mhz, freq_mhz + nfreq);
+  f->fs.ws = &f->ws;
+  f->bytes = need + (size_t)nfreq * n * sizeof(int);
+  wmom_status st;
+  {
+    std::lock_guard<std::mutex> lk(h->mu);  // the fill reads the plan's loads
+    st = factors_build(&f->fs, (cudaStream_t)stream);
+  }
+  if (st != WMOM_OK) {
+    wmom_factors_destroy(f);
+    return st;
+  }
+  *out = f;
+  return WMOM_OK;
+}
+
+wmom_status wmom_factors_solve(wmom_factors f, int first, int count, int ngap, float ampl, float phas_deg,
+                               double tol, double* currents, double* zin, wmom_report* reports, void* stream) {
+  if (!f || first < 0 || count <= 0 || first + count > (int)f->fs.freq.size() || ngap < 1 ||
+      ngap > f->fs.plan->npls)
+    return WMOM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(f->mu);
+  return factors_solve(&f->fs, first, count, ngap, ampl, phas_deg, tol > 0 ? tol : 1e-12, currents, zin, reports,
+                       (cudaStream_t)stream);
+}
+
+long long wmom_factors_device_bytes(wmom_factors f) { return f ? (long long)f->bytes : -1; }
+
+wmom_status wmom_factors_destroy(wmom_factors f) {
+  if (!f) return WMOM_ERR_ARG;
+  cudaDeviceSynchronize();
+  if (f->fs.z64) cudaFree(f->fs.z64);
+  if (f->fs.lu) cudaFree(f->fs.lu);
+  if (f->fs.ipiv) cudaFree(f->fs.ipiv);
+  lu_workspace_destroy(&f->ws);
+  delete f;
+  return WMOM_OK;
 }
 
 }  // extern "C"

@@ -18,6 +18,7 @@
 
 #include <cstdlib>
 
+#include "../../include/wmom.h"
 #include "stats.h"
 #include "wmom_internal.h"
 
@@ -37,6 +38,58 @@ struct Cx {
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// ------------------------------------------------------------------------
+// sin and cos of the phase k*R of the regular Green's function evaluations.
+// Table-driven method (Tang, "Table-driven implementation of the exponential
+// function", ACM TOMS 15(2), 1989, applied to sin/cos by angle addition):
+//   x = n*h + d,  h = pi/128,  |d| <= h/2 ~ 0.0123,
+//   sin x = S_j cos d + C_j sin d,  cos x = C_j cos d - S_j sin d,  j = n mod 256,
+// with (S_j, C_j) = (sin, cos)(j*pi/128) tabulated per block in shared memory by
+// sincospi(j/128) (an exact argument), d from a two-constant Cody-Waite reduction
+// (h_hi = double(pi)/128 exactly, h_lo = (pi - double(pi))/128), and sin d, cos d
+// from their Taylor series to d^7 and d^6 (truncation below 2e-20 relative).
+// Arguments beyond 1e6 rad take sincos() itself.
+// ------------------------------------------------------------------------
+constexpr int kSinTab = 256;
+constexpr double kInvH = 40.743665431525205957;    // 128/pi
+constexpr double kHHi = 3.141592653589793116 / 128;  // double(pi)/128, exact
+constexpr double kHLo = 1.2246467991473532e-16 / 128;  // (pi - double(pi))/128
+
+__device__ __forceinline__ void sin_table_init(double2* tab) {
+  for (int j = threadIdx.x; j < kSinTab; j += blockDim.x) {
+    double sj, cj;
+    sincospi(j / 128.0, &sj, &cj);
+    tab[j] = make_double2(sj, cj);
+  }
+}
+
+__device__ __forceinline__ void sincos_tab(double x, const double2* tab, double* s, double* c) {
+  if (!(fabs(x) < 1.0e6)) {
+    sincos(x, s, c);
+    return;
+  }
+  const double n = rint(x * kInvH);
+  double d = fma(-n, kHHi, x);
+  d = fma(-n, kHLo, d);
+  const double2 t = tab[(int)((long long)n & (kSinTab - 1))];
+  const double d2 = d * d;
+  const double sd = fma(d * d2, fma(d2, fma(d2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), d);
+  const double cd = fma(d2, fma(d2, fma(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+  *s = fma(t.x, cd, t.y * sd);
+  *c = fma(t.y, cd, -(t.x * sd));
+}
+
+// exp(-j*ka*R)/R for R^2 = r2: (cos(ka R)/R, -sin(ka R)/R), one reciprocal square
+// root instead of a square root and two divisions.
+__device__ __forceinline__ void green_reg(double r2, double ka, const double2* tab, double* gre, double* gim) {
+  const double ri = rsqrt(r2);
+  const double r = mul(r2, ri);
+  double sn, cs;
+  sincos_tab(mul(ka, r), tab, &sn, &cs);
+  *gre = mul(cs, ri);
+  *gim = -mul(sn, ri);
+}
 
 // Complete elliptic integral K, Hastings polynomial-log approximation with the
 // reference's coefficients (Zmatrix.cpp:738-747; Abramowitz & Stegun 17.3.34).
@@ -66,34 +119,64 @@ __device__ double ell_k(double bet) {
   return sub(a, mul(b, log(m1)));
 }
 
-// Regular source half: returns the ramped integral A and the plain integral P.
-__device__ void regular_half(const double rm[3], const double rs[3], const double dc[3],
-                             double dl, double an, double ka, bool falling, Cx* A, Cx* P) {
-  const double a = mul(0.5, dl);
-  const double c = mul(kGl2C, dl);
-  const double an2 = mul(an, an);
-  Cx sa = {0.0, 0.0}, sp = {0.0, 0.0};
+// Gauss sums of one regular (observation point, source half) pair, the 2-point rule
+// of the reference's cwire1_re/cwire2_re + ckmn (Zmatrix.cpp:237-339, 450-555,
+// 667-692): with g = exp(-j ka R)/R at the two abscissae s[0], s[1] and
+// ex = r_m - r_s,  up = sum s/dl g,  dn = sum (dl - s)/dl g,  pl = sum g.
+// The ramp weights come precomputed (the host's s/dl and (dl - s)/dl).  Distances
+// and weighted sums are FMA-contracted; both fill kernels call this one routine,
+// so they produce identical matrices.
+__device__ __forceinline__ void regular_sums(const double ex[3], const double dc[3], double an2, const double s[2],
+                                             const double wu[2], const double wd[2], double ka, const double2* tab,
+                                             Cx* up, Cx* dn, Cx* pl) {
+  Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
-    const double s = g == 0 ? add(a, c) : sub(a, c);
-    const double dx = sub(sub(rm[0], rs[0]), mul(s, dc[0]));
-    const double dy = sub(sub(rm[1], rs[1]), mul(s, dc[1]));
-    const double dz = sub(sub(rm[2], rs[2]), mul(s, dc[2]));
-    const double r = sqrt(add(add(add(an2, mul(dx, dx)), mul(dy, dy)), mul(dz, dz)));
-    double sn, cs;
-    sincos(mul(ka, r), &sn, &cs);
-    const double gre = __ddiv_rn(cs, r), gim = __ddiv_rn(-sn, r);
-    const double w = falling ? __ddiv_rn(sub(dl, s), dl) : __ddiv_rn(s, dl);
-    sa.re = add(sa.re, mul(w, gre));
-    sa.im = add(sa.im, mul(w, gim));
+    const double dx = fma(-s[g], dc[0], ex[0]);
+    const double dy = fma(-s[g], dc[1], ex[1]);
+    const double dz = fma(-s[g], dc[2], ex[2]);
+    double gre, gim;
+    green_reg(fma(dx, dx, fma(dy, dy, fma(dz, dz, an2))), ka, tab, &gre, &gim);
+    su.re = fma(wu[g], gre, su.re);
+    su.im = fma(wu[g], gim, su.im);
+    sd.re = fma(wd[g], gre, sd.re);
+    sd.im = fma(wd[g], gim, sd.im);
     sp.re = add(sp.re, gre);
     sp.im = add(sp.im, gim);
   }
-  const double h = mul(dl, 0.5);
-  A->re = mul(sa.re, h);
-  A->im = mul(sa.im, h);
-  P->re = mul(sp.re, h);
-  P->im = mul(sp.im, h);
+  *up = su;
+  *dn = sd;
+  *pl = sp;
+}
+
+// Abscissae and ramp weights of the 2-point rule on a source half of length dl, in
+// the host's order of operations (plan.cpp builds the same values for the tiles).
+__device__ __forceinline__ void gauss2(double dl, double s[2], double wu[2], double wd[2]) {
+  const double a = mul(0.5, dl);
+  const double c = mul(kGl2C, dl);
+  s[0] = add(a, c);
+  s[1] = sub(a, c);
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    wu[g] = __ddiv_rn(s[g], dl);
+    wd[g] = __ddiv_rn(sub(dl, s[g]), dl);
+  }
+}
+
+// One regular source half of the per-entry kernel: the ramped integral times the
+// projection t (rising ramp for S_n+, falling for S_n-) and the plain integral over
+// dl, i.e. (dl/2) sum g / dl = sum g / 2.
+__device__ void regular_half(const double rm[3], const double rs[3], const double dc[3], double dl, double an,
+                             double ka, bool falling, double t, const double2* tab, Cx* At, Cx* Pd) {
+  double s[2], wu[2], wd[2];
+  gauss2(dl, s, wu, wd);
+  const double ex[3] = {sub(rm[0], rs[0]), sub(rm[1], rs[1]), sub(rm[2], rs[2])};
+  Cx su, sd, sp;
+  regular_sums(ex, dc, mul(an, an), s, wu, wd, ka, tab, &su, &sd, &sp);
+  const double ht = mul(mul(dl, 0.5), t);
+  const Cx& sw = falling ? sd : su;
+  *At = Cx{mul(sw.re, ht), mul(sw.im, ht)};
+  *Pd = Cx{mul(0.5, sp.re), mul(0.5, sp.im)};
 }
 
 // Regularised self kernel bracket (Zmatrix.cpp:695-709) at parameter s.
@@ -167,6 +250,9 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
                                                          double2* __restrict__ Z, long long ldz,
                                                          long long zstride, int ienv,
                                                          float sgnenv) {
+  __shared__ double2 tab[kSinTab];
+  sin_table_init(tab);
+  __syncthreads();
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = blockIdx.y;
   const int k = blockIdx.z;
@@ -183,36 +269,45 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
       const SrcHalf sh = src[2 * n + sgm];
       const bool falling = sgm == 1;
       const bool same = (sh.nl == o.ml && sh.nr == o.mr) || (sh.nl == o.mr && sh.nr == o.ml);
-      Cx A, P;
-      if (same)
-        self_half(sh.dl, sh.an, ka, falling, &A, &P);
-      else
-        regular_half(o.rm, sh.rs, sh.dc, sh.dl, sh.an, ka, falling, &A, &P);
+      // At = ramped integral times the projection t, Pd = plain integral / dl
       const double t = dot3(sh.dc, o.lm);
-      av_re = add(av_re, mul(A.re, t));
-      av_im = add(av_im, mul(A.im, t));
-      Cx Ai, Pi;
+      Cx At, Pd;
+      if (same) {
+        Cx A, P;
+        self_half(sh.dl, sh.an, ka, falling, &A, &P);
+        At = Cx{mul(A.re, t), mul(A.im, t)};
+        Pd = Cx{__ddiv_rn(P.re, sh.dl), __ddiv_rn(P.im, sh.dl)};
+      } else {
+        regular_half(o.rm, sh.rs, sh.dc, sh.dl, sh.an, ka, falling, t, tab, &At, &Pd);
+      }
+      av_re = add(av_re, At.re);
+      av_im = add(av_im, At.im);
+      Cx Pid = {0.0, 0.0};
       if (ienv == 2) {
-        if (same && o.on_ground)
-          self_half(sh.dl, sh.an, ka, falling, &Ai, &Pi);
-        else
-          regular_half(o.rm, sh.rs_img, sh.dc_img, sh.dl, sh.an, ka, falling, &Ai, &Pi);
         const double ti = mul(dot3(sh.dc_img, o.lm), senv);
-        av_re = add(av_re, mul(Ai.re, ti));
-        av_im = add(av_im, mul(Ai.im, ti));
+        Cx Ait;
+        if (same && o.on_ground) {
+          Cx Ai, Pi;
+          self_half(sh.dl, sh.an, ka, falling, &Ai, &Pi);
+          Ait = Cx{mul(Ai.re, ti), mul(Ai.im, ti)};
+          Pid = Cx{__ddiv_rn(Pi.re, sh.dl), __ddiv_rn(Pi.im, sh.dl)};
+        } else {
+          regular_half(o.rm, sh.rs_img, sh.dc_img, sh.dl, sh.an, ka, falling, ti, tab, &Ait, &Pid);
+        }
+        av_re = add(av_re, Ait.re);
+        av_im = add(av_im, Ait.im);
       }
       // scalar potential: + P(S_n+)/dl - P(S_n-)/dl
-      const double pre = __ddiv_rn(P.re, sh.dl), pim = __ddiv_rn(P.im, sh.dl);
       if (!falling) {
-        sv_re = add(sv_re, pre);
-        sv_im = add(sv_im, pim);
+        sv_re = add(sv_re, Pd.re);
+        sv_im = add(sv_im, Pd.im);
       } else {
-        sv_re = sub(sv_re, pre);
-        sv_im = sub(sv_im, pim);
+        sv_re = sub(sv_re, Pd.re);
+        sv_im = sub(sv_im, Pd.im);
       }
       if (ienv == 2) {
-        const double f = __ddiv_rn(senv, sh.dl);
-        const double qre = mul(Pi.re, f), qim = mul(Pi.im, f);
+        // image: sgnenv * P_img / dl
+        const double qre = mul(Pid.re, senv), qim = mul(Pid.im, senv);
         if (!falling) {
           sv_re = add(sv_re, qre);
           sv_im = add(sv_im, qim);
@@ -306,7 +401,9 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
                                                         const FreqParams* __restrict__ fp,
                                                         double2* __restrict__ Z, long long ldz,
                                                         long long zstride) {
-  extern __shared__ __align__(16) unsigned char sm[];
+  extern __shared__ __align__(16) unsigned char sm_all[];
+  double2* tab = reinterpret_cast<double2*>(sm_all);
+  unsigned char* sm = sm_all + kSinTab * sizeof(double2);
   ObsInst* so = reinterpret_cast<ObsInst*>(sm);
   SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
   const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
@@ -324,6 +421,7 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
   const int q0 = ct_off[tc], nQ = ct_off[tc + 1] - q0;
   for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[rt_ids[o0 + i]];
   for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[ct_ids[q0 + i]];
+  sin_table_init(tab);
   __syncthreads();
   const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
 
@@ -333,39 +431,23 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
     const ObsInst& O = so[o];
     const SrcInst& S = sq[q];
     const bool same = (S.nl == O.ml && S.nr == O.mr) || (S.nl == O.mr && S.nr == O.ml);
-    Cx Au, Ad, P;
-    if (!same) {
-      const double an2 = mul(S.an, S.an);
-      Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const double s = S.s[g];
-        const double dx = sub(sub(O.rm[0], S.rs[0]), mul(s, S.dc[0]));
-        const double dy = sub(sub(O.rm[1], S.rs[1]), mul(s, S.dc[1]));
-        const double dz = sub(sub(O.rm[2], S.rs[2]), mul(s, S.dc[2]));
-        const double r = sqrt(add(add(add(an2, mul(dx, dx)), mul(dy, dy)), mul(dz, dz)));
-        double sn, cs;
-        sincos(mul(ka, r), &sn, &cs);
-        const double gre = __ddiv_rn(cs, r), gim = __ddiv_rn(-sn, r);
-        su.re = add(su.re, mul(S.w_up[g], gre));
-        su.im = add(su.im, mul(S.w_up[g], gim));
-        sd.re = add(sd.re, mul(S.w_dn[g], gre));
-        sd.im = add(sd.im, mul(S.w_dn[g], gim));
-        sp.re = add(sp.re, gre);
-        sp.im = add(sp.im, gim);
-      }
-      const double h = mul(S.dl, 0.5);
-      Au = Cx{mul(su.re, h), mul(su.im, h)};
-      Ad = Cx{mul(sd.re, h), mul(sd.im, h)};
-      P = Cx{mul(sp.re, h), mul(sp.im, h)};
-    } else {
-      self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
-    }
     const double t = dot3(S.dc, O.u);
     PairVal v;
-    v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
-    v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
-    v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
+    if (!same) {
+      const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
+      Cx su, sd, sp;
+      regular_sums(ex, S.dc, mul(S.an, S.an), S.s, S.w_up, S.w_dn, ka, tab, &su, &sd, &sp);
+      const double ht = mul(mul(S.dl, 0.5), t);
+      v.wu = make_double2(mul(su.re, ht), mul(su.im, ht));
+      v.wd = make_double2(mul(sd.re, ht), mul(sd.im, ht));
+      v.ph = make_double2(mul(0.5, sp.re), mul(0.5, sp.im));
+    } else {
+      Cx Au, Ad, P;
+      self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
+      v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
+      v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
+      v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
+    }
     pt[p] = v;
   }
   __syncthreads();
@@ -407,9 +489,26 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
   }
 }
 
+// Diagnostic: the table-driven sin/cos next to CUDA's sincos() on the same inputs.
+__global__ void sincos_diag_kernel(const double* __restrict__ x, long long n, double* __restrict__ out) {
+  __shared__ double2 tab[kSinTab];
+  sin_table_init(tab);
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double s, c, sr, cr;
+    sincos_tab(x[i], tab, &s, &c);
+    sincos(x[i], &sr, &cr);
+    out[4 * i] = s;
+    out[4 * i + 1] = c;
+    out[4 * i + 2] = sr;
+    out[4 * i + 3] = cr;
+  }
+}
+
 size_t pair_smem_bytes(const PairTiles& t) {
   const size_t head = ((size_t)t.max_o * sizeof(ObsInst) + (size_t)t.max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
-  return head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
+  return kSinTab * sizeof(double2) + head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
 }
 
 }  // namespace
@@ -420,7 +519,7 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
   const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
   if (p.pt.ok && p.d_tiles && !(force_entry && force_entry[0] == '1')) {
     const size_t smem = pair_smem_bytes(p.pt);
-    cudaError_t e = cudaFuncSetAttribute(fill_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem((const void*)fill_pair_kernel, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(p.pt.n_tiles, p.pt.n_tiles, nk);
     stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
@@ -440,3 +539,13 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
 }
 
 }  // namespace wmom
+
+extern "C" wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void* stream) {
+  if (n < 0 || (n > 0 && (!d_x || !d_out))) return WMOM_ERR_ARG;
+  if (n == 0) return WMOM_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long blocks = (n + 255) / 256;
+  wmom::sincos_diag_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(d_x, n, d_out);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return WMOM_ERR_CUDA;
+  return WMOM_OK;
+}

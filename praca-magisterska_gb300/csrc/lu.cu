@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <mutex>
 #include <vector>
 
@@ -46,22 +47,33 @@ template <typename C, int NB, int NT>
 __global__ void __launch_bounds__(NT) panel_kernel(C* __restrict__ A, long long lda, int n, int j0,
                                                    int nb, int rpc, int* __restrict__ ipiv,
                                                    PanelStage<C, NB>* __restrict__ st,
-                                                   GridBarrier* __restrict__ gb) {
+                                                   GridBarrier* __restrict__ gb, unsigned int bar_base,
+                                                   long long astride) {
   using R = decltype(C{}.x);
+  // FP32 panels gather every block's candidate into shared memory after the barrier
+  // (one parallel round trip); FP64 panels read the winner's row only
+  constexpr bool kGather = sizeof(R) == 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);  // column-major rpc x nb
   C* prow = tile + (size_t)rpc * NB;          // pivot row, nb entries
+  C* cdat = prow + NB;                        // gather: candidate rows, P x NB
+  C* dgr = cdat + (kGather ? (size_t)gridDim.x * NB : 0);  // gather: diagonal row
+  R* cval = reinterpret_cast<R*>(dgr + NB);                // gather: candidate values
+  int* crow = reinterpret_cast<int*>(cval + (kGather ? gridDim.x : 0));
   __shared__ R red_v[NT / 32];
   __shared__ int red_r[NT / 32];
   __shared__ int red_b[NT / 32];
-  __shared__ unsigned int gen_local;
 
+  // batch: blockIdx.y selects the matrix, its pivots, staging and barrier
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
+  st += blockIdx.y;
+  gb += blockIdx.y;
   const int tid = threadIdx.x;
   const int b = blockIdx.x;
   const int P = gridDim.x;
   const int base = j0 + b * rpc;
   const int cnt = max(0, min(rpc, n - base));
-  if (tid == 0) gen_local = ld_acquire_u32(&gb->gen);
 
   for (int c = 0; c < nb; ++c)
     for (int r = tid; r < cnt; r += NT) tile[(size_t)c * rpc + r] = A[(size_t)(j0 + c) * lda + base + r];
@@ -128,8 +140,62 @@ __global__ void __launch_bounds__(NT) panel_kernel(C* __restrict__ A, long long 
       for (int c = tid; c < nb; c += NT) st->diag_data[par][c] = tile[(size_t)c * rpc + (gj - base)];
     __syncthreads();  // red_* reuse below
     // 3. one grid-wide barrier per column
-    if (!grid_barrier(gb, (unsigned)P, &gen_local)) return;
+    if (!grid_barrier_count(gb, bar_base + (unsigned)P * (unsigned)(j + 1))) return;
     // 4. winner over all blocks (deterministic: largest value, then smallest row)
+    if constexpr (kGather) {
+      for (int q = tid; q < P; q += NT) {
+        cval[q] = __ldcg(&st->cand_val[par][q]);
+        crow[q] = __ldcg(&st->cand_row[par][q]);
+      }
+      for (int c = tid; c < nb; c += NT) dgr[c] = __ldcg(&st->diag_data[par][c]);
+      // the P candidate rows are one contiguous P x NB block of the staging area;
+      // kGatherILP independent loads per thread are in flight before any is stored
+      // (entries c >= nb of a narrow last panel are copied but never used)
+      {
+        constexpr int kGatherILP = 8;
+        const C* src = &st->cand_data[par][0][0];
+        const int tot = P * NB;
+        for (int i0 = tid; i0 < tot; i0 += NT * kGatherILP) {
+          C v[kGatherILP];
+#pragma unroll
+          for (int u = 0; u < kGatherILP; ++u)
+            if (i0 + u * NT < tot) v[u] = __ldcg(src + i0 + u * NT);
+#pragma unroll
+          for (int u = 0; u < kGatherILP; ++u)
+            if (i0 + u * NT < tot) cdat[i0 + u * NT] = v[u];
+        }
+      }
+      __syncthreads();
+      if (tid < 32) {
+        best = R(-1);
+        brow = INT_MAX;
+        int bblk = -1;
+        for (int q = tid; q < P; q += 32) {
+          if (cval[q] > best || (cval[q] == best && crow[q] < brow)) {
+            best = cval[q];
+            brow = crow[q];
+            bblk = q;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+          const int ob = __shfl_xor_sync(0xffffffffu, bblk, o);
+          if (ov > best || (ov == best && orow < brow)) {
+            best = ov;
+            brow = orow;
+            bblk = ob;
+          }
+        }
+        if (tid == 0) {
+          red_r[0] = brow;
+          red_b[0] = bblk;
+        }
+      }
+      __syncthreads();
+    }
+    if constexpr (!kGather) {
     best = R(-1);
     brow = INT_MAX;
     int bblk = -1;
@@ -181,26 +247,35 @@ __global__ void __launch_bounds__(NT) panel_kernel(C* __restrict__ A, long long 
       }
     }
     __syncthreads();
+    }  // FP64 candidate scan
     const int prw = red_r[0];
     const int pblk = red_b[0];
     if (b == 0 && tid == 0) ipiv[gj] = prw + 1;
     // 5. pivot row into shared memory; 6. interchange rows gj and prw
     for (int c = tid; c < nb; c += NT) {
-      const C* src = &st->cand_data[par][pblk][c];
-      C v;
-      v.x = *reinterpret_cast<const volatile R*>(&src->x);
-      v.y = *reinterpret_cast<const volatile R*>(&src->y);
-      prow[c] = v;
+      if constexpr (kGather) {
+        prow[c] = cdat[(size_t)pblk * NB + c];
+      } else {
+        const C* src = &st->cand_data[par][pblk][c];
+        C v;
+        v.x = *reinterpret_cast<const volatile R*>(&src->x);
+        v.y = *reinterpret_cast<const volatile R*>(&src->y);
+        prow[c] = v;
+      }
     }
     __syncthreads();
     if (prw != gj) {
       if (prw >= base && prw < base + cnt)
         for (int c = tid; c < nb; c += NT) {
-          const C* src = &st->diag_data[par][c];
-          C v;
-          v.x = *reinterpret_cast<const volatile R*>(&src->x);
-          v.y = *reinterpret_cast<const volatile R*>(&src->y);
-          tile[(size_t)c * rpc + (prw - base)] = v;
+          if constexpr (kGather) {
+            tile[(size_t)c * rpc + (prw - base)] = dgr[c];
+          } else {
+            const C* src = &st->diag_data[par][c];
+            C v;
+            v.x = *reinterpret_cast<const volatile R*>(&src->x);
+            v.y = *reinterpret_cast<const volatile R*>(&src->y);
+            tile[(size_t)c * rpc + (prw - base)] = v;
+          }
         }
       if (gj >= base && gj < base + cnt)
         for (int c = tid; c < nb; c += NT) tile[(size_t)c * rpc + (gj - base)] = prow[c];
@@ -240,8 +315,10 @@ __global__ void __launch_bounds__(NT) panel_kernel(C* __restrict__ A, long long 
 // [j_skip1, ncols) of A: one thread per column, interchanges in order.
 template <typename C>
 __global__ void laswp_kernel(C* __restrict__ A, long long lda, int ncols, int j_skip0, int j_skip1,
-                             int k0, int kn, const int* __restrict__ ipiv) {
+                             int k0, int kn, const int* __restrict__ ipiv, long long astride, int n) {
   __shared__ int piv[256];
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
   for (int i = threadIdx.x; i < kn && i < 256; i += blockDim.x) piv[i] = ipiv[k0 + i] - 1;
   __syncthreads();
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -268,8 +345,11 @@ constexpr int kTrsmCols = 16;
 
 template <typename C, bool UPPER>
 __global__ void __launch_bounds__(256) trsm_kernel(const C* __restrict__ T, long long ldt, C* __restrict__ B,
-                                                   long long ldb, int nb, int ncols) {
+                                                   long long ldb, int nb, int ncols, long long tstride,
+                                                   long long bstride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  T += (size_t)blockIdx.y * tstride;
+  B += (size_t)blockIdx.y * bstride;
   C* Ts = reinterpret_cast<C*>(smem_raw);  // nb x nb, column-major
   C* Bs = Ts + (size_t)nb * nb;            // nb x kTrsmCols, column-major
   const int tid = threadIdx.x;
@@ -322,9 +402,13 @@ template <typename C>
 __global__ void __launch_bounds__(256) gemm_sub_kernel(const C* __restrict__ Am, long long lda,
                                                        const C* __restrict__ Bm, long long ldb,
                                                        C* __restrict__ Cm, long long ldc, int M, int N,
-                                                       int K) {
+                                                       int K, long long bstride) {
   __shared__ C As[kGemmBK][kGemmBM + 1];
   __shared__ C Bs[kGemmBK][kGemmBN + 1];
+  // batch: blockIdx.z selects the matrix (all three operands live in it)
+  Am += (size_t)blockIdx.z * bstride;
+  Bm += (size_t)blockIdx.z * bstride;
+  Cm += (size_t)blockIdx.z * bstride;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int m0 = blockIdx.x * kGemmBM, n0 = blockIdx.y * kGemmBN;
@@ -380,10 +464,140 @@ __global__ void __launch_bounds__(256) gemm_sub_kernel(const C* __restrict__ Am,
   }
 }
 
+// --------------------------------------------------------------- trsv ----
+// One right-hand side, the whole triangular solve in ONE launch.  Each CTA owns a
+// block of 64 rows; it takes a ticket (atomicAdd) that fixes its block in
+// dependency order (forward for L, backward for U), so a CTA only ever waits on
+// CTAs that were scheduled before it.  It subtracts the contributions of the
+// finished blocks as their "ready" flags appear (release/acquire on a flag word
+// holding the call's epoch), solves its 64 x 64 diagonal block in one warp with
+// shuffles, publishes its part of x and raises its flag.  Waits are bounded.
+constexpr int kTrsvB = 64;
+constexpr unsigned long long kTrsvWaitNs = 1000000000ull;
+
+__device__ __forceinline__ int ld_acquire_i32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_i32(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <typename C, bool UPPER>
+__global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long long lda, int n, C* x,
+                                                   int* flags, unsigned int* ticket, int epoch, int* err,
+                                                   long long astride, int flag_stride) {
+  using R = decltype(C{}.x);
+  __shared__ C xs[kTrsvB];
+  __shared__ C part[4][kTrsvB];
+  __shared__ int s_b, s_ok;
+  // batch: blockIdx.y selects the matrix, its right-hand side, flags and ticket
+  A += (size_t)blockIdx.y * astride;
+  x += (size_t)blockIdx.y * n;
+  flags += (size_t)blockIdx.y * flag_stride;
+  ticket += blockIdx.y;
+  const int tid = threadIdx.x;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  if (tid == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    s_b = UPPER ? nblk - 1 - (int)t : (int)t;
+    s_ok = 1;
+  }
+  __syncthreads();
+  const int b = s_b;
+  if (b < 0 || b >= nblk) return;
+  const int r0 = b * kTrsvB;
+  const int rows = min(kTrsvB, n - r0);
+  const int r = tid & (kTrsvB - 1), g = tid >> 6;
+  // the diagonal block goes to shared memory first: its loads overlap the waits
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  C* Ds = reinterpret_cast<C*>(trsv_smem);  // kTrsvB x kTrsvB, column-major
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int c = idx / kTrsvB, q = idx - c * kTrsvB;
+    Ds[idx] = (c < rows && q < rows) ? A[(size_t)(r0 + c) * lda + r0 + q] : cmake<C>(0, 0);
+  }
+  C acc = cmake<C>(0, 0);
+  const int nsteps = UPPER ? nblk - 1 - b : b;
+  for (int step = 0; step < nsteps; ++step) {
+    const int j = UPPER ? nblk - 1 - step : step;
+    if (tid == 0) {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_i32(&flags[j]) != epoch) {
+        if (ld_volatile_i32(err) || global_ns() - t0 > kTrsvWaitNs) {
+          atomicExch(err, 1);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+    if (tid < cols) xs[tid] = __ldcg(&x[c0 + tid]);
+    __syncthreads();
+    if (r < rows) {
+      const C* col = A + (size_t)c0 * lda + r0 + r;
+      for (int c = g; c < cols; c += 4) acc = cfms(acc, col[(size_t)c * lda], xs[c]);
+    }
+    __syncthreads();
+  }
+  part[g][r] = acc;
+  __syncthreads();
+  if (tid < 32) {
+    // lane l holds rows l and l + 32 of the block; part[] already holds -sum(T x)
+    C s0 = cmake<C>(0, 0), s1 = cmake<C>(0, 0);
+    if (tid < rows) {
+      const C b0 = x[r0 + tid];
+      s0 = cmake<C>(b0.x + (part[0][tid].x + part[1][tid].x + part[2][tid].x + part[3][tid].x),
+                    b0.y + (part[0][tid].y + part[1][tid].y + part[2][tid].y + part[3][tid].y));
+    }
+    if (tid + 32 < rows) {
+      const int q = tid + 32;
+      const C b1 = x[r0 + q];
+      s1 = cmake<C>(b1.x + (part[0][q].x + part[1][q].x + part[2][q].x + part[3][q].x),
+                    b1.y + (part[0][q].y + part[1][q].y + part[2][q].y + part[3][q].y));
+    }
+    const C* D = Ds;  // diagonal block (leading dimension kTrsvB)
+    constexpr long long lda = kTrsvB;
+    if (!UPPER) {
+      for (int c = 0; c < rows; ++c) {
+        const R xr = __shfl_sync(0xffffffffu, c < 32 ? s0.x : s1.x, c & 31);
+        const R xi = __shfl_sync(0xffffffffu, c < 32 ? s0.y : s1.y, c & 31);
+        const C xc = cmake<C>(xr, xi);
+        if (tid > c && tid < rows) s0 = cfms(s0, D[(size_t)c * lda + tid], xc);
+        if (tid + 32 > c && tid + 32 < rows) s1 = cfms(s1, D[(size_t)c * lda + tid + 32], xc);
+      }
+    } else {
+      for (int c = rows - 1; c >= 0; --c) {
+        if (c < 32) {
+          if (tid == c) s0 = cdiv(s0, D[(size_t)c * lda + c]);
+        } else {
+          if (tid + 32 == c) s1 = cdiv(s1, D[(size_t)c * lda + c]);
+        }
+        const R xr = __shfl_sync(0xffffffffu, c < 32 ? s0.x : s1.x, c & 31);
+        const R xi = __shfl_sync(0xffffffffu, c < 32 ? s0.y : s1.y, c & 31);
+        const C xc = cmake<C>(xr, xi);
+        if (tid < c && tid < rows) s0 = cfms(s0, D[(size_t)c * lda + tid], xc);
+        if (tid + 32 < c && tid + 32 < rows) s1 = cfms(s1, D[(size_t)c * lda + tid + 32], xc);
+      }
+    }
+    if (tid < rows) x[r0 + tid] = s0;
+    if (tid + 32 < rows) x[r0 + tid + 32] = s1;
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) st_release_i32(&flags[b], epoch);
+}
+
 // ------------------------------------------------------- permutation ----
 // perm[i] = original row that ends up in row i after the interchanges ipiv[0..n).
 __global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm) {
   extern __shared__ int sp[];
+  ipiv += (size_t)blockIdx.x * n;  // one block per matrix of a batch
+  perm += (size_t)blockIdx.x * n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -402,10 +616,13 @@ __global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* 
 
 template <typename C>
 __global__ void gather_rows_kernel(const C* __restrict__ src, long long lds, C* __restrict__ dst,
-                                   long long ldd, const int* __restrict__ perm, int n, int nrhs) {
+                                   long long ldd, const int* __restrict__ perm, int n, int nrhs,
+                                   int perm_stride) {
+  // column c: a right-hand side of one matrix (perm_stride 0) or the right-hand
+  // side of matrix c of a batch (perm_stride n)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
-  if (i < n && c < nrhs) dst[(size_t)c * ldd + i] = src[(size_t)c * lds + perm[i]];
+  if (i < n && c < nrhs) dst[(size_t)c * ldd + i] = src[(size_t)c * lds + perm[(size_t)c * perm_stride + i]];
 }
 
 // ----------------------------------------------------------- host side ----
@@ -446,26 +663,47 @@ DeviceLimits device_limits() {
 }  // namespace
 
 size_t lu_workspace_bytes(int elem_bytes) {
-  // barrier + stage for the larger (FP64) configuration
+  // barrier + stage of one matrix, sized for the larger (FP64) configuration
   (void)elem_bytes;
   return sizeof(GridBarrier) + 256 + sizeof(PanelStage<double2, 64>) + 256;
 }
 
+// Dynamic shared memory of panel_kernel: the block's rows, the pivot row and, for
+// FP32, the gathered candidates (rows, values, row numbers) and the diagonal row.
+template <typename C, int NB>
+size_t panel_smem(int rpc, int P) {
+  using R = decltype(C{}.x);
+  size_t bytes = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  if (sizeof(R) == 4) bytes += (size_t)P * NB * sizeof(C) + NB * sizeof(C) + (size_t)P * (sizeof(R) + sizeof(int));
+  return bytes;
+}
+
+size_t lu_stage_offset(int max_batch) {
+  return ((size_t)max_batch * sizeof(GridBarrier) + 255) & ~(size_t)255;
+}
+
+size_t lu_stage_bytes(int max_batch) { return (size_t)max_batch * sizeof(PanelStage<double2, 64>); }
+
 template <typename C>
 cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, cudaStream_t s,
-                        GemmHook<C> gemm_hook) {
+                        GemmHook<C> gemm_hook, int batch, long long astride) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using Stage = PanelStage<C, NB>;
+  if (batch < 1 || batch > ws->max_batch || (batch > 1 && astride < lda * (long long)n))
+    return cudaErrorInvalidValue;
   const DeviceLimits lim = device_limits();
   GridBarrier* gb = ws->barrier;
   Stage* st = reinterpret_cast<Stage*>(ws->stage);
   cudaError_t e;
+  unsigned int bar_base = 0;  // arrivals of earlier panels on the counting barrier
+  // rows per block: FP64 rank-1 updates are costly, so many blocks share them; FP32
+  // panels are latency-bound, so fewer blocks make each barrier cheaper
+  constexpr int kMinRows = sizeof(decltype(C{}.x)) == 8 ? 16 : 128;
   for (int j0 = 0; j0 < n; j0 += NB) {
     const int nb = std::min(NB, n - j0);
     const int m = n - j0;
-    // panel: enough blocks that each holds a modest slice of rows
-    int P = std::min({lim.sms, kMaxPanelBlocks, (m + 15) / 16});
+    int P = std::min({lim.sms, kMaxPanelBlocks, (m + kMinRows - 1) / kMinRows});
     P = std::max(P, 1);
     int rpc = (m + P - 1) / P;
     size_t smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
@@ -475,28 +713,32 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
     }
     P = (m + rpc - 1) / rpc;
+    smem = panel_smem<C, NB>(rpc, P);
     auto kern = panel_kernel<C, NB, NT>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = allow_dynamic_smem((const void*)kern, smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
     if (e != cudaSuccess) return e;
-    if (per_sm * lim.sms < P) return cudaErrorCooperativeLaunchTooLarge;
+    if (per_sm * lim.sms < P * batch) return cudaErrorCooperativeLaunchTooLarge;
     C* Ap = A;
-    long long ldap = lda;
+    long long ldap = lda, astr = astride;
     int np = n, j0p = j0, nbp = nb, rpcp = rpc;
     int* ipivp = ipiv;
-    void* args[] = {&Ap, &ldap, &np, &j0p, &nbp, &rpcp, &ipivp, &st, &gb};
+    unsigned int basep = bar_base;
+    void* args[] = {&Ap, &ldap, &np, &j0p, &nbp, &rpcp, &ipivp, &st, &gb, &basep, &astr};
     {
-      stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)nb * nb / 2.0);
-      e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P), dim3(NT), args, smem, s);
+      stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)nb * nb / 2.0 * batch);
+      e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P, batch), dim3(NT), args, smem, s);
     }
     if (e != cudaSuccess) return e;
+    bar_base += (unsigned int)P * (unsigned int)nb;
     // interchanges on the other columns
     const int other = n - nb;
     if (other > 0) {
-      stats::Scope sc(stats::kLaswp, s, 2.0 * nb * other * sizeof(C));
-      laswp_kernel<C><<<(other + 127) / 128, 128, 0, s>>>(A, lda, n, j0, j0 + nb, j0, nb, ipiv);
+      stats::Scope sc(stats::kLaswp, s, 2.0 * nb * other * sizeof(C) * batch);
+      laswp_kernel<C><<<dim3((other + 127) / 128, batch), 128, 0, s>>>(A, lda, n, j0, j0 + nb, j0, nb, ipiv,
+                                                                       astride, n);
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
     }
@@ -507,21 +749,21 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       C* A21 = A + (size_t)j0 * lda + j0 + nb;
       C* A22 = A + (size_t)(j0 + nb) * lda + j0 + nb;
       const size_t tsmem = ((size_t)nb * nb + (size_t)nb * kTrsmCols) * sizeof(C);
-      e = cudaFuncSetAttribute(trsm_kernel<C, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)tsmem);
+      e = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
       if (e != cudaSuccess) return e;
       {
-        stats::Scope sc(stats::kTrsm, s, 4.0 * nb * (double)nb * rest);
-        trsm_kernel<C, false><<<(rest + kTrsmCols - 1) / kTrsmCols, 256, tsmem, s>>>(A11, lda, A12, lda, nb, rest);
+        stats::Scope sc(stats::kTrsm, s, 4.0 * nb * (double)nb * rest * batch);
+        trsm_kernel<C, false><<<dim3((rest + kTrsmCols - 1) / kTrsmCols, batch), 256, tsmem, s>>>(
+            A11, lda, A12, lda, nb, rest, astride, astride);
       }
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       if (gemm_hook) {
-        e = gemm_hook(A21, lda, A12, lda, A22, lda, rest, rest, nb, s);
+        e = gemm_hook(ws, A21, lda, A12, lda, A22, lda, rest, rest, nb, s, batch, astride);
       } else {
-        stats::Scope sc(stats::kGemm, s, 8.0 * rest * (double)rest * nb);
-        dim3 grid((rest + kGemmBM - 1) / kGemmBM, (rest + kGemmBN - 1) / kGemmBN);
-        gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A21, lda, A12, lda, A22, lda, rest, rest, nb);
+        stats::Scope sc(stats::kGemm, s, 8.0 * rest * (double)rest * nb * batch);
+        dim3 grid((rest + kGemmBM - 1) / kGemmBM, (rest + kGemmBN - 1) / kGemmBN, batch);
+        gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A21, lda, A12, lda, A22, lda, rest, rest, nb, astride);
         e = cudaGetLastError();
       }
       if (e != cudaSuccess) return e;
@@ -532,26 +774,51 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
-                       LuWorkspace* ws, cudaStream_t s) {
+                       LuWorkspace* ws, cudaStream_t s, int batch, long long astride) {
   constexpr int NB = PanelCfg<C>::NB;
   cudaError_t e;
+  if (batch < 1 || batch > ws->max_batch || (batch > 1 && (nrhs != 1 || ldb != n))) return cudaErrorInvalidValue;
+  if (n > ws->perm_cap) return cudaErrorInvalidValue;
   // row interchanges: B <- P B through a permutation gather into the scratch copy
   if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
-  e = cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(n * sizeof(int)));
+  e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
   if (e != cudaSuccess) return e;
   stats::count(stats::kMisc, 2);
-  pivots_to_perm_kernel<<<1, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm);
+  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm);
   C* tmp = reinterpret_cast<C*>(ws->rhs);
-  if ((size_t)n * nrhs * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
-  e = cudaMemcpy2DAsync(tmp, (size_t)n * sizeof(C), B, (size_t)ldb * sizeof(C), (size_t)n * sizeof(C), nrhs,
+  const int ncol = batch > 1 ? batch : nrhs;  // columns of the gathered block
+  if ((size_t)n * ncol * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
+  e = cudaMemcpy2DAsync(tmp, (size_t)n * sizeof(C), B, (size_t)ldb * sizeof(C), (size_t)n * sizeof(C), ncol,
                         cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return e;
-  gather_rows_kernel<C><<<dim3((n + 255) / 256, nrhs), 256, 0, s>>>(tmp, n, B, ldb, ws->perm, n, nrhs);
+  gather_rows_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(tmp, n, B, ldb, ws->perm, n, ncol,
+                                                                     batch > 1 ? n : 0);
+  if (nrhs == 1 && ws->flags) {
+    const int nblk = (n + kTrsvB - 1) / kTrsvB;
+    if (nblk > ws->flag_cap) return cudaErrorInvalidValue;
+    const size_t dsmem = sizeof(C) * kTrsvB * kTrsvB;
+    e = allow_dynamic_smem((const void*)trsv_kernel<C, false>, dsmem);
+    if (e != cudaSuccess) return e;
+    e = allow_dynamic_smem((const void*)trsv_kernel<C, true>, dsmem);
+    if (e != cudaSuccess) return e;
+    stats::Scope sc(stats::kTrsm, s, 8.0 * n * (double)n * batch, 2);
+    for (int pass = 0; pass < 2; ++pass) {
+      const int ep = ++ws->epoch;
+      e = cudaMemsetAsync(ws->ticket, 0, sizeof(unsigned int) * batch, s);
+      if (e != cudaSuccess) return e;
+      if (pass == 0)
+        trsv_kernel<C, false><<<dim3(nblk, batch), 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                                    &ws->barrier->err, astride, ws->flag_cap);
+      else
+        trsv_kernel<C, true><<<dim3(nblk, batch), 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                                   &ws->barrier->err, astride, ws->flag_cap);
+    }
+    return cudaGetLastError();
+  }
   const size_t tsmem = ((size_t)NB * NB + (size_t)NB * kTrsmCols) * sizeof(C);
-  e = cudaFuncSetAttribute(trsm_kernel<C, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
+  e = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(trsm_kernel<C, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
+  e = allow_dynamic_smem((const void*)trsm_kernel<C, true>, tsmem);
   if (e != cudaSuccess) return e;
   // forward: L unit lower
   const int nblocks = (n + NB - 1) / NB;
@@ -560,12 +827,12 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
     const int kb = std::min(NB, n - k0);
     const size_t sm = ((size_t)kb * kb + (size_t)kb * kTrsmCols) * sizeof(C);
     trsm_kernel<C, false><<<(nrhs + kTrsmCols - 1) / kTrsmCols, 256, sm, s>>>(
-        A + (size_t)k0 * lda + k0, lda, B + k0, ldb, kb, nrhs);
+        A + (size_t)k0 * lda + k0, lda, B + k0, ldb, kb, nrhs, 0, 0);
     const int below = n - k0 - kb;
     if (below > 0) {
       dim3 grid((below + kGemmBM - 1) / kGemmBM, (nrhs + kGemmBN - 1) / kGemmBN);
       gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A + (size_t)k0 * lda + k0 + kb, lda, B + k0, ldb, B + k0 + kb,
-                                              ldb, below, nrhs, kb);
+                                              ldb, below, nrhs, kb, 0);
     }
   }
   // backward: U non-unit upper
@@ -575,22 +842,50 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
     const int kb = std::min(NB, n - k0);
     const size_t sm = ((size_t)kb * kb + (size_t)kb * kTrsmCols) * sizeof(C);
     trsm_kernel<C, true><<<(nrhs + kTrsmCols - 1) / kTrsmCols, 256, sm, s>>>(
-        A + (size_t)k0 * lda + k0, lda, B + k0, ldb, kb, nrhs);
+        A + (size_t)k0 * lda + k0, lda, B + k0, ldb, kb, nrhs, 0, 0);
     if (k0 > 0) {
       dim3 grid((k0 + kGemmBM - 1) / kGemmBM, (nrhs + kGemmBN - 1) / kGemmBN);
-      gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A + (size_t)k0 * lda, lda, B + k0, ldb, B, ldb, k0, nrhs, kb);
+      gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A + (size_t)k0 * lda, lda, B + k0, ldb, B, ldb, k0, nrhs, kb, 0);
     }
   }
   return cudaGetLastError();
 }
 
+template <typename C>
+int lu_max_batch(int n) {
+  constexpr int NB = PanelCfg<C>::NB;
+  constexpr int NT = PanelCfg<C>::NT;
+  constexpr int kMinRows = sizeof(decltype(C{}.x)) == 8 ? 16 : 128;
+  const DeviceLimits lim = device_limits();
+  if (lim.sms <= 0 || n <= 0) return 1;
+  // the first panel (m = n) has the most blocks
+  int P = std::max(1, std::min({lim.sms, kMaxPanelBlocks, (n + kMinRows - 1) / kMinRows}));
+  int rpc = (n + P - 1) / P;
+  size_t smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  while (smem > (size_t)lim.smem_optin - 4096 && P < std::min(lim.sms, kMaxPanelBlocks)) {
+    ++P;
+    rpc = (n + P - 1) / P;
+    smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  }
+  P = (n + rpc - 1) / rpc;
+  smem = panel_smem<C, NB>(rpc, P);
+  auto kern = panel_kernel<C, NB, NT>;
+  if (allow_dynamic_smem((const void*)kern, smem) != cudaSuccess) return 1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) != cudaSuccess) return 1;
+  return std::max(1, std::min(kMaxLuBatch, per_sm * lim.sms / P));
+}
+
+template int lu_max_batch<double2>(int);
+template int lu_max_batch<float2>(int);
+
 template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWorkspace*, cudaStream_t,
-                                          GemmHook<double2>);
+                                          GemmHook<double2>, int, long long);
 template cudaError_t lu_factor_t<float2>(float2*, long long, int, int*, LuWorkspace*, cudaStream_t,
-                                         GemmHook<float2>);
+                                         GemmHook<float2>, int, long long);
 template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const int*, double2*, long long, int,
-                                         LuWorkspace*, cudaStream_t);
+                                         LuWorkspace*, cudaStream_t, int, long long);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,
-                                        LuWorkspace*, cudaStream_t);
+                                        LuWorkspace*, cudaStream_t, int, long long);
 
 }  // namespace wmom

@@ -106,6 +106,33 @@ __device__ __forceinline__ int ld_volatile_i32(const int* p) {
   return *reinterpret_cast<const volatile int*>(p);
 }
 
+// Counting barrier: the counter only grows, so arriving is one atomicAdd and
+// waiting is polling the counter until it reaches `target` (= the caller's
+// running total of arrivals expected so far).  Returns false on timeout.
+__device__ __forceinline__ bool grid_barrier_count(GridBarrier* gb, unsigned int target) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    // arrive: a release reduction (no round trip to wait for), ordered after the
+    // block's writes, which __syncthreads made visible to this thread
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gb->count) : "memory");
+    const unsigned long long t0 = global_ns();
+    while (ld_acquire_u32(&gb->count) < target) {
+      if (ld_volatile_i32(&gb->err)) break;
+      if (global_ns() - t0 > kBarrierTimeoutNs) {
+        atomicExch(&gb->err, 1);
+        break;
+      }
+    }
+    __threadfence();
+    if (ld_volatile_i32(&gb->err)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Returns false when the barrier timed out (here or in another block).
 __device__ __forceinline__ bool grid_barrier(GridBarrier* gb, unsigned int nblocks,
                                              unsigned int* gen_local) {

@@ -8,39 +8,67 @@
 namespace wmom {
 
 constexpr int kMaxPanelBlocks = 256;
+constexpr int kMaxLuBatch = 16;  // matrices per batched factorisation
+
+// Largest batch whose first panel launch fits co-resident on this device.
+template <typename C>
+int lu_max_batch(int n);
 
 struct GridBarrier;
 
-// Device scratch of one factorisation stream: the panel kernel's grid barrier and
-// candidate staging, the row permutation of a solve and a right-hand-side copy.
+// Device scratch of one factorisation stream, for up to max_batch matrices of one
+// batched factorisation: per matrix the panel kernel's grid barrier and candidate
+// staging, the row permutation of a solve, and a right-hand-side copy.
 struct LuWorkspace {
-  GridBarrier* barrier = nullptr;
-  void* stage = nullptr;
-  int* perm = nullptr;
+  GridBarrier* barrier = nullptr;  // [max_batch]
+  void* stage = nullptr;           // [max_batch] panel staging (FP64-sized)
+  int* perm = nullptr;             // [max_batch * perm_cap]
   void* rhs = nullptr;
   size_t rhs_bytes = 0;
   int perm_cap = 0;
+  int max_batch = 1;
+  // single-launch triangular solves: per-block ready flags (epoch-tagged), ticket
+  int* flags = nullptr;            // [max_batch * flag_cap]
+  unsigned int* ticket = nullptr;  // [max_batch]
+  int flag_cap = 0;
+  int epoch = 0;
+  // tensor-core trailing update: packed TF32 operand planes, grown on first use
+  // (never inside a stream capture; tc_gen counts reallocations, so that a captured
+  // factorisation is replayed only over the buffer it was captured with) and the
+  // flag its bounded waits set on timeout
+  float* tc_buf = nullptr;
+  size_t tc_cap = 0;  // floats
+  unsigned tc_gen = 0;
+  int* tc_err = nullptr;
 };
 
-size_t lu_workspace_bytes(int elem_bytes);
+size_t lu_workspace_bytes(int elem_bytes);  // one matrix: barrier + staging
+size_t lu_stage_offset(int max_batch);      // byte offset of the staging array
+size_t lu_stage_bytes(int max_batch);
 
-// Optional replacement of the trailing-update GEMM (Cm -= Am * Bm).
+// Optional replacement of the trailing-update GEMM (Cm -= Am * Bm) for `batch`
+// matrices whose operands are `bstride` elements apart; its scratch lives in `ws`.
 template <typename C>
-using GemmHook = cudaError_t (*)(const C* Am, long long lda, const C* Bm, long long ldb, C* Cm,
-                                 long long ldc, int M, int N, int K, cudaStream_t s);
+using GemmHook = cudaError_t (*)(LuWorkspace* ws, const C* Am, long long lda, const C* Bm, long long ldb, C* Cm,
+                                 long long ldc, int M, int N, int K, cudaStream_t s, int batch,
+                                 long long bstride);
 
+// In-place LU of `batch` n x n matrices astride elements apart (pivots n apart).
 template <typename C>
 cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, cudaStream_t s,
-                        GemmHook<C> gemm_hook);
+                        GemmHook<C> gemm_hook, int batch = 1, long long astride = 0);
 
+// Solves with the factors; batch > 1 needs nrhs == 1 and right-hand sides n apart.
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
-                       LuWorkspace* ws, cudaStream_t s);
+                       LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0);
 
 // Workspace management (api.cu).
-cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max);
+cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch = 1);
 void lu_workspace_destroy(LuWorkspace* ws);
 cudaError_t lu_workspace_reset_barrier(LuWorkspace* ws, cudaStream_t s);
-int lu_workspace_read_status(LuWorkspace* ws, int* info, cudaStream_t s);
+// Returns nonzero when a wait of the last factorisation timed out; info[b] = the
+// first zero-pivot column of matrix b (info may be null; batch entries read).
+int lu_workspace_read_status(LuWorkspace* ws, int* info, cudaStream_t s, int batch = 1);
 
 }  // namespace wmom

@@ -13,18 +13,20 @@
 // which keeps the product close to FP32 accuracy; the FP64 refinement of the
 // solver then removes the remaining FP32-level error.
 //
-// Kernel: one CTA (4 warps) per 128 x 128 real output tile (128 rows, 64 complex
-// columns).  Thread 0 streams K in chunks of 32 FP32 (one 128-byte swizzle row)
-// with TMA into a 2-stage ring (head and tail planes of A' and B'), waits on the
-// stage's mbarrier and issues 3 x 4 tcgen05.mma (M=128, N=128, K=8) per chunk;
-// tcgen05.commit releases the stage.  After the last commit the 4 warps read
-// their 32-lane quarter of the accumulator with tcgen05.ld and subtract it from C
-// with coalesced float2 accesses.  All waits are bounded; on timeout the kernel
-// records an error, skips the rest and still frees its TMEM.
+// Kernel: persistent, one CTA (6 warps) per SM, each walking 128 x 128 real output
+// tiles (128 rows, 64 complex columns).  A producer thread streams K in chunks of 32
+// FP32 (one 128-byte swizzle row) with TMA into a 3-stage ring (head and tail
+// planes of A' and B'); an MMA thread issues 3 x 4 tcgen05.mma (M=128, N=128, K=8)
+// per chunk into one of two TMEM accumulators; four epilogue warps read their
+// 32-lane quarter of a finished accumulator with tcgen05.ld and subtract it from C
+// with coalesced float2 accesses while the next tile is being multiplied.  All
+// waits are bounded; on timeout the kernel records an error, skips the rest and
+// still frees its TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -40,12 +42,13 @@ namespace tc {
 constexpr int BM = 128;  // accumulator lanes = rows of C per CTA
 constexpr int BN = 128;  // accumulator FP32 columns = 64 complex columns of C
 constexpr int KC = 32;   // FP32 elements of K per chunk (128 bytes)
-constexpr int STAGES = 2;
+constexpr int STAGES = 3;
 constexpr int A_BYTES = BM * KC * 4;  // 16 KB per plane
 constexpr int B_BYTES = BN * KC * 4;  // 16 KB per plane
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
-constexpr int NTHREADS = 128;
+constexpr int NTHREADS = 192;         // producer warp, MMA warp, 4 epilogue warps
+constexpr int TMEM_COLS = 2 * BN;     // two accumulators
 constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -72,22 +75,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
-// Bounded wait on an mbarrier phase; false on timeout or when another CTA of the
-// launch has already recorded one (err != 0).
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const int* err) {
-  const unsigned long long t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*reinterpret_cast<const volatile int*>(err)) return false;
-    if (global_ns() - t0 > kWaitNs) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+// 3-D tiled TMA load (x = K element, y = row, z = matrix of the batch).
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
       : "memory");
 }
 
@@ -131,7 +125,11 @@ __device__ __forceinline__ float tf32_rna(float x) {
 // A (M x K complex, col-major) -> hi/lo planes, row-major M x K2p FP32 (re, im
 // interleaved along K, zero padding up to K2p).
 __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int K2p,
-                              float* __restrict__ hi, float* __restrict__ lo) {
+                              float* __restrict__ hi, float* __restrict__ lo, long long astride) {
+  // batch: blockIdx.z selects the matrix; its planes follow each other
+  A += (size_t)blockIdx.z * astride;
+  hi += (size_t)blockIdx.z * M * K2p;
+  lo += (size_t)blockIdx.z * M * K2p;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y;  // complex column, K2p/2 of them
   if (m >= M) return;
@@ -148,7 +146,10 @@ __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M
 // B (K x N complex, col-major) -> hi/lo planes of B'^T, row-major 2N x K2p FP32:
 // row 2n = (Br, -Bi) pairs, row 2n+1 = (Bi, Br) pairs along K.
 __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int K2p,
-                              float* __restrict__ hi, float* __restrict__ lo) {
+                              float* __restrict__ hi, float* __restrict__ lo, long long bstride) {
+  B += (size_t)blockIdx.z * bstride;
+  hi += (size_t)blockIdx.z * 2 * N * K2p;
+  lo += (size_t)blockIdx.z * 2 * N * K2p;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;  // complex row of B, K2p/2 of them
   const int n = blockIdx.y;
   if (2 * k >= K2p) return;
@@ -169,127 +170,231 @@ __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K
 }
 
 // ---------------------------------------------------------------- gemm ----
+// Persistent, warp-specialised: CTA b takes output tiles b, b + grid, ... (tiles
+// ordered rows fastest, then columns, then matrices of the batch).
+//   warp 0 (one thread): TMA producer, K chunks of successive tiles into the
+//                        STAGES-deep ring (full[s] completes when a stage lands);
+//   warp 1 (one thread): MMA issuer, 3 x 4 tcgen05.mma per chunk into accumulator
+//                        tl % 2 of TMEM; commit to empty[s] frees the stage, commit
+//                        to tfull[b] hands a finished tile to the epilogue;
+//   warps 2-5:           epilogue, C -= accumulator b (TMEM lane quarter warp % 4,
+//                        one row of C per thread), then arrive on tempty[b].
+// The two accumulators let the tensor cores work on tile i + 1 while tile i's C
+// traffic is in flight.  Every wait is bounded (kWaitNs) and also gives up once
+// another role or CTA has recorded a failure; a role that gives up lets its own
+// copies and MMAs in flight land (bounded) before the CTA frees its TMEM.
+struct TileCoord {
+  int mat, m0, j0;
+};
+
+__device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n) {
+  const int per_mat = tiles_m * tiles_n;
+  const int mat = t / per_mat;
+  const int r = t - mat * per_mat;
+  const int tn = r / tiles_m;
+  return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
+}
+
+// Bounded wait that also ends when this CTA has failed (s_fail) or, through err,
+// another CTA of the launch.
+__device__ __forceinline__ bool role_wait(uint32_t bar, uint32_t parity, const int* err, const volatile int* s_fail) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*s_fail || *reinterpret_cast<const volatile int*>(err)) return false;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
     cgemm_sub_tc_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                         const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
-                        float2* __restrict__ C, long long ldc, int M, int N, int nchunks, int* __restrict__ err) {
+                        float2* __restrict__ C, long long ldc, int M, int N, int nchunks, int tiles_m,
+                        int tiles_n, int ntiles, int* __restrict__ err, long long cstride) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);  // full[2], done[2]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2]
   __shared__ uint32_t tmem_base;
-  __shared__ int s_fail;
-
+  __shared__ volatile int s_fail;
   const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const int m0 = blockIdx.x * BM;
-  const int j0 = blockIdx.y * BN;  // real column of the accumulator = row of B'^T
+  const int warp = tid >> 5, lane = tid & 31;
+  auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
+  auto empty_bar = [&](int s) { return smem_u32(&bars[STAGES + s]); };
+  auto tfull_bar = [&](int b) { return smem_u32(&bars[2 * STAGES + b]); };
+  auto tempty_bar = [&](int b) { return smem_u32(&bars[2 * STAGES + 2 + b]); };
 
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(BN)
+                 "r"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int i = 0; i < 2 * STAGES; ++i) mbar_init(smem_u32(&bars[i]), 1);
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull_bar(b), 1);
+      mbar_init(tempty_bar(b), NTHREADS / 32 - 2);  // one arrival per epilogue warp
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s_fail = 0;
+    s_fail = *reinterpret_cast<const volatile int*>(err) != 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  if (tid == 0) {
-    bool ok = *reinterpret_cast<const volatile int*>(err) == 0;
-    int issued_last = -1;
-    int tma_pending = -1;  // chunk whose copies were issued but not yet seen complete
-    for (int c = 0; c < nchunks && ok; ++c) {
-      const int s = c % STAGES;
-      const uint32_t full = smem_u32(&bars[s]);
-      const uint32_t done = smem_u32(&bars[STAGES + s]);
-      if (c >= STAGES) ok = mbar_wait(done, ((c - STAGES) / STAGES) & 1, err);
-      if (!ok) break;
-      unsigned char* st = base + s * STAGE_BYTES;
-      const uint32_t a_hi = smem_u32(st), a_lo = a_hi + A_BYTES;
-      const uint32_t b_hi = a_hi + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
-      mbar_expect_tx(full, STAGE_BYTES);
-      tma_load_2d(a_hi, &mapAhi, c * KC, m0, full);
-      tma_load_2d(a_lo, &mapAlo, c * KC, m0, full);
-      tma_load_2d(b_hi, &mapBhi, c * KC, j0, full);
-      tma_load_2d(b_lo, &mapBlo, c * KC, j0, full);
-      tma_pending = c;
-      ok = mbar_wait(full, (c / STAGES) & 1, err);
-      if (!ok) break;
-      tma_pending = -1;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // tail terms first, head product last
-      const uint32_t as[3] = {a_lo, a_hi, a_hi};
-      const uint32_t bs[3] = {b_hi, b_lo, b_hi};
-#pragma unroll
-      for (int sp = 0; sp < 3; ++sp)
-#pragma unroll
-        for (int kk = 0; kk < KC / 8; ++kk)
-          mma_tf32(tmem, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), (c | sp | kk) != 0 ? 1u : 0u);
-      mma_commit(done);
-      issued_last = c;
-    }
-    if (ok && issued_last >= 0) {
-      const int s = issued_last % STAGES;
-      ok = mbar_wait(smem_u32(&bars[STAGES + s]), (issued_last / STAGES) & 1, err);
-    }
-    if (!ok) {
-      s_fail = 1;
-      atomicExch(err, 1);
-      // before leaving, give this CTA's own copies and MMAs in flight a bounded
-      // chance to land, so nothing writes shared memory or TMEM after release
-      const int zero = 0;
-      if (tma_pending >= 0) mbar_wait(smem_u32(&bars[tma_pending % STAGES]), (tma_pending / STAGES) & 1, &zero);
-      if (issued_last >= 0)
-        mbar_wait(smem_u32(&bars[STAGES + issued_last % STAGES]), (issued_last / STAGES) & 1, &zero);
-    }
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-  if (!s_fail) {
-    const int row = m0 + warp * 32 + (tid & 31);
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
-    for (int cc = 0; cc < BN / 32; ++cc) {
-      uint32_t r[32];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(tmem + lane_base + (uint32_t)(cc * 32))
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
-        const int n0 = (j0 >> 1) + cc * 16;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = n0 + j;
-          if (n < N) {
-            float2* p = C + (size_t)n * ldc + row;
-            float2 v = *p;
-            v.x -= __uint_as_float(r[2 * j]);
-            v.y -= __uint_as_float(r[2 * j + 1]);
-            *p = v;
-          }
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------ TMA producer
+      int it = 0;  // chunks issued
+      bool ok = !s_fail;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+        for (int c = 0; c < nchunks; ++c) {
+          const int s = it % STAGES, use = it / STAGES;
+          if (use > 0 && !(ok = role_wait(empty_bar(s), (use - 1) & 1, err, &s_fail))) break;
+          const uint32_t a_hi = smem_u32(base + s * STAGE_BYTES), a_lo = a_hi + A_BYTES;
+          const uint32_t b_hi = a_hi + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
+          mbar_expect_tx(full_bar(s), STAGE_BYTES);
+          tma_load_3d(a_hi, &mapAhi, c * KC, tc.m0, tc.mat, full_bar(s));
+          tma_load_3d(a_lo, &mapAlo, c * KC, tc.m0, tc.mat, full_bar(s));
+          tma_load_3d(b_hi, &mapBhi, c * KC, tc.j0, tc.mat, full_bar(s));
+          tma_load_3d(b_lo, &mapBlo, c * KC, tc.j0, tc.mat, full_bar(s));
+          ++it;
         }
       }
+      if (!ok) {
+        s_fail = 1;
+        atomicExch(err, 1);
+        // the copies of the last STAGES chunks may still be landing
+        const int zero = 0;
+        const volatile int no_fail = 0;
+        for (int i = it > STAGES ? it - STAGES : 0; i < it; ++i)
+          role_wait(full_bar(i % STAGES), (i / STAGES) & 1, &zero, &no_fail);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ------------------------------------------------------- MMA issuer
+      int it = 0, tl = 0;
+      bool ok = !s_fail;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tl) {
+        const int b = tl & 1, use = tl >> 1;
+        if (use > 0 && !(ok = role_wait(tempty_bar(b), (use - 1) & 1, err, &s_fail))) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + (uint32_t)(b * BN);
+        for (int c = 0; c < nchunks; ++c) {
+          const int s = it % STAGES;
+          if (!(ok = role_wait(full_bar(s), (it / STAGES) & 1, err, &s_fail))) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a_hi = smem_u32(base + s * STAGE_BYTES), a_lo = a_hi + A_BYTES;
+          const uint32_t b_hi = a_hi + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
+          // tail terms first, head product last
+          const uint32_t as[3] = {a_lo, a_hi, a_hi};
+          const uint32_t bs[3] = {b_hi, b_lo, b_hi};
+#pragma unroll
+          for (int sp = 0; sp < 3; ++sp)
+#pragma unroll
+            for (int kk = 0; kk < KC / 8; ++kk)
+              mma_tf32(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), (c | sp | kk) != 0 ? 1u : 0u);
+          mma_commit(empty_bar(s));
+          ++it;
+        }
+        if (!ok) break;
+        mma_commit(tfull_bar(b));
+      }
+      if (!ok) {
+        s_fail = 1;
+        atomicExch(err, 1);
+        // the last commit covers every MMA this thread issued
+        if (it > 0) {
+          const int zero = 0;
+          const volatile int no_fail = 0;
+          role_wait(empty_bar((it - 1) % STAGES), ((it - 1) / STAGES) & 1, &zero, &no_fail);
+        }
+      }
+    }
+  } else {
+    // ----------------------------------------------------------- epilogue
+    const int q = warp & 3;  // TMEM lanes 32q..32q+31 are the ones this warp may read
+    int tl = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
+      const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+      float2* Cm = C + (size_t)tc.mat * cstride;
+      const int row = tc.m0 + q * 32 + lane;
+      const bool row_ok = row < M;
+      auto load_c_chunk = [&](int cc, float2* dst) {
+        const int n0 = (tc.j0 >> 1) + cc * 16;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          dst[j] = (row_ok && n0 + j < N) ? Cm[(size_t)(n0 + j) * ldc + row] : make_float2(0.f, 0.f);
+      };
+      float2 cbuf[16], nxt[16];
+      load_c_chunk(0, cbuf);  // in flight while the accumulator is being computed
+      const int b = tl & 1, use = tl >> 1;
+      int ok = 0;
+      if (lane == 0) ok = role_wait(tfull_bar(b), use & 1, err, &s_fail) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform from here on
+      if (!ok) {
+        if (lane == 0) {
+          s_fail = 1;
+          atomicExch(err, 1);
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+#pragma unroll
+      for (int cc = 0; cc < BN / 32; ++cc) {
+        if (cc + 1 < BN / 32) load_c_chunk(cc + 1, nxt);
+        uint32_t r[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr + (uint32_t)(cc * 32)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row_ok) {
+          const int n0 = (tc.j0 >> 1) + cc * 16;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            if (n0 + j < N) {
+              float2 v = cbuf[j];
+              v.x -= __uint_as_float(r[2 * j]);
+              v.y -= __uint_as_float(r[2 * j + 1]);
+              Cm[(size_t)(n0 + j) * ldc + row] = v;
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) cbuf[j] = nxt[j];
+      }
+      // accumulator b read out: the MMA issuer may overwrite it
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty_bar(b));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1) {
+    __syncwarp();  // lane 0 ran the MMA loop alone: converge before the .aligned op
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
@@ -312,99 +417,108 @@ EncodeFn encode_fn() {
   return fn;
 }
 
-bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p) {
+// 3-D map over `batch` planes of rows x k2p FP32 (row-major), 32 x 128 boxes.
+bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch) {
   EncodeFn enc = encode_fn();
   if (!enc) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)k2p, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)k2p * sizeof(float)};
-  cuuint32_t box[2] = {(cuuint32_t)KC, (cuuint32_t)BM};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
+  cuuint64_t dims[3] = {(cuuint64_t)k2p, (cuuint64_t)rows, (cuuint64_t)batch};
+  cuuint64_t strides[2] = {(cuuint64_t)k2p * sizeof(float), (cuuint64_t)rows * k2p * sizeof(float)};
+  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)BM, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(ptr), dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
-struct TcWorkspace {
-  float* buf = nullptr;
-  size_t cap = 0;  // floats
-  int* err = nullptr;
-};
-
-std::mutex g_mu;
-std::vector<TcWorkspace> g_ws;
-
-cudaError_t get_ws(size_t floats, TcWorkspace** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Grows ws->tc_buf to `floats`.  Inside a stream capture it refuses (the capture
+// then fails and the caller launches directly, which grows the buffer); otherwise
+// the old buffer is released only after the work queued on `s` has finished.
+cudaError_t tc_scratch(LuWorkspace* ws, size_t floats, cudaStream_t s) {
+  if (!ws->tc_err) {
+    cudaError_t e = cudaMalloc(&ws->tc_err, sizeof(int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(ws->tc_err, 0, sizeof(int));
+    if (e != cudaSuccess) return e;
+  }
+  if (ws->tc_cap >= floats) return cudaSuccess;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
   if (e != cudaSuccess) return e;
-  if ((int)g_ws.size() <= dev) g_ws.resize(dev + 1);
-  TcWorkspace& w = g_ws[dev];
-  if (!w.err) {
-    e = cudaMalloc(&w.err, sizeof(int));
+  if (cs != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
+  if (ws->tc_buf) {
+    e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
-    e = cudaMemset(w.err, 0, sizeof(int));
-    if (e != cudaSuccess) return e;
+    cudaFree(ws->tc_buf);
+    ws->tc_buf = nullptr;
+    ws->tc_cap = 0;
   }
-  if (w.cap < floats) {
-    if (w.buf) {
-      cudaDeviceSynchronize();
-      cudaFree(w.buf);
-      w.buf = nullptr;
-    }
-    e = cudaMalloc(&w.buf, floats * sizeof(float));
-    if (e != cudaSuccess) {
-      w.cap = 0;
-      return e;
-    }
-    w.cap = floats;
+  e = cudaMalloc(&ws->tc_buf, floats * sizeof(float));
+  if (e != cudaSuccess) {
+    ws->tc_buf = nullptr;
+    return e;
   }
-  *out = &w;
+  ws->tc_cap = floats;
+  ++ws->tc_gen;
   return cudaSuccess;
 }
 
+// Scratch of the stand-alone entry point wmom_cgemm_sub_tc: one per device,
+// serialised by a mutex (that entry point synchronises before returning).
+std::mutex g_mu;
+std::vector<LuWorkspace> g_ws;
+
 }  // namespace
 
-cudaError_t cgemm_sub_tc(const float2* A, long long lda, const float2* B, long long ldb, float2* C, long long ldc,
-                         int M, int N, int K, cudaStream_t s) {
+cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const float2* B, long long ldb,
+                         float2* C, long long ldc, int M, int N, int K, cudaStream_t s, int batch,
+                         long long bstride) {
   if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  if (!ws || batch < 1 || batch > 65535 || N > 65535) return cudaErrorInvalidValue;
   const int K2p = ((2 * K + KC - 1) / KC) * KC;
-  const size_t a_pl = (size_t)M * K2p, b_pl = (size_t)2 * N * K2p;
-  std::lock_guard<std::mutex> lk(g_mu);
-  TcWorkspace* w = nullptr;
-  cudaError_t e = get_ws(2 * a_pl + 2 * b_pl, &w);
+  const size_t a_pl = (size_t)M * K2p * batch, b_pl = (size_t)2 * N * K2p * batch;
+  cudaError_t e = tc_scratch(ws, 2 * a_pl + 2 * b_pl, s);
   if (e != cudaSuccess) return e;
-  float* ahi = w->buf;
+  float* ahi = ws->tc_buf;
   float* alo = ahi + a_pl;
   float* bhi = alo + a_pl;
   float* blo = bhi + b_pl;
   stats::count(stats::kMisc, 2);
-  pack_a_kernel<<<dim3((M + 127) / 128, K2p / 2), 128, 0, s>>>(A, lda, M, K, K2p, ahi, alo);
-  pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo);
+  pack_a_kernel<<<dim3((M + 127) / 128, K2p / 2, batch), 128, 0, s>>>(A, lda, M, K, K2p, ahi, alo, bstride);
+  pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
   CUtensorMap mah, mal, mbh, mbl;
-  if (!make_map(&mah, ahi, M, K2p) || !make_map(&mal, alo, M, K2p) || !make_map(&mbh, bhi, 2 * N, K2p) ||
-      !make_map(&mbl, blo, 2 * N, K2p))
+  if (!make_map(&mah, ahi, M, K2p, batch) || !make_map(&mal, alo, M, K2p, batch) ||
+      !make_map(&mbh, bhi, 2 * N, K2p, batch) || !make_map(&mbl, blo, 2 * N, K2p, batch))
     return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
-    e = cudaFuncSetAttribute(cgemm_sub_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  e = allow_dynamic_smem((const void*)cgemm_sub_tc_kernel, SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
+  const long long ntiles = (long long)tiles_m * tiles_n * batch;
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    attr_set = true;
   }
-  dim3 grid((M + BM - 1) / BM, (2 * N + BN - 1) / BN);
-  stats::Scope sc(stats::kTcGemm, s, 8.0 * M * (double)N * K);
-  cgemm_sub_tc_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / KC, w->err);
+  const int grid = (int)std::min<long long>(ntiles, nsm);
+  stats::Scope sc(stats::kTcGemm, s, 8.0 * M * (double)N * K * batch);
+  cgemm_sub_tc_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / KC, tiles_m,
+                                                          tiles_n, (int)ntiles, ws->tc_err, bstride);
   return cudaGetLastError();
 }
 
-int read_and_clear_error() {
-  std::lock_guard<std::mutex> lk(g_mu);
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if ((int)g_ws.size() <= dev || !g_ws[dev].err) return 0;
+int read_and_clear_error(LuWorkspace* ws, cudaStream_t s) {
+  if (!ws || !ws->tc_err) return 0;
   int h = 0;
-  cudaMemcpy(&h, g_ws[dev].err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (h) cudaMemset(g_ws[dev].err, 0, sizeof(int));
+  if (cudaMemcpyAsync(&h, ws->tc_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return 1;
+  if (h) {
+    cudaMemsetAsync(ws->tc_err, 0, sizeof(int), s);
+    cudaStreamSynchronize(s);
+  }
   return h;
 }
 
@@ -427,12 +541,17 @@ extern "C" wmom_status wmom_cgemm_sub_tc(int m, int n, int k, const void* a_dev,
   if (m < 0 || n < 0 || k < 0 || (m && (!a_dev || !c_dev || lda < m || ldc < m)) || (n && (!b_dev || ldb < k)))
     return WMOM_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = wmom::tc::cgemm_sub_tc(reinterpret_cast<const float2*>(a_dev), lda,
-                                         reinterpret_cast<const float2*>(b_dev), ldb, reinterpret_cast<float2*>(c_dev),
-                                         ldc, m, n, k, s);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "cgemm_sub_tc device");
+  std::lock_guard<std::mutex> lk(wmom::tc::g_mu);
+  if ((int)wmom::tc::g_ws.size() <= dev) wmom::tc::g_ws.resize(dev + 1);
+  wmom::LuWorkspace* ws = &wmom::tc::g_ws[dev];
+  e = wmom::tc::cgemm_sub_tc(ws, reinterpret_cast<const float2*>(a_dev), lda, reinterpret_cast<const float2*>(b_dev),
+                             ldb, reinterpret_cast<float2*>(c_dev), ldc, m, n, k, s, 1, 0);
   if (e != cudaSuccess) return wmom_fail_cuda(e, "cgemm_sub_tc");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return wmom_fail_cuda(e, "cgemm_sub_tc sync");
-  if (wmom::tc::read_and_clear_error()) return WMOM_ERR_TIMEOUT;
+  if (wmom::tc::read_and_clear_error(ws, s)) return WMOM_ERR_TIMEOUT;
   return WMOM_OK;
 }

@@ -5,15 +5,23 @@
 // FP64 form: fill (FP64) -> LU (FP64) -> solve (FP64).
 // Mixed form: fill (FP64, kept) -> FP32 copy -> LU (FP32, tensor-core trailing
 // updates) -> solve (FP32) -> iterative refinement: r = V - Z I in FP64 with the
-// FP64 Z, correction solved with the FP32 factors, I += d in FP64; when the
-// residual stops shrinking (or the FP32 factorisation hits a zero pivot) the FP64
-// LU is used instead, and the report says so.
+// FP64 Z, correction solved with the FP32 factors, I += d in FP64; a matrix whose
+// residual stops shrinking (or whose FP32 factorisation hits a zero pivot) is
+// solved with the FP64 LU instead, and its report says so.
+//
+// Frequencies are processed in groups of B matrices that go through ONE batched
+// launch sequence (fill, factor, solves, refinement with a per-matrix activity
+// mask).  B is picked per (order, form) by timing the candidate batch widths on
+// the first group (autotuner; WMOM_LU_BATCH overrides).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "lu_common.cuh"
@@ -26,11 +34,14 @@ namespace wmom {
 constexpr int kGemvRows = 128;
 constexpr int kGemvChunk = 512;
 
-// partial[chunk*n + i] = sum over columns of chunk of Z[i, j] x[j]
+// partial[chunk*n + i] = sum over the columns of a chunk of Z[i, j] x[j]; blockIdx.z = matrix
 __global__ void __launch_bounds__(kGemvRows) gemv_partial_kernel(const double2* __restrict__ Z, long long ldz,
-                                                                 const double2* __restrict__ x, int n,
-                                                                 double2* __restrict__ partial) {
+                                                                 long long zstride, const double2* __restrict__ x,
+                                                                 int n, double2* __restrict__ partial) {
   __shared__ double2 xs[kGemvChunk];
+  Z += (size_t)blockIdx.z * zstride;
+  x += (size_t)blockIdx.z * n;
+  partial += (size_t)blockIdx.z * gridDim.y * n;
   const int i = blockIdx.x * kGemvRows + threadIdx.x;
   const int c0 = blockIdx.y * kGemvChunk;
   const int c1 = min(n, c0 + kGemvChunk);
@@ -48,9 +59,12 @@ __global__ void __launch_bounds__(kGemvRows) gemv_partial_kernel(const double2* 
   partial[(size_t)blockIdx.y * n + i] = make_double2(re, im);
 }
 
+// r = v - sum of the partials in chunk order (deterministic); blockIdx.y = matrix
 __global__ void residual_finish_kernel(const double2* __restrict__ v, const double2* __restrict__ partial,
                                        int nchunks, int n, double2* __restrict__ r) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  partial += (size_t)blockIdx.y * nchunks * n;
+  r += (size_t)blockIdx.y * n;
   if (i >= n) return;
   double re = 0.0, im = 0.0;
   for (int c = 0; c < nchunks; ++c) {
@@ -61,10 +75,11 @@ __global__ void residual_finish_kernel(const double2* __restrict__ v, const doub
   r[i] = make_double2(v[i].x - re, v[i].y - im);
 }
 
-// Deterministic sum of |x_i|^2 in one block (fixed order: strided partials, then a
-// fixed tree).
+// Deterministic sum of |x_i|^2 per vector (one block per vector of a batch: fixed
+// strided partials, then a fixed tree).
 __global__ void __launch_bounds__(1024) sumsq_kernel(const double2* __restrict__ x, int n, double* out) {
   __shared__ double sh[1024];
+  x += (size_t)blockIdx.x * n;
   double acc = 0.0;
   for (int i = threadIdx.x; i < n; i += 1024) acc = fma(x[i].x, x[i].x, fma(x[i].y, x[i].y, acc));
   sh[threadIdx.x] = acc;
@@ -73,15 +88,17 @@ __global__ void __launch_bounds__(1024) sumsq_kernel(const double2* __restrict__
     if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = sh[0];
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
-__global__ void __launch_bounds__(1024) sumsq_f32_kernel(const float2* __restrict__ x, int n, double scale,
-                                                         double* out) {
+__global__ void __launch_bounds__(1024) sumsq_f32_kernel(const float2* __restrict__ x, int n,
+                                                         const double* __restrict__ scale, double* out) {
   __shared__ double sh[1024];
+  x += (size_t)blockIdx.x * n;
+  const double sc = scale[blockIdx.x];
   double acc = 0.0;
   for (int i = threadIdx.x; i < n; i += 1024) {
-    const double a = (double)x[i].x * scale, b = (double)x[i].y * scale;
+    const double a = (double)x[i].x * sc, b = (double)x[i].y * sc;
     acc = fma(a, a, fma(b, b, acc));
   }
   sh[threadIdx.x] = acc;
@@ -90,71 +107,74 @@ __global__ void __launch_bounds__(1024) sumsq_f32_kernel(const float2* __restric
     if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = sh[0];
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
 }
 
-__global__ void convert_matrix_kernel(const double2* __restrict__ src, long long lds, float2* __restrict__ dst,
-                                      long long ldd, int rows, int cols) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i < rows && j < cols) {
-    const double2 a = src[(size_t)j * lds + i];
-    dst[(size_t)j * ldd + i] = make_float2((float)a.x, (float)a.y);
+__global__ void convert_flat_kernel(const double2* __restrict__ src, float2* __restrict__ dst, size_t count) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 a = src[i];
+    dst[i] = make_float2((float)a.x, (float)a.y);
   }
 }
 
-__global__ void convert_vec_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int n,
-                                   double scale) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = make_float2((float)(src[i].x * scale), (float)(src[i].y * scale));
+// dst[b] = (float)(src[b] * scale[b]) for the vectors of a batch
+__global__ void convert_vec_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int n, int nvec,
+                                   const double* __restrict__ scale) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * nvec) return;
+  const double sc = scale ? scale[i / n] : 1.0;
+  dst[i] = make_float2((float)(src[i].x * sc), (float)(src[i].y * sc));
 }
 
-__global__ void accumulate_vec_kernel(double2* __restrict__ x, const float2* __restrict__ d, int n,
-                                      double scale) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    x[i].x += (double)d[i].x * scale;
-    x[i].y += (double)d[i].y * scale;
+// x[b] += d[b] * inv[b] where active[b]
+__global__ void accumulate_vec_kernel(double2* __restrict__ x, const float2* __restrict__ d, int n, int nvec,
+                                      const double* __restrict__ inv, const int* __restrict__ active) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * nvec) return;
+  const size_t b = i / n;
+  if (!active[b]) return;
+  x[i].x += (double)d[i].x * inv[b];
+  x[i].y += (double)d[i].y * inv[b];
+}
+
+__global__ void widen_vec_kernel(const float2* __restrict__ d, double2* __restrict__ x, size_t count) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < count) x[i] = make_double2((double)d[i].x, (double)d[i].y);
+}
+
+// Lumped loads: one thread per matrix adds its loads in list order.
+__global__ void add_loads_kernel(double2* __restrict__ Z, long long ldz, long long zstride, const int* __restrict__ idx,
+                                 const double2* __restrict__ val, int nloads, int nk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  for (int l = 0; l < nloads; ++l) {
+    const int d = idx[l] - 1;
+    double2* p = Z + (size_t)k * zstride + (size_t)d * ldz + d;
+    const double2 a = val[(size_t)k * nloads + l];
+    p->x += a.x;
+    p->y += a.y;
   }
 }
 
-__global__ void widen_vec_kernel(const float2* __restrict__ d, double2* __restrict__ x, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] = make_double2((double)d[i].x, (double)d[i].y);
-}
-
-cudaError_t residual_fp64(const double2* Z, long long ldz, const double2* x, const double2* v, int n,
-                          double2* r, double2* partial, cudaStream_t s) {
+cudaError_t residual_fp64(const double2* Z, long long ldz, long long zstride, const double2* x, const double2* v,
+                          int n, double2* r, double2* partial, int nvec, cudaStream_t s) {
   const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
-  stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n, 2);
-  gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks), kGemvRows, 0, s>>>(Z, ldz, x, n,
-                                                                                           partial);
-  residual_finish_kernel<<<(n + 255) / 256, 256, 0, s>>>(v, partial, nchunks, n, r);
+  stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n * nvec, 2);
+  gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks, nvec), kGemvRows, 0, s>>>(Z, ldz, zstride,
+                                                                                                 x, n, partial);
+  residual_finish_kernel<<<dim3((n + 255) / 256, nvec), 256, 0, s>>>(v, partial, nchunks, n, r);
   return cudaGetLastError();
 }
 
-cudaError_t sumsq_fp64(const double2* x, int n, double* out, cudaStream_t s) {
+cudaError_t sumsq_fp64(const double2* x, int n, double* out, int nvec, cudaStream_t s) {
   stats::count(stats::kMisc);
-  sumsq_kernel<<<1, 1024, 0, s>>>(x, n, out);
+  sumsq_kernel<<<nvec, 1024, 0, s>>>(x, n, out);
   return cudaGetLastError();
 }
 
-cudaError_t convert_matrix_64_to_32(const double2* src, long long lds, float2* dst, long long ldd, int rows,
-                                    int cols, cudaStream_t s) {
-  stats::Scope sc(stats::kMisc, s, 24.0 * rows * (double)cols);
-  convert_matrix_kernel<<<dim3((rows + 255) / 256, cols), 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
-  return cudaGetLastError();
-}
-
-cudaError_t convert_vec_64_to_32(const double2* src, float2* dst, int n, double scale, cudaStream_t s) {
-  stats::count(stats::kMisc);
-  convert_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(src, dst, n, scale);
-  return cudaGetLastError();
-}
-
-cudaError_t accumulate_vec_32_to_64(double2* x, const float2* d, int n, double scale, cudaStream_t s) {
-  stats::count(stats::kMisc);
-  accumulate_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(x, d, n, scale);
+cudaError_t convert_flat_64_to_32(const double2* src, float2* dst, size_t count, cudaStream_t s) {
+  stats::Scope sc(stats::kMisc, s, 24.0 * (double)count);
+  convert_flat_kernel<<<4 * 152, 256, 0, s>>>(src, dst, count);
   return cudaGetLastError();
 }
 
@@ -177,215 +197,874 @@ struct DevBuf {
   }
 };
 
-#define SWEEP_TRY(call)                                 \
-  do {                                                  \
-    cudaError_t _e = (call);                            \
+#define SWEEP_TRY(call)                                      \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
     if (_e != cudaSuccess) return wmom_fail_cuda(_e, #call); \
   } while (0)
 
-struct Scalars {
+// Per-matrix scalars of a group, one D2H per refinement step.
+struct GroupScalars {
+  double rnorm2[kMaxLuBatch];
+  double dnorm2[kMaxLuBatch];
+  double xnorm2[kMaxLuBatch];
   double vnorm2;
-  double rnorm2;
-  double dnorm2;  // last refinement correction
-  double xnorm2;  // solution before that correction
 };
 
+// Autotuned batch width per (order bucket, form).
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tuned;
+
+int env_batch() {
+  const char* e = std::getenv("WMOM_LU_BATCH");
+  if (!e) return 0;
+  const int b = std::atoi(e);
+  return (b >= 1 && b <= kMaxLuBatch) ? b : 0;
+}
+
 }  // namespace
+
+// Vectors, scalars and the FP64-fallback factor of one group of up to B matrices.
+struct GroupScratch {
+  int n = 0, B = 0;
+  cudaStream_t s = nullptr;
+  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv;
+  std::vector<double> vh;  // excitation on the host
+  double vnorm = 0.0;
+  GroupScalars hs{};
+};
+
+namespace {
+
+wmom_status scratch_init(GroupScratch* g, int n, int B, int ngap, float ampl, float phas, cudaStream_t s) {
+  g->n = n;
+  g->B = B;
+  g->s = s;
+  const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
+  g->vh.assign(2 * (size_t)n, 0.0);
+  wmom_status st = wmom_excitation(n, ngap, ampl, phas, g->vh.data());
+  if (st != WMOM_OK) return st;
+  SWEEP_TRY(g->vrep.alloc(sizeof(double2) * (size_t)n * B, s));
+  SWEEP_TRY(g->x64.alloc(sizeof(double2) * (size_t)n * B, s));
+  SWEEP_TRY(g->r64.alloc(sizeof(double2) * (size_t)n * B, s));
+  SWEEP_TRY(g->d32.alloc(sizeof(float2) * (size_t)n * B, s));
+  SWEEP_TRY(g->part.alloc(sizeof(double2) * (size_t)n * nchunks * B, s));
+  SWEEP_TRY(g->sc.alloc(sizeof(GroupScalars), s));
+  SWEEP_TRY(g->scal.alloc(sizeof(double) * 2 * kMaxLuBatch, s));
+  SWEEP_TRY(g->actv.alloc(sizeof(int) * kMaxLuBatch, s));
+  for (int b = 0; b < B; ++b)
+    SWEEP_TRY(cudaMemcpyAsync(g->vrep.as<double2>() + (size_t)b * n, g->vh.data(), sizeof(double2) * n,
+                              cudaMemcpyHostToDevice, s));
+  GroupScalars* dsc = g->sc.as<GroupScalars>();
+  SWEEP_TRY(sumsq_fp64(g->vrep.as<double2>(), n, &dsc->vnorm2, 1, s));
+  SWEEP_TRY(cudaMemcpyAsync(&g->hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+  SWEEP_TRY(cudaStreamSynchronize(s));
+  g->vnorm = std::sqrt(g->hs.vnorm2);
+  return WMOM_OK;
+}
+
+// relative residuals of x64[0..nb) against Z (nb matrices, contiguous)
+wmom_status group_residuals(GroupScratch& g, const double2* Z, int nb) {
+  const int n = g.n;
+  GroupScalars* dsc = g.sc.as<GroupScalars>();
+  SWEEP_TRY(residual_fp64(Z, n, (long long)n * n, g.x64.as<double2>(), g.vrep.as<double2>(), n,
+                          g.r64.as<double2>(), g.part.as<double2>(), nb, g.s));
+  SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dsc->rnorm2, nb, g.s));
+  SWEEP_TRY(cudaMemcpyAsync(&g.hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, g.s));
+  SWEEP_TRY(cudaStreamSynchronize(g.s));
+  return WMOM_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- GMRES-IR ----
+// Left-preconditioned restarted GMRES in FP64 on M^-1 Z d = M^-1 r with M = the FP32
+// LU factors: the refinement for systems too ill-conditioned for the plain FP32
+// correction (kappa * u_fp32 >~ 1), before resorting to the FP64 LU.
+
+// y = sum of the partial products (chunk order)
+__global__ void matvec_finish_kernel(const double2* __restrict__ partial, int nchunks, int n,
+                                     double2* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double re = 0.0, im = 0.0;
+  for (int c = 0; c < nchunks; ++c) {
+    const double2 p = partial[(size_t)c * n + i];
+    re += p.x;
+    im += p.y;
+  }
+  y[i] = make_double2(re, im);
+}
+
+// h[i] = conj(V_i) . w, one block per vector, fixed reduction order
+__global__ void __launch_bounds__(1024) cdot_many_kernel(const double2* __restrict__ V, int n,
+                                                         const double2* __restrict__ w, double2* __restrict__ h) {
+  __shared__ double sr[1024], si[1024];
+  const double2* v = V + (size_t)blockIdx.x * n;
+  double re = 0.0, im = 0.0;
+  for (int i = threadIdx.x; i < n; i += 1024) {
+    const double2 a = v[i], b = w[i];
+    re = fma(a.x, b.x, fma(a.y, b.y, re));
+    im = fma(a.x, b.y, fma(-a.y, b.x, im));
+  }
+  sr[threadIdx.x] = re;
+  si[threadIdx.x] = im;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) h[blockIdx.x] = make_double2(sr[0], si[0]);
+}
+
+// w -= sum_i h[i] V_i   (sign = -1)   or   w += sum_i h[i] V_i   (sign = +1)
+__global__ void caxpy_many_kernel(double2* __restrict__ w, const double2* __restrict__ V, int k, int n,
+                                  const double2* __restrict__ h, double sign) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double re = w[i].x, im = w[i].y;
+  for (int q = 0; q < k; ++q) {
+    const double2 c = h[q], v = V[(size_t)q * n + i];
+    re = fma(sign * c.x, v.x, fma(-sign * c.y, v.y, re));
+    im = fma(sign * c.x, v.y, fma(sign * c.y, v.x, im));
+  }
+  w[i] = make_double2(re, im);
+}
+
+__global__ void rscale_kernel(const double2* __restrict__ w, double2* __restrict__ v, int n, double s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = make_double2(w[i].x * s, w[i].y * s);
+}
+
+namespace {
+
+struct Cplx {
+  double re, im;
+};
+inline Cplx cm(Cplx a, Cplx b) { return Cplx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+inline Cplx cconj(Cplx a) { return Cplx{a.re, -a.im}; }
+inline double cabsd(Cplx a) { return std::hypot(a.re, a.im); }
+
+}  // namespace
+
+// d = GMRES(m) solution of M^-1 Z d = M^-1 r for ONE matrix.  z/lu/ipiv address that
+// matrix; r (device, n) is the right-hand side; d (device, n) receives the
+// correction.  Returns the inner steps taken in *steps.
+wmom_status gmres_correction(int n, const double2* Z, const float2* lu, const int* ipiv, const double2* r,
+                             double2* d, LuWorkspace* ws, cudaStream_t s, int m, int max_cycles, double inner_tol,
+                             int* steps) {
+  const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
+  DevBuf V, w, part, h, f32, nrm;
+  SWEEP_TRY(V.alloc(sizeof(double2) * (size_t)n * (m + 1), s));
+  SWEEP_TRY(w.alloc(sizeof(double2) * n, s));
+  SWEEP_TRY(part.alloc(sizeof(double2) * (size_t)n * nchunks, s));
+  SWEEP_TRY(h.alloc(sizeof(double2) * (m + 2) * 2, s));
+  SWEEP_TRY(f32.alloc(sizeof(float2) * n, s));
+  SWEEP_TRY(nrm.alloc(sizeof(double) * 2, s));
+  const unsigned vb = (unsigned)((n + 255) / 256);
+  double2* Vp = V.as<double2>();
+  double2* wp = w.as<double2>();
+  double2* hp = h.as<double2>();
+  double* np_ = nrm.as<double>();
+  // preconditioner: dst = M^-1 src (FP32 solve of the src scaled into range)
+  auto precond = [&](const double2* src, double2* dst) -> wmom_status {
+    double ss = 0.0;
+    SWEEP_TRY(sumsq_fp64(src, n, np_, 1, s));
+    SWEEP_TRY(cudaMemcpyAsync(&ss, np_, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SWEEP_TRY(cudaStreamSynchronize(s));
+    const double rn = std::sqrt(ss);
+    const double scl = (rn > 0 && std::isfinite(rn)) ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
+    DevBuf sc2;
+    SWEEP_TRY(sc2.alloc(sizeof(double) * 2, s));
+    const double hsc[2] = {scl, 1.0 / scl};
+    SWEEP_TRY(cudaMemcpyAsync(sc2.p, hsc, sizeof(hsc), cudaMemcpyHostToDevice, s));
+    stats::count(stats::kMisc, 2);
+    convert_vec_kernel<<<vb, 256, 0, s>>>(src, f32.as<float2>(), n, 1, sc2.as<double>());
+    SWEEP_TRY(lu_solve_t<float2>(lu, n, n, ipiv, f32.as<float2>(), n, 1, ws, s, 1, 0));
+    widen_vec_kernel<<<vb, 256, 0, s>>>(f32.as<float2>(), dst, (size_t)n);
+    rscale_kernel<<<vb, 256, 0, s>>>(dst, dst, n, 1.0 / scl);
+    SWEEP_TRY(cudaStreamSynchronize(s));  // hsc lives on this frame
+    return cudaGetLastError() == cudaSuccess ? WMOM_OK : WMOM_ERR_CUDA;
+  };
+  auto norm = [&](const double2* x, double* out) -> wmom_status {
+    SWEEP_TRY(sumsq_fp64(x, n, np_, 1, s));
+    double ss = 0.0;
+    SWEEP_TRY(cudaMemcpyAsync(&ss, np_, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SWEEP_TRY(cudaStreamSynchronize(s));
+    *out = std::sqrt(ss);
+    return WMOM_OK;
+  };
+  SWEEP_TRY(cudaMemsetAsync(d, 0, sizeof(double2) * n, s));
+  *steps = 0;
+  // initial residual of the preconditioned system for d = 0: M^-1 r
+  DevBuf r0;
+  SWEEP_TRY(r0.alloc(sizeof(double2) * n, s));
+  SWEEP_TRY(cudaMemcpyAsync(r0.p, r, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  double beta0 = -1.0;
+  for (int cycle = 0; cycle < max_cycles; ++cycle) {
+    wmom_status st = precond(r0.as<double2>(), wp);
+    if (st != WMOM_OK) return st;
+    double beta = 0.0;
+    st = norm(wp, &beta);
+    if (st != WMOM_OK) return st;
+    if (beta0 < 0) beta0 = beta;
+    if (!(beta > 0) || beta <= inner_tol * beta0) break;
+    stats::count(stats::kMisc);
+    rscale_kernel<<<vb, 256, 0, s>>>(wp, Vp, n, 1.0 / beta);
+    std::vector<Cplx> H((size_t)(m + 1) * m, Cplx{0, 0}), g(m + 1, Cplx{0, 0});
+    std::vector<double> cs(m);
+    std::vector<Cplx> sn(m);
+    g[0] = Cplx{beta, 0.0};
+    int jlast = -1;
+    for (int j = 0; j < m; ++j) {
+      // w = M^-1 Z v_j
+      stats::count(stats::kMisc, 1);
+      {
+        stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n, 1);
+        gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks, 1), kGemvRows, 0, s>>>(
+            Z, n, 0, Vp + (size_t)j * n, n, part.as<double2>());
+      }
+      matvec_finish_kernel<<<vb, 256, 0, s>>>(part.as<double2>(), nchunks, n, wp);
+      st = precond(wp, wp);
+      if (st != WMOM_OK) return st;
+      // classical Gram-Schmidt, twice
+      std::vector<double2> hh(2 * (j + 1));
+      stats::count(stats::kMisc, 4);
+      cdot_many_kernel<<<j + 1, 1024, 0, s>>>(Vp, n, wp, hp);
+      caxpy_many_kernel<<<vb, 256, 0, s>>>(wp, Vp, j + 1, n, hp, -1.0);
+      cdot_many_kernel<<<j + 1, 1024, 0, s>>>(Vp, n, wp, hp + (m + 2));
+      caxpy_many_kernel<<<vb, 256, 0, s>>>(wp, Vp, j + 1, n, hp + (m + 2), -1.0);
+      SWEEP_TRY(cudaMemcpyAsync(hh.data(), hp, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, s));
+      SWEEP_TRY(cudaMemcpyAsync(hh.data() + (j + 1), hp + (m + 2), sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost,
+                                s));
+      double hn = 0.0;
+      st = norm(wp, &hn);
+      if (st != WMOM_OK) return st;
+      for (int i = 0; i <= j; ++i)
+        H[(size_t)i * m + j] = Cplx{hh[i].x + hh[j + 1 + i].x, hh[i].y + hh[j + 1 + i].y};
+      H[(size_t)(j + 1) * m + j] = Cplx{hn, 0.0};
+      // previous rotations, then a new one zeroing H[j+1][j]
+      for (int i = 0; i < j; ++i) {
+        const Cplx a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+        const Cplx t1 = Cplx{cs[i] * a.re + (sn[i].re * b.re - sn[i].im * b.im), cs[i] * a.im + (sn[i].re * b.im + sn[i].im * b.re)};
+        const Cplx cb = cm(cconj(sn[i]), a);
+        H[(size_t)(i + 1) * m + j] = Cplx{-cb.re + cs[i] * b.re, -cb.im + cs[i] * b.im};
+        H[(size_t)i * m + j] = t1;
+      }
+      const Cplx a = H[(size_t)j * m + j];
+      const double bb = hn, aa = cabsd(a);
+      const double rr = std::hypot(aa, bb);
+      if (rr == 0.0) {
+        jlast = j - 1;
+        break;
+      }
+      cs[j] = aa / rr;
+      sn[j] = aa > 0 ? Cplx{(a.re / aa) * bb / rr, (a.im / aa) * bb / rr} : Cplx{1.0, 0.0};
+      // with this phase choice the rotated entry is (a/|a|) * rr
+      H[(size_t)j * m + j] = aa > 0 ? Cplx{a.re / aa * rr, a.im / aa * rr} : Cplx{rr, 0.0};
+      H[(size_t)(j + 1) * m + j] = Cplx{0.0, 0.0};
+      const Cplx gj = g[j];
+      g[j + 1] = Cplx{-(sn[j].re * gj.re + sn[j].im * gj.im) / 1.0, -(sn[j].re * gj.im - sn[j].im * gj.re)};
+      g[j] = Cplx{cs[j] * gj.re, cs[j] * gj.im};
+      // keep the rotation consistent: g_{j+1} = -conj(s) g_j, g_j = c g_j
+      ++*steps;
+      jlast = j;
+      const double resid = cabsd(g[j + 1]);
+      if (resid <= inner_tol * beta0 || hn == 0.0) break;
+      if (j + 1 < m) {
+        stats::count(stats::kMisc);
+        rscale_kernel<<<vb, 256, 0, s>>>(wp, Vp + (size_t)(j + 1) * n, n, 1.0 / hn);
+      }
+    }
+    if (jlast < 0) break;
+    // y = H^-1 g (upper triangular), d += V y
+    const int k = jlast + 1;
+    std::vector<Cplx> y(k);
+    for (int i = k - 1; i >= 0; --i) {
+      Cplx acc = g[i];
+      for (int q = i + 1; q < k; ++q) {
+        const Cplx t = cm(H[(size_t)i * m + q], y[q]);
+        acc = Cplx{acc.re - t.re, acc.im - t.im};
+      }
+      const Cplx hd = H[(size_t)i * m + i];
+      const double den = hd.re * hd.re + hd.im * hd.im;
+      y[i] = Cplx{(acc.re * hd.re + acc.im * hd.im) / den, (acc.im * hd.re - acc.re * hd.im) / den};
+    }
+    std::vector<double2> yd(k);
+    for (int i = 0; i < k; ++i) yd[i] = make_double2(y[i].re, y[i].im);
+    SWEEP_TRY(cudaMemcpyAsync(hp, yd.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, s));
+    stats::count(stats::kMisc);
+    caxpy_many_kernel<<<vb, 256, 0, s>>>(d, Vp, k, n, hp, +1.0);
+    SWEEP_TRY(cudaStreamSynchronize(s));  // yd lives on this frame
+    // next cycle: r0 = r - Z d (FP64)
+    SWEEP_TRY(residual_fp64(Z, n, 0, d, r, n, r0.as<double2>(), part.as<double2>(), 1, s));
+    double cur = 0.0;
+    st = precond(r0.as<double2>(), wp);
+    if (st != WMOM_OK) return st;
+    st = norm(wp, &cur);
+    if (st != WMOM_OK) return st;
+    if (cur <= inner_tol * beta0) break;
+  }
+  return WMOM_OK;
+}
+
+// Factorises bg matrices Z64 (contiguous).  Mixed: FP32 copy into lu32, tensor-core
+// LU; FP64: copy into lu64, FP64 LU.  info[b] = LAPACK info of matrix b.  When ms
+// is given the factorisation is timed with events on the stream.
+// A captured factorisation (CUDA graph) of one (order, batch, buffers) combination:
+// every group of a sweep factors into the same buffers, so the whole launch sequence
+// of the blocked LU (a cooperative panel launch, interchanges, triangular solve and
+// tensor-core update per panel) is captured once and replayed per group.
+struct FactorGraph {
+  cudaGraphExec_t exec = nullptr;
+  int mode = -1, n = 0, bg = 0;
+  const void* lu = nullptr;
+  const int* ipiv = nullptr;
+  const float* tc_buf = nullptr;  // tensor-core scratch the capture used
+  unsigned tc_gen = 0;
+  bool failed = false;  // capture unsupported here: launch directly
+  long long launches[stats::kNumCls] = {};  // kernel launches of one replay
+  ~FactorGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+namespace {
+bool graphs_enabled() {
+  const char* e = std::getenv("WMOM_NO_GRAPHS");
+  return !(e && e[0] == '1');
+}
+}  // namespace
+
+wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu32, double2* lu64, int* ipiv,
+                         LuWorkspace* ws, cudaStream_t s, int* info, float* ms, FactorGraph* graph) {
+  const size_t nn = (size_t)n * n;
+  SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
+  if (mode == WMOM_MODE_MIXED)
+    SWEEP_TRY(convert_flat_64_to_32(Z64, lu32, nn * bg, s));
+  else
+    SWEEP_TRY(cudaMemcpyAsync(lu64, Z64, sizeof(double2) * nn * bg, cudaMemcpyDeviceToDevice, s));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ms) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+  }
+  const GemmHook<float2> hook32 = tc_gemm_hook();
+  const void* lu = mode == WMOM_MODE_MIXED ? (const void*)lu32 : (const void*)lu64;
+  auto direct = [&]() -> cudaError_t {
+    return mode == WMOM_MODE_MIXED ? lu_factor_t<float2>(lu32, n, n, ipiv, ws, s, hook32, bg, (long long)nn)
+                                   : lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, nullptr, bg, (long long)nn);
+  };
+  cudaError_t fe = cudaSuccess;
+  if (graph && graph->exec && (graph->tc_buf != ws->tc_buf || graph->tc_gen != ws->tc_gen)) {
+    // the scratch was reallocated since the capture: capture again on the next use
+    cudaGraphExecDestroy(graph->exec);
+    graph->exec = nullptr;
+  }
+  if (graph && graph->exec && graph->mode == mode && graph->n == n && graph->bg == bg && graph->lu == lu &&
+      graph->ipiv == ipiv) {
+    stats::add_counts(graph->launches);
+    fe = cudaGraphLaunch(graph->exec, s);
+  } else if (graph && !graph->failed && graphs_enabled() && graph->mode == mode && graph->n == n &&
+             graph->bg == bg && graph->lu == lu && graph->ipiv == ipiv) {
+    // second use of these buffers: capture the sequence, then replay it from now on
+    cudaGraph_t g = nullptr;
+    long long before[stats::kNumCls], after[stats::kNumCls];
+    stats::snapshot(before);
+    fe = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (fe == cudaSuccess) {
+      const cudaError_t ce = direct();
+      fe = cudaStreamEndCapture(s, &g);
+      if (ce != cudaSuccess) fe = ce;
+    }
+    stats::snapshot(after);
+    for (int i = 0; i < stats::kNumCls; ++i) graph->launches[i] = after[i] - before[i];
+    if (fe == cudaSuccess) fe = cudaGraphInstantiate(&graph->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    graph->tc_buf = ws->tc_buf;
+    graph->tc_gen = ws->tc_gen;
+    if (fe == cudaSuccess) {
+      fe = cudaGraphLaunch(graph->exec, s);
+    } else {
+      // the capture counted launches that never ran
+      for (int i = 0; i < stats::kNumCls; ++i) graph->launches[i] = -graph->launches[i];
+      stats::add_counts(graph->launches);
+      cudaGetLastError();  // clear the capture error, launch directly from now on
+      graph->failed = true;
+      if (graph->exec) {
+        cudaGraphExecDestroy(graph->exec);
+        graph->exec = nullptr;
+      }
+      fe = direct();
+    }
+  } else {
+    if (graph && !graph->exec) {
+      // remember the shape; the next group with the same shape is captured
+      graph->mode = mode;
+      graph->n = n;
+      graph->bg = bg;
+      graph->lu = lu;
+      graph->ipiv = ipiv;
+    }
+    fe = direct();
+  }
+  if (ms) {
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t");
+  int err = lu_workspace_read_status(ws, info, s, bg);
+  if (mode == WMOM_MODE_MIXED && hook32) err |= tc::read_and_clear_error(ws, s);
+  SWEEP_TRY(cudaGetLastError());
+  return err ? WMOM_ERR_TIMEOUT : WMOM_OK;
+}
+
+// Solves bg systems Z64[b] x = V with the factors of factor_group; the solutions end
+// in g.x64[0..bg).  Mixed: FP32 solve, FP64 refinement with a per-matrix activity
+// mask, FP64 LU for the matrices that stall.
+wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float2* lu32, const double2* lu64,
+                        const int* ipiv, const int* info, double tol, LuWorkspace* ws, GroupScratch& g,
+                        wmom_report* rep) {
+  const size_t nn = (size_t)n * n;
+  cudaStream_t s = g.s;
+  GroupScalars& hs = g.hs;
+  GroupScalars* dsc = g.sc.as<GroupScalars>();
+  for (int b = 0; b < bg; ++b) {
+    rep[b] = wmom_report{};
+    rep[b].rel_residual = -1.0;
+    rep[b].info = info[b];
+  }
+  if (mode == WMOM_MODE_FP64) {
+    SWEEP_TRY(cudaMemcpyAsync(g.x64.p, g.vrep.p, sizeof(double2) * n * bg, cudaMemcpyDeviceToDevice, s));
+    SWEEP_TRY(lu_solve_t<double2>(lu64, n, n, ipiv, g.x64.as<double2>(), n, 1, ws, s, bg, (long long)nn));
+    const wmom_status rs = group_residuals(g, Z64, bg);
+    if (rs != WMOM_OK) return rs;
+    for (int b = 0; b < bg; ++b) {
+      rep[b].status = info[b] ? WMOM_ERR_SINGULAR : WMOM_OK;
+      rep[b].rel_residual = std::sqrt(hs.rnorm2[b]) / g.vnorm;
+    }
+    return WMOM_OK;
+  }
+  bool fallback[kMaxLuBatch] = {}, active[kMaxLuBatch] = {};
+  int stall[kMaxLuBatch] = {};
+  double prev[kMaxLuBatch];
+  for (int b = 0; b < bg; ++b) {
+    fallback[b] = info[b] != 0;
+    active[b] = !fallback[b];
+    prev[b] = HUGE_VAL;
+  }
+  const unsigned vgrid = (unsigned)(((size_t)n * bg + 255) / 256);
+  // initial solve in FP32
+  stats::count(stats::kMisc, 2);
+  convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
+  SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+  widen_vec_kernel<<<vgrid, 256, 0, s>>>(g.d32.as<float2>(), g.x64.as<double2>(), (size_t)n * bg);
+  SWEEP_TRY(cudaGetLastError());
+  std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
+  std::vector<int> hact(kMaxLuBatch, 0);
+  const int max_it = 40;
+  for (int it = 0;; ++it) {
+    const wmom_status rs = group_residuals(g, Z64, bg);
+    if (rs != WMOM_OK) return rs;
+    int nact = 0;
+    for (int b = 0; b < bg; ++b) {
+      if (!active[b]) continue;
+      const double rel = std::sqrt(hs.rnorm2[b]) / g.vnorm;
+      rep[b].rel_residual = rel;
+      rep[b].iterations = it;
+      // converged: the target is met, or the last correction no longer changes the
+      // solution at FP64 resolution (systems whose FP64 residual floor lies above
+      // the target); stalled or diverged: FP64 fallback
+      const double corr = it > 0 ? std::sqrt(hs.dnorm2[b] / hs.xnorm2[b]) : HUGE_VAL;
+      if (!(rel == rel)) {
+        fallback[b] = true;
+        active[b] = false;
+      } else if (rel <= tol || corr <= 0x1p-48) {
+        active[b] = false;
+      } else if (rel > 0.5 * prev[b] && ++stall[b] >= 2) {
+        fallback[b] = true;
+        active[b] = false;
+      } else if (it >= max_it) {
+        fallback[b] = true;
+        active[b] = false;
+      } else {
+        if (rel <= 0.5 * prev[b]) stall[b] = 0;
+        prev[b] = std::min(prev[b], rel);
+        ++nact;
+      }
+    }
+    if (nact == 0) break;
+    // correction d = (LU32)^-1 r per active matrix, scaled by a power of two
+    for (int b = 0; b < bg; ++b) {
+      const double rn = std::sqrt(hs.rnorm2[b]);
+      const double scl = (active[b] && rn > 0 && std::isfinite(rn)) ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
+      hscale[b] = scl;
+      hscale[kMaxLuBatch + b] = 1.0 / scl;
+      hact[b] = active[b] ? 1 : 0;
+    }
+    SWEEP_TRY(cudaMemcpyAsync(g.scal.p, hscale.data(), sizeof(double) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+    SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+    const double* dscale = g.scal.as<double>();
+    const double* dinv = dscale + kMaxLuBatch;
+    stats::count(stats::kMisc, 4);
+    convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
+    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+    sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
+    sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);
+    accumulate_vec_kernel<<<vgrid, 256, 0, s>>>(g.x64.as<double2>(), g.d32.as<float2>(), n, bg, dinv,
+                                                g.actv.as<int>());
+    SWEEP_TRY(cudaGetLastError());
+  }
+  int tmp_info[kMaxLuBatch];
+  if (lu_workspace_read_status(ws, tmp_info, s, 1)) return WMOM_ERR_TIMEOUT;
+  // GMRES-IR for the matrices whose plain refinement stalled (their FP32 factors are
+  // still a good preconditioner); the FP64 LU only if that stalls as well
+  for (int b = 0; b < bg; ++b) {
+    if (!fallback[b] || info[b] != 0) continue;
+    double2* xb = g.x64.as<double2>() + (size_t)b * n;
+    const double2* Zb = Z64 + (size_t)b * nn;
+    const float2* lub = lu32 + (size_t)b * nn;
+    const int* ipb = ipiv + (size_t)b * n;
+    DevBuf dv;
+    SWEEP_TRY(dv.alloc(sizeof(double2) * n, s));
+    // budget: a correction must cut the residual by kKrylovGain, else the FP32
+    // factors are too poor a preconditioner here and the FP64 LU takes over
+    constexpr double kKrylovGain = 1e-2;
+    double prevr = HUGE_VAL, corr = HUGE_VAL;
+    bool ok = false;
+    for (int outer = 0; outer < 6; ++outer) {
+      SWEEP_TRY(residual_fp64(Zb, n, 0, xb, g.vrep.as<double2>(), n, g.r64.as<double2>(), g.part.as<double2>(), 1,
+                              s));
+      SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dsc->rnorm2, 1, s));
+      SWEEP_TRY(sumsq_fp64(xb, n, dsc->xnorm2, 1, s));
+      SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+      SWEEP_TRY(cudaStreamSynchronize(s));
+      const double rel = std::sqrt(hs.rnorm2[0]) / g.vnorm;
+      if (!(rel == rel)) {
+        // diverged plain refinement: start the Krylov refinement from zero
+        SWEEP_TRY(cudaMemsetAsync(xb, 0, sizeof(double2) * n, s));
+        prevr = HUGE_VAL;
+        continue;
+      }
+      rep[b].rel_residual = rel;
+      if (rel <= tol || corr <= 0x1p-48) {
+        ok = true;
+        break;
+      }
+      if (rel > kKrylovGain * prevr) break;
+      prevr = rel;
+      int steps = 0;
+      const wmom_status gs = gmres_correction(n, Zb, lub, ipb, g.r64.as<double2>(), dv.as<double2>(), ws, s, 30, 2,
+                                              1e-10, &steps);
+      if (gs != WMOM_OK) return gs;
+      rep[b].krylov_steps += steps;
+      rep[b].iterations += 1;
+      const double xn = std::sqrt(hs.xnorm2[0]);
+      SWEEP_TRY(sumsq_fp64(dv.as<double2>(), n, dsc->dnorm2, 1, s));
+      SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+      SWEEP_TRY(cudaStreamSynchronize(s));
+      corr = xn > 0 ? std::sqrt(hs.dnorm2[0]) / xn : HUGE_VAL;
+      // x += d
+      stats::count(stats::kMisc);
+      std::vector<double2> onec(1, make_double2(1.0, 0.0));
+      DevBuf cbuf;
+      SWEEP_TRY(cbuf.alloc(sizeof(double2), s));
+      SWEEP_TRY(cudaMemcpyAsync(cbuf.p, onec.data(), sizeof(double2), cudaMemcpyHostToDevice, s));
+      caxpy_many_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(xb, dv.as<double2>(), 1, n, cbuf.as<double2>(),
+                                                                    +1.0);
+      SWEEP_TRY(cudaStreamSynchronize(s));
+    }
+    if (ok) fallback[b] = false;
+  }
+  for (int b = 0; b < bg; ++b)
+    if (!fallback[b]) rep[b].status = WMOM_OK;
+  // FP64 fallback, one matrix at a time, in the scratch factor buffer
+  for (int b = 0; b < bg; ++b) {
+    if (!fallback[b]) continue;
+    rep[b].fell_back = 1;
+    if (!g.fb_lu.p) {
+      SWEEP_TRY(g.fb_lu.alloc(sizeof(double2) * nn, s));
+      SWEEP_TRY(g.fb_ipiv.alloc(sizeof(int) * n, s));
+    }
+    int inf1 = 0;
+    const wmom_status fst = factor_group(WMOM_MODE_FP64, n, Z64 + (size_t)b * nn, 1, nullptr,
+                                         g.fb_lu.as<double2>(), g.fb_ipiv.as<int>(), ws, s, &inf1, nullptr, nullptr);
+    if (fst != WMOM_OK) return fst;
+    // solve into slot b: move the vector through x64[0]
+    DevBuf keep;
+    SWEEP_TRY(keep.alloc(sizeof(double2) * n, s));
+    SWEEP_TRY(cudaMemcpyAsync(keep.p, g.x64.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    SWEEP_TRY(cudaMemcpyAsync(g.x64.p, g.vrep.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    SWEEP_TRY(lu_solve_t<double2>(g.fb_lu.as<double2>(), n, n, g.fb_ipiv.as<int>(), g.x64.as<double2>(), n, 1, ws,
+                                  s, 1, (long long)nn));
+    const wmom_status rs = group_residuals(g, Z64 + (size_t)b * nn, 1);
+    if (rs != WMOM_OK) return rs;
+    rep[b].rel_residual = std::sqrt(hs.rnorm2[0]) / g.vnorm;
+    rep[b].info = inf1;
+    rep[b].status = inf1 ? WMOM_ERR_SINGULAR : WMOM_OK;
+    if (b != 0) {
+      SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)b * n, g.x64.p, sizeof(double2) * n,
+                                cudaMemcpyDeviceToDevice, s));
+      SWEEP_TRY(cudaMemcpyAsync(g.x64.p, keep.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  return WMOM_OK;
+}
+
+namespace {
+
+// Currents / Z_in / reports of a solved group to the caller's host arrays.
+wmom_status group_results(GroupScratch& g, int bg, int ngap, const wmom_report* rep, int f, double* currents,
+                          double* zin, wmom_report* reports, wmom_status* overall) {
+  const int n = g.n;
+  std::vector<double2> xh((size_t)n * bg);
+  if (currents) {
+    SWEEP_TRY(cudaMemcpyAsync(currents + 2 * (size_t)f * n, g.x64.p, sizeof(double2) * (size_t)n * bg,
+                              cudaMemcpyDeviceToHost, g.s));
+    SWEEP_TRY(cudaStreamSynchronize(g.s));
+    std::memcpy(xh.data(), currents + 2 * (size_t)f * n, sizeof(double2) * (size_t)n * bg);
+  } else {
+    for (int b = 0; b < bg; ++b)
+      SWEEP_TRY(cudaMemcpyAsync(xh.data() + (size_t)b * n + (ngap - 1), g.x64.as<double2>() + (size_t)b * n + (ngap - 1),
+                                sizeof(double2), cudaMemcpyDeviceToHost, g.s));
+    SWEEP_TRY(cudaStreamSynchronize(g.s));
+  }
+  for (int b = 0; b < bg; ++b) {
+    if (zin) {
+      // Z_in = V[ngap-1] / I[ngap-1], Smith's formula
+      const double vr = g.vh[2 * (ngap - 1)], vi = g.vh[2 * (ngap - 1) + 1];
+      const double br = xh[(size_t)b * n + ngap - 1].x, bi = xh[(size_t)b * n + ngap - 1].y;
+      double zr, zi;
+      if (std::fabs(br) >= std::fabs(bi)) {
+        const double r = bi / br, d = br + bi * r;
+        zr = (vr + vi * r) / d;
+        zi = (vi - vr * r) / d;
+      } else {
+        const double r = br / bi, d = bi + br * r;
+        zr = (vr * r + vi) / d;
+        zi = (vi * r - vr) / d;
+      }
+      zin[2 * (size_t)(f + b)] = zr;
+      zin[2 * (size_t)(f + b) + 1] = zi;
+    }
+    if (rep[b].status != WMOM_OK && *overall == WMOM_OK) *overall = (wmom_status)rep[b].status;
+    if (reports) reports[f + b] = rep[b];
+  }
+  return WMOM_OK;
+}
+
+// Fills nk matrices (frequencies freq[0..nk)) into Z and adds the plan's loads.
+wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cudaStream_t s) {
+  const int n = p.npls;
+  const size_t nn = (size_t)n * n;
+  const double pi = std::acos(-1.0);
+  std::vector<double> fph(3 * (size_t)nk);
+  for (int i = 0; i < nk; ++i) {
+    const double ka = ka_from_mhz(freq[i]);
+    const double eta0 = 120. * pi;
+    fph[3 * i] = ka;
+    fph[3 * i + 1] = ka * ka;
+    fph[3 * i + 2] = eta0 / (4.0 * pi * ka);
+  }
+  DevBuf fpb;
+  SWEEP_TRY(fpb.alloc(sizeof(double) * 3 * nk, s));
+  SWEEP_TRY(cudaMemcpyAsync(fpb.p, fph.data(), sizeof(double) * 3 * nk, cudaMemcpyHostToDevice, s));
+  SWEEP_TRY(launch_fill(p, fpb.as<double>(), nk, Z, n, (long long)nn, s));
+  if (!p.load_idx.empty()) {
+    // R + j*2*pi*f[MHz]*L[uH] on the loaded diagonal entries (REF/Wire_MoM.cu:346-363)
+    const int nl = (int)p.load_idx.size();
+    std::vector<double2> lv((size_t)nk * nl);
+    for (int i = 0; i < nk; ++i)
+      for (int l = 0; l < nl; ++l)
+        lv[(size_t)i * nl + l] = make_double2(p.load_r[l], 2. * pi * freq[i] * p.load_l_uh[l]);
+    DevBuf li, lvd;
+    SWEEP_TRY(li.alloc(sizeof(int) * nl, s));
+    SWEEP_TRY(lvd.alloc(sizeof(double2) * lv.size(), s));
+    SWEEP_TRY(cudaMemcpyAsync(li.p, p.load_idx.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
+    SWEEP_TRY(cudaMemcpyAsync(lvd.p, lv.data(), sizeof(double2) * lv.size(), cudaMemcpyHostToDevice, s));
+    stats::count(stats::kMisc);
+    add_loads_kernel<<<(nk + 127) / 128, 128, 0, s>>>(Z, n, (long long)nn, li.as<int>(), lvd.as<double2>(), nl, nk);
+    SWEEP_TRY(cudaGetLastError());
+  }
+  SWEEP_TRY(cudaStreamSynchronize(s));  // host staging vectors end with this scope
+  return WMOM_OK;
+}
+
+}  // namespace
+
+// Batch width: env override, else the autotuned value for (order bucket, form),
+// else tuned now on Z64 (the first matrix of the work) by timing 1, 2, 4, ...
+wmom_status choose_batch(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
+                         size_t budget, int* out) {
+  const size_t nn = (size_t)n * n;
+  const size_t mat = mode == WMOM_MODE_MIXED ? sizeof(float2) * nn : sizeof(double2) * nn;
+  int bmax = std::min({ws->max_batch, kMaxLuBatch, limit,
+                       mode == WMOM_MODE_MIXED ? lu_max_batch<float2>(n) : lu_max_batch<double2>(n)});
+  while (bmax > 1 && (size_t)bmax * mat > budget / 4) bmax /= 2;
+  bmax = std::max(bmax, 1);
+  const int eb = env_batch();
+  if (eb) {
+    *out = std::min(eb, bmax);
+    return WMOM_OK;
+  }
+  const std::pair<int, int> key{(n + 255) / 256, mode};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      *out = std::min(it->second, bmax);
+      return WMOM_OK;
+    }
+  }
+  if (bmax == 1 || mode != WMOM_MODE_MIXED) {
+    // the FP64 form is bound by the FP64 pipe at every width worth batching
+    *out = mode == WMOM_MODE_MIXED ? 1 : (n <= 2048 ? bmax : 1);
+    return WMOM_OK;
+  }
+  int best_b = 1;
+  float best_t = 1e30f;
+  DevBuf rep64, lu, piv;
+  SWEEP_TRY(rep64.alloc(sizeof(double2) * nn * bmax, s));
+  SWEEP_TRY(lu.alloc(sizeof(float2) * nn * bmax, s));
+  SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * bmax, s));
+  for (int b = 0; b < bmax; ++b)
+    SWEEP_TRY(cudaMemcpyAsync(rep64.as<double2>() + (size_t)b * nn, Z64, sizeof(double2) * nn,
+                              cudaMemcpyDeviceToDevice, s));
+  for (int cand = 1; cand <= bmax; cand *= 2) {
+    float ms = 0.f;
+    int info[kMaxLuBatch];
+    const wmom_status st = factor_group(mode, n, rep64.as<double2>(), cand, lu.as<float2>(), nullptr,
+                                        piv.as<int>(), ws, s, info, &ms, nullptr);
+    if (st != WMOM_OK) return st;
+    const float per = ms / cand;
+    if (per < best_t * 0.95f) {
+      best_t = per;
+      best_b = cand;
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best_b;
+  }
+  *out = best_b;
+  return WMOM_OK;
+}
 
 wmom_status run_sweep(const SweepArgs& a) {
   const Plan& p = *a.plan;
   const int n = p.npls;
   cudaStream_t s = a.stream;
-  const size_t mat64 = sizeof(double2) * (size_t)n * n;
-  const size_t mat32 = sizeof(float2) * (size_t)n * n;
+  const bool mixed = a.mode == WMOM_MODE_MIXED;
+  const size_t nn = (size_t)n * n;
+  const size_t mat64 = sizeof(double2) * nn;
+  const size_t mat32 = sizeof(float2) * nn;
   size_t budget = a.mem_budget;
   if (budget == 0) {
     size_t fr = 0, tot = 0;
     SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
     budget = fr / 2;
   }
-  const size_t fixed = mat64 + (a.mode == WMOM_MODE_MIXED ? mat32 : 0);
-  if (budget < fixed + mat64) return WMOM_ERR_NOMEM;
-  const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)a.nfreq, (budget - fixed) / mat64));
-
-  // excitation
-  std::vector<double> vh(2 * (size_t)n);
-  wmom_status st = wmom_excitation(n, a.ngap, a.ampl, a.phas_deg, vh.data());
-  if (st != WMOM_OK) return st;
-
-  DevBuf zall, zf, z32, ipiv, v64, x64, r64, d32, part, fpb, sc;
-  SWEEP_TRY(zall.alloc(mat64 * batch, s));
-  SWEEP_TRY(zf.alloc(mat64, s));
-  if (a.mode == WMOM_MODE_MIXED) SWEEP_TRY(z32.alloc(mat32, s));
-  SWEEP_TRY(ipiv.alloc(sizeof(int) * n, s));
-  SWEEP_TRY(v64.alloc(sizeof(double2) * n, s));
-  SWEEP_TRY(x64.alloc(sizeof(double2) * n, s));
-  SWEEP_TRY(r64.alloc(sizeof(double2) * n, s));
-  SWEEP_TRY(d32.alloc(sizeof(float2) * n, s));
-  const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
-  SWEEP_TRY(part.alloc(sizeof(double2) * (size_t)n * nchunks, s));
-  SWEEP_TRY(fpb.alloc(sizeof(double) * 3 * batch, s));
-  SWEEP_TRY(sc.alloc(sizeof(Scalars), s));
-  SWEEP_TRY(cudaMemcpyAsync(v64.p, vh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, s));
-  SWEEP_TRY(sumsq_fp64(v64.as<double2>(), n, &sc.as<Scalars>()->vnorm2, s));
-  Scalars hs{};
-  SWEEP_TRY(cudaMemcpyAsync(&hs, sc.p, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-  SWEEP_TRY(cudaStreamSynchronize(s));
-  const double vnorm = std::sqrt(hs.vnorm2);
-
-  const GemmHook<float2> hook32 = tc_gemm_hook();
-  std::vector<double> fph(3 * (size_t)batch);
-  std::vector<double2> xh(n);
-  const double pi = std::acos(-1.0);
+  // first fill batch: at least one matrix, so the batch width can be tuned on it
+  const size_t reserve = (size_t)kMaxLuBatch * (mixed ? mat32 : mat64);
+  if (budget < reserve + 2 * mat64) return WMOM_ERR_NOMEM;
+  int nbf = (int)std::max<size_t>(1, std::min<size_t>((size_t)a.nfreq, (budget - reserve) / mat64));
+  DevBuf zall;
+  SWEEP_TRY(zall.alloc(mat64 * nbf, s));
   wmom_status overall = WMOM_OK;
-
-  auto factor64 = [&](const double2* Zk, int* info) -> wmom_status {
-    SWEEP_TRY(cudaMemcpyAsync(zf.p, Zk, mat64, cudaMemcpyDeviceToDevice, s));
-    SWEEP_TRY(lu_workspace_reset_barrier(a.ws, s));
-    SWEEP_TRY(lu_factor_t<double2>(zf.as<double2>(), n, n, ipiv.as<int>(), a.ws, s, nullptr));
-    const int err = lu_workspace_read_status(a.ws, info, s);
-    SWEEP_TRY(cudaGetLastError());
-    if (err) return WMOM_ERR_TIMEOUT;
-    SWEEP_TRY(cudaMemcpyAsync(x64.p, v64.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-    SWEEP_TRY(lu_solve_t<double2>(zf.as<double2>(), n, n, ipiv.as<int>(), x64.as<double2>(), n, 1, a.ws, s));
-    return *info ? WMOM_ERR_SINGULAR : WMOM_OK;
-  };
-  auto residual_norm = [&](const double2* Zk, double* rel) -> wmom_status {
-    SWEEP_TRY(residual_fp64(Zk, n, x64.as<double2>(), v64.as<double2>(), n, r64.as<double2>(),
-                            part.as<double2>(), s));
-    SWEEP_TRY(sumsq_fp64(r64.as<double2>(), n, &sc.as<Scalars>()->rnorm2, s));
-    SWEEP_TRY(cudaMemcpyAsync(&hs, sc.p, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-    SWEEP_TRY(cudaStreamSynchronize(s));
-    *rel = std::sqrt(hs.rnorm2) / vnorm;
-    return WMOM_OK;
-  };
-
-  for (int f0 = 0; f0 < a.nfreq; f0 += batch) {
-    const int nb = std::min(batch, a.nfreq - f0);
-    for (int i = 0; i < nb; ++i) {
-      const double ka = ka_from_mhz(a.freq_mhz[f0 + i]);
-      const double eta0 = 120. * pi;
-      fph[3 * i] = ka;
-      fph[3 * i + 1] = ka * ka;
-      fph[3 * i + 2] = eta0 / (4.0 * pi * ka);
+  int B = 0;
+  std::vector<wmom_report> rep(kMaxLuBatch);
+  DevBuf lu, piv;
+  GroupScratch g;
+  FactorGraph graph;
+  for (int f0 = 0; f0 < a.nfreq; f0 += nbf) {
+    const int nb = std::min(nbf, a.nfreq - f0);
+    wmom_status st = fill_batch(p, a.freq_mhz + f0, nb, zall.as<double2>(), s);
+    if (st != WMOM_OK) return st;
+    if (B == 0) {
+      st = choose_batch(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &B);
+      if (st != WMOM_OK) return st;
+      SWEEP_TRY(lu.alloc((mixed ? mat32 : mat64) * B, s));
+      SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * B, s));
+      st = scratch_init(&g, n, B, a.ngap, a.ampl, a.phas_deg, s);
+      if (st != WMOM_OK) return st;
     }
-    SWEEP_TRY(cudaMemcpyAsync(fpb.p, fph.data(), sizeof(double) * 3 * nb, cudaMemcpyHostToDevice, s));
-    SWEEP_TRY(launch_fill(p, fpb.as<double>(), nb, zall.as<double2>(), n, (long long)n * n, s));
-    for (int i = 0; i < nb; ++i) {
-      const int f = f0 + i;
-      const double2* Zk = zall.as<double2>() + (size_t)i * n * n;
-      wmom_report rep{};
-      rep.rel_residual = -1.0;
-      int info = 0;
-      wmom_status fst = WMOM_OK;
-      if (a.mode == WMOM_MODE_FP64) {
-        fst = factor64(Zk, &info);
-        rep.info = info;
-        if (fst == WMOM_OK || fst == WMOM_ERR_SINGULAR) {
-          const wmom_status rs = residual_norm(Zk, &rep.rel_residual);
-          if (rs != WMOM_OK) return rs;
-        }
-      } else {
-        // FP32 factorisation of the FP64 matrix
-        SWEEP_TRY(convert_matrix_64_to_32(Zk, n, z32.as<float2>(), n, n, n, s));
-        SWEEP_TRY(lu_workspace_reset_barrier(a.ws, s));
-        SWEEP_TRY(lu_factor_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), a.ws, s, hook32));
-        const int err = lu_workspace_read_status(a.ws, &info, s) | (hook32 ? tc::read_and_clear_error() : 0);
-        SWEEP_TRY(cudaGetLastError());
-        if (err) return WMOM_ERR_TIMEOUT;
-        bool fallback = info != 0;
-        if (!fallback) {
-          // initial solve in FP32
-          SWEEP_TRY(convert_vec_64_to_32(v64.as<double2>(), d32.as<float2>(), n, 1.0, s));
-          SWEEP_TRY(lu_solve_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), d32.as<float2>(), n, 1, a.ws, s));
-          stats::count(stats::kMisc);
-          widen_vec_kernel<<<(n + 255) / 256, 256, 0, s>>>(d32.as<float2>(), x64.as<double2>(), n);
-          SWEEP_TRY(cudaGetLastError());
-          double prev = HUGE_VAL;
-          int stall = 0;
-          const int max_it = 40;
-          for (int it = 0;; ++it) {
-            double rel = 0.0;
-            const wmom_status rs = residual_norm(Zk, &rel);
-            if (rs != WMOM_OK) return rs;
-            rep.rel_residual = rel;
-            rep.iterations = it;
-            if (!(rel == rel)) {  // NaN: refinement diverged
-              fallback = true;
-              break;
-            }
-            // converged: the residual target is met, or the last correction no longer
-            // changes the solution at FP64 resolution (ill-conditioned systems whose
-            // FP64 residual floor lies above the target)
-            const double corr = it > 0 ? std::sqrt(hs.dnorm2 / hs.xnorm2) : HUGE_VAL;
-            if (rel <= a.tol || corr <= 0x1p-48) break;
-            if (rel > 0.5 * prev) {
-              if (++stall >= 2) {
-                fallback = true;
-                break;
-              }
-            } else {
-              stall = 0;
-            }
-            if (it >= max_it) {
-              fallback = true;
-              break;
-            }
-            prev = std::min(prev, rel);
-            // correction: d = (LU32)^-1 r, scaled by a power of two to keep FP32 in range
-            const double rn = rel * vnorm;
-            const double scale = rn > 0 ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
-            SWEEP_TRY(convert_vec_64_to_32(r64.as<double2>(), d32.as<float2>(), n, scale, s));
-            SWEEP_TRY(lu_solve_t<float2>(z32.as<float2>(), n, n, ipiv.as<int>(), d32.as<float2>(), n, 1, a.ws, s));
-            stats::count(stats::kMisc);
-            sumsq_f32_kernel<<<1, 1024, 0, s>>>(d32.as<float2>(), n, 1.0 / scale, &sc.as<Scalars>()->dnorm2);
-            SWEEP_TRY(sumsq_fp64(x64.as<double2>(), n, &sc.as<Scalars>()->xnorm2, s));
-            SWEEP_TRY(accumulate_vec_32_to_64(x64.as<double2>(), d32.as<float2>(), n, 1.0 / scale, s));
-          }
-        }
-        if (fallback) {
-          rep.fell_back = 1;
-          fst = factor64(Zk, &info);
-          if (fst == WMOM_OK || fst == WMOM_ERR_SINGULAR) {
-            const wmom_status rs = residual_norm(Zk, &rep.rel_residual);
-            if (rs != WMOM_OK) return rs;
-          }
-        }
-        rep.info = info;
-      }
-      if (fst == WMOM_ERR_TIMEOUT) return fst;
-      rep.status = fst;
-      if (fst != WMOM_OK && overall == WMOM_OK) overall = fst;
-      // results
-      if (a.currents) {
-        SWEEP_TRY(cudaMemcpyAsync(a.currents + 2 * (size_t)f * n, x64.p, sizeof(double2) * n,
-                                  cudaMemcpyDeviceToHost, s));
-        SWEEP_TRY(cudaStreamSynchronize(s));
-        std::memcpy(xh.data(), a.currents + 2 * (size_t)f * n, sizeof(double2) * n);
-      } else {
-        SWEEP_TRY(cudaMemcpyAsync(xh.data() + (a.ngap - 1), x64.as<double2>() + (a.ngap - 1), sizeof(double2),
-                                  cudaMemcpyDeviceToHost, s));
-        SWEEP_TRY(cudaStreamSynchronize(s));
-      }
-      if (a.zin) {
-        // Z_in = V[ngap-1] / I[ngap-1], Smith's formula
-        const double vr = vh[2 * (a.ngap - 1)], vi = vh[2 * (a.ngap - 1) + 1];
-        const double br = xh[a.ngap - 1].x, bi = xh[a.ngap - 1].y;
-        double zr, zi;
-        if (std::fabs(br) >= std::fabs(bi)) {
-          const double r = bi / br, d = br + bi * r;
-          zr = (vr + vi * r) / d;
-          zi = (vi - vr * r) / d;
-        } else {
-          const double r = br / bi, d = bi + br * r;
-          zr = (vr * r + vi) / d;
-          zi = (vi * r - vr) / d;
-        }
-        a.zin[2 * (size_t)f] = zr;
-        a.zin[2 * (size_t)f + 1] = zi;
-      }
-      if (a.reports) a.reports[f] = rep;
+    for (int g0 = 0; g0 < nb; g0 += B) {
+      const int bg = std::min(B, nb - g0);
+      const double2* Zg = zall.as<double2>() + (size_t)g0 * nn;
+      int info[kMaxLuBatch] = {};
+      st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, s, info, nullptr,
+                        &graph);
+      if (st != WMOM_OK) return st;
+      st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
+                       rep.data());
+      if (st != WMOM_OK) return st;
+      st = group_results(g, bg, a.ngap, rep.data(), f0 + g0, a.currents, a.zin, a.reports, &overall);
+      if (st != WMOM_OK) return st;
     }
+  }
+  SWEEP_TRY(cudaStreamSynchronize(s));
+  return overall;
+}
+
+// ------------------------------------------------------- resident factors ----
+wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
+  const Plan& p = *fs->plan;
+  const int n = p.npls;
+  const size_t nn = (size_t)n * n;
+  const bool mixed = fs->mode == WMOM_MODE_MIXED;
+  const int nf = (int)fs->freq.size();
+  SWEEP_TRY(cudaMalloc(&fs->z64, sizeof(double2) * nn * nf));
+  SWEEP_TRY(cudaMalloc(&fs->lu, (mixed ? sizeof(float2) : sizeof(double2)) * nn * nf));
+  SWEEP_TRY(cudaMalloc(&fs->ipiv, sizeof(int) * (size_t)n * nf));
+  fs->info.assign(nf, 0);
+  wmom_status st = fill_batch(p, fs->freq.data(), nf, fs->z64, s);
+  if (st != WMOM_OK) return st;
+  size_t fr = 0, tot = 0;
+  SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
+  st = choose_batch(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &fs->batch);
+  if (st != WMOM_OK) return st;
+  for (int g0 = 0; g0 < nf; g0 += fs->batch) {
+    const int bg = std::min(fs->batch, nf - g0);
+    float2* l32 = reinterpret_cast<float2*>(fs->lu) + (size_t)g0 * nn;
+    double2* l64 = reinterpret_cast<double2*>(fs->lu) + (size_t)g0 * nn;
+    st = factor_group(fs->mode, n, fs->z64 + (size_t)g0 * nn, bg, l32, l64, fs->ipiv + (size_t)g0 * n, fs->ws, s,
+                      fs->info.data() + g0, nullptr, nullptr);
+    if (st != WMOM_OK) return st;
+  }
+  SWEEP_TRY(cudaStreamSynchronize(s));
+  return WMOM_OK;
+}
+
+wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
+                          double* currents, double* zin, wmom_report* reports, cudaStream_t s) {
+  const int n = fs->plan->npls;
+  const size_t nn = (size_t)n * n;
+  const bool mixed = fs->mode == WMOM_MODE_MIXED;
+  const int B = std::max(1, fs->batch);
+  GroupScratch g;
+  wmom_status st = scratch_init(&g, n, B, ngap, ampl, phas, s);
+  if (st != WMOM_OK) return st;
+  wmom_status overall = WMOM_OK;
+  std::vector<wmom_report> rep(kMaxLuBatch);
+  // groups aligned with the factorisation's, so each group's factors are contiguous
+  for (int f = first; f < first + count;) {
+    const int bg = std::min(B, first + count - f);
+    const float2* l32 = reinterpret_cast<const float2*>(fs->lu) + (size_t)f * nn;
+    const double2* l64 = reinterpret_cast<const double2*>(fs->lu) + (size_t)f * nn;
+    st = solve_group(fs->mode, n, fs->z64 + (size_t)f * nn, bg, mixed ? l32 : nullptr, mixed ? nullptr : l64,
+                     fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data());
+    if (st != WMOM_OK) return st;
+    // results are indexed from `first` in the caller's arrays
+    st = group_results(g, bg, ngap, rep.data(), f - first, currents, zin, reports, &overall);
+    if (st != WMOM_OK) return st;
+    f += bg;
   }
   SWEEP_TRY(cudaStreamSynchronize(s));
   return overall;

@@ -27,20 +27,38 @@ struct SweepArgs {
 
 wmom_status run_sweep(const SweepArgs& a);
 
+// Z and its factors kept resident for a list of frequencies of one plan, so that new
+// excitations only run the solves (and refinement).
+struct FactorSet {
+  const Plan* plan = nullptr;
+  int mode = WMOM_MODE_MIXED;
+  std::vector<float> freq;
+  LuWorkspace* ws = nullptr;  // owned by the set
+  int batch = 1;
+  double2* z64 = nullptr;     // nf matrices, FP64 (kept for the residual)
+  void* lu = nullptr;         // nf factors: float2 (mixed) or double2 (FP64)
+  int* ipiv = nullptr;        // nf * n
+  std::vector<int> info;
+};
+
+wmom_status factors_build(FactorSet* fs, cudaStream_t s);
+wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
+                          double* currents, double* zin, wmom_report* reports, cudaStream_t s);
+
 // Device helpers (solve.cu).
-cudaError_t residual_fp64(const double2* Z, long long ldz, const double2* x, const double2* v, int n,
-                          double2* r, double2* partial, cudaStream_t s);
-cudaError_t sumsq_fp64(const double2* x, int n, double* out, cudaStream_t s);
-cudaError_t convert_matrix_64_to_32(const double2* src, long long lds, float2* dst, long long ldd, int rows,
-                                    int cols, cudaStream_t s);
-cudaError_t convert_vec_64_to_32(const double2* src, float2* dst, int n, double scale, cudaStream_t s);
-cudaError_t accumulate_vec_32_to_64(double2* x, const float2* d, int n, double scale, cudaStream_t s);
+// r[b] = v - Z[b] x[b] for nvec matrices zstride apart (vectors n apart), FP64.
+cudaError_t residual_fp64(const double2* Z, long long ldz, long long zstride, const double2* x, const double2* v,
+                          int n, double2* r, double2* partial, int nvec, cudaStream_t s);
+// out[b] = sum |x[b]_i|^2 for nvec vectors n apart (deterministic order).
+cudaError_t sumsq_fp64(const double2* x, int n, double* out, int nvec, cudaStream_t s);
+cudaError_t convert_flat_64_to_32(const double2* src, float2* dst, size_t count, cudaStream_t s);
 
 // FP32 trailing-update GEMM on the tensor cores (lu_tc.cu); nullptr when the
 // device has no tcgen05 path, in which case the SIMT GEMM is used.
 GemmHook<float2> tc_gemm_hook();
 namespace tc {
-int read_and_clear_error();  // 1 if a tensor-core GEMM wait timed out since the last call
+// 1 if a tensor-core GEMM wait on `ws` timed out since the last call (synchronises s)
+int read_and_clear_error(LuWorkspace* ws, cudaStream_t s);
 }
 
 }  // namespace wmom

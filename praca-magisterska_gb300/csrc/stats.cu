@@ -1,6 +1,7 @@
 // stats.cu -- see stats.h.
 #include "stats.h"
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -63,9 +64,19 @@ bool timing_enabled() { return g_timing.load(std::memory_order_relaxed); }
 
 void count(Cls c, int launches) { g_launches[c].fetch_add(launches, std::memory_order_relaxed); }
 
+void snapshot(long long out[kNumCls]) {
+  for (int i = 0; i < kNumCls; ++i) out[i] = g_launches[i].load(std::memory_order_relaxed);
+}
+
+void add_counts(const long long delta[kNumCls]) {
+  for (int i = 0; i < kNumCls; ++i) g_launches[i].fetch_add(delta[i], std::memory_order_relaxed);
+}
+
 Scope::Scope(Cls c, cudaStream_t s, double work, int launches) : c_(c), s_(s), work_(work) {
   count(c, launches);
-  if (timing_enabled()) {
+  // no timing inside a stream capture: the events would become graph nodes
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (timing_enabled() && cudaStreamIsCapturing(s_, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
     std::lock_guard<std::mutex> lk(g_mu);
     e0_ = get_event();
     cudaEventRecord(e0_, s_);
@@ -81,10 +92,44 @@ Scope::~Scope() {
   if (g_recs.size() > 4096) drain(false);
 }
 
+// CH independent FMA chains per thread; the loop count is a kernel argument, so the
+// kernel always ends.
+template <int CH>
+__global__ void fp64_fma_probe_kernel(double* out, double a, double b, int iters) {
+  double x[CH];
+#pragma unroll
+  for (int c = 0; c < CH; ++c) x[c] = threadIdx.x + c;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < CH; ++c) x[c] = fma(x[c], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < CH; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace stats
 }  // namespace wmom
 
 using namespace wmom::stats;
+
+namespace {
+
+template <int CH>
+double probe_once(double* buf, int blocks, int threads, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+  const int iters = 4096;
+  fp64_fma_probe_kernel<CH><<<blocks, threads, 0, s>>>(buf, 1.0000001, 1e-9, iters);  // warm-up
+  cudaEventRecord(e0, s);
+  fp64_fma_probe_kernel<CH><<<blocks, threads, 0, s>>>(buf, 1.0000001, 1e-9, iters);
+  cudaEventRecord(e1, s);
+  if (cudaEventSynchronize(e1) != cudaSuccess) return 0.0;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  return ms > 0.f ? 2.0 * CH * iters * double(blocks) * threads / (ms * 1e-3) / 1e12 : 0.0;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -112,6 +157,36 @@ int wmom_stats_read(double* ms, long long* launches, long long* timed, double* w
     if (work) work[i] = g_work[i];
   }
   return kNumCls;
+}
+
+wmom_status wmom_probe_fp64_tflops(double* tflops) {
+  if (!tflops) return WMOM_ERR_ARG;
+  *tflops = 0.0;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+    return WMOM_ERR_CUDA;
+  const int max_blocks = nsm * 8, max_threads = 256;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * max_blocks * max_threads) != cudaSuccess) return WMOM_ERR_NOMEM;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  best = std::max(best, probe_once<8>(buf, nsm * 4, 256, s, e0, e1));
+  best = std::max(best, probe_once<16>(buf, nsm * 4, 256, s, e0, e1));
+  best = std::max(best, probe_once<16>(buf, nsm * 8, 128, s, e0, e1));
+  best = std::max(best, probe_once<32>(buf, nsm * 2, 256, s, e0, e1));
+  const cudaError_t err = cudaStreamSynchronize(s);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  cudaFree(buf);
+  if (err != cudaSuccess || best <= 0.0) return WMOM_ERR_CUDA;
+  *tflops = best;
+  return WMOM_OK;
 }
 
 }  // extern "C"

@@ -25,6 +25,9 @@ enum Cls : int {
 
 bool timing_enabled();
 void count(Cls c, int launches = 1);
+// Launch counters, for crediting the launches of a replayed CUDA graph.
+void snapshot(long long out[kNumCls]);
+void add_counts(const long long delta[kNumCls]);
 
 // Brackets the launches issued in its lifetime on `s` with events (when enabled).
 class Scope {

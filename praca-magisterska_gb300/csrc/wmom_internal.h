@@ -111,6 +111,9 @@ struct Plan {
   SrcInst* d_si = nullptr;
   int* d_tiles = nullptr;  // rt_off | rt_ids | ct_off | ct_ids | row_local | col_local
   int off_rt_ids = 0, off_ct_off = 0, off_ct_ids = 0, off_row_local = 0, off_col_local = 0;
+  // lumped series loads R + j*2*pi*f[MHz]*L[uH] on diagonal entries (1-based index)
+  std::vector<int> load_idx;
+  std::vector<double> load_r, load_l_uh;
 };
 
 int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, const float* rad,
@@ -127,6 +130,11 @@ namespace wmom {
 // Fill launcher (fill.cu).
 cudaError_t launch_fill(const Plan& p, const double* d_ka, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream);
+// Lets `func` launch with up to `bytes` of dynamic shared memory.  The cap is process-
+// wide state of the kernel, so it is only ever raised (to the device's opt-in maximum,
+// once per device and kernel): setting it per launch would race with another host
+// thread that launches the same kernel with more shared memory.
+cudaError_t allow_dynamic_smem(const void* func, size_t bytes);
 }  // namespace wmom
 
 #define WMOM_CUDA_TRY(call)                                   \

@@ -98,3 +98,24 @@ def test_ground_plane_uses_per_entry_fill(cuda, wmom):
     plan = wmom.Plan(wmom.Topology(str(d["geo"]), ienv=2))
     assert plan.fill_variant == "entry"
     plan.close()
+
+
+def test_table_sincos_against_cuda_sincos(cuda, wmom):
+    """The fill's table-driven sin/cos against CUDA's sincos() over the phase range
+    the fill meets (k*R up to ~1e3 rad), the table nodes j*pi/128 and their
+    half-way points, tiny and zero arguments, and the 1e6 hand-over to sincos()."""
+    import torch
+    rng = np.random.default_rng(7)
+    h = np.pi / 128
+    j = np.arange(-600, 60000, dtype=np.float64)
+    x = np.concatenate([
+        rng.uniform(0.0, 30.0, 200000), rng.uniform(0.0, 1e3, 200000), 10.0 ** rng.uniform(-12, 0, 20000),
+        j * h, (j + 0.5) * h, np.nextafter((j + 0.5) * h, 0), -rng.uniform(0, 50, 1000),
+        [0.0, -0.0, 5e-324, 999999.0, 1e6, 1e6 + 0.5, 3e7]])
+    s, c, sr, cr = (t.cpu().numpy() for t in wmom.diag_sincos(torch.from_numpy(x).cuda()))
+    err = max(np.max(np.abs(s - sr)), np.max(np.abs(c - cr)))
+    # a few units in the last place of a number of magnitude <= 1
+    assert err <= 4.5e-16, err
+    small = np.abs(x) < 1e-3
+    assert np.max(np.abs(s[small] - sr[small]) / np.maximum(np.abs(sr[small]), 1e-300)) <= 4.5e-16
+    assert np.all(np.abs(s * s + c * c - 1.0) <= 1e-15)

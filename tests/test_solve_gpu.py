@@ -120,3 +120,24 @@ def test_dropin_zmatrix_symbol(cuda, wmom, orc):
       p(topo.ise, ip), p(topo.rad, fp), n, orc.ka(20.0), topo.nsmax, 1, 1.0, 1.0, 1.0, 1.0)
     zr = orc.fill(topo.arrays(), 20.0)
     assert np.max(np.abs(cz - zr) / np.max(np.abs(zr), axis=0)) < 1e-13
+
+
+def test_batch_width_does_not_change_results(cuda, wmom):
+    # the same frequencies factored one matrix per launch and four per launch
+    topo = wmom.Topology(wmom.geometry.precision_grid(2048))
+    freqs = np.array([0.002, 0.05, 1.0, 7.0, 20.0], np.float32)
+    out = {}
+    for width in ("1", "4"):
+        os.environ["WMOM_LU_BATCH"] = width
+        try:
+            plan = wmom.Plan(topo)
+            for mode in (0, 1):
+                out[(width, mode)] = plan.solve(freqs, 1000, mode=mode)
+            plan.close()
+        finally:
+            del os.environ["WMOM_LU_BATCH"]
+    for mode in (0, 1):
+        c1, z1, r1 = out[("1", mode)]
+        c4, z4, r4 = out[("4", mode)]
+        assert np.array_equal(c1, c4)
+        assert [r["iterations"] for r in r1] == [r["iterations"] for r in r4]

@@ -10,8 +10,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+# shapes: one tile; ragged edges; a few tiles per CTA; K of one chunk; many tiles per
+# CTA (both accumulators reused many times); long K (the stage ring wraps often)
 @pytest.mark.parametrize("m,n,k", [(128, 64, 64), (130, 70, 64), (1000, 900, 64), (257, 33, 17), (64, 500, 5),
-                                   (4096, 4096, 64)])
+                                   (4096, 4096, 64), (300, 200, 300), (2000, 3000, 200)])
 def test_cgemm_sub_tc_matches_complex128(cuda, wmom, m, n, k):
     rng = np.random.default_rng(m * 7 + n + k)
     a = (rng.normal(size=(m, k)) + 1j * rng.normal(size=(m, k))).astype(np.complex64)
