@@ -296,6 +296,22 @@ def run_wmom(args):
     roof.update({"achieved": achieved, "frac": achieved / roof["peak"], "traffic": None,
                  "avg_launch_ms": avg_ms, "launches": d["timed"],
                  "share_of_device_time": d["ms"] / max(sum(v["ms"] for v in st.values()), 1e-9)})
+    # DRAM traffic per launch: bytes per unit from one ncu capture of a smaller case,
+    # scaled by the units this launch processed (traffic grows in proportion)
+    units = {"fill": work_per_launch / 384.0,            # Z entries (384 flop-eq each)
+             "tc_gemm": work_per_launch / (8.0 * 64)}.get(dom)  # complex entries of C (K = 64)
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            cap = json.load(f).get(roof["kernel"].split("::")[-1])
+    except (OSError, ValueError):
+        cap = None
+    if cap and units:
+        roof["traffic"] = cap["dram_bytes"] / cap["units"] * units
+        roof["traffic_source"] = "ncu capture of a smaller case (%s), scaled by units" % cap["unit"]
+    if dom == "fill":
+        alg = 16.0 * units  # each complex128 entry written once
+        roof["hbm_view"] = {"algorithmic_bytes": alg, "achieved_gbs": alg / (avg_ms / 1e3) / 1e9,
+                            "frac_of_hbm": alg / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

@@ -107,6 +107,12 @@ wmom_status wmom_fill(wmom_plan plan, const double* ka, int nk, void* z_dev, lon
  * also returns WMOM_ERR_SINGULAR).  Synchronises `stream`. */
 wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream);
 
+/* The same factorisation of an n x n complex64 device matrix, as the precision form
+ * runs it: FP32 panels and triangular solves, trailing updates on the tensor cores
+ * (3xTF32) where the device has them.  LAPACK cgetrf semantics and results to FP32
+ * rounding.  No reference counterpart (the reference factors in FP64 only). */
+wmom_status wmom_cgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream);
+
 /* Solves A x = b with the factors from wmom_zgetrf for nrhs right-hand sides held
  * column-major in b_dev (ldb >= n); b_dev is overwritten with x. */
 wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const int* ipiv_dev,

@@ -87,6 +87,7 @@ _plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
 _plan_set_loads = _sig("wmom_plan_set_loads", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
 _zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
+_cgetrf = _sig("wmom_cgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
 _zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
                [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_longlong, _vp, _vp, ctypes.c_longlong, _vp])
 _zgesv_like = _sig("wmom_zgesv_like", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _ip, _ip])
@@ -347,6 +348,15 @@ def zgetrf_device(a_ptr, n, lda, ipiv_ptr, stream=0):
     st = _zgetrf(n, a_ptr, lda, ipiv_ptr, ctypes.byref(info), stream)
     if st not in (WMOM_OK, 3):
         raise WmomError(st, "wmom_zgetrf")
+    return info.value
+
+
+def cgetrf_device(a_ptr, n, lda, ipiv_ptr, stream=0):
+    """FP32 (complex64) LU of the precision form on a device matrix; returns info."""
+    info = ctypes.c_int(0)
+    st = _cgetrf(n, a_ptr, lda, ipiv_ptr, ctypes.byref(info), stream)
+    if st not in (WMOM_OK, 3):
+        raise WmomError(st, "wmom_cgetrf")
     return info.value
 
 

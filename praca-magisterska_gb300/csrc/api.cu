@@ -367,6 +367,25 @@ wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* i
   return inf ? WMOM_ERR_SINGULAR : WMOM_OK;
 }
 
+wmom_status wmom_cgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream) {
+  if (n <= 0 || !a_dev || lda < n || !ipiv_dev) return WMOM_ERR_ARG;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(default_ws().mu);
+  LuWorkspace* ws = nullptr;
+  WMOM_CUDA_TRY(get_default_ws(n, 1, &ws));
+  WMOM_CUDA_TRY(lu_workspace_reset_barrier(ws, s));
+  const GemmHook<float2> hook = tc_gemm_hook();
+  WMOM_CUDA_TRY(lu_factor_t<float2>(reinterpret_cast<float2*>(a_dev), lda, n, ipiv_dev, ws, s, hook));
+  int inf = 0;
+  int err = lu_workspace_read_status(ws, &inf, s);
+  if (hook) err |= tc::read_and_clear_error(ws, s);
+  WMOM_CUDA_TRY(cudaGetLastError());
+  if (info) *info = inf;
+  if (err) return WMOM_ERR_TIMEOUT;
+  return inf ? WMOM_ERR_SINGULAR : WMOM_OK;
+}
+
 wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const int* ipiv_dev,
                         void* b_dev, long long ldb, void* stream) {
   if (n <= 0 || nrhs <= 0 || !a_dev || lda < n || !ipiv_dev || !b_dev || ldb < n) return WMOM_ERR_ARG;

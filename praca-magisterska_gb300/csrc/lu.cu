@@ -24,7 +24,9 @@
 #include <algorithm>
 #include <climits>
 #include <cstddef>
+#include <map>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "lu_common.cuh"
@@ -310,6 +312,163 @@ __global__ void __launch_bounds__(NT) panel_kernel(C* __restrict__ A, long long 
     for (int r = tid; r < cnt; r += NT) A[(size_t)(j0 + c) * lda + base + r] = tile[(size_t)c * rpc + r];
 }
 
+// Row-owner panel (FP32 precision form).  Each thread owns one row of the block's
+// slab (rpc <= NT) for the whole column loop: it finds its own candidate, swaps,
+// scales and updates its own row, so a column needs only two block barriers (the
+// pivot reduction and the candidate gather) besides the grid-wide one.  Same
+// pivot rule and order of operations per row as panel_kernel.
+template <typename C, int NB, int NT>
+__global__ void __launch_bounds__(NT) panel_rows_kernel(C* __restrict__ A, long long lda, int n, int j0, int nb,
+                                                        int rpc, int* __restrict__ ipiv,
+                                                        PanelStage<C, NB>* __restrict__ st,
+                                                        GridBarrier* __restrict__ gb, unsigned int bar_base,
+                                                        long long astride) {
+  using R = decltype(C{}.x);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);          // column-major rpc x NB
+  C* cdat = tile + (size_t)rpc * NB;                  // candidate rows, P x NB
+  C* dgr = cdat + (size_t)gridDim.x * NB;             // diagonal row, NB
+  R* cval = reinterpret_cast<R*>(dgr + NB);           // candidate values, P
+  int* crow = reinterpret_cast<int*>(cval + gridDim.x);  // candidate rows, P
+  __shared__ R red_v[2][NT / 32];
+  __shared__ int red_r[2][NT / 32];
+
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
+  st += blockIdx.y;
+  gb += blockIdx.y;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int b = blockIdx.x;
+  const int P = gridDim.x;
+  const int base = j0 + b * rpc;
+  const int cnt = max(0, min(rpc, n - base));
+  const bool own = t < cnt;  // this thread's row: base + t
+  const int gr = base + t;
+
+  if (own)
+    for (int c = 0; c < nb; ++c) tile[(size_t)c * rpc + t] = A[(size_t)(j0 + c) * lda + gr];
+  __syncthreads();
+
+  for (int j = 0; j < nb; ++j) {
+    const int gj = j0 + j;
+    const int par = j & 1;
+    // 1. candidate: largest |re|+|im| in column j on rows >= gj, first row on ties
+    R best = R(-1);
+    int brow = INT_MAX;
+    if (own && gr >= gj) {
+      best = cabs1(tile[(size_t)j * rpc + t]);
+      brow = gr;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      if (ov > best || (ov == best && orow < brow)) {
+        best = ov;
+        brow = orow;
+      }
+    }
+    if (lane == 0) {
+      red_v[par][warp] = best;
+      red_r[par][warp] = brow;
+    }
+    __syncthreads();
+    // every thread reduces the per-warp results itself (no second barrier)
+    best = R(-1);
+    brow = INT_MAX;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) {
+      const R v = red_v[par][w];
+      const int r = red_r[par][w];
+      if (v > best || (v == best && r < brow)) {
+        best = v;
+        brow = r;
+      }
+    }
+    // 2. publish the candidate and, from its owner, the diagonal row
+    if (t == 0) {
+      st->cand_val[par][b] = best;
+      st->cand_row[par][b] = brow;
+    }
+    if (t < nb) {
+      if (best >= R(0)) st->cand_data[par][b][t] = tile[(size_t)t * rpc + (brow - base)];
+      if (gj >= base && gj < base + cnt) st->diag_data[par][t] = tile[(size_t)t * rpc + (gj - base)];
+    }
+    // 3. one grid-wide barrier per column
+    if (!grid_barrier_count(gb, bar_base + (unsigned)P * (unsigned)(j + 1))) return;
+    // 4. gather every block's candidate (one round trip, kILP loads in flight)
+    for (int q = t; q < P; q += NT) {
+      cval[q] = __ldcg(&st->cand_val[par][q]);
+      crow[q] = __ldcg(&st->cand_row[par][q]);
+    }
+    if (t < nb) dgr[t] = __ldcg(&st->diag_data[par][t]);
+    {
+      constexpr int kILP = 8;
+      const C* src = &st->cand_data[par][0][0];
+      const int tot = P * NB;
+      for (int i0 = t; i0 < tot; i0 += NT * kILP) {
+        C v[kILP];
+#pragma unroll
+        for (int u = 0; u < kILP; ++u)
+          if (i0 + u * NT < tot) v[u] = __ldcg(src + i0 + u * NT);
+#pragma unroll
+        for (int u = 0; u < kILP; ++u)
+          if (i0 + u * NT < tot) cdat[i0 + u * NT] = v[u];
+      }
+    }
+    __syncthreads();
+    // winner over all blocks, computed by every warp (deterministic: largest value,
+    // then smallest row)
+    best = R(-1);
+    brow = INT_MAX;
+    int bblk = -1;
+    for (int q = lane; q < P; q += 32) {
+      if (cval[q] > best || (cval[q] == best && crow[q] < brow)) {
+        best = cval[q];
+        brow = crow[q];
+        bblk = q;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      const int ob = __shfl_xor_sync(0xffffffffu, bblk, o);
+      if (ov > best || (ov == best && orow < brow)) {
+        best = ov;
+        brow = orow;
+        bblk = ob;
+      }
+    }
+    const int prw = brow;
+    const C* prow = cdat + (size_t)bblk * NB;  // the pivot row
+    if (b == 0 && t == 0) ipiv[gj] = prw + 1;
+    const C piv = prow[j];
+    const bool zero = piv.x == R(0) && piv.y == R(0);
+    if (zero && b == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
+    // 5. this thread's row: interchange, then scale and rank-1 update below gj
+    if (own) {
+      if (prw != gj) {
+        if (gr == prw)
+          for (int c = 0; c < nb; ++c) tile[(size_t)c * rpc + t] = dgr[c];
+        else if (gr == gj)
+          for (int c = 0; c < nb; ++c) tile[(size_t)c * rpc + t] = prow[c];
+      }
+      if (gr > gj) {
+        C l = tile[(size_t)j * rpc + t];
+        if (!zero) {
+          l = cmul(l, crecip(piv));
+          tile[(size_t)j * rpc + t] = l;
+        }
+        for (int c = j + 1; c < nb; ++c) tile[(size_t)c * rpc + t] = cfms(tile[(size_t)c * rpc + t], l, prow[c]);
+      }
+    }
+  }
+  __syncthreads();
+  if (own)
+    for (int c = 0; c < nb; ++c) A[(size_t)(j0 + c) * lda + gr] = tile[(size_t)c * rpc + t];
+}
+
 // ------------------------------------------------------------- laswp ----
 // Interchanges of pivots [k0, k0+kn) applied to the columns [0, j_skip0) and
 // [j_skip1, ncols) of A: one thread per column, interchanges in order.
@@ -387,6 +546,56 @@ __global__ void __launch_bounds__(256) trsm_kernel(const C* __restrict__ T, long
   for (int idx = tid; idx < total; idx += blockDim.x) {
     const int c = idx / nb, r = idx - c * nb;
     B[(size_t)(c0 + c) * ldb + r] = Bs[idx];
+  }
+}
+
+// FP32 unit-lower TRSM of the factorisation, B <- L^-1 B for an nb x nb unit lower L
+// (nb <= 64), one thread per column of B.  L is staged once per block in shared
+// memory and read by broadcast; the thread's column lives in registers, so the
+// substitution needs no barrier.  The order of operations is trsm_kernel's
+// (for k: for r > k: b_r -= l_rk b_k), so both give identical results.  Rows and
+// columns of L beyond nb are padded with the identity.
+constexpr int kTrsmColThreads = 128;
+
+__global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const float2* __restrict__ T, long long ldt,
+                                                                         float2* __restrict__ B, long long ldb,
+                                                                         int nb, int ncols, long long tstride,
+                                                                         long long bstride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* Ls = reinterpret_cast<float2*>(smem_raw);  // [64][64] row-major: Ls[r*64 + k] = l_rk
+  float2* Bs = Ls + 64 * 64;                          // [64][kTrsmColThreads + 1]
+  constexpr int ldbs = kTrsmColThreads + 1;
+  T += (size_t)blockIdx.y * tstride;
+  B += (size_t)blockIdx.y * bstride;
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * kTrsmColThreads;
+  const int nc = min(kTrsmColThreads, ncols - c0);
+  for (int idx = tid; idx < 64 * 64; idx += kTrsmColThreads) {
+    const int k = idx >> 6, r = idx & 63;  // column k, row r of L (reads down columns)
+    float2 v = make_float2(0.f, 0.f);
+    if (r < nb && k < nb && r > k) v = T[(size_t)k * ldt + r];
+    Ls[r * 64 + k] = v;
+  }
+  for (int idx = tid; idx < 64 * nc; idx += kTrsmColThreads) {
+    const int c = idx >> 6, r = idx & 63;
+    Bs[r * ldbs + c] = r < nb ? B[(size_t)(c0 + c) * ldb + r] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (tid < nc) {
+    float2 x[64];
+#pragma unroll
+    for (int r = 0; r < 64; ++r) x[r] = Bs[r * ldbs + tid];
+#pragma unroll
+    for (int k = 0; k < 63; ++k)
+#pragma unroll
+      for (int r = k + 1; r < 64; ++r) x[r] = cfms(x[r], Ls[r * 64 + k], x[k]);
+#pragma unroll
+    for (int r = 0; r < 64; ++r) Bs[r * ldbs + tid] = x[r];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < 64 * nc; idx += kTrsmColThreads) {
+    const int c = idx >> 6, r = idx & 63;
+    if (r < nb) B[(size_t)(c0 + c) * ldb + r] = Bs[r * ldbs + c];
   }
 }
 
@@ -678,6 +887,50 @@ size_t panel_smem(int rpc, int P) {
   return bytes;
 }
 
+// Launch shape of one panel of m rows.  FP32: the row-owner kernel with one row per
+// thread (rpc <= NT) while its shared memory fits.  Otherwise panel_kernel with at
+// least kMinRows rows per block: FP64 rank-1 updates are costly, so many blocks share
+// them; FP32 panels are latency-bound, so fewer blocks make each barrier cheaper.
+struct PanelLaunch {
+  bool rows = false;
+  int P = 1, rpc = 1;
+  size_t smem = 0;
+};
+
+template <typename C>
+PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
+  constexpr int NB = PanelCfg<C>::NB;
+  constexpr int NT = PanelCfg<C>::NT;
+  using R = decltype(C{}.x);
+  PanelLaunch pl;
+  const size_t cap = (size_t)lim.smem_optin - 4096;
+  if (sizeof(R) == 4) {
+    const int P = (m + NT - 1) / NT;
+    const int rpc = (m + P - 1) / P;
+    const size_t smem = ((size_t)rpc + (size_t)P + 1) * NB * sizeof(C) + (size_t)P * (sizeof(R) + sizeof(int));
+    if (P <= std::min(lim.sms, kMaxPanelBlocks) && smem <= cap) {
+      pl.rows = true;
+      pl.P = P;
+      pl.rpc = rpc;
+      pl.smem = smem;
+      return pl;
+    }
+  }
+  constexpr int kMinRows = sizeof(R) == 8 ? 16 : 128;
+  int P = std::max(1, std::min({lim.sms, kMaxPanelBlocks, (m + kMinRows - 1) / kMinRows}));
+  int rpc = (m + P - 1) / P;
+  size_t smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  while (smem > cap && P < std::min(lim.sms, kMaxPanelBlocks)) {
+    ++P;
+    rpc = (m + P - 1) / P;
+    smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  }
+  pl.P = (m + rpc - 1) / rpc;
+  pl.rpc = rpc;
+  pl.smem = panel_smem<C, NB>(rpc, pl.P);
+  return pl;
+}
+
 size_t lu_stage_offset(int max_batch) {
   return ((size_t)max_batch * sizeof(GridBarrier) + 255) & ~(size_t)255;
 }
@@ -686,7 +939,7 @@ size_t lu_stage_bytes(int max_batch) { return (size_t)max_batch * sizeof(PanelSt
 
 template <typename C>
 cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, cudaStream_t s,
-                        GemmHook<C> gemm_hook, int batch, long long astride) {
+                        GemmHook<C> gemm_hook, int batch, long long astride, int span) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using Stage = PanelStage<C, NB>;
@@ -697,78 +950,116 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   Stage* st = reinterpret_cast<Stage*>(ws->stage);
   cudaError_t e;
   unsigned int bar_base = 0;  // arrivals of earlier panels on the counting barrier
-  // rows per block: FP64 rank-1 updates are costly, so many blocks share them; FP32
-  // panels are latency-bound, so fewer blocks make each barrier cheaper
-  constexpr int kMinRows = sizeof(decltype(C{}.x)) == 8 ? 16 : 128;
-  for (int j0 = 0; j0 < n; j0 += NB) {
-    const int nb = std::min(NB, n - j0);
-    const int m = n - j0;
-    int P = std::min({lim.sms, kMaxPanelBlocks, (m + kMinRows - 1) / kMinRows});
-    P = std::max(P, 1);
-    int rpc = (m + P - 1) / P;
-    size_t smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
-    while (smem > (size_t)lim.smem_optin - 4096 && P < std::min(lim.sms, kMaxPanelBlocks)) {
-      ++P;
-      rpc = (m + P - 1) / P;
-      smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
-    }
-    P = (m + rpc - 1) / rpc;
-    smem = panel_smem<C, NB>(rpc, P);
-    auto kern = panel_kernel<C, NB, NT>;
-    e = allow_dynamic_smem((const void*)kern, smem);
-    if (e != cudaSuccess) return e;
+
+  // panel of columns [jp, jp + w), rows jp..n-1 (cooperative launch)
+  auto panel = [&](int jp, int w) -> cudaError_t {
+    const int m = n - jp;
+    const PanelLaunch pl = panel_launch<C>(m, lim);
+    const int P = pl.P;
+    const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
+    cudaError_t pe = allow_dynamic_smem(kern, pl.smem);
+    if (pe != cudaSuccess) return pe;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
-    if (e != cudaSuccess) return e;
+    pe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, pl.smem);
+    if (pe != cudaSuccess) return pe;
     if (per_sm * lim.sms < P * batch) return cudaErrorCooperativeLaunchTooLarge;
     C* Ap = A;
     long long ldap = lda, astr = astride;
-    int np = n, j0p = j0, nbp = nb, rpcp = rpc;
+    int np = n, j0p = jp, nbp = w, rpcp = pl.rpc;
     int* ipivp = ipiv;
     unsigned int basep = bar_base;
     void* args[] = {&Ap, &ldap, &np, &j0p, &nbp, &rpcp, &ipivp, &st, &gb, &basep, &astr};
     {
-      stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)nb * nb / 2.0 * batch);
-      e = cudaLaunchCooperativeKernel((const void*)kern, dim3(P, batch), dim3(NT), args, smem, s);
+      stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
+      pe = cudaLaunchCooperativeKernel(kern, dim3(P, batch), dim3(NT), args, pl.smem, s);
     }
-    if (e != cudaSuccess) return e;
-    bar_base += (unsigned int)P * (unsigned int)nb;
-    // interchanges on the other columns
-    const int other = n - nb;
-    if (other > 0) {
-      stats::Scope sc(stats::kLaswp, s, 2.0 * nb * other * sizeof(C) * batch);
-      laswp_kernel<C><<<dim3((other + 127) / 128, batch), 128, 0, s>>>(A, lda, n, j0, j0 + nb, j0, nb, ipiv,
-                                                                       astride, n);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
+    bar_base += (unsigned int)P * (unsigned int)w;
+    return pe;
+  };
+  // the interchanges of panel [jp, jp + w) on every other column
+  auto laswp = [&](int jp, int w) -> cudaError_t {
+    const int other = n - w;
+    if (other <= 0) return cudaSuccess;
+    stats::Scope sc(stats::kLaswp, s, 2.0 * w * other * sizeof(C) * batch);
+    laswp_kernel<C><<<dim3((other + 127) / 128, batch), 128, 0, s>>>(A, lda, n, jp, jp + w, jp, w, ipiv, astride, n);
+    return cudaGetLastError();
+  };
+  // rows [jp, jp + w) of columns [c0, c0 + nc) <- L(jp..jp+w)^-1 times themselves
+  auto trsm = [&](int jp, int w, int c0, int nc) -> cudaError_t {
+    if (nc <= 0) return cudaSuccess;
+    const C* T = A + (size_t)jp * lda + jp;
+    C* Bb = A + (size_t)c0 * lda + jp;
+    cudaError_t te;
+    if constexpr (std::is_same<C, float2>::value) {
+      const size_t tsmem = (64 * 64 + 64 * (kTrsmColThreads + 1)) * sizeof(float2);
+      te = allow_dynamic_smem((const void*)trsm_lower_cols_kernel, tsmem);
+      if (te != cudaSuccess) return te;
+      stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
+      trsm_lower_cols_kernel<<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads, tsmem,
+                               s>>>(T, lda, Bb, lda, w, nc, astride, astride);
+    } else {
+      const size_t tsmem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(C);
+      te = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
+      if (te != cudaSuccess) return te;
+      stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
+      trsm_kernel<C, false><<<dim3((nc + kTrsmCols - 1) / kTrsmCols, batch), 256, tsmem, s>>>(T, lda, Bb, lda, w, nc,
+                                                                                             astride, astride);
     }
-    const int rest = n - j0 - nb;
+    return cudaGetLastError();
+  };
+  // A[r0:r0+M, c0:c0+N] -= A[r0:r0+M, k0:k0+K] * A[k0:k0+K, c0:c0+N]
+  auto update = [&](int r0, int c0, int M, int N, int k0, int K) -> cudaError_t {
+    if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+    const C* Am = A + (size_t)k0 * lda + r0;
+    const C* Bm = A + (size_t)c0 * lda + k0;
+    C* Cm = A + (size_t)c0 * lda + r0;
+    if (gemm_hook) return gemm_hook(ws, Am, lda, Bm, lda, Cm, lda, M, N, K, s, batch, astride);
+    stats::Scope sc(stats::kGemm, s, 8.0 * M * (double)N * K * batch);
+    dim3 grid((M + kGemmBM - 1) / kGemmBM, (N + kGemmBN - 1) / kGemmBN, batch);
+    gemm_sub_kernel<C><<<grid, 256, 0, s>>>(Am, lda, Bm, lda, Cm, lda, M, N, K, astride);
+    return cudaGetLastError();
+  };
+#define LU_TRY(x)                  \
+  do {                             \
+    e = (x);                       \
+    if (e != cudaSuccess) return e; \
+  } while (0)
+
+  // With the tensor-core update, `span` panels share one trailing update (K = span
+  // NB): inside the group each panel is first brought up to date, left-looking, by
+  // thin updates from the group's earlier panels, so the large update reads and
+  // writes the trailing matrix 1/span as often.  Without the hook (FP64 SIMT GEMM,
+  // bound by the FP64 pipe rather than by traffic) span is 1.
+  const int S = gemm_hook ? std::max(1, std::min(span > 0 ? span : 2, kMaxSpan)) : 1;
+  for (int j0 = 0; j0 < n; j0 += S * NB) {
+    int c[kMaxSpan + 1], w[kMaxSpan];
+    int np = 0;
+    c[0] = j0;
+    while (np < S && c[np] < n) {
+      w[np] = std::min(NB, n - c[np]);
+      c[np + 1] = c[np] + w[np];
+      ++np;
+    }
+    const int cr = c[np], rest = n - cr;
+    for (int q = 0; q < np; ++q) {
+      // panel q: apply the group's earlier panels to its columns, then factor it
+      for (int p = 0; p < q; ++p) {
+        LU_TRY(trsm(c[p], w[p], c[q], w[q]));
+        LU_TRY(update(c[p + 1], c[q], n - c[p + 1], w[q], c[p], w[p]));
+      }
+      LU_TRY(panel(c[q], w[q]));
+      LU_TRY(laswp(c[q], w[q]));
+    }
     if (rest > 0) {
-      C* A11 = A + (size_t)j0 * lda + j0;
-      C* A12 = A + (size_t)(j0 + nb) * lda + j0;
-      C* A21 = A + (size_t)j0 * lda + j0 + nb;
-      C* A22 = A + (size_t)(j0 + nb) * lda + j0 + nb;
-      const size_t tsmem = ((size_t)nb * nb + (size_t)nb * kTrsmCols) * sizeof(C);
-      e = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
-      if (e != cudaSuccess) return e;
-      {
-        stats::Scope sc(stats::kTrsm, s, 4.0 * nb * (double)nb * rest * batch);
-        trsm_kernel<C, false><<<dim3((rest + kTrsmCols - 1) / kTrsmCols, batch), 256, tsmem, s>>>(
-            A11, lda, A12, lda, nb, rest, astride, astride);
+      // U rows of the group for the trailing columns, then one update with K = c[np] - j0
+      for (int p = 0; p < np; ++p) {
+        LU_TRY(trsm(c[p], w[p], cr, rest));
+        if (p + 1 < np) LU_TRY(update(c[p + 1], cr, cr - c[p + 1], rest, c[p], w[p]));
       }
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-      if (gemm_hook) {
-        e = gemm_hook(ws, A21, lda, A12, lda, A22, lda, rest, rest, nb, s, batch, astride);
-      } else {
-        stats::Scope sc(stats::kGemm, s, 8.0 * rest * (double)rest * nb * batch);
-        dim3 grid((rest + kGemmBM - 1) / kGemmBM, (rest + kGemmBN - 1) / kGemmBN, batch);
-        gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A21, lda, A12, lda, A22, lda, rest, rest, nb, astride);
-        e = cudaGetLastError();
-      }
-      if (e != cudaSuccess) return e;
+      LU_TRY(update(cr, cr, rest, rest, j0, cr - j0));
     }
   }
+#undef LU_TRY
   return cudaSuccess;
 }
 
@@ -855,34 +1146,41 @@ template <typename C>
 int lu_max_batch(int n) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
-  constexpr int kMinRows = sizeof(decltype(C{}.x)) == 8 ? 16 : 128;
   const DeviceLimits lim = device_limits();
   if (lim.sms <= 0 || n <= 0) return 1;
-  // the first panel (m = n) has the most blocks
-  int P = std::max(1, std::min({lim.sms, kMaxPanelBlocks, (n + kMinRows - 1) / kMinRows}));
-  int rpc = (n + P - 1) / P;
-  size_t smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
-  while (smem > (size_t)lim.smem_optin - 4096 && P < std::min(lim.sms, kMaxPanelBlocks)) {
-    ++P;
-    rpc = (n + P - 1) / P;
-    smem = (size_t)rpc * NB * sizeof(C) + NB * sizeof(C);
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, int> cache;  // (device, n) -> batch
+  int dev = 0;
+  cudaGetDevice(&dev);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({dev, n});
+    if (it != cache.end()) return it->second;
   }
-  P = (n + rpc - 1) / rpc;
-  smem = panel_smem<C, NB>(rpc, P);
-  auto kern = panel_kernel<C, NB, NT>;
-  if (allow_dynamic_smem((const void*)kern, smem) != cudaSuccess) return 1;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) != cudaSuccess) return 1;
-  return std::max(1, std::min(kMaxLuBatch, per_sm * lim.sms / P));
+  // every panel's cooperative launch must fit co-resident; shapes change as the
+  // panels shrink, so the smallest batch over all of them is the limit
+  int best = kMaxLuBatch;
+  for (int j0 = 0; j0 < n && best > 1; j0 += NB) {
+    const PanelLaunch pl = panel_launch<C>(n - j0, lim);
+    const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
+    if (allow_dynamic_smem(kern, pl.smem) != cudaSuccess) return 1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, pl.smem) != cudaSuccess) return 1;
+    best = std::min(best, per_sm * lim.sms / pl.P);
+  }
+  best = std::max(1, best);
+  std::lock_guard<std::mutex> lk(mu);
+  cache[{dev, n}] = best;
+  return best;
 }
 
 template int lu_max_batch<double2>(int);
 template int lu_max_batch<float2>(int);
 
 template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWorkspace*, cudaStream_t,
-                                          GemmHook<double2>, int, long long);
+                                          GemmHook<double2>, int, long long, int);
 template cudaError_t lu_factor_t<float2>(float2*, long long, int, int*, LuWorkspace*, cudaStream_t,
-                                         GemmHook<float2>, int, long long);
+                                         GemmHook<float2>, int, long long, int);
 template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const int*, double2*, long long, int,
                                          LuWorkspace*, cudaStream_t, int, long long);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,

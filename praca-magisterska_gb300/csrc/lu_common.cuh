@@ -106,27 +106,38 @@ __device__ __forceinline__ int ld_volatile_i32(const int* p) {
   return *reinterpret_cast<const volatile int*>(p);
 }
 
-// Counting barrier: the counter only grows, so arriving is one atomicAdd and
-// waiting is polling the counter until it reaches `target` (= the caller's
-// running total of arrivals expected so far).  Returns false on timeout.
+// Counting barrier: the counter only grows, so arriving is one release reduction and
+// waiting is polling the counter with acquire loads until it reaches `target` (= the
+// caller's running total of arrivals expected so far).  The acquire that reads the
+// final count synchronises with every block's release, and the closing
+// __syncthreads passes that on to the rest of the block.  The error word and the
+// clock are looked at every 64 polls only, so a poll is one L2 round trip.  Returns
+// false on timeout, or when another block has recorded one.
 __device__ __forceinline__ bool grid_barrier_count(GridBarrier* gb, unsigned int target) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    // arrive: a release reduction (no round trip to wait for), ordered after the
-    // block's writes, which __syncthreads made visible to this thread
+    // arrive, ordered after the block's writes (which __syncthreads ordered before
+    // this thread's release)
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gb->count) : "memory");
-    const unsigned long long t0 = global_ns();
-    while (ld_acquire_u32(&gb->count) < target) {
-      if (ld_volatile_i32(&gb->err)) break;
-      if (global_ns() - t0 > kBarrierTimeoutNs) {
-        atomicExch(&gb->err, 1);
-        break;
+    if (ld_acquire_u32(&gb->count) < target) {
+      const unsigned long long t0 = global_ns();
+      unsigned int polls = 0;
+      while (ld_acquire_u32(&gb->count) < target) {
+        if ((++polls & 63u) == 0) {
+          if (ld_volatile_i32(&gb->err)) {
+            ok = 0;
+            break;
+          }
+          if (global_ns() - t0 > kBarrierTimeoutNs) {
+            atomicExch(&gb->err, 1);
+            ok = 0;
+            break;
+          }
+        }
       }
     }
-    __threadfence();
-    if (ld_volatile_i32(&gb->err)) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

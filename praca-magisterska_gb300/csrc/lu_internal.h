@@ -54,9 +54,12 @@ using GemmHook = cudaError_t (*)(LuWorkspace* ws, const C* Am, long long lda, co
                                  long long bstride);
 
 // In-place LU of `batch` n x n matrices astride elements apart (pivots n apart).
+// With a GEMM hook, `span` panels (1..kMaxSpan, 0 = default 2) share one trailing
+// update.
+constexpr int kMaxSpan = 4;
 template <typename C>
 cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, cudaStream_t s,
-                        GemmHook<C> gemm_hook, int batch = 1, long long astride = 0);
+                        GemmHook<C> gemm_hook, int batch = 1, long long astride = 0, int span = 0);
 
 // Solves with the factors; batch > 1 needs nrhs == 1 and right-hand sides n apart.
 template <typename C>

@@ -211,15 +211,15 @@ struct GroupScalars {
   double vnorm2;
 };
 
-// Autotuned batch width per (order bucket, form).
+// Autotuned factorisation shape per (order bucket, form).
 std::mutex g_tune_mu;
-std::map<std::pair<int, int>, int> g_tuned;
+std::map<std::pair<int, int>, LuConfig> g_tuned;
 
-int env_batch() {
-  const char* e = std::getenv("WMOM_LU_BATCH");
+int env_int(const char* name, int lo, int hi) {
+  const char* e = std::getenv(name);
   if (!e) return 0;
   const int b = std::atoi(e);
-  return (b >= 1 && b <= kMaxLuBatch) ? b : 0;
+  return (b >= lo && b <= hi) ? b : 0;
 }
 
 }  // namespace
@@ -523,6 +523,7 @@ struct FactorGraph {
   int mode = -1, n = 0, bg = 0;
   const void* lu = nullptr;
   const int* ipiv = nullptr;
+  int span = 0;
   const float* tc_buf = nullptr;  // tensor-core scratch the capture used
   unsigned tc_gen = 0;
   bool failed = false;  // capture unsupported here: launch directly
@@ -540,7 +541,7 @@ bool graphs_enabled() {
 }  // namespace
 
 wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu32, double2* lu64, int* ipiv,
-                         LuWorkspace* ws, cudaStream_t s, int* info, float* ms, FactorGraph* graph) {
+                         LuWorkspace* ws, cudaStream_t s, int* info, float* ms, FactorGraph* graph, int span) {
   const size_t nn = (size_t)n * n;
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
   if (mode == WMOM_MODE_MIXED)
@@ -556,7 +557,7 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
   const GemmHook<float2> hook32 = tc_gemm_hook();
   const void* lu = mode == WMOM_MODE_MIXED ? (const void*)lu32 : (const void*)lu64;
   auto direct = [&]() -> cudaError_t {
-    return mode == WMOM_MODE_MIXED ? lu_factor_t<float2>(lu32, n, n, ipiv, ws, s, hook32, bg, (long long)nn)
+    return mode == WMOM_MODE_MIXED ? lu_factor_t<float2>(lu32, n, n, ipiv, ws, s, hook32, bg, (long long)nn, span)
                                    : lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, nullptr, bg, (long long)nn);
   };
   cudaError_t fe = cudaSuccess;
@@ -566,11 +567,11 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
     graph->exec = nullptr;
   }
   if (graph && graph->exec && graph->mode == mode && graph->n == n && graph->bg == bg && graph->lu == lu &&
-      graph->ipiv == ipiv) {
+      graph->ipiv == ipiv && graph->span == span) {
     stats::add_counts(graph->launches);
     fe = cudaGraphLaunch(graph->exec, s);
   } else if (graph && !graph->failed && graphs_enabled() && graph->mode == mode && graph->n == n &&
-             graph->bg == bg && graph->lu == lu && graph->ipiv == ipiv) {
+             graph->bg == bg && graph->lu == lu && graph->ipiv == ipiv && graph->span == span) {
     // second use of these buffers: capture the sequence, then replay it from now on
     cudaGraph_t g = nullptr;
     long long before[stats::kNumCls], after[stats::kNumCls];
@@ -609,6 +610,7 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
       graph->bg = bg;
       graph->lu = lu;
       graph->ipiv = ipiv;
+      graph->span = span;
     }
     fe = direct();
   }
@@ -795,7 +797,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     }
     int inf1 = 0;
     const wmom_status fst = factor_group(WMOM_MODE_FP64, n, Z64 + (size_t)b * nn, 1, nullptr,
-                                         g.fb_lu.as<double2>(), g.fb_ipiv.as<int>(), ws, s, &inf1, nullptr, nullptr);
+                                         g.fb_lu.as<double2>(), g.fb_ipiv.as<int>(), ws, s, &inf1, nullptr, nullptr,
+                                         1);
     if (fst != WMOM_OK) return fst;
     // solve into slot b: move the vector through x64[0]
     DevBuf keep;
@@ -901,17 +904,28 @@ wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cud
 
 // Batch width: env override, else the autotuned value for (order bucket, form),
 // else tuned now on Z64 (the first matrix of the work) by timing 1, 2, 4, ...
-wmom_status choose_batch(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
-                         size_t budget, int* out) {
+// Picks the factorisation shape for order n: the batch width (matrices per launch,
+// up to what the cooperative panel keeps co-resident and a quarter of `budget`) and,
+// for the precision form, the span (panels per tensor-core trailing update).  It times
+// factorisations of copies of the first matrix -- spans 1, 2, 4 at width 1, then
+// widths 1, 2, 4, ... at the best span -- and keeps the best time per matrix.
+// Results are cached per (n / 256, form); WMOM_LU_BATCH and WMOM_LU_SPAN override.
+wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
+                             size_t budget, LuConfig* out) {
   const size_t nn = (size_t)n * n;
   const size_t mat = mode == WMOM_MODE_MIXED ? sizeof(float2) * nn : sizeof(double2) * nn;
   int bmax = std::min({ws->max_batch, kMaxLuBatch, limit,
                        mode == WMOM_MODE_MIXED ? lu_max_batch<float2>(n) : lu_max_batch<double2>(n)});
   while (bmax > 1 && (size_t)bmax * mat > budget / 4) bmax /= 2;
   bmax = std::max(bmax, 1);
-  const int eb = env_batch();
-  if (eb) {
-    *out = std::min(eb, bmax);
+  const int eb = env_int("WMOM_LU_BATCH", 1, kMaxLuBatch), es = env_int("WMOM_LU_SPAN", 1, kMaxSpan);
+  if (mode != WMOM_MODE_MIXED) {
+    // the FP64 form is bound by the FP64 pipe at every width worth batching
+    *out = LuConfig{eb ? std::min(eb, bmax) : (n <= 2048 ? bmax : 1), 1};
+    return WMOM_OK;
+  }
+  if (eb && es) {
+    *out = LuConfig{std::min(eb, bmax), es};
     return WMOM_OK;
   }
   const std::pair<int, int> key{(n + 255) / 256, mode};
@@ -919,41 +933,56 @@ wmom_status choose_batch(int mode, int n, int limit, const double2* Z64, LuWorks
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
-      *out = std::min(it->second, bmax);
+      *out = LuConfig{eb ? std::min(eb, bmax) : std::min(it->second.batch, bmax), es ? es : it->second.span};
       return WMOM_OK;
     }
   }
-  if (bmax == 1 || mode != WMOM_MODE_MIXED) {
-    // the FP64 form is bound by the FP64 pipe at every width worth batching
-    *out = mode == WMOM_MODE_MIXED ? 1 : (n <= 2048 ? bmax : 1);
-    return WMOM_OK;
-  }
-  int best_b = 1;
-  float best_t = 1e30f;
+  const int bcap = eb ? std::min(eb, bmax) : bmax;
   DevBuf rep64, lu, piv;
-  SWEEP_TRY(rep64.alloc(sizeof(double2) * nn * bmax, s));
-  SWEEP_TRY(lu.alloc(sizeof(float2) * nn * bmax, s));
-  SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * bmax, s));
-  for (int b = 0; b < bmax; ++b)
+  SWEEP_TRY(rep64.alloc(sizeof(double2) * nn * bcap, s));
+  SWEEP_TRY(lu.alloc(sizeof(float2) * nn * bcap, s));
+  SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * bcap, s));
+  for (int b = 0; b < bcap; ++b)
     SWEEP_TRY(cudaMemcpyAsync(rep64.as<double2>() + (size_t)b * nn, Z64, sizeof(double2) * nn,
                               cudaMemcpyDeviceToDevice, s));
-  for (int cand = 1; cand <= bmax; cand *= 2) {
+  auto time_one = [&](int batch, int span, float* per) -> wmom_status {
     float ms = 0.f;
     int info[kMaxLuBatch];
-    const wmom_status st = factor_group(mode, n, rep64.as<double2>(), cand, lu.as<float2>(), nullptr,
-                                        piv.as<int>(), ws, s, info, &ms, nullptr);
-    if (st != WMOM_OK) return st;
-    const float per = ms / cand;
-    if (per < best_t * 0.95f) {
-      best_t = per;
-      best_b = cand;
+    const wmom_status st = factor_group(mode, n, rep64.as<double2>(), batch, lu.as<float2>(), nullptr,
+                                        piv.as<int>(), ws, s, info, &ms, nullptr, span);
+    *per = ms / batch;
+    return st;
+  };
+  LuConfig best{eb ? bcap : 1, es ? es : 2};
+  float best_t = 1e30f;
+  if (!es) {
+    for (int span = 1; span <= kMaxSpan; span *= 2) {
+      float per = 0.f;
+      const wmom_status st = time_one(best.batch, span, &per);
+      if (st != WMOM_OK) return st;
+      if (per < best_t * 0.97f) {
+        best_t = per;
+        best.span = span;
+      }
+    }
+  }
+  if (!eb) {
+    best_t = 1e30f;
+    for (int cand = 1; cand <= bcap; cand *= 2) {
+      float per = 0.f;
+      const wmom_status st = time_one(cand, best.span, &per);
+      if (st != WMOM_OK) return st;
+      if (per < best_t * 0.95f) {
+        best_t = per;
+        best.batch = cand;
+      }
     }
   }
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tuned[key] = best_b;
+    g_tuned[key] = best;
   }
-  *out = best_b;
+  *out = best;
   return WMOM_OK;
 }
 
@@ -979,6 +1008,7 @@ wmom_status run_sweep(const SweepArgs& a) {
   SWEEP_TRY(zall.alloc(mat64 * nbf, s));
   wmom_status overall = WMOM_OK;
   int B = 0;
+  LuConfig cfg;
   std::vector<wmom_report> rep(kMaxLuBatch);
   DevBuf lu, piv;
   GroupScratch g;
@@ -988,8 +1018,9 @@ wmom_status run_sweep(const SweepArgs& a) {
     wmom_status st = fill_batch(p, a.freq_mhz + f0, nb, zall.as<double2>(), s);
     if (st != WMOM_OK) return st;
     if (B == 0) {
-      st = choose_batch(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &B);
+      st = choose_lu_config(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &cfg);
       if (st != WMOM_OK) return st;
+      B = cfg.batch;
       SWEEP_TRY(lu.alloc((mixed ? mat32 : mat64) * B, s));
       SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * B, s));
       st = scratch_init(&g, n, B, a.ngap, a.ampl, a.phas_deg, s);
@@ -1000,7 +1031,7 @@ wmom_status run_sweep(const SweepArgs& a) {
       const double2* Zg = zall.as<double2>() + (size_t)g0 * nn;
       int info[kMaxLuBatch] = {};
       st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, s, info, nullptr,
-                        &graph);
+                        &graph, cfg.span);
       if (st != WMOM_OK) return st;
       st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
                        rep.data());
@@ -1028,14 +1059,17 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
   if (st != WMOM_OK) return st;
   size_t fr = 0, tot = 0;
   SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
-  st = choose_batch(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &fs->batch);
+  LuConfig cfg;
+  st = choose_lu_config(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &cfg);
   if (st != WMOM_OK) return st;
+  fs->batch = cfg.batch;
+  fs->span = cfg.span;
   for (int g0 = 0; g0 < nf; g0 += fs->batch) {
     const int bg = std::min(fs->batch, nf - g0);
     float2* l32 = reinterpret_cast<float2*>(fs->lu) + (size_t)g0 * nn;
     double2* l64 = reinterpret_cast<double2*>(fs->lu) + (size_t)g0 * nn;
     st = factor_group(fs->mode, n, fs->z64 + (size_t)g0 * nn, bg, l32, l64, fs->ipiv + (size_t)g0 * n, fs->ws, s,
-                      fs->info.data() + g0, nullptr, nullptr);
+                      fs->info.data() + g0, nullptr, nullptr, fs->span);
     if (st != WMOM_OK) return st;
   }
   SWEEP_TRY(cudaStreamSynchronize(s));

@@ -29,12 +29,20 @@ wmom_status run_sweep(const SweepArgs& a);
 
 // Z and its factors kept resident for a list of frequencies of one plan, so that new
 // excitations only run the solves (and refinement).
+// Factorisation shape chosen by the autotuner: matrices per batched launch and
+// panels per tensor-core trailing update.
+struct LuConfig {
+  int batch = 1;
+  int span = 0;
+};
+
 struct FactorSet {
   const Plan* plan = nullptr;
   int mode = WMOM_MODE_MIXED;
   std::vector<float> freq;
   LuWorkspace* ws = nullptr;  // owned by the set
   int batch = 1;
+  int span = 0;               // panels per tensor-core trailing update (tuned)
   double2* z64 = nullptr;     // nf matrices, FP64 (kept for the residual)
   void* lu = nullptr;         // nf factors: float2 (mixed) or double2 (FP64)
   int* ipiv = nullptr;        // nf * n

@@ -78,3 +78,37 @@ def test_large_lu_residual(cuda, wmom):
     x = bt.cpu().numpy().T
     r = np.linalg.norm(a @ x - b) / (np.linalg.norm(a, 1) * np.linalg.norm(x, 1))
     assert r < 1e-14
+
+
+def _plu_backward_error(a, lu, ipiv):
+    n = a.shape[0]
+    L = np.tril(lu, -1) + np.eye(n)
+    U = np.triu(lu)
+    pa = a.copy()
+    for i, p in enumerate(ipiv - 1):
+        pa[[i, p]] = pa[[p, i]]
+    return np.linalg.norm(pa - L @ U) / np.linalg.norm(a), np.max(np.abs(L))
+
+
+# sizes: one row per thread of a single panel block, panel edges, several blocks per
+# panel (the row-owner panel's grid barrier), several panels with tensor-core updates
+@pytest.mark.parametrize("n", [1, 63, 65, 257, 700, 2000, 4100])
+def test_fp32_lu_backward_error(cuda, wmom, n):
+    """The precision form's LU (FP32 panels, 3xTF32 tensor-core updates): P A = L U to
+    FP32 accuracy.  Bound: ||PA - LU||_F / ||A||_F at most 10x that of LAPACK cgetrf
+    (FP32) on the same matrix: a 3xTF32 product hi*hi' + hi*lo' + lo*hi' keeps a
+    relative error of about 3 * 2^-22 (TF32 tails, lo*lo' dropped) against FP32's
+    2^-24 rounding; observed 2-5x.  And |l_ij| <= sqrt(2) (|re|+|im| pivoting)."""
+    from scipy.linalg import lapack
+    a = _rand(n, 1000 + n).astype(np.complex64)
+    at = cuda.from_numpy(np.ascontiguousarray(a.T)).to("cuda")
+    ipiv = cuda.zeros(n, dtype=cuda.int32, device="cuda")
+    info = wmom.cgetrf_device(at.data_ptr(), n, n, ipiv.data_ptr())
+    cuda.cuda.synchronize()
+    assert info == 0
+    lu = at.cpu().numpy().T.astype(np.complex128)
+    err, lmax = _plu_backward_error(a.astype(np.complex128), lu, ipiv.cpu().numpy())
+    lu_c, piv_c, info_c = lapack.cgetrf(a)
+    err_c, _ = _plu_backward_error(a.astype(np.complex128), lu_c.astype(np.complex128), piv_c + 1)
+    assert err <= 10.0 * err_c + 1e-7, (err, err_c)
+    assert lmax <= np.sqrt(2.0) * (1 + 1e-5), lmax
