@@ -232,6 +232,12 @@ wmom_status wmom_probe_fp64_tflops(double* tflops);
  * counterpart. */
 wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void* stream);
 
+/* The factorisation shape the autotuner chose for order n in `mode` in this process
+ * (matrices per batched launch, panels per tensor-core trailing update); returns
+ * WMOM_ERR_ARG when no sweep of that order has been tuned yet.  No reference
+ * counterpart. */
+wmom_status wmom_tuned_config(int n, int mode, int* batch, int* span);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,7 @@ _stats_read = _sig("wmom_stats_read", ctypes.c_int,
 
 _probe_fp64 = _sig("wmom_probe_fp64_tflops", ctypes.c_int, [_dp])
 _diag_sincos = _sig("wmom_diag_sincos", ctypes.c_int, [_vp, ctypes.c_longlong, _vp, _vp])
+_tuned_config = _sig("wmom_tuned_config", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip])
 
 STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc"]
 
@@ -150,6 +151,14 @@ def diag_sincos(x):
     _check(_diag_sincos(x.data_ptr(), x.numel(), out.data_ptr(), torch.cuda.current_stream().cuda_stream),
            "wmom_diag_sincos")
     return out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+
+
+def tuned_config(n, mode):
+    """(batch, span) the autotuner chose for order n in this process, or None."""
+    b, sp = ctypes.c_int(0), ctypes.c_int(0)
+    if _tuned_config(n, mode, ctypes.byref(b), ctypes.byref(sp)) != WMOM_OK:
+        return None
+    return b.value, sp.value
 
 
 def _check(st, what):

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <mutex>
+#include <vector>
 
 #include "../../include/wmom.h"
 #include "stats.h"
@@ -45,8 +47,9 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 // function", ACM TOMS 15(2), 1989, applied to sin/cos by angle addition):
 //   x = n*h + d,  h = pi/128,  |d| <= h/2 ~ 0.0123,
 //   sin x = S_j cos d + C_j sin d,  cos x = C_j cos d - S_j sin d,  j = n mod 256,
-// with (S_j, C_j) = (sin, cos)(j*pi/128) tabulated per block in shared memory by
-// sincospi(j/128) (an exact argument), d from a two-constant Cody-Waite reduction
+// with (S_j, C_j) = (sin, cos)(j*pi/128) tabulated once per device by sincospi(j/128)
+// (an exact argument) and read through the read-only cache, d from a two-constant
+// Cody-Waite reduction
 // (h_hi = double(pi)/128 exactly, h_lo = (pi - double(pi))/128), and sin d, cos d
 // from their Taylor series to d^7 and d^6 (truncation below 2e-20 relative).
 // Arguments beyond 1e6 rad take sincos() itself.
@@ -56,23 +59,31 @@ constexpr double kInvH = 40.743665431525205957;    // 128/pi
 constexpr double kHHi = 3.141592653589793116 / 128;  // double(pi)/128, exact
 constexpr double kHLo = 1.2246467991473532e-16 / 128;  // (pi - double(pi))/128
 
-__device__ __forceinline__ void sin_table_init(double2* tab) {
-  for (int j = threadIdx.x; j < kSinTab; j += blockDim.x) {
+__device__ double2 g_sin_tab[kSinTab];
+
+__global__ void sin_table_setup_kernel() {
+  const int j = threadIdx.x;
+  if (j < kSinTab) {
     double sj, cj;
     sincospi(j / 128.0, &sj, &cj);
-    tab[j] = make_double2(sj, cj);
+    g_sin_tab[j] = make_double2(sj, cj);
   }
 }
 
 __device__ __forceinline__ void sincos_tab(double x, const double2* tab, double* s, double* c) {
-  if (!(fabs(x) < 1.0e6)) {
+  // |x| < 1e6 (and not NaN), tested on the high word: 1e6 = 0x412E8480'00000000
+  if ((__double2hiint(x) & 0x7fffffff) >= 0x412E8480) {
     sincos(x, s, c);
     return;
   }
-  const double n = rint(x * kInvH);
+  // n = x/h rounded to nearest by adding 1.5 * 2^52 (exact for |x/h| < 2^51); the
+  // low word of the sum is then n modulo 2^32, whose low bits index the table
+  constexpr double kRound = 6755399441055744.0;  // 1.5 * 2^52
+  const double tn = fma(x, kInvH, kRound);
+  const double n = tn - kRound;
   double d = fma(-n, kHHi, x);
   d = fma(-n, kHLo, d);
-  const double2 t = tab[(int)((long long)n & (kSinTab - 1))];
+  const double2 t = __ldg(&tab[__double2loint(tn) & (kSinTab - 1)]);
   const double d2 = d * d;
   const double sd = fma(d * d2, fma(d2, fma(d2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), d);
   const double cd = fma(d2, fma(d2, fma(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
@@ -250,9 +261,7 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
                                                          double2* __restrict__ Z, long long ldz,
                                                          long long zstride, int ienv,
                                                          float sgnenv) {
-  __shared__ double2 tab[kSinTab];
-  sin_table_init(tab);
-  __syncthreads();
+  const double2* tab = g_sin_tab;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = blockIdx.y;
   const int k = blockIdx.z;
@@ -393,7 +402,7 @@ __device__ void self_pair(double dl, double an, double ka, Cx* Au, Cx* Ad, Cx* P
   *P = Cx{add(tp.re, res3), tp.im};
 }
 
-__global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restrict__ oinst,
+__global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __restrict__ oinst,
                                                         const SrcInst* __restrict__ sinst,
                                                         const int* __restrict__ tiles, int off_rt_ids,
                                                         int off_ct_off, int off_ct_ids, int off_row_local,
@@ -401,9 +410,8 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
                                                         const FreqParams* __restrict__ fp,
                                                         double2* __restrict__ Z, long long ldz,
                                                         long long zstride) {
-  extern __shared__ __align__(16) unsigned char sm_all[];
-  double2* tab = reinterpret_cast<double2*>(sm_all);
-  unsigned char* sm = sm_all + kSinTab * sizeof(double2);
+  extern __shared__ __align__(16) unsigned char sm[];
+  const double2* tab = g_sin_tab;
   ObsInst* so = reinterpret_cast<ObsInst*>(sm);
   SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
   const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
@@ -421,7 +429,6 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
   const int q0 = ct_off[tc], nQ = ct_off[tc + 1] - q0;
   for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[rt_ids[o0 + i]];
   for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[ct_ids[q0 + i]];
-  sin_table_init(tab);
   __syncthreads();
   const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
 
@@ -491,9 +498,7 @@ __global__ void __launch_bounds__(256) fill_pair_kernel(const ObsInst* __restric
 
 // Diagnostic: the table-driven sin/cos next to CUDA's sincos() on the same inputs.
 __global__ void sincos_diag_kernel(const double* __restrict__ x, long long n, double* __restrict__ out) {
-  __shared__ double2 tab[kSinTab];
-  sin_table_init(tab);
-  __syncthreads();
+  const double2* tab = g_sin_tab;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     double s, c, sr, cr;
@@ -508,7 +513,29 @@ __global__ void sincos_diag_kernel(const double* __restrict__ x, long long n, do
 
 size_t pair_smem_bytes(const PairTiles& t) {
   const size_t head = ((size_t)t.max_o * sizeof(ObsInst) + (size_t)t.max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
-  return kSinTab * sizeof(double2) + head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
+  return head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
+}
+
+// Builds the sin/cos table of the current device once (on its own stream, waited for,
+// so every later launch on any stream sees it).
+cudaError_t ensure_sin_table() {
+  static std::mutex mu;
+  static std::vector<char> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+  if (done[dev]) return cudaSuccess;
+  cudaStream_t s = nullptr;
+  e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  sin_table_setup_kernel<<<1, kSinTab, 0, s>>>();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e == cudaSuccess) done[dev] = 1;
+  return e;
 }
 
 }  // namespace
@@ -516,6 +543,8 @@ size_t pair_smem_bytes(const PairTiles& t) {
 cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream) {
   if (nk <= 0 || p.npls <= 0) return cudaSuccess;
+  cudaError_t te = ensure_sin_table();
+  if (te != cudaSuccess) return te;
   const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
   if (p.pt.ok && p.d_tiles && !(force_entry && force_entry[0] == '1')) {
     const size_t smem = pair_smem_bytes(p.pt);
@@ -543,6 +572,7 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
 extern "C" wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void* stream) {
   if (n < 0 || (n > 0 && (!d_x || !d_out))) return WMOM_ERR_ARG;
   if (n == 0) return WMOM_OK;
+  if (wmom::ensure_sin_table() != cudaSuccess) return WMOM_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const long long blocks = (n + 255) / 256;
   wmom::sincos_diag_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(d_x, n, d_out);

@@ -345,8 +345,18 @@ __global__ void __launch_bounds__(NT) panel_rows_kernel(C* __restrict__ A, long 
   const bool own = t < cnt;  // this thread's row: base + t
   const int gr = base + t;
 
-  if (own)
-    for (int c = 0; c < nb; ++c) tile[(size_t)c * rpc + t] = A[(size_t)(j0 + c) * lda + gr];
+  if (own) {
+    // the row, 16 loads in flight at a time
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+      C v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < nb) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < nb) tile[(size_t)(c0 + u) * rpc + t] = v[u];
+    }
+  }
   __syncthreads();
 
   for (int j = 0; j < nb; ++j) {
@@ -550,47 +560,73 @@ __global__ void __launch_bounds__(256) trsm_kernel(const C* __restrict__ T, long
 }
 
 // FP32 unit-lower TRSM of the factorisation, B <- L^-1 B for an nb x nb unit lower L
-// (nb <= 64), one thread per column of B.  L is staged once per block in shared
-// memory and read by broadcast; the thread's column lives in registers, so the
-// substitution needs no barrier.  The order of operations is trsm_kernel's
-// (for k: for r > k: b_r -= l_rk b_k), so both give identical results.  Rows and
-// columns of L beyond nb are padded with the identity.
+// (nb <= 64), one thread per column of B.  L and the B block are staged once per
+// block in shared memory (loads batched, kILP in flight per thread); L is read by
+// broadcast.  Rows are solved in four blocks of 16 whose unknowns live in registers:
+// the block's own triangle, then its contribution to every row below.  For each row
+// the updates come in increasing k, i.e. in trsm_kernel's order of operations, so
+// both kernels give identical results.  Rows and columns of L beyond nb are zero.
 constexpr int kTrsmColThreads = 128;
 
 __global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const float2* __restrict__ T, long long ldt,
                                                                          float2* __restrict__ B, long long ldb,
                                                                          int nb, int ncols, long long tstride,
                                                                          long long bstride) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* Ls = reinterpret_cast<float2*>(smem_raw);  // [64][64] row-major: Ls[r*64 + k] = l_rk
-  float2* Bs = Ls + 64 * 64;                          // [64][kTrsmColThreads + 1]
+  constexpr int kILP = 8;
   constexpr int ldbs = kTrsmColThreads + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* Ls = reinterpret_cast<float2*>(smem_raw);  // [64][64] column-major: Ls[k*64 + r] = l_rk
+  float2* Bs = Ls + 64 * 64;                          // [64][ldbs]: Bs[r*ldbs + c]
   T += (size_t)blockIdx.y * tstride;
   B += (size_t)blockIdx.y * bstride;
   const int tid = threadIdx.x;
   const int c0 = blockIdx.x * kTrsmColThreads;
   const int nc = min(kTrsmColThreads, ncols - c0);
-  for (int idx = tid; idx < 64 * 64; idx += kTrsmColThreads) {
-    const int k = idx >> 6, r = idx & 63;  // column k, row r of L (reads down columns)
-    float2 v = make_float2(0.f, 0.f);
-    if (r < nb && k < nb && r > k) v = T[(size_t)k * ldt + r];
-    Ls[r * 64 + k] = v;
+  for (int i0 = tid; i0 < 64 * 64; i0 += kTrsmColThreads * kILP) {
+    float2 v[kILP];
+#pragma unroll
+    for (int u = 0; u < kILP; ++u) {
+      const int idx = i0 + u * kTrsmColThreads, k = idx >> 6, r = idx & 63;
+      v[u] = (idx < 64 * 64 && r < nb && k < nb && r > k) ? T[(size_t)k * ldt + r] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kILP; ++u)
+      if (i0 + u * kTrsmColThreads < 64 * 64) Ls[i0 + u * kTrsmColThreads] = v[u];
   }
-  for (int idx = tid; idx < 64 * nc; idx += kTrsmColThreads) {
-    const int c = idx >> 6, r = idx & 63;
-    Bs[r * ldbs + c] = r < nb ? B[(size_t)(c0 + c) * ldb + r] : make_float2(0.f, 0.f);
+  for (int i0 = tid; i0 < 64 * nc; i0 += kTrsmColThreads * kILP) {
+    float2 v[kILP];
+#pragma unroll
+    for (int u = 0; u < kILP; ++u) {
+      const int idx = i0 + u * kTrsmColThreads, c = idx >> 6, r = idx & 63;
+      v[u] = (idx < 64 * nc && r < nb) ? B[(size_t)(c0 + c) * ldb + r] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kILP; ++u) {
+      const int idx = i0 + u * kTrsmColThreads;
+      if (idx < 64 * nc) Bs[(idx & 63) * ldbs + (idx >> 6)] = v[u];
+    }
   }
   __syncthreads();
   if (tid < nc) {
-    float2 x[64];
+#pragma unroll 1
+    for (int r0 = 0; r0 < 64; r0 += 16) {
+      float2 x[16];
 #pragma unroll
-    for (int r = 0; r < 64; ++r) x[r] = Bs[r * ldbs + tid];
+      for (int i = 0; i < 16; ++i) x[i] = Bs[(r0 + i) * ldbs + tid];
 #pragma unroll
-    for (int k = 0; k < 63; ++k)
+      for (int k = 0; k < 15; ++k)
 #pragma unroll
-      for (int r = k + 1; r < 64; ++r) x[r] = cfms(x[r], Ls[r * 64 + k], x[k]);
+        for (int i = k + 1; i < 16; ++i) x[i] = cfms(x[i], Ls[(r0 + k) * 64 + r0 + i], x[k]);
 #pragma unroll
-    for (int r = 0; r < 64; ++r) Bs[r * ldbs + tid] = x[r];
+      for (int i = 0; i < 16; ++i) Bs[(r0 + i) * ldbs + tid] = x[i];
+#pragma unroll 1
+      for (int r = r0 + 16; r < 64; ++r) {
+        float2 b = Bs[r * ldbs + tid];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) b = cfms(b, Ls[(r0 + k) * 64 + r], x[k]);
+        Bs[r * ldbs + tid] = b;
+      }
+    }
   }
   __syncthreads();
   for (int idx = tid; idx < 64 * nc; idx += kTrsmColThreads) {

@@ -910,8 +910,11 @@ wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cud
 // factorisations of copies of the first matrix -- spans 1, 2, 4 at width 1, then
 // widths 1, 2, 4, ... at the best span -- and keeps the best time per matrix.
 // Results are cached per (n / 256, form); WMOM_LU_BATCH and WMOM_LU_SPAN override.
+// Without `timing` (requests on a serving path, where trial factorisations would add
+// to a request's latency) a cached result is used if there is one, else the widest
+// batch up to `limit` at span 2, and nothing is cached.
 wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
-                             size_t budget, LuConfig* out) {
+                             size_t budget, LuConfig* out, bool timing) {
   const size_t nn = (size_t)n * n;
   const size_t mat = mode == WMOM_MODE_MIXED ? sizeof(float2) * nn : sizeof(double2) * nn;
   int bmax = std::min({ws->max_batch, kMaxLuBatch, limit,
@@ -922,6 +925,8 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   if (mode != WMOM_MODE_MIXED) {
     // the FP64 form is bound by the FP64 pipe at every width worth batching
     *out = LuConfig{eb ? std::min(eb, bmax) : (n <= 2048 ? bmax : 1), 1};
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[{(n + 255) / 256, mode}] = *out;
     return WMOM_OK;
   }
   if (eb && es) {
@@ -938,6 +943,10 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     }
   }
   const int bcap = eb ? std::min(eb, bmax) : bmax;
+  if (!timing) {
+    *out = LuConfig{bcap, es ? es : 2};
+    return WMOM_OK;
+  }
   DevBuf rep64, lu, piv;
   SWEEP_TRY(rep64.alloc(sizeof(double2) * nn * bcap, s));
   SWEEP_TRY(lu.alloc(sizeof(float2) * nn * bcap, s));
@@ -953,21 +962,11 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     *per = ms / batch;
     return st;
   };
+  // widths first (at the default span), then spans at the chosen width: the span's
+  // saving is trailing-matrix traffic, which only shows at the width that will run
   LuConfig best{eb ? bcap : 1, es ? es : 2};
   float best_t = 1e30f;
-  if (!es) {
-    for (int span = 1; span <= kMaxSpan; span *= 2) {
-      float per = 0.f;
-      const wmom_status st = time_one(best.batch, span, &per);
-      if (st != WMOM_OK) return st;
-      if (per < best_t * 0.97f) {
-        best_t = per;
-        best.span = span;
-      }
-    }
-  }
   if (!eb) {
-    best_t = 1e30f;
     for (int cand = 1; cand <= bcap; cand *= 2) {
       float per = 0.f;
       const wmom_status st = time_one(cand, best.span, &per);
@@ -975,6 +974,21 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
       if (per < best_t * 0.95f) {
         best_t = per;
         best.batch = cand;
+      }
+    }
+  }
+  if (!es) {
+    best_t = 1e30f;
+    int cur = best.span;
+    for (int span = 1; span <= kMaxSpan; span *= 2) {
+      float per = 0.f;
+      const wmom_status st = time_one(best.batch, span, &per);
+      if (st != WMOM_OK) return st;
+      // keep the default unless another span is clearly faster
+      const float margin = span == cur ? 1.0f : 0.97f;
+      if (per < best_t * margin) {
+        best_t = per;
+        best.span = span;
       }
     }
   }
@@ -1018,7 +1032,7 @@ wmom_status run_sweep(const SweepArgs& a) {
     wmom_status st = fill_batch(p, a.freq_mhz + f0, nb, zall.as<double2>(), s);
     if (st != WMOM_OK) return st;
     if (B == 0) {
-      st = choose_lu_config(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &cfg);
+      st = choose_lu_config(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &cfg, true);
       if (st != WMOM_OK) return st;
       B = cfg.batch;
       SWEEP_TRY(lu.alloc((mixed ? mat32 : mat64) * B, s));
@@ -1060,7 +1074,7 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
   size_t fr = 0, tot = 0;
   SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
   LuConfig cfg;
-  st = choose_lu_config(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &cfg);
+  st = choose_lu_config(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &cfg, false);
   if (st != WMOM_OK) return st;
   fs->batch = cfg.batch;
   fs->span = cfg.span;
@@ -1105,3 +1119,13 @@ wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float a
 }
 
 }  // namespace wmom
+
+extern "C" wmom_status wmom_tuned_config(int n, int mode, int* batch, int* span) {
+  if (n <= 0 || (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED)) return WMOM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(wmom::g_tune_mu);
+  auto it = wmom::g_tuned.find({(n + 255) / 256, mode});
+  if (it == wmom::g_tuned.end()) return WMOM_ERR_ARG;
+  if (batch) *batch = it->second.batch;
+  if (span) *span = it->second.span;
+  return WMOM_OK;
+}
