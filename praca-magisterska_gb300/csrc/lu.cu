@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <climits>
 #include <cstddef>
+#include <cstdlib>
+#include <cstdint>
 #include <map>
 #include <mutex>
 #include <type_traits>
@@ -479,6 +481,192 @@ __global__ void __launch_bounds__(NT) panel_rows_kernel(C* __restrict__ A, long 
     for (int c = 0; c < nb; ++c) A[(size_t)(j0 + c) * lda + gr] = tile[(size_t)c * rpc + t];
 }
 
+// Cluster panel (FP32 precision form).  One thread-block cluster of CS CTAs per
+// matrix holds the panel (m rows x w columns) in the CTAs' shared memory, one row per
+// thread.  Per column: each CTA reduces its candidate, publishes it (value, row and
+// the candidate row) in its own shared memory, and the cluster meets at the hardware
+// cluster barrier; every CTA then reads the CS candidates and the winning row through
+// distributed shared memory.  No global memory and no software barrier on the
+// column path, and clusters do not depend on one another.  Same pivot rule and order
+// of operations per row as panel_kernel / panel_rows_kernel.
+constexpr int kClusterMax = 16;
+constexpr int kClusterThreads = 512;
+
+struct ClusterPub {
+  float val;
+  int row;
+  int pad[2];
+  float2 cand[64];
+  float2 diag[64];
+};
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
+  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p)), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float ld_cluster_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_cluster_s32(uint32_t a) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ float2 ld_cluster_f2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float2* __restrict__ A, long long lda,
+                                                                           int n, int j0, int w, int rpc,
+                                                                           int* __restrict__ ipiv,
+                                                                           GridBarrier* __restrict__ gb,
+                                                                           long long astride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ClusterPub* pub = reinterpret_cast<ClusterPub*>(smem_raw);  // [2]
+  float2* prow = reinterpret_cast<float2*>(pub + 2);         // winner row, 64
+  float2* dgr = prow + 64;                                    // diagonal row, 64
+  float2* tile = dgr + 64;                                    // column-major rpc x w
+  __shared__ float red_v[2][kClusterThreads / 32];
+  __shared__ int red_r[2][kClusterThreads / 32];
+
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
+  gb += blockIdx.y;
+  const unsigned cs = gridDim.x;  // the cluster spans blockIdx.x
+  const unsigned rank = cluster_rank();
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int base = j0 + (int)rank * rpc;
+  const int cnt = max(0, min(rpc, n - base));
+  const bool own = t < cnt;
+  const int gr = base + t;
+
+  if (own) {
+    for (int c0 = 0; c0 < w; c0 += 16) {
+      float2 v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + t] = v[u];
+    }
+  }
+  __syncthreads();
+
+  for (int j = 0; j < w; ++j) {
+    const int gj = j0 + j;
+    const int par = j & 1;
+    // 1. this CTA's candidate
+    float best = -1.f;
+    int brow = INT_MAX;
+    if (own && gr >= gj) {
+      best = cabs1(tile[(size_t)j * rpc + t]);
+      brow = gr;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      if (ov > best || (ov == best && orow < brow)) {
+        best = ov;
+        brow = orow;
+      }
+    }
+    if (lane == 0) {
+      red_v[par][warp] = best;
+      red_r[par][warp] = brow;
+    }
+    __syncthreads();
+    best = -1.f;
+    brow = INT_MAX;
+#pragma unroll
+    for (int q = 0; q < kClusterThreads / 32; ++q) {
+      const float v = red_v[par][q];
+      const int r = red_r[par][q];
+      if (v > best || (v == best && r < brow)) {
+        best = v;
+        brow = r;
+      }
+    }
+    // 2. publish it in this CTA's shared memory
+    ClusterPub& my = pub[par];
+    if (t == 0) {
+      my.val = best;
+      my.row = brow;
+    }
+    if (t < w) {
+      if (best >= 0.f) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
+      if (gj >= base && gj < base + cnt) my.diag[t] = tile[(size_t)t * rpc + (gj - base)];
+    }
+    // 3. the cluster meets (also orders this CTA's own threads)
+    cluster_sync_all();
+    // 4. winner over the cluster, computed by every warp from the CTAs' shared memory
+    float v = -1.f;
+    int r = INT_MAX, q = -1;
+    if (lane < (int)cs) {
+      v = ld_cluster_f32(map_rank(&pub[par].val, lane));
+      r = ld_cluster_s32(map_rank(&pub[par].row, lane));
+      q = lane;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, r, o);
+      const int oq = __shfl_xor_sync(0xffffffffu, q, o);
+      if (ov > v || (ov == v && orow < r)) {
+        v = ov;
+        r = orow;
+        q = oq;
+      }
+    }
+    const int prw = r;
+    const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
+    if (t < w) {
+      prow[t] = ld_cluster_f2(map_rank(&pub[par].cand[t], (unsigned)q));
+      if (prw != gj) dgr[t] = ld_cluster_f2(map_rank(&pub[par].diag[t], owner_gj));
+    }
+    __syncthreads();
+    if (rank == 0 && t == 0) ipiv[gj] = prw + 1;
+    const float2 piv = prow[j];
+    const bool zero = piv.x == 0.f && piv.y == 0.f;
+    if (zero && rank == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
+    // 5. this thread's row: interchange, then scale and rank-1 update below gj
+    if (own) {
+      if (prw != gj) {
+        if (gr == prw)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = dgr[c];
+        else if (gr == gj)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = prow[c];
+      }
+      if (gr > gj) {
+        float2 l = tile[(size_t)j * rpc + t];
+        if (!zero) {
+          l = cmul(l, crecip(piv));
+          tile[(size_t)j * rpc + t] = l;
+        }
+        for (int c = j + 1; c < w; ++c) tile[(size_t)c * rpc + t] = cfms(tile[(size_t)c * rpc + t], l, prow[c]);
+      }
+    }
+  }
+  // no CTA leaves while another may still read its shared memory
+  cluster_sync_all();
+  if (own)
+    for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + gr] = tile[(size_t)c * rpc + t];
+}
+
 // ------------------------------------------------------------- laswp ----
 // Interchanges of pivots [k0, k0+kn) applied to the columns [0, j_skip0) and
 // [j_skip1, ncols) of A: one thread per column, interchanges in order.
@@ -764,6 +952,21 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   }
   C acc = cmake<C>(0, 0);
   const int nsteps = UPPER ? nblk - 1 - b : b;
+  // this thread's 16 entries of an off-diagonal 64 x 64 tile: row r, columns g + 4i;
+  // the next tile is loaded (independent loads) before the wait for its x
+  constexpr int kPer = kTrsvB / 4;
+  auto load_tile = [&](int j, C* dst) {
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+    const C* col = A + (size_t)c0 * lda + r0 + r;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int c = g + 4 * i;
+      dst[i] = (r < rows && c < cols) ? col[(size_t)c * lda] : cmake<C>(0, 0);
+    }
+  };
+  C a_cur[kPer];
+  if (nsteps > 0) load_tile(UPPER ? nblk - 1 : 0, a_cur);
   for (int step = 0; step < nsteps; ++step) {
     const int j = UPPER ? nblk - 1 - step : step;
     if (tid == 0) {
@@ -783,10 +986,15 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
     const int cols = min(kTrsvB, n - c0);
     if (tid < cols) xs[tid] = __ldcg(&x[c0 + tid]);
     __syncthreads();
+    C a_next[kPer];
+    if (step + 1 < nsteps) load_tile(UPPER ? j - 1 : j + 1, a_next);
     if (r < rows) {
-      const C* col = A + (size_t)c0 * lda + r0 + r;
-      for (int c = g; c < cols; c += 4) acc = cfms(acc, col[(size_t)c * lda], xs[c]);
+#pragma unroll
+      for (int i = 0; i < kPer; ++i)
+        if (g + 4 * i < cols) acc = cfms(acc, a_cur[i], xs[g + 4 * i]);
     }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) a_cur[i] = a_next[i];
     __syncthreads();
   }
   part[g][r] = acc;
@@ -927,11 +1135,57 @@ size_t panel_smem(int rpc, int P) {
 // thread (rpc <= NT) while its shared memory fits.  Otherwise panel_kernel with at
 // least kMinRows rows per block: FP64 rank-1 updates are costly, so many blocks share
 // them; FP32 panels are latency-bound, so fewer blocks make each barrier cheaper.
+// WMOM_NO_CLUSTER_PANEL=1 keeps the FP32 panels on the cooperative kernels.
+bool cluster_panels_disabled() {
+  const char* e = std::getenv("WMOM_NO_CLUSTER_PANEL");
+  return e && e[0] == '1';
+}
+
 struct PanelLaunch {
   bool rows = false;
+  bool cluster = false;  // panel_cluster_kernel: P = cluster size
   int P = 1, rpc = 1;
+  int w = 64;            // panel width
   size_t smem = 0;
 };
+
+// Largest cluster size this device schedules for panel_cluster_kernel (8 is the
+// portable limit; 16 where the device allows it), probed once per device.
+int max_cluster_size(const DeviceLimits& lim) {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int best = 0;
+  const size_t smem = (size_t)lim.smem_optin - 4096;
+  if (allow_dynamic_smem((const void*)panel_cluster_kernel, smem) == cudaSuccess &&
+      cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaSuccess) {
+    for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs, 1, 1);
+      cfg.blockDim = dim3(kClusterThreads, 1, 1);
+      cfg.dynamicSmemBytes = smem;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)panel_cluster_kernel, &cfg) == cudaSuccess &&
+          nclusters >= 1)
+        best = cs;
+    }
+  }
+  cudaGetLastError();
+  cache[dev] = best;
+  return best;
+}
 
 template <typename C>
 PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
@@ -940,6 +1194,26 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
   using R = decltype(C{}.x);
   PanelLaunch pl;
   const size_t cap = (size_t)lim.smem_optin - 4096;
+  if (sizeof(R) == 4 && !cluster_panels_disabled()) {
+    // the smallest cluster whose CTAs hold at most 256 rows (512 if it must: the
+    // per-column row updates of a CTA grow with its rows), one per thread, and a panel
+    // at least 32 wide (64 where it fits)
+    const int csmax = max_cluster_size(lim);
+    const size_t head = 2 * sizeof(ClusterPub) + 2 * 64 * sizeof(float2);
+    for (int cs = 1; cs <= csmax; cs *= 2) {
+      const int rpc = (m + cs - 1) / cs;
+      if (rpc > kClusterThreads || (rpc > kClusterThreads / 2 && cs < csmax)) continue;
+      int w = (int)std::min<size_t>(64, (cap - head) / ((size_t)rpc * sizeof(float2)));
+      if (w < 64) w &= ~7;
+      if (w < 32) continue;
+      pl.cluster = true;
+      pl.P = cs;
+      pl.rpc = rpc;
+      pl.w = w;
+      pl.smem = head + (size_t)rpc * w * sizeof(float2);
+      return pl;
+    }
+  }
   if (sizeof(R) == 4) {
     const int P = (m + NT - 1) / NT;
     const int rpc = (m + P - 1) / P;
@@ -992,6 +1266,27 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     const int m = n - jp;
     const PanelLaunch pl = panel_launch<C>(m, lim);
     const int P = pl.P;
+    if constexpr (std::is_same<C, float2>::value) {
+      if (pl.cluster) {
+        if (w > pl.w) return cudaErrorInvalidValue;
+        cudaError_t ce = allow_dynamic_smem((const void*)panel_cluster_kernel, pl.smem);
+        if (ce != cudaSuccess) return ce;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(P, batch, 1);
+        cfg.blockDim = dim3(kClusterThreads, 1, 1);
+        cfg.dynamicSmemBytes = pl.smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = P;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
+        return cudaLaunchKernelEx(&cfg, panel_cluster_kernel, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
+      }
+    }
     const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
     cudaError_t pe = allow_dynamic_smem(kern, pl.smem);
     if (pe != cudaSuccess) return pe;
@@ -1067,12 +1362,12 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   // writes the trailing matrix 1/span as often.  Without the hook (FP64 SIMT GEMM,
   // bound by the FP64 pipe rather than by traffic) span is 1.
   const int S = gemm_hook ? std::max(1, std::min(span > 0 ? span : 2, kMaxSpan)) : 1;
-  for (int j0 = 0; j0 < n; j0 += S * NB) {
+  for (int j0 = 0; j0 < n;) {
     int c[kMaxSpan + 1], w[kMaxSpan];
     int np = 0;
     c[0] = j0;
     while (np < S && c[np] < n) {
-      w[np] = std::min(NB, n - c[np]);
+      w[np] = std::min(panel_launch<C>(n - c[np], lim).w, n - c[np]);
       c[np + 1] = c[np] + w[np];
       ++np;
     }
@@ -1094,6 +1389,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       }
       LU_TRY(update(cr, cr, rest, rest, j0, cr - j0));
     }
+    j0 = cr;
   }
 #undef LU_TRY
   return cudaSuccess;
@@ -1198,6 +1494,7 @@ int lu_max_batch(int n) {
   int best = kMaxLuBatch;
   for (int j0 = 0; j0 < n && best > 1; j0 += NB) {
     const PanelLaunch pl = panel_launch<C>(n - j0, lim);
+    if (pl.cluster) continue;  // clusters are independent of one another
     const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
     if (allow_dynamic_smem(kern, pl.smem) != cudaSuccess) return 1;
     int per_sm = 0;

@@ -112,3 +112,29 @@ def test_fp32_lu_backward_error(cuda, wmom, n):
     err_c, _ = _plu_backward_error(a.astype(np.complex128), lu_c.astype(np.complex128), piv_c + 1)
     assert err <= 10.0 * err_c + 1e-7, (err, err_c)
     assert lmax <= np.sqrt(2.0) * (1 + 1e-5), lmax
+
+
+def test_fp32_lu_large_panels(cuda, wmom):
+    """A size whose first panels need the widest clusters and a panel narrower than 64
+    columns (n = 7500): P A = L U checked on random probe vectors (a wrong update or
+    interchange gives an O(1) residual; FP32 rounding gives ~1e-5)."""
+    n = 7500
+    rng = np.random.default_rng(7500)
+    a = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))).astype(np.complex64)
+    at = cuda.from_numpy(np.ascontiguousarray(a.T)).to("cuda")
+    ipiv = cuda.zeros(n, dtype=cuda.int32, device="cuda")
+    info = wmom.cgetrf_device(at.data_ptr(), n, n, ipiv.data_ptr())
+    cuda.cuda.synchronize()
+    assert info == 0
+    lu = at.cpu().numpy().T
+    piv = ipiv.cpu().numpy() - 1
+    perm = np.arange(n)
+    for i, p in enumerate(piv):
+        perm[[i, p]] = perm[[p, i]]
+    x = (rng.normal(size=(n, 4)) + 1j * rng.normal(size=(n, 4))).astype(np.complex128)
+    ux = np.triu(lu).astype(np.complex128) @ x
+    lux = np.tril(lu, -1).astype(np.complex128) @ ux + ux
+    pax = a.astype(np.complex128)[perm] @ x
+    err = np.linalg.norm(pax - lux) / (np.linalg.norm(a.astype(np.complex128)) * np.linalg.norm(x) / np.sqrt(n))
+    assert err <= 3e-4, err
+    assert np.max(np.abs(np.tril(lu, -1))) <= np.sqrt(2.0) * (1 + 1e-5)
