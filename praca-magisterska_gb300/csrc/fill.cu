@@ -45,27 +45,27 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 // sin and cos of the phase k*R of the regular Green's function evaluations.
 // Table-driven method (Tang, "Table-driven implementation of the exponential
 // function", ACM TOMS 15(2), 1989, applied to sin/cos by angle addition):
-//   x = n*h + d,  h = pi/128,  |d| <= h/2 ~ 0.0123,
-//   sin x = S_j cos d + C_j sin d,  cos x = C_j cos d - S_j sin d,  j = n mod 256,
-// with (S_j, C_j) = (sin, cos)(j*pi/128) tabulated once per device by sincospi(j/128)
+//   x = n*h + d,  h = pi/512,  |d| <= h/2 ~ 0.00307,
+//   sin x = S_j cos d + C_j sin d,  cos x = C_j cos d - S_j sin d,  j = n mod 1024,
+// with (S_j, C_j) = (sin, cos)(j*pi/512) tabulated once per device by sincospi(j/512)
 // (an exact argument) and read through the read-only cache, d from a two-constant
 // Cody-Waite reduction
-// (h_hi = double(pi)/128 exactly, h_lo = (pi - double(pi))/128), and sin d, cos d
-// from their Taylor series to d^7 and d^6 (truncation below 2e-20 relative).
+// (h_hi = double(pi)/512 exactly, h_lo = (pi - double(pi))/512), and sin d, cos d
+// from their Taylor series to d^5 and d^4 (truncation below 2e-17 relative).
 // Arguments beyond 1e6 rad take sincos() itself.
 // ------------------------------------------------------------------------
-constexpr int kSinTab = 256;
-constexpr double kInvH = 40.743665431525205957;    // 128/pi
-constexpr double kHHi = 3.141592653589793116 / 128;  // double(pi)/128, exact
-constexpr double kHLo = 1.2246467991473532e-16 / 128;  // (pi - double(pi))/128
+constexpr int kSinTab = 1024;
+constexpr double kInvH = 162.97466172610082383;      // 512/pi
+constexpr double kHHi = 3.141592653589793116 / 512;  // double(pi)/512, exact
+constexpr double kHLo = 1.2246467991473532e-16 / 512;  // (pi - double(pi))/512
 
 __device__ double2 g_sin_tab[kSinTab];
 
 __global__ void sin_table_setup_kernel() {
-  const int j = threadIdx.x;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < kSinTab) {
     double sj, cj;
-    sincospi(j / 128.0, &sj, &cj);
+    sincospi(j / 512.0, &sj, &cj);
     g_sin_tab[j] = make_double2(sj, cj);
   }
 }
@@ -85,22 +85,12 @@ __device__ __forceinline__ void sincos_tab(double x, const double2* tab, double*
   d = fma(-n, kHLo, d);
   const double2 t = __ldg(&tab[__double2loint(tn) & (kSinTab - 1)]);
   const double d2 = d * d;
-  const double sd = fma(d * d2, fma(d2, fma(d2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), d);
-  const double cd = fma(d2, fma(d2, fma(d2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+  const double sd = fma(d * d2, fma(d2, 1.0 / 120.0, -1.0 / 6.0), d);
+  const double cd = fma(d2, fma(d2, 1.0 / 24.0, -0.5), 1.0);
   *s = fma(t.x, cd, t.y * sd);
   *c = fma(t.y, cd, -(t.x * sd));
 }
 
-// exp(-j*ka*R)/R for R^2 = r2: (cos(ka R)/R, -sin(ka R)/R), one reciprocal square
-// root instead of a square root and two divisions.
-__device__ __forceinline__ void green_reg(double r2, double ka, const double2* tab, double* gre, double* gim) {
-  const double ri = rsqrt(r2);
-  const double r = mul(r2, ri);
-  double sn, cs;
-  sincos_tab(mul(ka, r), tab, &sn, &cs);
-  *gre = mul(cs, ri);
-  *gim = -mul(sn, ri);
-}
 
 // Complete elliptic integral K, Hastings polynomial-log approximation with the
 // reference's coefficients (Zmatrix.cpp:738-747; Abramowitz & Stegun 17.3.34).
@@ -130,24 +120,37 @@ __device__ double ell_k(double bet) {
   return sub(a, mul(b, log(m1)));
 }
 
-// Gauss sums of one regular (observation point, source half) pair, the 2-point rule
-// of the reference's cwire1_re/cwire2_re + ckmn (Zmatrix.cpp:237-339, 450-555,
-// 667-692): with g = exp(-j ka R)/R at the two abscissae s[0], s[1] and
-// ex = r_m - r_s,  up = sum s/dl g,  dn = sum (dl - s)/dl g,  pl = sum g.
-// The ramp weights come precomputed (the host's s/dl and (dl - s)/dl).  Distances
-// and weighted sums are FMA-contracted; both fill kernels call this one routine,
-// so they produce identical matrices.
-__device__ __forceinline__ void regular_sums(const double ex[3], const double dc[3], double an2, const double s[2],
-                                             const double wu[2], const double wd[2], double ka, const double2* tab,
-                                             Cx* up, Cx* dn, Cx* pl) {
-  Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
+// One regular (observation point, source half) pair, the 2-point rule of the
+// reference's cwire1_re/cwire2_re + ckmn (Zmatrix.cpp:237-339, 450-555, 667-692),
+// in two parts.  The frequency-independent part gives R and 1/R at the two abscissae
+// s[0], s[1] (R^2 = a_n^2 + |ex - s dc|^2, ex = r_m - r_s, one reciprocal square
+// root).  The frequency part gives, with g = exp(-j ka R)/R,
+//   up = sum s/dl g,  dn = sum (dl - s)/dl g,  pl = sum g,
+// from the ramp weights the host precomputed.  Distances and weighted sums are
+// FMA-contracted; every fill kernel calls these routines, so all of them produce
+// identical matrices.
+__device__ __forceinline__ void gauss_geometry(const double ex[3], const double dc[3], double an2, const double s[2],
+                                               double r[2], double ri[2]) {
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
     const double dx = fma(-s[g], dc[0], ex[0]);
     const double dy = fma(-s[g], dc[1], ex[1]);
     const double dz = fma(-s[g], dc[2], ex[2]);
-    double gre, gim;
-    green_reg(fma(dx, dx, fma(dy, dy, fma(dz, dz, an2))), ka, tab, &gre, &gim);
+    const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, an2)));
+    ri[g] = rsqrt(r2);
+    r[g] = mul(r2, ri[g]);
+  }
+}
+
+__device__ __forceinline__ void gauss_sums(const double r[2], const double ri[2], const double wu[2],
+                                           const double wd[2], double ka, const double2* tab, Cx* up, Cx* dn,
+                                           Cx* pl) {
+  Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    double sn, cs;
+    sincos_tab(mul(ka, r[g]), tab, &sn, &cs);
+    const double gre = mul(cs, ri[g]), gim = -mul(sn, ri[g]);
     su.re = fma(wu[g], gre, su.re);
     su.im = fma(wu[g], gim, su.im);
     sd.re = fma(wd[g], gre, sd.re);
@@ -158,6 +161,14 @@ __device__ __forceinline__ void regular_sums(const double ex[3], const double dc
   *up = su;
   *dn = sd;
   *pl = sp;
+}
+
+__device__ __forceinline__ void regular_sums(const double ex[3], const double dc[3], double an2, const double s[2],
+                                             const double wu[2], const double wd[2], double ka, const double2* tab,
+                                             Cx* up, Cx* dn, Cx* pl) {
+  double r[2], ri[2];
+  gauss_geometry(ex, dc, an2, s, r, ri);
+  gauss_sums(r, ri, wu, wd, ka, tab, up, dn, pl);
 }
 
 // Abscissae and ramp weights of the 2-point rule on a source half of length dl, in
@@ -402,73 +413,63 @@ __device__ void self_pair(double dl, double an, double ka, Cx* Au, Cx* Ad, Cx* P
   *P = Cx{add(tp.re, res3), tp.im};
 }
 
-__global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __restrict__ oinst,
-                                                        const SrcInst* __restrict__ sinst,
-                                                        const int* __restrict__ tiles, int off_rt_ids,
-                                                        int off_ct_off, int off_ct_ids, int off_row_local,
-                                                        int off_col_local, int npls, int max_o, int max_q,
-                                                        const FreqParams* __restrict__ fp,
-                                                        double2* __restrict__ Z, long long ldz,
-                                                        long long zstride) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const double2* tab = g_sin_tab;
-  ObsInst* so = reinterpret_cast<ObsInst*>(sm);
-  SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
-  const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
-  PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
-  const int* rt_off = tiles;
-  const int* rt_ids = tiles + off_rt_ids;
-  const int* ct_off = tiles + off_ct_off;
-  const int* ct_ids = tiles + off_ct_ids;
-  const int* row_local = tiles + off_row_local;
-  const int* col_local = tiles + off_col_local;
+// The tile's index lists (offsets into one int array).
+struct TileLists {
+  const int* rt_off;
+  const int* rt_ids;
+  const int* ct_off;
+  const int* ct_ids;
+  const int* row_local;
+  const int* col_local;
+};
 
-  const int tr = blockIdx.x, tc = blockIdx.y, k = blockIdx.z;
-  const int tid = threadIdx.x;
-  const int o0 = rt_off[tr], nO = rt_off[tr + 1] - o0;
-  const int q0 = ct_off[tc], nQ = ct_off[tc + 1] - q0;
-  for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[rt_ids[o0 + i]];
-  for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[ct_ids[q0 + i]];
-  __syncthreads();
-  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+__device__ __forceinline__ TileLists tile_lists(const int* tiles, int off_rt_ids, int off_ct_off, int off_ct_ids,
+                                                int off_row_local, int off_col_local) {
+  return TileLists{tiles, tiles + off_rt_ids, tiles + off_ct_off, tiles + off_ct_ids, tiles + off_row_local,
+                   tiles + off_col_local};
+}
 
-  // phase A: distinct pairs of the tile
-  for (int p = tid; p < nO * nQ; p += blockDim.x) {
-    const int o = p / nQ, q = p - o * nQ;
-    const ObsInst& O = so[o];
-    const SrcInst& S = sq[q];
-    const bool same = (S.nl == O.ml && S.nr == O.mr) || (S.nl == O.mr && S.nr == O.ml);
-    const double t = dot3(S.dc, O.u);
-    PairVal v;
-    if (!same) {
-      const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
-      Cx su, sd, sp;
-      regular_sums(ex, S.dc, mul(S.an, S.an), S.s, S.w_up, S.w_dn, ka, tab, &su, &sd, &sp);
-      const double ht = mul(mul(S.dl, 0.5), t);
-      v.wu = make_double2(mul(su.re, ht), mul(su.im, ht));
-      v.wd = make_double2(mul(sd.re, ht), mul(sd.im, ht));
-      v.ph = make_double2(mul(0.5, sp.re), mul(0.5, sp.im));
-    } else {
-      Cx Au, Ad, P;
-      self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
-      v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
-      v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
-      v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
-    }
-    pt[p] = v;
-  }
-  __syncthreads();
+__device__ __forceinline__ bool same_segment(const ObsInst& O, const SrcInst& S) {
+  return (S.nl == O.ml && S.nr == O.mr) || (S.nl == O.mr && S.nr == O.ml);
+}
 
-  // phase B: entries of the tile (consecutive threads = consecutive rows)
-  for (int e = tid; e < kPairTile * kPairTile; e += blockDim.x) {
+// Phase A value of a regular pair from its R, 1/R and projection t.
+__device__ __forceinline__ PairVal regular_pair_value(const double r[2], const double ri[2], double t,
+                                                      const SrcInst& S, double ka, const double2* tab) {
+  Cx su, sd, sp;
+  gauss_sums(r, ri, S.w_up, S.w_dn, ka, tab, &su, &sd, &sp);
+  const double ht = mul(S.half, t);
+  PairVal v;
+  v.wu = make_double2(mul(su.re, ht), mul(su.im, ht));
+  v.wd = make_double2(mul(sd.re, ht), mul(sd.im, ht));
+  v.ph = make_double2(mul(0.5, sp.re), mul(0.5, sp.im));
+  return v;
+}
+
+// Phase A value of a self pair (identical segments).
+__device__ __forceinline__ PairVal self_pair_value(double t, const SrcInst& S, double ka) {
+  Cx Au, Ad, P;
+  self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
+  PairVal v;
+  v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
+  v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
+  v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
+  return v;
+}
+
+// Phase B: the entries of tile (tr, tc) from the pair values, consecutive threads
+// on consecutive rows (coalesced 16-byte stores), in the reference's order.
+__device__ __forceinline__ void assemble_tile(const PairVal* pt, int nQ, const TileLists& L, int tr, int tc, int npls,
+                                              double ka2, double cq, double2* __restrict__ Zk, long long ldz) {
+  for (int e = threadIdx.x; e < kPairTile * kPairTile; e += blockDim.x) {
     const int r = e % kPairTile, c = e / kPairTile;
     const int m = tr * kPairTile + r, n = tc * kPairTile + c;
     if (m >= npls || n >= npls) continue;
-    const int c0 = col_local[2 * n], c1 = col_local[2 * n + 1];
+    const int c0 = L.col_local[2 * n], c1 = L.col_local[2 * n + 1];
     double acc_re = 0.0, acc_im = 0.0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int rl = row_local[2 * m + h];
+      const int rl = L.row_local[2 * m + h];
       const int o = rl & 0x3FFFFFFF;
       const PairVal& pu = pt[o * nQ + c0];
       const PairVal& pd = pt[o * nQ + c1];
@@ -492,7 +493,108 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
     double2 out;
     out.x = -mul(cq, acc_im);
     out.y = mul(cq, acc_re);
-    Z[(size_t)k * zstride + (size_t)n * ldz + m] = out;
+    Zk[(size_t)n * ldz + m] = out;
+  }
+}
+
+// One CTA per tile and frequency (blockIdx.z).
+__global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __restrict__ oinst,
+                                                        const SrcInst* __restrict__ sinst,
+                                                        const int* __restrict__ tiles, int off_rt_ids,
+                                                        int off_ct_off, int off_ct_ids, int off_row_local,
+                                                        int off_col_local, int npls, int max_o, int max_q,
+                                                        const FreqParams* __restrict__ fp,
+                                                        double2* __restrict__ Z, long long ldz,
+                                                        long long zstride) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const double2* tab = g_sin_tab;
+  ObsInst* so = reinterpret_cast<ObsInst*>(sm);
+  SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
+  const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
+  PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
+  const TileLists L = tile_lists(tiles, off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local);
+  const int tr = blockIdx.x, tc = blockIdx.y, k = blockIdx.z;
+  const int tid = threadIdx.x;
+  const int o0 = L.rt_off[tr], nO = L.rt_off[tr + 1] - o0;
+  const int q0 = L.ct_off[tc], nQ = L.ct_off[tc + 1] - q0;
+  for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[L.rt_ids[o0 + i]];
+  for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[L.ct_ids[q0 + i]];
+  __syncthreads();
+  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+
+  // phase A: distinct pairs of the tile
+  for (int p = tid; p < nO * nQ; p += blockDim.x) {
+    const int o = p / nQ, q = p - o * nQ;
+    const ObsInst& O = so[o];
+    const SrcInst& S = sq[q];
+    const double t = dot3(S.dc, O.u);
+    if (!same_segment(O, S)) {
+      const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
+      double r[2], ri[2];
+      gauss_geometry(ex, S.dc, S.an2, S.s, r, ri);
+      pt[p] = regular_pair_value(r, ri, t, S, ka, tab);
+    } else {
+      pt[p] = self_pair_value(t, S, ka);
+    }
+  }
+  __syncthreads();
+  assemble_tile(pt, nQ, L, tr, tc, npls, ka2, cq, Z + (size_t)k * zstride, ldz);
+}
+
+// Frequency-independent values of a pair, kept in shared memory across frequencies.
+struct PairGeo {
+  double r[2], ri[2], t;
+};
+
+constexpr int kMultiThreads = 512;
+
+// One CTA of 16 warps per tile for all nk frequencies: the pairs' geometry (R, 1/R,
+// projection) is computed once, then for each frequency phase A (phase and ramps
+// only) and phase B.  The arithmetic per pair and entry is fill_pair_kernel's.
+__global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
+    const ObsInst* __restrict__ oinst, const SrcInst* __restrict__ sinst, const int* __restrict__ tiles,
+    int off_rt_ids, int off_ct_off, int off_ct_ids, int off_row_local, int off_col_local, int npls, int max_o,
+    int max_q, const FreqParams* __restrict__ fp, int nk, double2* __restrict__ Z, long long ldz,
+    long long zstride) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const double2* tab = g_sin_tab;
+  ObsInst* so = reinterpret_cast<ObsInst*>(sm);
+  SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
+  const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
+  PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
+  PairGeo* geo = reinterpret_cast<PairGeo*>(sm + pt_off + (size_t)max_o * max_q * sizeof(PairVal));
+  const TileLists L = tile_lists(tiles, off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local);
+  const int tr = blockIdx.x, tc = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int o0 = L.rt_off[tr], nO = L.rt_off[tr + 1] - o0;
+  const int q0 = L.ct_off[tc], nQ = L.ct_off[tc + 1] - q0;
+  for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[L.rt_ids[o0 + i]];
+  for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[L.ct_ids[q0 + i]];
+  __syncthreads();
+  for (int p = tid; p < nO * nQ; p += blockDim.x) {
+    const int o = p / nQ, q = p - o * nQ;
+    const ObsInst& O = so[o];
+    const SrcInst& S = sq[q];
+    PairGeo g;
+    g.t = dot3(S.dc, O.u);
+    if (!same_segment(O, S)) {
+      const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
+      gauss_geometry(ex, S.dc, S.an2, S.s, g.r, g.ri);
+    }
+    geo[p] = g;
+  }
+  __syncthreads();
+  for (int k = 0; k < nk; ++k) {
+    const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+    for (int p = tid; p < nO * nQ; p += blockDim.x) {
+      const int o = p / nQ, q = p - o * nQ;
+      const SrcInst& S = sq[q];
+      const PairGeo& g = geo[p];
+      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, ka) : regular_pair_value(g.r, g.ri, g.t, S, ka, tab);
+    }
+    __syncthreads();
+    assemble_tile(pt, nQ, L, tr, tc, npls, ka2, cq, Z + (size_t)k * zstride, ldz);
+    __syncthreads();
   }
 }
 
@@ -516,6 +618,10 @@ size_t pair_smem_bytes(const PairTiles& t) {
   return head + (size_t)t.max_o * t.max_q * sizeof(PairVal);
 }
 
+size_t pair_multi_smem_bytes(const PairTiles& t) {
+  return pair_smem_bytes(t) + (size_t)t.max_o * t.max_q * sizeof(PairGeo);
+}
+
 // Builds the sin/cos table of the current device once (on its own stream, waited for,
 // so every later launch on any stream sees it).
 cudaError_t ensure_sin_table() {
@@ -530,7 +636,7 @@ cudaError_t ensure_sin_table() {
   cudaStream_t s = nullptr;
   e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   if (e != cudaSuccess) return e;
-  sin_table_setup_kernel<<<1, kSinTab, 0, s>>>();
+  sin_table_setup_kernel<<<(kSinTab + 255) / 256, 256, 0, s>>>();
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
@@ -547,6 +653,23 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
   if (te != cudaSuccess) return te;
   const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
   if (p.pt.ok && p.d_tiles && !(force_entry && force_entry[0] == '1')) {
+    // several frequencies: one CTA of 16 warps per tile for all of them, when its
+    // shared memory fits (the geometry of the pairs is then computed once per tile)
+    const size_t msmem = pair_multi_smem_bytes(p.pt);
+    int dev = 0, smem_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const char* single = std::getenv("WMOM_FILL_SINGLE");
+    if (nk > 1 && msmem + 1024 <= (size_t)smem_optin && !(single && single[0] == '1')) {
+      cudaError_t e = allow_dynamic_smem((const void*)fill_pair_multi_kernel, msmem);
+      if (e != cudaSuccess) return e;
+      dim3 grid(p.pt.n_tiles, p.pt.n_tiles, 1);
+      stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
+      fill_pair_multi_kernel<<<grid, kMultiThreads, msmem, stream>>>(
+          p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off, p.off_ct_ids, p.off_row_local, p.off_col_local,
+          p.npls, p.pt.max_o, p.pt.max_q, reinterpret_cast<const FreqParams*>(d_fp), nk, z, ldz, zstride);
+      return cudaGetLastError();
+    }
     const size_t smem = pair_smem_bytes(p.pt);
     cudaError_t e = allow_dynamic_smem((const void*)fill_pair_kernel, smem);
     if (e != cudaSuccess) return e;

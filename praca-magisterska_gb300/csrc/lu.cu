@@ -1195,14 +1195,14 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
   PanelLaunch pl;
   const size_t cap = (size_t)lim.smem_optin - 4096;
   if (sizeof(R) == 4 && !cluster_panels_disabled()) {
-    // the smallest cluster whose CTAs hold at most 256 rows (512 if it must: the
-    // per-column row updates of a CTA grow with its rows), one per thread, and a panel
-    // at least 32 wide (64 where it fits)
+    // the smallest cluster whose CTAs hold one row per thread and a panel at least 32
+    // wide (64 where it fits): the cluster barrier and the remote reads cost more per
+    // column as the cluster grows, more than the rows a CTA saves
     const int csmax = max_cluster_size(lim);
     const size_t head = 2 * sizeof(ClusterPub) + 2 * 64 * sizeof(float2);
     for (int cs = 1; cs <= csmax; cs *= 2) {
       const int rpc = (m + cs - 1) / cs;
-      if (rpc > kClusterThreads || (rpc > kClusterThreads / 2 && cs < csmax)) continue;
+      if (rpc > kClusterThreads) continue;
       int w = (int)std::min<size_t>(64, (cap - head) / ((size_t)rpc * sizeof(float2)));
       if (w < 64) w &= ~7;
       if (w < 32) continue;

@@ -183,6 +183,8 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
         }
         si.dl = sh.dl;
         si.an = sh.an;
+        si.an2 = sh.an * sh.an;
+        si.half = sh.dl * 0.5;
         const double aa = 0.5 * (0.0 + sh.dl), bb = sh.dl - 0.0, cc = kGl2C * bb;
         si.s[0] = aa + cc;
         si.s[1] = aa - cc;

@@ -222,6 +222,17 @@ int env_int(const char* name, int lo, int hi) {
   return (b >= lo && b <= hi) ? b : 0;
 }
 
+// Krylov space per GMRES cycle and cycles per correction of the Krylov refinement
+// (WMOM_GMRES_RESTART, WMOM_GMRES_CYCLES override).
+int gmres_restart() {
+  const int v = env_int("WMOM_GMRES_RESTART", 4, 400);
+  return v ? v : 30;
+}
+int gmres_cycles() {
+  const int v = env_int("WMOM_GMRES_CYCLES", 1, 20);
+  return v ? v : 2;
+}
+
 }  // namespace
 
 // Vectors, scalars and the FP64-fallback factor of one group of up to B matrices.
@@ -763,8 +774,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       if (rel > kKrylovGain * prevr) break;
       prevr = rel;
       int steps = 0;
-      const wmom_status gs = gmres_correction(n, Zb, lub, ipb, g.r64.as<double2>(), dv.as<double2>(), ws, s, 30, 2,
-                                              1e-10, &steps);
+      const wmom_status gs = gmres_correction(n, Zb, lub, ipb, g.r64.as<double2>(), dv.as<double2>(), ws, s,
+                                              gmres_restart(), gmres_cycles(), 1e-10, &steps);
       if (gs != WMOM_OK) return gs;
       rep[b].krylov_steps += steps;
       rep[b].iterations += 1;

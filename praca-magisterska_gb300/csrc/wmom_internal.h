@@ -74,6 +74,7 @@ struct SrcInst {
   double rs[3];
   double dc[3];
   double dl, an;
+  double an2, half;  // an * an and dl * 0.5, as the per-entry kernel computes them
   double s[2];
   double w_up[2];  // s / dl        (rising ramp of S_n+)
   double w_dn[2];  // (dl - s) / dl (falling ramp of S_n-)

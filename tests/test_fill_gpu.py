@@ -119,3 +119,18 @@ def test_table_sincos_against_cuda_sincos(cuda, wmom):
     small = np.abs(x) < 1e-3
     assert np.max(np.abs(s[small] - sr[small]) / np.maximum(np.abs(sr[small]), 1e-300)) <= 4.5e-16
     assert np.all(np.abs(s * s + c * c - 1.0) <= 1e-15)
+
+
+@pytest.mark.parametrize("geo", ["random", "grid"])
+def test_multi_frequency_fill_equals_per_frequency_fill(cuda, wmom, geo, monkeypatch):
+    """The tile kernel that keeps each pair's geometry across a batch of frequencies
+    gives bit-identical matrices to the one-frequency-per-CTA kernel."""
+    topo = wmom.Topology(wmom.geometry.random_wires(700, seed=3) if geo == "random"
+                         else wmom.geometry.grid(8, 1.0, 1.0, 5e-3, None, 4))
+    freqs = [0.01, 0.7, 3.0, 10.0]
+    plan = wmom.Plan(topo)
+    z_multi = plan.fill(freqs).cpu().numpy()
+    monkeypatch.setenv("WMOM_FILL_SINGLE", "1")
+    z_single = plan.fill(freqs).cpu().numpy()
+    plan.close()
+    assert np.array_equal(z_multi, z_single)
