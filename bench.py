@@ -289,7 +289,8 @@ def run_wmom(args):
                 "peak_source": peak_src}
     else:
         achieved = work_per_launch / (avg_ms / 1e3) / 1e12
-        roof = {"kernel": {"fill": "fill_pair_kernel", "panel": "panel_kernel"}.get(dom, dom), "bound": "fp64",
+        fill_kernel = "fill_pair_multi_kernel" if plan.multi_frequency_fill and nf > 1 else "fill_pair_kernel"
+        roof = {"kernel": {"fill": fill_kernel, "panel": "panel_cluster_kernel"}.get(dom, dom), "bound": "fp64",
                 "unit": "TFLOP/s", "peak": fp64_peak,
                 "peak_source": "FP64 FMA pipe, measured in this run by wmom_probe_fp64_tflops "
                                "(MEASURED_PEAKS.json has no FP64 figure)"}
@@ -299,7 +300,7 @@ def run_wmom(args):
     # DRAM traffic per launch: bytes per unit from one ncu capture of a smaller case,
     # scaled by the units this launch processed (traffic grows in proportion)
     units = {"fill": work_per_launch / 384.0,            # Z entries (384 flop-eq each)
-             "tc_gemm": work_per_launch / (8.0 * 64)}.get(dom)  # complex entries of C (K = 64)
+             "tc_gemm": work_per_launch / (8.0 * 96)}.get(dom)  # complex entries of C (K = 96)
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             cap = json.load(f).get(roof["kernel"].split("::")[-1])
@@ -311,8 +312,8 @@ def run_wmom(args):
     if dom == "fill":
         roof["note"] = ("achieved counts 384 flop-eq per entry (8 Green's-function evaluations, as the reference "
                         "evaluates them); the pair-tiled kernel shares evaluations between neighbouring basis "
-                        "functions (about 2.1 per entry), so the fraction can exceed 1; the FP64 pipe itself is "
-                        "86% busy in the ncu capture")
+                        "functions (about 2.1 per entry) and their geometry between frequencies, so the fraction "
+                        "can exceed 1; the FP64 pipe itself is 81% busy in the ncu capture")
         alg = 16.0 * units  # each complex128 entry written once
         roof["hbm_view"] = {"algorithmic_bytes": alg, "achieved_gbs": alg / (avg_ms / 1e3) / 1e9,
                             "frac_of_hbm": alg / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"]}

@@ -88,9 +88,11 @@ wmom_status wmom_plan_destroy(wmom_plan plan);
 int wmom_plan_npls(wmom_plan plan);
 /* Bytes of per-geometry tables the plan uploaded to the device. */
 long long wmom_plan_upload_bytes(wmom_plan plan);
-/* 1 when the plan fills with the pair-tiled kernel (free space), 0 when with the
- * per-entry kernel (PEC ground image terms).  Setting WMOM_FILL_ENTRY=1 in the
- * environment forces the per-entry kernel. */
+/* 1 when the plan fills with the pair-tiled kernel (free space), 2 when it does and
+ * also fills a batch of frequencies with one CTA per tile for all of them, 0 when
+ * it fills with the per-entry kernel (PEC ground image terms).  WMOM_FILL_ENTRY=1 in
+ * the environment forces the per-entry kernel, WMOM_FILL_SINGLE=1 one CTA per tile
+ * and frequency. */
 int wmom_plan_fill_variant(wmom_plan plan);
 
 /* Fills nk impedance matrices, one per wave number ka[i] (host array), in FP64.

@@ -255,7 +255,9 @@ class Plan:
         self._h = h
         self.npls = topo.npls
         self.upload_bytes = int(_plan_upload_bytes(h))
-        self.fill_variant = "pair" if _plan_fill_variant(h) == 1 else "entry"
+        fv = _plan_fill_variant(h)
+        self.fill_variant = "pair" if fv >= 1 else "entry"
+        self.multi_frequency_fill = fv == 2
 
     def close(self):
         if self._h:

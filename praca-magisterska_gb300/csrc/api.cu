@@ -303,7 +303,11 @@ wmom_status wmom_plan_destroy(wmom_plan h) {
 
 int wmom_plan_npls(wmom_plan h) { return h ? h->p.npls : -1; }
 
-int wmom_plan_fill_variant(wmom_plan h) { return h ? (h->p.pt.ok ? 1 : 0) : -1; }
+int wmom_plan_fill_variant(wmom_plan h) {
+  if (!h) return -1;
+  if (!h->p.pt.ok) return 0;
+  return fill_multi_fits(h->p) ? 2 : 1;
+}
 
 wmom_status wmom_plan_set_loads(wmom_plan h, int nloads, const int* idx, const double* r_ohm,
                                 const double* l_uh) {

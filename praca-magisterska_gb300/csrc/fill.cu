@@ -646,6 +646,17 @@ cudaError_t ensure_sin_table() {
 
 }  // namespace
 
+bool fill_multi_fits(const Plan& p) {
+  if (!p.pt.ok) return false;
+  const char* single = std::getenv("WMOM_FILL_SINGLE");
+  if (single && single[0] == '1') return false;
+  int dev = 0, smem_optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return false;
+  return pair_multi_smem_bytes(p.pt) + 1024 <= (size_t)smem_optin;
+}
+
 cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream) {
   if (nk <= 0 || p.npls <= 0) return cudaSuccess;
@@ -656,11 +667,7 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
     // several frequencies: one CTA of 16 warps per tile for all of them, when its
     // shared memory fits (the geometry of the pairs is then computed once per tile)
     const size_t msmem = pair_multi_smem_bytes(p.pt);
-    int dev = 0, smem_optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const char* single = std::getenv("WMOM_FILL_SINGLE");
-    if (nk > 1 && msmem + 1024 <= (size_t)smem_optin && !(single && single[0] == '1')) {
+    if (nk > 1 && fill_multi_fits(p)) {
       cudaError_t e = allow_dynamic_smem((const void*)fill_pair_multi_kernel, msmem);
       if (e != cudaSuccess) return e;
       dim3 grid(p.pt.n_tiles, p.pt.n_tiles, 1);

@@ -131,6 +131,8 @@ namespace wmom {
 // Fill launcher (fill.cu).
 cudaError_t launch_fill(const Plan& p, const double* d_ka, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream);
+// True when batches of frequencies are filled with one CTA per tile for all of them.
+bool fill_multi_fits(const Plan& p);
 // Lets `func` launch with up to `bytes` of dynamic shared memory.  The cap is process-
 // wide state of the kernel, so it is only ever raised (to the device's opt-in maximum,
 // once per device and kernel): setting it per launch would race with another host
