@@ -978,7 +978,12 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   LuConfig best{eb ? bcap : 1, es ? es : 2};
   float best_t = 1e30f;
   if (!eb) {
-    for (int cand = 1; cand <= bcap; cand *= 2) {
+    // widths 1, 2, 4, ... and the widest one allowed (e.g. a whole 12-frequency sweep in
+    // one group: its panels then run once for all of them)
+    std::vector<int> cands;
+    for (int c = 1; c <= bcap; c *= 2) cands.push_back(c);
+    if (cands.back() != bcap) cands.push_back(bcap);
+    for (int cand : cands) {
       float per = 0.f;
       const wmom_status st = time_one(cand, best.span, &per);
       if (st != WMOM_OK) return st;
