@@ -529,6 +529,10 @@ __device__ __forceinline__ float2 ld_cluster_f2(uint32_t a) {
   return v;
 }
 
+// RPT rows per thread (1, or 2 for panels whose rows would otherwise need a cluster
+// wider than the GPU can hold for a whole batch at once): thread t owns rows t and
+// t + kClusterThreads of its CTA's slab.
+template <int RPT>
 __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float2* __restrict__ A, long long lda,
                                                                            int n, int j0, int w, int rpc,
                                                                            int* __restrict__ ipiv,
@@ -550,18 +554,21 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int base = j0 + (int)rank * rpc;
   const int cnt = max(0, min(rpc, n - base));
-  const bool own = t < cnt;
-  const int gr = base + t;
 
-  if (own) {
-    for (int c0 = 0; c0 < w; c0 += 16) {
-      float2 v[16];
 #pragma unroll
-      for (int u = 0; u < 16; ++u)
-        if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+  for (int rr = 0; rr < RPT; ++rr) {
+    const int lr = t + rr * kClusterThreads;  // local row
+    if (lr < cnt) {
+      const int gr = base + lr;
+      for (int c0 = 0; c0 < w; c0 += 16) {
+        float2 v[16];
 #pragma unroll
-      for (int u = 0; u < 16; ++u)
-        if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + t] = v[u];
+        for (int u = 0; u < 16; ++u)
+          if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+          if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + lr] = v[u];
+      }
     }
   }
   __syncthreads();
@@ -569,12 +576,19 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
   for (int j = 0; j < w; ++j) {
     const int gj = j0 + j;
     const int par = j & 1;
-    // 1. this CTA's candidate
+    // 1. this CTA's candidate (the thread's rows in increasing order: first on ties)
     float best = -1.f;
     int brow = INT_MAX;
-    if (own && gr >= gj) {
-      best = cabs1(tile[(size_t)j * rpc + t]);
-      brow = gr;
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int lr = t + rr * kClusterThreads;
+      if (lr < cnt && base + lr >= gj) {
+        const float v = cabs1(tile[(size_t)j * rpc + lr]);
+        if (v > best) {
+          best = v;
+          brow = base + lr;
+        }
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -643,28 +657,36 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
     const float2 piv = prow[j];
     const bool zero = piv.x == 0.f && piv.y == 0.f;
     if (zero && rank == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
-    // 5. this thread's row: interchange, then scale and rank-1 update below gj
-    if (own) {
+    // 5. this thread's rows: interchange, then scale and rank-1 update below gj
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int lr = t + rr * kClusterThreads;
+      if (lr >= cnt) continue;
+      const int gr = base + lr;
       if (prw != gj) {
         if (gr == prw)
-          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = dgr[c];
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + lr] = dgr[c];
         else if (gr == gj)
-          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = prow[c];
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + lr] = prow[c];
       }
       if (gr > gj) {
-        float2 l = tile[(size_t)j * rpc + t];
+        float2 l = tile[(size_t)j * rpc + lr];
         if (!zero) {
           l = cmul(l, crecip(piv));
-          tile[(size_t)j * rpc + t] = l;
+          tile[(size_t)j * rpc + lr] = l;
         }
-        for (int c = j + 1; c < w; ++c) tile[(size_t)c * rpc + t] = cfms(tile[(size_t)c * rpc + t], l, prow[c]);
+        for (int c = j + 1; c < w; ++c) tile[(size_t)c * rpc + lr] = cfms(tile[(size_t)c * rpc + lr], l, prow[c]);
       }
     }
   }
   // no CTA leaves while another may still read its shared memory
   cluster_sync_all();
-  if (own)
-    for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + gr] = tile[(size_t)c * rpc + t];
+#pragma unroll
+  for (int rr = 0; rr < RPT; ++rr) {
+    const int lr = t + rr * kClusterThreads;
+    if (lr < cnt)
+      for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + base + lr] = tile[(size_t)c * rpc + lr];
+  }
 }
 
 // ------------------------------------------------------------- laswp ----
@@ -1144,6 +1166,7 @@ bool cluster_panels_disabled() {
 struct PanelLaunch {
   bool rows = false;
   bool cluster = false;  // panel_cluster_kernel: P = cluster size
+  int rpt = 1;           // rows per thread of panel_cluster_kernel
   int P = 1, rpc = 1;
   int w = 64;            // panel width
   size_t smem = 0;
@@ -1161,8 +1184,11 @@ int max_cluster_size(const DeviceLimits& lim) {
   if (it != cache.end()) return it->second;
   int best = 0;
   const size_t smem = (size_t)lim.smem_optin - 4096;
-  if (allow_dynamic_smem((const void*)panel_cluster_kernel, smem) == cudaSuccess &&
-      cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+  if (allow_dynamic_smem((const void*)panel_cluster_kernel<1>, smem) == cudaSuccess &&
+      allow_dynamic_smem((const void*)panel_cluster_kernel<2>, smem) == cudaSuccess &&
+      cudaFuncSetAttribute(panel_cluster_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(panel_cluster_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
           cudaSuccess) {
     for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
       cudaLaunchConfig_t cfg = {};
@@ -1177,7 +1203,7 @@ int max_cluster_size(const DeviceLimits& lim) {
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)panel_cluster_kernel, &cfg) == cudaSuccess &&
+      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)panel_cluster_kernel<1>, &cfg) == cudaSuccess &&
           nclusters >= 1)
         best = cs;
     }
@@ -1195,24 +1221,33 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
   PanelLaunch pl;
   const size_t cap = (size_t)lim.smem_optin - 4096;
   if (sizeof(R) == 4 && !cluster_panels_disabled()) {
-    // the smallest cluster whose CTAs hold one row per thread and a panel at least 32
-    // wide (64 where it fits): the cluster barrier and the remote reads cost more per
-    // column as the cluster grows, more than the rows a CTA saves
+    // Preference: one row per thread in the smallest cluster (the cluster barrier and
+    // the remote reads cost more per column as the cluster grows); two rows per thread
+    // only for panels taller than 16 x 512 rows, which would otherwise need the
+    // cooperative kernel.  Two rows per thread in 8 CTAs instead of one in 16 for an
+    // N = 8192 batch of 12 was measured: the panel became 40% faster, but its
+    // 24-column width cost more in triangular solves, updates and launches.  The panel
+    // is 64 columns wide where the rows leave room, else narrower.
     const int csmax = max_cluster_size(lim);
     const size_t head = 2 * sizeof(ClusterPub) + 2 * 64 * sizeof(float2);
-    for (int cs = 1; cs <= csmax; cs *= 2) {
-      const int rpc = (m + cs - 1) / cs;
-      if (rpc > kClusterThreads) continue;
-      int w = (int)std::min<size_t>(64, (cap - head) / ((size_t)rpc * sizeof(float2)));
-      if (w < 64) w &= ~7;
-      if (w < 32) continue;
-      pl.cluster = true;
-      pl.P = cs;
-      pl.rpc = rpc;
-      pl.w = w;
-      pl.smem = head + (size_t)rpc * w * sizeof(float2);
-      return pl;
-    }
+    auto try_shape = [&](int rpt, int cs_lo, int cs_hi, int wmin) -> bool {
+      for (int cs = cs_lo; cs <= std::min(cs_hi, csmax); cs *= 2) {
+        const int rpc = (m + cs - 1) / cs;
+        if (rpc > rpt * kClusterThreads || (rpt > 1 && rpc <= kClusterThreads)) continue;
+        int w = (int)std::min<size_t>(64, (cap - head) / ((size_t)rpc * sizeof(float2)));
+        if (w < 64) w &= ~7;
+        if (w < wmin) continue;
+        pl.cluster = true;
+        pl.rpt = rpt;
+        pl.P = cs;
+        pl.rpc = rpc;
+        pl.w = w;
+        pl.smem = head + (size_t)rpc * w * sizeof(float2);
+        return true;
+      }
+      return false;
+    };
+    if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
   }
   if (sizeof(R) == 4) {
     const int P = (m + NT - 1) / NT;
@@ -1269,7 +1304,8 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     if constexpr (std::is_same<C, float2>::value) {
       if (pl.cluster) {
         if (w > pl.w) return cudaErrorInvalidValue;
-        cudaError_t ce = allow_dynamic_smem((const void*)panel_cluster_kernel, pl.smem);
+        const void* ck = pl.rpt == 2 ? (const void*)panel_cluster_kernel<2> : (const void*)panel_cluster_kernel<1>;
+        cudaError_t ce = allow_dynamic_smem(ck, pl.smem);
         if (ce != cudaSuccess) return ce;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(P, batch, 1);
@@ -1284,7 +1320,9 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
-        return cudaLaunchKernelEx(&cfg, panel_cluster_kernel, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
+        return pl.rpt == 2
+                   ? cudaLaunchKernelEx(&cfg, panel_cluster_kernel<2>, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride)
+                   : cudaLaunchKernelEx(&cfg, panel_cluster_kernel<1>, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
       }
     }
     const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;

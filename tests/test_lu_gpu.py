@@ -114,12 +114,13 @@ def test_fp32_lu_backward_error(cuda, wmom, n):
     assert lmax <= np.sqrt(2.0) * (1 + 1e-5), lmax
 
 
-def test_fp32_lu_large_panels(cuda, wmom):
-    """A size whose first panels need the widest clusters and a panel narrower than 64
-    columns (n = 7500): P A = L U checked on random probe vectors (a wrong update or
-    interchange gives an O(1) residual; FP32 rounding gives ~1e-5)."""
-    n = 7500
-    rng = np.random.default_rng(7500)
+@pytest.mark.parametrize("n", [7500, 9000])
+def test_fp32_lu_large_panels(cuda, wmom, n):
+    """Sizes whose first panels need the widest clusters and a panel narrower than 64
+    columns (n = 7500), or two rows per thread (n = 9000): P A = L U checked on random
+    probe vectors (a wrong update or interchange gives an O(1) residual; FP32 rounding
+    gives ~1e-5)."""
+    rng = np.random.default_rng(n)
     a = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))).astype(np.complex64)
     at = cuda.from_numpy(np.ascontiguousarray(a.T)).to("cuda")
     ipiv = cuda.zeros(n, dtype=cuda.int32, device="cuda")
