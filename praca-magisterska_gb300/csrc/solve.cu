@@ -667,11 +667,11 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   }
   bool fallback[kMaxLuBatch] = {}, active[kMaxLuBatch] = {};
   int stall[kMaxLuBatch] = {};
-  double prev[kMaxLuBatch];
+  double prev[kMaxLuBatch], rel_first[kMaxLuBatch], rel_best[kMaxLuBatch];
   for (int b = 0; b < bg; ++b) {
     fallback[b] = info[b] != 0;
     active[b] = !fallback[b];
-    prev[b] = HUGE_VAL;
+    prev[b] = rel_first[b] = rel_best[b] = HUGE_VAL;
   }
   const unsigned vgrid = (unsigned)(((size_t)n * bg + 255) / 256);
   // initial solve in FP32
@@ -692,6 +692,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       const double rel = std::sqrt(hs.rnorm2[b]) / g.vnorm;
       rep[b].rel_residual = rel;
       rep[b].iterations = it;
+      if (it == 0) rel_first[b] = rel;
+      if (rel < rel_best[b]) rel_best[b] = rel;
       // converged: the target is met, or the last correction no longer changes the
       // solution at FP64 resolution (systems whose FP64 residual floor lies above
       // the target); stalled or diverged: FP64 fallback
@@ -737,10 +739,14 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   }
   int tmp_info[kMaxLuBatch];
   if (lu_workspace_read_status(ws, tmp_info, s, 1)) return WMOM_ERR_TIMEOUT;
-  // GMRES-IR for the matrices whose plain refinement stalled (their FP32 factors are
-  // still a good preconditioner); the FP64 LU only if that stalls as well
+  // GMRES-IR for the matrices whose plain refinement made progress (at least a
+  // factor kKrylovEntry below the first residual) before it stalled: their FP32
+  // factors are still a usable preconditioner.  The others -- refinement diverged or
+  // barely moved, i.e. kappa * u_fp32 >> 1 -- go straight to the FP64 LU.
+  constexpr double kKrylovEntry = 1e-3;
   for (int b = 0; b < bg; ++b) {
     if (!fallback[b] || info[b] != 0) continue;
+    if (!(rel_best[b] <= kKrylovEntry * rel_first[b])) continue;
     double2* xb = g.x64.as<double2>() + (size_t)b * n;
     const double2* Zb = Z64 + (size_t)b * nn;
     const float2* lub = lu32 + (size_t)b * nn;
