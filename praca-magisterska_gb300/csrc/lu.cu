@@ -946,22 +946,27 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   using R = decltype(C{}.x);
   __shared__ C xs[kTrsvB];
   __shared__ C part[4][kTrsvB];
-  __shared__ int s_b, s_ok;
-  // batch: blockIdx.y selects the matrix, its right-hand side, flags and ticket
-  A += (size_t)blockIdx.y * astride;
-  x += (size_t)blockIdx.y * n;
-  flags += (size_t)blockIdx.y * flag_stride;
-  ticket += blockIdx.y;
+  __shared__ int s_b, s_m, s_ok;
   const int tid = threadIdx.x;
   const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  const int batch = (int)gridDim.x / nblk;  // the grid holds nblk blocks of each matrix
+  // One ticket counter per launch orders the CTAs: ticket t is block t / batch (in
+  // dependency order) of matrix t % batch.  The chains of all matrices of a batch
+  // advance together, and a CTA only waits on CTAs that took smaller tickets.
   if (tid == 0) {
     const unsigned t = atomicAdd(ticket, 1u);
-    s_b = UPPER ? nblk - 1 - (int)t : (int)t;
+    const int bi = (int)(t / (unsigned)batch);
+    s_m = (int)(t % (unsigned)batch);
+    s_b = UPPER ? nblk - 1 - bi : bi;
     s_ok = 1;
   }
   __syncthreads();
   const int b = s_b;
   if (b < 0 || b >= nblk) return;
+  // the matrix, its right-hand side and flags
+  A += (size_t)s_m * astride;
+  x += (size_t)s_m * n;
+  flags += (size_t)s_m * flag_stride;
   const int r0 = b * kTrsvB;
   const int rows = min(kTrsvB, n - r0);
   const int r = tid & (kTrsvB - 1), g = tid >> 6;
@@ -1468,11 +1473,11 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
       e = cudaMemsetAsync(ws->ticket, 0, sizeof(unsigned int) * batch, s);
       if (e != cudaSuccess) return e;
       if (pass == 0)
-        trsv_kernel<C, false><<<dim3(nblk, batch), 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                                    &ws->barrier->err, astride, ws->flag_cap);
+        trsv_kernel<C, false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                               &ws->barrier->err, astride, ws->flag_cap);
       else
-        trsv_kernel<C, true><<<dim3(nblk, batch), 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                                   &ws->barrier->err, astride, ws->flag_cap);
+        trsv_kernel<C, true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                              &ws->barrier->err, astride, ws->flag_cap);
     }
     return cudaGetLastError();
   }
