@@ -239,7 +239,8 @@ int gmres_cycles() {
 struct GroupScratch {
   int n = 0, B = 0;
   cudaStream_t s = nullptr;
-  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv;
+  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv, fb_x;
+  int fb_cap = 0;          // matrices per batched FP64 fallback factorisation
   std::vector<double> vh;  // excitation on the host
   double vnorm = 0.0;
   GroupScalars hs{};
@@ -557,7 +558,7 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
   if (mode == WMOM_MODE_MIXED)
     SWEEP_TRY(convert_flat_64_to_32(Z64, lu32, nn * bg, s));
-  else
+  else if (Z64 != lu64)  // Z64 == lu64: the matrices were copied in already
     SWEEP_TRY(cudaMemcpyAsync(lu64, Z64, sizeof(double2) * nn * bg, cudaMemcpyDeviceToDevice, s));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (ms) {
@@ -638,6 +639,9 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
   SWEEP_TRY(cudaGetLastError());
   return err ? WMOM_ERR_TIMEOUT : WMOM_OK;
 }
+
+wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
+                             size_t budget, LuConfig* out, bool timing);
 
 // Solves bg systems Z64[b] x = V with the factors of factor_group; the solutions end
 // in g.x64[0..bg).  Mixed: FP32 solve, FP64 refinement with a per-matrix activity
@@ -804,37 +808,51 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   }
   for (int b = 0; b < bg; ++b)
     if (!fallback[b]) rep[b].status = WMOM_OK;
-  // FP64 fallback, one matrix at a time, in the scratch factor buffer
-  for (int b = 0; b < bg; ++b) {
-    if (!fallback[b]) continue;
-    rep[b].fell_back = 1;
-    if (!g.fb_lu.p) {
-      SWEEP_TRY(g.fb_lu.alloc(sizeof(double2) * nn, s));
-      SWEEP_TRY(g.fb_ipiv.alloc(sizeof(int) * n, s));
-    }
-    int inf1 = 0;
-    const wmom_status fst = factor_group(WMOM_MODE_FP64, n, Z64 + (size_t)b * nn, 1, nullptr,
-                                         g.fb_lu.as<double2>(), g.fb_ipiv.as<int>(), ws, s, &inf1, nullptr, nullptr,
-                                         1);
-    if (fst != WMOM_OK) return fst;
-    // solve into slot b: move the vector through x64[0]
-    DevBuf keep;
-    SWEEP_TRY(keep.alloc(sizeof(double2) * n, s));
-    SWEEP_TRY(cudaMemcpyAsync(keep.p, g.x64.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-    SWEEP_TRY(cudaMemcpyAsync(g.x64.p, g.vrep.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-    SWEEP_TRY(lu_solve_t<double2>(g.fb_lu.as<double2>(), n, n, g.fb_ipiv.as<int>(), g.x64.as<double2>(), n, 1, ws,
-                                  s, 1, (long long)nn));
-    const wmom_status rs = group_residuals(g, Z64 + (size_t)b * nn, 1);
-    if (rs != WMOM_OK) return rs;
-    rep[b].rel_residual = std::sqrt(hs.rnorm2[0]) / g.vnorm;
-    rep[b].info = inf1;
-    rep[b].status = inf1 ? WMOM_ERR_SINGULAR : WMOM_OK;
-    if (b != 0) {
-      SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)b * n, g.x64.p, sizeof(double2) * n,
+  // FP64 fallback.  The matrices that fell back are copied into the scratch factor
+  // buffer and factored together, as wide as the plain FP64 form batches at this
+  // order: their panels then run side by side instead of one matrix after another.
+  int nfb = 0, fb[kMaxLuBatch];
+  for (int b = 0; b < bg; ++b)
+    if (fallback[b]) fb[nfb++] = b;
+  if (nfb == 0) return WMOM_OK;
+  if (g.fb_cap == 0) {
+    size_t fr = 0, tot = 0;
+    SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
+    LuConfig c64;
+    const wmom_status cs = choose_lu_config(WMOM_MODE_FP64, n, g.B, nullptr, ws, s, fr / 2, &c64, false);
+    if (cs != WMOM_OK) return cs;
+    const int cap = std::max(1, std::min(c64.batch, g.B));
+    SWEEP_TRY(g.fb_lu.alloc(sizeof(double2) * nn * cap, s));
+    SWEEP_TRY(g.fb_ipiv.alloc(sizeof(int) * (size_t)n * cap, s));
+    SWEEP_TRY(g.fb_x.alloc(sizeof(double2) * (size_t)n * cap, s));
+    g.fb_cap = cap;
+  }
+  double2* flu = g.fb_lu.as<double2>();
+  double2* fx = g.fb_x.as<double2>();
+  for (int c0 = 0; c0 < nfb; c0 += g.fb_cap) {
+    const int cn = std::min(g.fb_cap, nfb - c0);
+    for (int j = 0; j < cn; ++j)
+      SWEEP_TRY(cudaMemcpyAsync(flu + (size_t)j * nn, Z64 + (size_t)fb[c0 + j] * nn, sizeof(double2) * nn,
                                 cudaMemcpyDeviceToDevice, s));
-      SWEEP_TRY(cudaMemcpyAsync(g.x64.p, keep.p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    int inf[kMaxLuBatch] = {};
+    const wmom_status fst = factor_group(WMOM_MODE_FP64, n, flu, cn, nullptr, flu, g.fb_ipiv.as<int>(), ws, s, inf,
+                                         nullptr, nullptr, 1);
+    if (fst != WMOM_OK) return fst;
+    // every slot of vrep holds the excitation
+    SWEEP_TRY(cudaMemcpyAsync(fx, g.vrep.p, sizeof(double2) * (size_t)n * cn, cudaMemcpyDeviceToDevice, s));
+    SWEEP_TRY(lu_solve_t<double2>(flu, n, n, g.fb_ipiv.as<int>(), fx, n, 1, ws, s, cn, (long long)nn));
+    for (int j = 0; j < cn; ++j) {
+      const int b = fb[c0 + j];
+      SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)b * n, fx + (size_t)j * n, sizeof(double2) * n,
+                                cudaMemcpyDeviceToDevice, s));
+      rep[b].fell_back = 1;
+      rep[b].info = inf[j];
+      rep[b].status = inf[j] ? WMOM_ERR_SINGULAR : WMOM_OK;
     }
   }
+  const wmom_status rs = group_residuals(g, Z64, bg);
+  if (rs != WMOM_OK) return rs;
+  for (int j = 0; j < nfb; ++j) rep[fb[j]].rel_residual = std::sqrt(hs.rnorm2[fb[j]]) / g.vnorm;
   return WMOM_OK;
 }
 
