@@ -147,6 +147,16 @@ wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, in
 wmom_status wmom_cgemm_sub_tc(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
                               long long ldb, void* c_dev, long long ldc, void* stream);
 
+/* The precision form's second-tier trailing update: C -= A * B for complex FP64
+ * (double2) column-major device matrices, C m x n, A m x k, B k x n, to FP64-grade
+ * accuracy on the bf16 tensor cores.  Each row of A and column of B is split into
+ * six 8-bit digit planes under a power-of-two scale (an error-free transformation);
+ * digit products of the same weight are summed exactly in FP32 accumulators and
+ * the weights are recombined in FP64.  Normwise error about 2^-45 relative to
+ * k * max|A| * max|B|.  No reference counterpart; exposed for testing. */
+wmom_status wmom_zgemm_sub_emul(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
+                                long long ldb, void* c_dev, long long ldc, void* stream);
+
 /* ----------------------------------------------------------- solver ---- */
 typedef enum wmom_mode {
   WMOM_MODE_FP64 = 0, /* plain form: FP64 fill, FP64 LU, FP64 solves */
@@ -158,11 +168,14 @@ typedef enum wmom_mode {
 typedef struct wmom_report {
   double rel_residual;  /* ||V - Z I||_2 / ||V||_2 of the returned currents (FP64) */
   int iterations;       /* refinement steps taken (0 for WMOM_MODE_FP64) */
-  int fell_back;        /* 1 if the FP64 LU was used after refinement stalled */
+  int fell_back;        /* 1 if the FP32 factors were left for FP64-grade ones (tier 2 or 3) */
   int info;             /* LAPACK-style info of the factorisation that produced I */
   int status;           /* wmom_status of this frequency */
   int krylov_steps;     /* GMRES steps of the Krylov refinement (0 when plain refinement
                            converged or for WMOM_MODE_FP64) */
+  int tier;             /* factors behind I: 1 FP32 tensor-core LU + FP64 refinement,
+                           2 FP64 LU with tensor-core (digit-plane) trailing updates +
+                           FP64 refinement, 3 plain FP64 LU; 0 for WMOM_MODE_FP64 */
 } wmom_report;
 
 /* Lumped series loads for the sweeps of this plan: Z[k-1, k-1] += r_ohm + j*2*pi*f*l_uh
@@ -212,7 +225,8 @@ const char* wmom_last_error(void);
 /* Launch counters per kernel class are always kept.  With timing enabled every
  * launch is also bracketed by CUDA events on its own stream.  Classes, in order:
  * 0 fill, 1 panel, 2 tensor-core GEMM, 3 SIMT GEMM, 4 triangular solves,
- * 5 row interchanges, 6 FP64 residual, 7 other.  wmom_stats_read fills up to n
+ * 5 row interchanges, 6 FP64 residual, 7 other, 8 FP64-grade tensor-core GEMM
+ * (the precision form's second tier).  wmom_stats_read fills up to n
  * entries of each array (any may be NULL) and returns the number of classes;
  * ms = summed device time, launches = launches issued, timed = launches timed,
  * work = algorithmic flops (bytes for the residual) of the timed launches.  The

@@ -63,7 +63,7 @@ class _Topology(ctypes.Structure):
 class _Report(ctypes.Structure):
     _fields_ = [("rel_residual", ctypes.c_double), ("iterations", ctypes.c_int),
                 ("fell_back", ctypes.c_int), ("info", ctypes.c_int), ("status", ctypes.c_int),
-                ("krylov_steps", ctypes.c_int)]
+                ("krylov_steps", ctypes.c_int), ("tier", ctypes.c_int)]
 
 
 def _sig(name, res, args):
@@ -112,7 +112,7 @@ _probe_fp64 = _sig("wmom_probe_fp64_tflops", ctypes.c_int, [_dp])
 _diag_sincos = _sig("wmom_diag_sincos", ctypes.c_int, [_vp, ctypes.c_longlong, _vp, _vp])
 _tuned_config = _sig("wmom_tuned_config", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip])
 
-STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc"]
+STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc", "emul_gemm"]
 
 
 def stats_enable(on=True):
@@ -309,7 +309,7 @@ class Plan:
         if st not in (WMOM_OK, 3):
             raise WmomError(st, "wmom_solve_sweep")
         reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
-                        info=r.info, status=r.status, krylov_steps=r.krylov_steps) for r in reps]
+                        info=r.info, status=r.status, krylov_steps=r.krylov_steps, tier=r.tier) for r in reps]
         return cur, zin, reports
 
 
@@ -338,7 +338,7 @@ class Factors:
         if st not in (WMOM_OK, 3):
             raise WmomError(st, "wmom_factors_solve")
         reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
-                        info=r.info, status=r.status, krylov_steps=r.krylov_steps) for r in reps]
+                        info=r.info, status=r.status, krylov_steps=r.krylov_steps, tier=r.tier) for r in reps]
         return cur, zin, reports
 
     def close(self):

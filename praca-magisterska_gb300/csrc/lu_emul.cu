@@ -1,0 +1,499 @@
+// lu_emul.cu -- FP64-grade complex trailing update of the LU on the bf16 tensor
+// cores (tcgen05 kind::f16), the second tier of the precision form:
+//
+//   C (M x N complex128, column-major) -= A (M x K complex) * B (K x N complex)
+//
+// Method: error-free splitting in the manner of Ozaki, Ogita, Oishi and Rump
+// ("Error-free transformations of matrix multiplication by using fast routines of
+// matrix multiplication and its applications", Numer. Algorithms 59, 2012),
+// arranged for FP32 tensor-core accumulation:
+//   * complex -> real as in lu_tc.cu: A' (M x 2K) interleaves (re, im) along K,
+//     B'^T (2N x 2K) has rows 2n = (Br, -Bi) and 2n+1 = (Bi, Br);
+//   * row m of A' is scaled by 2^-ea[m] (ea = the exponent of its largest entry,
+//     so the scaled entries lie in (-1, 1)), column n of B by 2^-eb[n];
+//   * a scaled entry x is written as NS signed 8-bit digits,
+//       x = sum_t d_t 2^(-8(t+1)) + rest,  d_t = rint(256 x_t), x_(t+1) = 256 x_t - d_t,
+//     every step exact in FP64, |d_0| <= 256, |d_t| <= 128; plane t stores
+//     d_t 2^(-8t), exact in bf16;
+//   * the product of planes i and j has weight 2^(-8(i+j)) ("level" i + j); the
+//     levels 0, 1 and 2 each go to their own TMEM accumulator, where their sums
+//     are exact in FP32 as long as 2K <= 192 (|level-2 sum| <= 192 (2*256*128 +
+//     128^2) 2^-16 < 2^24 2^-16); levels 3..NS-1 share a fourth accumulator,
+//     whose FP32 rounding is below 2^-48 of the leading term;
+//   * the epilogue adds the four accumulators in FP64, scales by 2^(ea + eb - 16)
+//     and subtracts the result from C.
+// Dropped levels (i + j >= NS) and the digit remainder are about 2^-45 of
+// K * max|A| * max|B|, so the factorisation this update serves is FP64-grade
+// (backward error near FP64 LU's); the FP64 refinement checks every solution.
+//
+// Kernel: persistent, one CTA (6 warps) per SM, 128 x 128 real output tiles
+// (64 complex columns).  A producer thread streams K in chunks of 32 bf16 (one
+// 64-byte swizzle row) of all 2 x NS planes with 4-D TMA into a 2-stage ring; an
+// MMA thread issues the 21 plane products (2 K-steps each) of a chunk into the four
+// accumulators; four epilogue warps read their 32-lane quarter with tcgen05.ld and
+// update C.  The accumulators fill TMEM (4 x 128 columns), so the epilogue of a
+// tile and the MMAs of the next one do not overlap.  Every wait is bounded; on
+// timeout the kernel records an error, skips the rest and still frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <mutex>
+#include <vector>
+
+#include "lu_common.cuh"
+#include "solve_internal.h"
+#include "stats.h"
+#include "tcgen05_util.cuh"
+
+namespace wmom {
+namespace emul {
+
+using namespace tc;
+
+constexpr int BM = 128;                           // accumulator lanes = rows of C per tile
+constexpr int BN = 128;                           // real columns = 64 complex columns of C
+constexpr int KC = 32;                            // bf16 of K per chunk (64 bytes)
+constexpr int NS = 6;                             // digit planes per operand
+constexpr int NLEV = 4;                           // accumulators: levels 0, 1, 2, then 3..NS-1
+constexpr int STAGES = 2;
+constexpr int TILE_BYTES = BM * KC * 2;           // one plane's tile (A and B alike)
+constexpr int STAGE_BYTES = 2 * NS * TILE_BYTES;  // 96 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
+constexpr int NTHREADS = 192;                     // producer warp, MMA warp, 4 epilogue warps
+constexpr int TMEM_COLS = NLEV * BN;              // 512: all of TMEM
+constexpr int kMaxK = 96;                         // complex K per launch (2K <= 192)
+
+static_assert(BN == BM, "A and B tiles share TILE_BYTES");
+static_assert(NS * (NS + 1) / 2 == 21, "plane products per chunk");
+
+// Instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+// 2^e as a double (exact; ldexp outside the normal range).
+__device__ __forceinline__ double pow2(int e) {
+  if (e >= -1022 && e <= 1023) return __hiloint2double((e + 1023) << 20, 0);
+  return ldexp(1.0, e);
+}
+
+// Plane values of x in (-1, 1): p[t] = d_t 2^(-8t) with the digits above.
+__device__ __forceinline__ void digit_planes(double x, float p[NS]) {
+  float w = 1.0f;
+#pragma unroll
+  for (int t = 0; t < NS; ++t) {
+    const double y = x * 256.0;
+    const double d = rint(y);
+    p[t] = (float)d * w;
+    x = y - d;
+    w *= 0x1p-8f;
+  }
+}
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// ---------------------------------------------------------------- pack ----
+// A (M x K complex, column-major) -> NS planes of A' (row-major M x K2p bf16,
+// zero beyond 2K) and the row exponents ea.  One thread per row.
+__global__ void emul_pack_a_kernel(const double2* __restrict__ A, long long lda, int M, int K, int K2p,
+                                   __nv_bfloat16* __restrict__ planes, size_t plane_elems,
+                                   int* __restrict__ ea, long long astride) {
+  const int b = blockIdx.y;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  A += (size_t)b * astride;
+  double mx = 0.0;
+  for (int k = 0; k < K; ++k) {
+    const double2 v = A[(size_t)k * lda + m];
+    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+  }
+  int e = 0;
+  frexp(mx, &e);  // mx < 2^e; e = 0 for a zero row
+  ea[(size_t)b * M + m] = e;
+  const double sc = pow2(-e);
+  __nv_bfloat16* row = planes + ((size_t)b * M + m) * K2p;
+  for (int k0 = 0; k0 < K2p / 2; k0 += 4) {  // 4 complex = 8 bf16 = 16 bytes per plane
+    float pr[4][NS], pi[4][NS];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      double2 v = make_double2(0.0, 0.0);
+      if (k0 + u < K) v = A[(size_t)(k0 + u) * lda + m];
+      digit_planes(v.x * sc, pr[u]);
+      digit_planes(v.y * sc, pi[u]);
+    }
+#pragma unroll
+    for (int t = 0; t < NS; ++t) {
+      uint4 q;
+      q.x = bf16x2(pr[0][t], pi[0][t]);
+      q.y = bf16x2(pr[1][t], pi[1][t]);
+      q.z = bf16x2(pr[2][t], pi[2][t]);
+      q.w = bf16x2(pr[3][t], pi[3][t]);
+      *reinterpret_cast<uint4*>(row + (size_t)t * plane_elems + 2 * k0) = q;
+    }
+  }
+}
+
+// B (K x N complex, column-major) -> NS planes of B'^T (row-major 2N x K2p bf16)
+// and the column exponents eb.  One warp per column (lanes along K).
+__global__ void emul_pack_b_kernel(const double2* __restrict__ B, long long ldb, int K, int N, int K2p,
+                                   __nv_bfloat16* __restrict__ planes, size_t plane_elems,
+                                   int* __restrict__ eb, long long bstride) {
+  const int b = blockIdx.y;
+  const int lane = threadIdx.x & 31;
+  const int n = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (n >= N) return;  // warp-uniform
+  B += (size_t)b * bstride + (size_t)n * ldb;
+  double mx = 0.0;
+  for (int k = lane; k < K; k += 32) {
+    const double2 v = B[k];
+    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  frexp(mx, &e);
+  if (lane == 0) eb[(size_t)b * N + n] = e;
+  const double sc = pow2(-e);
+  __nv_bfloat16* r0 = planes + ((size_t)b * 2 * N + 2 * (size_t)n) * K2p;
+  __nv_bfloat16* r1 = r0 + K2p;
+  for (int k = lane; k < K2p / 2; k += 32) {
+    double2 v = make_double2(0.0, 0.0);
+    if (k < K) v = B[k];
+    float pr[NS], pi[NS];
+    digit_planes(v.x * sc, pr);
+    digit_planes(v.y * sc, pi);
+#pragma unroll
+    for (int t = 0; t < NS; ++t) {
+      *reinterpret_cast<uint32_t*>(r0 + (size_t)t * plane_elems + 2 * k) = bf16x2(pr[t], -pi[t]);
+      *reinterpret_cast<uint32_t*>(r1 + (size_t)t * plane_elems + 2 * k) = bf16x2(pi[t], pr[t]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- gemm ----
+struct TileCoord {
+  int mat, m0, j0;
+};
+
+__device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n) {
+  const int per_mat = tiles_m * tiles_n;
+  const int mat = t / per_mat;
+  const int r = t - mat * per_mat;
+  const int tn = r / tiles_m;
+  return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    zgemm_sub_emul_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                          const int* __restrict__ ea, const int* __restrict__ eb, double2* __restrict__ C,
+                          long long ldc, int M, int N, int nchunks, int tiles_m, int tiles_n, int ntiles,
+                          int* __restrict__ err, long long cstride) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+  // bars: full[STAGES], empty[STAGES], tfull, tempty
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int s_fail;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
+  auto empty_bar = [&](int s) { return smem_u32(&bars[STAGES + s]); };
+  const uint32_t tfull_bar = smem_u32(&bars[2 * STAGES]);
+  const uint32_t tempty_bar = smem_u32(&bars[2 * STAGES + 1]);
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    mbar_init(tfull_bar, 1);
+    mbar_init(tempty_bar, NTHREADS / 32 - 2);  // one arrival per epilogue warp
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = *reinterpret_cast<const volatile int*>(err) != 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------ TMA producer
+      int it = 0;
+      bool ok = !s_fail;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+        for (int c = 0; c < nchunks; ++c) {
+          const int s = it % STAGES, use = it / STAGES;
+          if (use > 0 && !(ok = role_wait(empty_bar(s), (use - 1) & 1, err, &s_fail))) break;
+          const uint32_t a0 = smem_u32(base + s * STAGE_BYTES);
+          const uint32_t b0 = a0 + NS * TILE_BYTES;
+          mbar_expect_tx(full_bar(s), STAGE_BYTES);
+#pragma unroll
+          for (int p = 0; p < NS; ++p) {
+            tma_load_4d(a0 + p * TILE_BYTES, &mapA, c * KC, tc.m0, tc.mat, p, full_bar(s));
+            tma_load_4d(b0 + p * TILE_BYTES, &mapB, c * KC, tc.j0, tc.mat, p, full_bar(s));
+          }
+          ++it;
+        }
+      }
+      if (!ok) {
+        s_fail = 1;
+        atomicExch(err, 1);
+        const int zero = 0;
+        const volatile int no_fail = 0;
+        for (int i = it > STAGES ? it - STAGES : 0; i < it; ++i)
+          role_wait(full_bar(i % STAGES), (i / STAGES) & 1, &zero, &no_fail);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ------------------------------------------------------- MMA issuer
+      int it = 0, tl = 0;
+      bool ok = !s_fail;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tl) {
+        if (tl > 0 && !(ok = role_wait(tempty_bar, (tl - 1) & 1, err, &s_fail))) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int c = 0; c < nchunks; ++c) {
+          const int s = it % STAGES;
+          if (!(ok = role_wait(full_bar(s), (it / STAGES) & 1, err, &s_fail))) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a0 = smem_u32(base + s * STAGE_BYTES);
+          const uint32_t b0 = a0 + NS * TILE_BYTES;
+#pragma unroll
+          for (int L = 0; L < NS; ++L) {
+            const uint32_t acc = tmem + (uint32_t)(min(L, NLEV - 1) * BN);
+#pragma unroll
+            for (int i = 0; i <= L; ++i) {
+              const int j = L - i;
+#pragma unroll
+              for (int kk = 0; kk < KC / 16; ++kk) {
+                // the first product into accumulators 0..NLEV-1 of a tile overwrites
+                const uint32_t accum = (c == 0 && i == 0 && kk == 0 && L < NLEV) ? 0u : 1u;
+                mma_bf16(acc, sdesc_sw<64>(a0 + i * TILE_BYTES + kk * 32),
+                         sdesc_sw<64>(b0 + j * TILE_BYTES + kk * 32), accum);
+              }
+            }
+          }
+          mma_commit(empty_bar(s));
+          ++it;
+        }
+        if (!ok) break;
+        mma_commit(tfull_bar);
+      }
+      if (!ok) {
+        s_fail = 1;
+        atomicExch(err, 1);
+        if (it > 0) {
+          const int zero = 0;
+          const volatile int no_fail = 0;
+          role_wait(empty_bar((it - 1) % STAGES), ((it - 1) / STAGES) & 1, &zero, &no_fail);
+        }
+      }
+    }
+  } else {
+    // ----------------------------------------------------------- epilogue
+    const int q = warp & 3;  // TMEM lanes 32q..32q+31
+    int tl = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
+      const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+      double2* Cm = C + (size_t)tc.mat * cstride;
+      const int* ebm = eb + (size_t)tc.mat * N;
+      const int row = tc.m0 + q * 32 + lane;
+      const bool row_ok = row < M;
+      const int erow = row_ok ? ea[(size_t)tc.mat * M + row] - 16 : 0;
+      auto load_c_chunk = [&](int cc, double2* dst) {
+        const int n0 = (tc.j0 >> 1) + cc * 8;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          dst[j] = (row_ok && n0 + j < N) ? Cm[(size_t)(n0 + j) * ldc + row] : make_double2(0.0, 0.0);
+      };
+      double2 cbuf[8], nxt[8];
+      load_c_chunk(0, cbuf);
+      int ok = 0;
+      if (lane == 0) ok = role_wait(tfull_bar, tl & 1, err, &s_fail) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) {
+          s_fail = 1;
+          atomicExch(err, 1);
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 16; ++cc) {
+        if (cc + 1 < BN / 16) load_c_chunk(cc + 1, nxt);
+        uint32_t r[NLEV][16];
+#pragma unroll
+        for (int L = 0; L < NLEV; ++L)
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+              : "=r"(r[L][0]), "=r"(r[L][1]), "=r"(r[L][2]), "=r"(r[L][3]), "=r"(r[L][4]), "=r"(r[L][5]),
+                "=r"(r[L][6]), "=r"(r[L][7]), "=r"(r[L][8]), "=r"(r[L][9]), "=r"(r[L][10]), "=r"(r[L][11]),
+                "=r"(r[L][12]), "=r"(r[L][13]), "=r"(r[L][14]), "=r"(r[L][15])
+              : "r"(taddr + (uint32_t)(L * BN + cc * 16)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row_ok) {
+          const int n0 = (tc.j0 >> 1) + cc * 8;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if (n0 + j < N) {
+              double vr = (double)__uint_as_float(r[3][2 * j]) + (double)__uint_as_float(r[2][2 * j]);
+              double vi = (double)__uint_as_float(r[3][2 * j + 1]) + (double)__uint_as_float(r[2][2 * j + 1]);
+              vr = (vr + (double)__uint_as_float(r[1][2 * j])) + (double)__uint_as_float(r[0][2 * j]);
+              vi = (vi + (double)__uint_as_float(r[1][2 * j + 1])) + (double)__uint_as_float(r[0][2 * j + 1]);
+              const double sc = pow2(erow + ebm[n0 + j]);
+              double2 v = cbuf[j];
+              v.x = fma(-vr, sc, v.x);
+              v.y = fma(-vi, sc, v.y);
+              Cm[(size_t)(n0 + j) * ldc + row] = v;
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cbuf[j] = nxt[j];
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty_bar);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// ----------------------------------------------------------- host side ----
+namespace {
+
+// 4-D map over NS planes of `batch` matrices of rows x k2p bf16 (row-major),
+// 32 x 128 boxes with 64-byte swizzle.
+bool make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int k2p, int batch) {
+  EncodeFn enc = encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[4] = {(cuuint64_t)k2p, (cuuint64_t)rows, (cuuint64_t)batch, (cuuint64_t)NS};
+  cuuint64_t strides[3] = {(cuuint64_t)k2p * 2, (cuuint64_t)rows * k2p * 2, (cuuint64_t)batch * rows * k2p * 2};
+  cuuint32_t box[4] = {(cuuint32_t)KC, (cuuint32_t)BM, 1, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(ptr), dims, strides, box,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+std::mutex g_mu;
+std::vector<LuWorkspace> g_ws;
+
+}  // namespace
+
+cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, const double2* B, long long ldb,
+                           double2* C, long long ldc, int M, int N, int K, cudaStream_t s, int batch,
+                           long long bstride) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  if (!ws || batch < 1 || batch > 65535) return cudaErrorInvalidValue;
+  if (K > kMaxK) {
+    // K slabs of at most kMaxK, one after another on C (keeps levels 0-2 exact)
+    for (int k0 = 0; k0 < K; k0 += kMaxK) {
+      const int kk = std::min(kMaxK, K - k0);
+      const cudaError_t e = zgemm_sub_emul(ws, A + (size_t)k0 * lda, lda, B + k0, ldb, C, ldc, M, N, kk, s, batch,
+                                           bstride);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  const int K2p = ((2 * K + KC - 1) / KC) * KC;
+  const size_t a_pl = (size_t)M * K2p * batch, b_pl = (size_t)2 * N * K2p * batch;  // bf16 per plane
+  const size_t plane_bytes = 2 * (size_t)NS * (a_pl + b_pl);
+  const size_t exp_bytes = sizeof(int) * ((size_t)M + N) * batch;
+  cudaError_t e = tc_scratch(ws, (plane_bytes + exp_bytes) / sizeof(float) + 64, s);
+  if (e != cudaSuccess) return e;
+  __nv_bfloat16* pa = reinterpret_cast<__nv_bfloat16*>(ws->tc_buf);
+  __nv_bfloat16* pb = pa + NS * a_pl;
+  int* ea = reinterpret_cast<int*>(pb + NS * b_pl);
+  int* eb = ea + (size_t)M * batch;
+  stats::count(stats::kMisc, 2);
+  emul_pack_a_kernel<<<dim3((M + 127) / 128, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
+  emul_pack_b_kernel<<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, pa, M, K2p, batch) || !make_map(&mb, pb, 2 * N, K2p, batch)) return cudaErrorInvalidValue;
+  e = allow_dynamic_smem((const void*)zgemm_sub_emul_kernel, SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
+  const long long ntiles = (long long)tiles_m * tiles_n * batch;
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  const int grid = (int)std::min<long long>(ntiles, nsm);
+  stats::Scope sc(stats::kEmulGemm, s, 8.0 * M * (double)N * K * batch);
+  zgemm_sub_emul_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m, tiles_n,
+                                                           (int)ntiles, ws->tc_err, bstride);
+  return cudaGetLastError();
+}
+
+}  // namespace emul
+
+GemmHook<double2> emul_gemm_hook() {
+  if (std::getenv("WMOM_NO_EMUL")) return nullptr;
+  int dev = 0, major = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  if (major != 10) return nullptr;
+  return &emul::zgemm_sub_emul;
+}
+
+}  // namespace wmom
+
+extern "C" wmom_status wmom_zgemm_sub_emul(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
+                                           long long ldb, void* c_dev, long long ldc, void* stream) {
+  if (m < 0 || n < 0 || k < 0 || (m && (!a_dev || !c_dev || lda < m || ldc < m)) || (n && (!b_dev || ldb < k)))
+    return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "zgemm_sub_emul device");
+  std::lock_guard<std::mutex> lk(wmom::emul::g_mu);
+  if ((int)wmom::emul::g_ws.size() <= dev) wmom::emul::g_ws.resize(dev + 1);
+  wmom::LuWorkspace* ws = &wmom::emul::g_ws[dev];
+  e = wmom::emul::zgemm_sub_emul(ws, reinterpret_cast<const double2*>(a_dev), lda,
+                                 reinterpret_cast<const double2*>(b_dev), ldb, reinterpret_cast<double2*>(c_dev), ldc,
+                                 m, n, k, s, 1, 0);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "zgemm_sub_emul");
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "zgemm_sub_emul sync");
+  if (wmom::tc::read_and_clear_error(ws, s)) return WMOM_ERR_TIMEOUT;
+  return WMOM_OK;
+}

@@ -35,6 +35,7 @@
 #include "lu_common.cuh"
 #include "solve_internal.h"
 #include "stats.h"
+#include "tcgen05_util.cuh"
 
 namespace wmom {
 namespace tc {
@@ -49,53 +50,8 @@ constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
 constexpr int NTHREADS = 192;         // producer warp, MMA warp, 4 epilogue warps
 constexpr int TMEM_COLS = 2 * BN;     // two accumulators
-constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred P1;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
-      "selp.b32 %0, 1, 0, P1;\n\t}"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-// 3-D tiled TMA load (x = K element, y = row, z = matrix of the batch).
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B
-// apart (stride byte offset), descriptor version 1.
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)(16u >> 4) << 16;
-  d |= (uint64_t)(1024u >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) { return sdesc_sw<128>(addr); }
 
 // Instruction descriptor: D = F32, A = B = TF32, both K-major, N = BN, M = BM.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -108,11 +64,6 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
       : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
 }
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -193,21 +144,6 @@ __device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n)
   const int r = t - mat * per_mat;
   const int tn = r / tiles_m;
   return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
-}
-
-// Bounded wait that also ends when this CTA has failed (s_fail) or, through err,
-// another CTA of the launch.
-__device__ __forceinline__ bool role_wait(uint32_t bar, uint32_t parity, const int* err, const volatile int* s_fail) {
-  const unsigned long long t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*s_fail || *reinterpret_cast<const volatile int*>(err)) return false;
-    if (global_ns() - t0 > kWaitNs) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -399,10 +335,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 // ----------------------------------------------------------- host side ----
-namespace {
-
-using EncodeFn = PFN_cuTensorMapEncodeTiled_v12000;
-
 EncodeFn encode_fn() {
   static EncodeFn fn = nullptr;
   static std::once_flag once;
@@ -417,6 +349,8 @@ EncodeFn encode_fn() {
   return fn;
 }
 
+namespace {
+
 // 3-D map over `batch` planes of rows x k2p FP32 (row-major), 32 x 128 boxes.
 bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch) {
   EncodeFn enc = encode_fn();
@@ -430,6 +364,8 @@ bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch) 
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
+
+}  // namespace
 
 // Grows ws->tc_buf to `floats`.  Inside a stream capture it refuses (the capture
 // then fails and the caller launches directly, which grows the buffer); otherwise
@@ -462,6 +398,8 @@ cudaError_t tc_scratch(LuWorkspace* ws, size_t floats, cudaStream_t s) {
   ++ws->tc_gen;
   return cudaSuccess;
 }
+
+namespace {
 
 // Scratch of the stand-alone entry point wmom_cgemm_sub_tc: one per device,
 // serialised by a mutex (that entry point synchronises before returning).

@@ -137,6 +137,60 @@ __global__ void accumulate_vec_kernel(double2* __restrict__ x, const float2* __r
   x[i].y += (double)d[i].y * inv[b];
 }
 
+// x[b] += d[b] where active[b] (FP64 corrections of the second tier)
+__global__ void accumulate64_kernel(double2* __restrict__ x, const double2* __restrict__ d, int n, int nvec,
+                                    const int* __restrict__ active) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * nvec) return;
+  if (!active[i / n]) return;
+  x[i].x += d[i].x;
+  x[i].y += d[i].y;
+}
+
+// partial[chunk*n + i] = sum over the chunk's columns of cabs1(Z[i, j]) cabs1(x[j]),
+// cabs1(z) = |re z| + |im z|: the |Z| |x| of the componentwise backward error
+__global__ void __launch_bounds__(kGemvRows) absgemv_partial_kernel(const double2* __restrict__ Z, long long ldz,
+                                                                    const double2* __restrict__ x, int n,
+                                                                    double* __restrict__ partial) {
+  __shared__ double xs[kGemvChunk];
+  const int i = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * kGemvChunk;
+  const int c1 = min(n, c0 + kGemvChunk);
+  for (int j = c0 + threadIdx.x; j < c1; j += kGemvRows) xs[j - c0] = fabs(x[j].x) + fabs(x[j].y);
+  __syncthreads();
+  if (i >= n) return;
+  double acc = 0.0;
+  const double2* zp = Z + (size_t)c0 * ldz + i;
+  for (int j = c0; j < c1; ++j, zp += ldz) {
+    const double2 a = *zp;
+    acc = fma(fabs(a.x) + fabs(a.y), xs[j - c0], acc);
+  }
+  partial[(size_t)blockIdx.y * n + i] = acc;
+}
+
+// *out = max_i cabs1(r_i) / ((|Z| |x|)_i + cabs1(v_i)) (one block; the Oettli-Prager
+// componentwise backward error of x, as LAPACK's zgerfs measures it)
+__global__ void __launch_bounds__(1024) berr_finish_kernel(const double2* __restrict__ r,
+                                                           const double2* __restrict__ v,
+                                                           const double* __restrict__ partial, int nchunks, int n,
+                                                           double* out) {
+  __shared__ double sh[1024];
+  double w = 0.0;
+  for (int i = threadIdx.x; i < n; i += 1024) {
+    double den = fabs(v[i].x) + fabs(v[i].y);
+    for (int c = 0; c < nchunks; ++c) den += partial[(size_t)c * n + i];
+    const double num = fabs(r[i].x) + fabs(r[i].y);
+    if (num > 0.0) w = fmax(w, den > 0.0 ? num / den : HUGE_VAL);
+  }
+  sh[threadIdx.x] = w;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
 __global__ void widen_vec_kernel(const float2* __restrict__ d, double2* __restrict__ x, size_t count) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < count) x[i] = make_double2((double)d[i].x, (double)d[i].y);
@@ -208,6 +262,7 @@ struct GroupScalars {
   double rnorm2[kMaxLuBatch];
   double dnorm2[kMaxLuBatch];
   double xnorm2[kMaxLuBatch];
+  double berr[kMaxLuBatch];    // componentwise backward errors of the second tier
   double vnorm2;
 };
 
@@ -239,8 +294,8 @@ int gmres_cycles() {
 struct GroupScratch {
   int n = 0, B = 0;
   cudaStream_t s = nullptr;
-  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv, fb_x;
-  int fb_cap = 0;          // matrices per batched FP64 fallback factorisation
+  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv, fb_x, fb_r;
+  int fb_cap = 0;          // matrices per batched FP64-grade factorisation (tiers 2, 3)
   std::vector<double> vh;  // excitation on the host
   double vnorm = 0.0;
   GroupScalars hs{};
@@ -643,6 +698,23 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
 wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
                              size_t budget, LuConfig* out, bool timing);
 
+namespace {
+
+// In-place FP64 LU of the bg matrices in lu64 (n*n apart) whose trailing updates
+// run through `hook` (the digit-plane tensor-core GEMM): the second tier's factors.
+wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws, cudaStream_t s, int* info,
+                        GemmHook<double2> hook) {
+  SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
+  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, 1);
+  if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t (tier 2)");
+  int err = lu_workspace_read_status(ws, info, s, bg);
+  err |= tc::read_and_clear_error(ws, s);
+  SWEEP_TRY(cudaGetLastError());
+  return err ? WMOM_ERR_TIMEOUT : WMOM_OK;
+}
+
+}  // namespace
+
 // Solves bg systems Z64[b] x = V with the factors of factor_group; the solutions end
 // in g.x64[0..bg).  Mixed: FP32 solve, FP64 refinement with a per-matrix activity
 // mask, FP64 LU for the matrices that stall.
@@ -807,10 +879,23 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     if (ok) fallback[b] = false;
   }
   for (int b = 0; b < bg; ++b)
-    if (!fallback[b]) rep[b].status = WMOM_OK;
-  // FP64 fallback.  The matrices that fell back are copied into the scratch factor
-  // buffer and factored together, as wide as the plain FP64 form batches at this
-  // order: their panels then run side by side instead of one matrix after another.
+    if (!fallback[b]) {
+      rep[b].status = WMOM_OK;
+      rep[b].tier = 1;
+    }
+  // The matrices the FP32 factors could not serve get FP64-grade factors, batched
+  // as wide as the plain FP64 form batches at this order (copies in the scratch
+  // factor buffer, so that their panels run side by side).
+  //   Tier 2: FP64 LU whose trailing updates run on the bf16 tensor cores from
+  //   digit planes (lu_emul.cu), then FP64 refinement as above.  A matrix is accepted
+  //   when its residual meets tol or the correction no longer changes x at FP64
+  //   resolution; when its refinement stalls instead (the FP64 residual floor of an
+  //   ill-conditioned system), it is accepted if its componentwise backward error
+  //   max_i |r_i| / (|Z||x| + |V|)_i (LAPACK zgerfs' measure, with |z| = |re| + |im|)
+  //   is at most 4 sqrt(n) eps, eps = 2^-53: such a solution is as good as an FP64
+  //   LU's, from which it differs by about kappa * eps.
+  //   Tier 3: plain FP64 LU for the matrices whose tier-2 refinement stalled, and for
+  //   every matrix when the device has no tensor-core path (or WMOM_NO_EMUL is set).
   int nfb = 0, fb[kMaxLuBatch];
   for (int b = 0; b < bg; ++b)
     if (fallback[b]) fb[nfb++] = b;
@@ -825,30 +910,136 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     SWEEP_TRY(g.fb_lu.alloc(sizeof(double2) * nn * cap, s));
     SWEEP_TRY(g.fb_ipiv.alloc(sizeof(int) * (size_t)n * cap, s));
     SWEEP_TRY(g.fb_x.alloc(sizeof(double2) * (size_t)n * cap, s));
+    SWEEP_TRY(g.fb_r.alloc(sizeof(double2) * (size_t)n * cap, s));
     g.fb_cap = cap;
   }
+  const GemmHook<double2> emul = emul_gemm_hook();
   double2* flu = g.fb_lu.as<double2>();
   double2* fx = g.fb_x.as<double2>();
+  double2* frr = g.fb_r.as<double2>();
+  int* fpiv = g.fb_ipiv.as<int>();
+  const double eps64 = 0x1p-53;
   for (int c0 = 0; c0 < nfb; c0 += g.fb_cap) {
     const int cn = std::min(g.fb_cap, nfb - c0);
-    for (int j = 0; j < cn; ++j)
-      SWEEP_TRY(cudaMemcpyAsync(flu + (size_t)j * nn, Z64 + (size_t)fb[c0 + j] * nn, sizeof(double2) * nn,
-                                cudaMemcpyDeviceToDevice, s));
-    int inf[kMaxLuBatch] = {};
-    const wmom_status fst = factor_group(WMOM_MODE_FP64, n, flu, cn, nullptr, flu, g.fb_ipiv.as<int>(), ws, s, inf,
-                                         nullptr, nullptr, 1);
-    if (fst != WMOM_OK) return fst;
-    // every slot of vrep holds the excitation
-    SWEEP_TRY(cudaMemcpyAsync(fx, g.vrep.p, sizeof(double2) * (size_t)n * cn, cudaMemcpyDeviceToDevice, s));
-    SWEEP_TRY(lu_solve_t<double2>(flu, n, n, g.fb_ipiv.as<int>(), fx, n, 1, ws, s, cn, (long long)nn));
+    bool plain[kMaxLuBatch];
     for (int j = 0; j < cn; ++j) {
-      const int b = fb[c0 + j];
-      SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)b * n, fx + (size_t)j * n, sizeof(double2) * n,
-                                cudaMemcpyDeviceToDevice, s));
-      rep[b].fell_back = 1;
-      rep[b].info = inf[j];
-      rep[b].status = inf[j] ? WMOM_ERR_SINGULAR : WMOM_OK;
+      plain[j] = true;
+      rep[fb[c0 + j]].fell_back = 1;
     }
+    if (emul) {
+      for (int j = 0; j < cn; ++j)
+        SWEEP_TRY(cudaMemcpyAsync(flu + (size_t)j * nn, Z64 + (size_t)fb[c0 + j] * nn, sizeof(double2) * nn,
+                                  cudaMemcpyDeviceToDevice, s));
+      int inf[kMaxLuBatch] = {};
+      const wmom_status fst = factor_emul(n, flu, cn, fpiv, ws, s, inf, emul);
+      if (fst != WMOM_OK) return fst;
+      // x = LU^-1 V (every slot of vrep holds the excitation)
+      SWEEP_TRY(cudaMemcpyAsync(fx, g.vrep.p, sizeof(double2) * (size_t)n * cn, cudaMemcpyDeviceToDevice, s));
+      SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, fx, n, 1, ws, s, cn, (long long)nn));
+      bool act[kMaxLuBatch];
+      int stall2[kMaxLuBatch] = {};
+      double prev2[kMaxLuBatch];
+      for (int j = 0; j < cn; ++j) {
+        act[j] = inf[j] == 0;
+        prev2[j] = HUGE_VAL;
+      }
+      for (int it = 0;; ++it) {
+        for (int j = 0; j < cn; ++j)
+          if (act[j])
+            SWEEP_TRY(residual_fp64(Z64 + (size_t)fb[c0 + j] * nn, n, 0, fx + (size_t)j * n, g.vrep.as<double2>(), n,
+                                    frr + (size_t)j * n, g.part.as<double2>(), 1, s));
+        SWEEP_TRY(sumsq_fp64(frr, n, dsc->rnorm2, cn, s));
+        SWEEP_TRY(sumsq_fp64(fx, n, dsc->xnorm2, cn, s));
+        SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+        SWEEP_TRY(cudaStreamSynchronize(s));
+        int nact = 0;
+        bool stalled[kMaxLuBatch] = {};
+        for (int j = 0; j < cn; ++j) {
+          if (!act[j]) continue;
+          const int b = fb[c0 + j];
+          const double xn = std::sqrt(hs.xnorm2[j]);
+          const double rel = std::sqrt(hs.rnorm2[j]) / g.vnorm;
+          const double corr = it > 0 && xn > 0 ? std::sqrt(hs.dnorm2[j]) / xn : HUGE_VAL;
+          rep[b].iterations += it > 0 ? 1 : 0;
+          if (!(rel == rel)) {
+            act[j] = false;
+          } else if (rel <= tol || corr <= 0x1p-48) {
+            act[j] = false;
+            plain[j] = false;
+          } else if ((rel > 0.5 * prev2[j] && ++stall2[j] >= 2) || it >= max_it) {
+            act[j] = false;
+            stalled[j] = true;
+          } else {
+            if (rel <= 0.5 * prev2[j]) stall2[j] = 0;
+            prev2[j] = std::min(prev2[j], rel);
+            ++nact;
+          }
+        }
+        // stalled: accepted at FP64 level of the componentwise backward error
+        bool any_stalled = false;
+        for (int j = 0; j < cn; ++j) {
+          if (!stalled[j]) continue;
+          any_stalled = true;
+          const int nch = (n + kGemvChunk - 1) / kGemvChunk;
+          double* part = reinterpret_cast<double*>(g.part.p);
+          stats::count(stats::kMisc, 2);
+          absgemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nch), kGemvRows, 0, s>>>(
+              Z64 + (size_t)fb[c0 + j] * nn, n, fx + (size_t)j * n, n, part);
+          berr_finish_kernel<<<1, 1024, 0, s>>>(frr + (size_t)j * n, g.vrep.as<double2>(), part, nch, n,
+                                                &dsc->berr[j]);
+          SWEEP_TRY(cudaGetLastError());
+        }
+        if (any_stalled) {
+          SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+          SWEEP_TRY(cudaStreamSynchronize(s));
+          for (int j = 0; j < cn; ++j)
+            if (stalled[j] && hs.berr[j] <= 4.0 * std::sqrt((double)n) * eps64) plain[j] = false;
+        }
+        if (nact == 0) break;
+        // d = LU^-1 r for the chunk; x += d where active
+        for (int j = 0; j < cn; ++j) hact[j] = act[j] ? 1 : 0;
+        SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+        SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, cn, (long long)nn));
+        SWEEP_TRY(sumsq_fp64(frr, n, dsc->dnorm2, cn, s));
+        stats::count(stats::kMisc);
+        accumulate64_kernel<<<(unsigned)(((size_t)n * cn + 255) / 256), 256, 0, s>>>(fx, frr, n, cn,
+                                                                                   g.actv.as<int>());
+        SWEEP_TRY(cudaGetLastError());
+      }
+      for (int j = 0; j < cn; ++j)
+        if (!plain[j]) {
+          const int b = fb[c0 + j];
+          rep[b].tier = 2;
+          rep[b].info = 0;
+          rep[b].status = WMOM_OK;
+        }
+    }
+    // tier 3: the chunk's remaining matrices, compacted into the scratch buffer
+    int n3 = 0, idx3[kMaxLuBatch];
+    for (int j = 0; j < cn; ++j)
+      if (plain[j]) idx3[n3++] = j;
+    if (n3 > 0) {
+      for (int i = 0; i < n3; ++i)
+        SWEEP_TRY(cudaMemcpyAsync(flu + (size_t)i * nn, Z64 + (size_t)fb[c0 + idx3[i]] * nn, sizeof(double2) * nn,
+                                  cudaMemcpyDeviceToDevice, s));
+      int inf[kMaxLuBatch] = {};
+      const wmom_status fst = factor_group(WMOM_MODE_FP64, n, flu, n3, nullptr, flu, fpiv, ws, s, inf, nullptr,
+                                           nullptr, 1);
+      if (fst != WMOM_OK) return fst;
+      SWEEP_TRY(cudaMemcpyAsync(frr, g.vrep.p, sizeof(double2) * (size_t)n * n3, cudaMemcpyDeviceToDevice, s));
+      SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, n3, (long long)nn));
+      for (int i = 0; i < n3; ++i) {
+        const int j = idx3[i], b = fb[c0 + j];
+        SWEEP_TRY(cudaMemcpyAsync(fx + (size_t)j * n, frr + (size_t)i * n, sizeof(double2) * n,
+                                  cudaMemcpyDeviceToDevice, s));
+        rep[b].tier = 3;
+        rep[b].info = inf[i];
+        rep[b].status = inf[i] ? WMOM_ERR_SINGULAR : WMOM_OK;
+      }
+    }
+    for (int j = 0; j < cn; ++j)
+      SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)fb[c0 + j] * n, fx + (size_t)j * n,
+                                sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
   }
   const wmom_status rs = group_residuals(g, Z64, bg);
   if (rs != WMOM_OK) return rs;

@@ -64,6 +64,9 @@ cudaError_t convert_flat_64_to_32(const double2* src, float2* dst, size_t count,
 // FP32 trailing-update GEMM on the tensor cores (lu_tc.cu); nullptr when the
 // device has no tcgen05 path, in which case the SIMT GEMM is used.
 GemmHook<float2> tc_gemm_hook();
+// FP64-grade trailing-update GEMM on the bf16 tensor cores (lu_emul.cu), the second
+// tier of the precision form; nullptr without a tcgen05 device or with WMOM_NO_EMUL.
+GemmHook<double2> emul_gemm_hook();
 namespace tc {
 // 1 if a tensor-core GEMM wait on `ws` timed out since the last call (synchronises s)
 int read_and_clear_error(LuWorkspace* ws, cudaStream_t s);

@@ -20,6 +20,7 @@ enum Cls : int {
   kLaswp,      // row interchanges
   kResidual,   // FP64 residual GEMV (work: bytes of Z read)
   kMisc,       // conversions, norms, packing, permutations
+  kEmulGemm,   // FP64-grade trailing update on the bf16 tensor cores (8*M*N*K real flops)
   kNumCls
 };
 

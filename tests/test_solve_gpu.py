@@ -141,3 +141,32 @@ def test_batch_width_does_not_change_results(cuda, wmom):
         c4, z4, r4 = out[("4", mode)]
         assert np.array_equal(c1, c4)
         assert [r["iterations"] for r in r1] == [r["iterations"] for r in r4]
+
+
+def test_second_tier_serves_ill_conditioned_grid(cuda, wmom):
+    # 21 x 21 junction grid at 10 and 30 kHz: kappa * u_fp32 >> 1, so the FP32 factors
+    # stall.  The second tier (FP64 LU with digit-plane tensor-core trailing updates,
+    # then FP64 refinement) must reach the plain FP64 solve's backward error, and
+    # differ from that solve by about kappa * eps, as any two FP64 solves do (kappa is
+    # near 1e10 here; the fixture test above bounds the same difference by 1e-6).
+    topo = wmom.Topology(wmom.geometry.precision_grid(2048))
+    freqs = np.array([0.01, 0.03], np.float32)
+    plan = wmom.Plan(topo)
+    c64, z64, r64 = plan.solve(freqs, 1000, mode=0)
+    cm, zm, rm = plan.solve(freqs, 1000, mode=1)
+    for k in range(len(freqs)):
+        assert rm[k]["status"] == 0 and rm[k]["fell_back"] == 1 and rm[k]["tier"] == 2, rm[k]
+        assert rm[k]["rel_residual"] <= 4 * r64[k]["rel_residual"] + 1e-15, (rm[k], r64[k])
+        assert _rel(cm[k], c64[k]) < 1e-6
+        assert r64[k]["tier"] == 0
+    # without the tensor-core tier the same matrices take the plain FP64 LU, whose
+    # solution is the FP64 form's bit for bit
+    os.environ["WMOM_NO_EMUL"] = "1"
+    try:
+        cp, zp, rp = plan.solve(freqs, 1000, mode=1)
+    finally:
+        del os.environ["WMOM_NO_EMUL"]
+    for k in range(len(freqs)):
+        assert rp[k]["tier"] == 3 and rp[k]["status"] == 0
+        assert np.array_equal(cp[k], c64[k])
+    plan.close()
