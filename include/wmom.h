@@ -226,7 +226,8 @@ const char* wmom_last_error(void);
  * launch is also bracketed by CUDA events on its own stream.  Classes, in order:
  * 0 fill, 1 panel, 2 tensor-core GEMM, 3 SIMT GEMM, 4 triangular solves,
  * 5 row interchanges, 6 FP64 residual, 7 other, 8 FP64-grade tensor-core GEMM
- * (the precision form's second tier).  wmom_stats_read fills up to n
+ * (the precision form's second tier), 9 single-right-hand-side triangular solves
+ * (solutions and refinement).  wmom_stats_read fills up to n
  * entries of each array (any may be NULL) and returns the number of classes;
  * ms = summed device time, launches = launches issued, timed = launches timed,
  * work = algorithmic flops (bytes for the residual) of the timed launches.  The

@@ -112,7 +112,7 @@ _probe_fp64 = _sig("wmom_probe_fp64_tflops", ctypes.c_int, [_dp])
 _diag_sincos = _sig("wmom_diag_sincos", ctypes.c_int, [_vp, ctypes.c_longlong, _vp, _vp])
 _tuned_config = _sig("wmom_tuned_config", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip])
 
-STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc", "emul_gemm"]
+STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc", "emul_gemm", "trsv"]
 
 
 def stats_enable(on=True):

@@ -492,12 +492,14 @@ __global__ void __launch_bounds__(NT) panel_rows_kernel(C* __restrict__ A, long 
 constexpr int kClusterMax = 16;
 constexpr int kClusterThreads = 512;
 
+template <typename C>
 struct ClusterPub {
-  float val;
+  using R = decltype(C{}.x);
+  R val;
   int row;
-  int pad[2];
-  float2 cand[64];
-  float2 diag[64];
+  int pad[sizeof(R) == 8 ? 1 : 2];  // cand starts 16-byte aligned
+  C cand[64];
+  C diag[64];
 };
 
 __device__ __forceinline__ unsigned cluster_rank() {
@@ -528,22 +530,39 @@ __device__ __forceinline__ float2 ld_cluster_f2(uint32_t a) {
   asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
   return v;
 }
+__device__ __forceinline__ double ld_cluster_f64(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 ld_cluster_d2(uint32_t a) {
+  double2 v;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ float ld_cluster_r(const float*, uint32_t a) { return ld_cluster_f32(a); }
+__device__ __forceinline__ double ld_cluster_r(const double*, uint32_t a) { return ld_cluster_f64(a); }
+__device__ __forceinline__ float2 ld_cluster_c(const float2*, uint32_t a) { return ld_cluster_f2(a); }
+__device__ __forceinline__ double2 ld_cluster_c(const double2*, uint32_t a) { return ld_cluster_d2(a); }
 
 // RPT rows per thread (1, or 2 for panels whose rows would otherwise need a cluster
 // wider than the GPU can hold for a whole batch at once): thread t owns rows t and
-// t + kClusterThreads of its CTA's slab.
-template <int RPT>
-__global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float2* __restrict__ A, long long lda,
-                                                                           int n, int j0, int w, int rpc,
+// t + kClusterThreads of its CTA's slab.  C = float2 (precision form) or double2
+// (plain form and the precision form's FP64-grade tiers).
+template <typename C, int RPT>
+__global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __restrict__ A, long long lda, int n,
+                                                                           int j0, int w, int rpc,
                                                                            int* __restrict__ ipiv,
                                                                            GridBarrier* __restrict__ gb,
                                                                            long long astride) {
+  using R = decltype(C{}.x);
+  using Pub = ClusterPub<C>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ClusterPub* pub = reinterpret_cast<ClusterPub*>(smem_raw);  // [2]
-  float2* prow = reinterpret_cast<float2*>(pub + 2);         // winner row, 64
-  float2* dgr = prow + 64;                                    // diagonal row, 64
-  float2* tile = dgr + 64;                                    // column-major rpc x w
-  __shared__ float red_v[2][kClusterThreads / 32];
+  Pub* pub = reinterpret_cast<Pub*>(smem_raw);  // [2]
+  C* prow = reinterpret_cast<C*>(pub + 2);      // winner row, 64
+  C* dgr = prow + 64;                           // diagonal row, 64
+  C* tile = dgr + 64;                           // column-major rpc x w
+  __shared__ R red_v[2][kClusterThreads / 32];
   __shared__ int red_r[2][kClusterThreads / 32];
 
   A += (size_t)blockIdx.y * astride;
@@ -561,7 +580,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
     if (lr < cnt) {
       const int gr = base + lr;
       for (int c0 = 0; c0 < w; c0 += 16) {
-        float2 v[16];
+        C v[16];
 #pragma unroll
         for (int u = 0; u < 16; ++u)
           if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
@@ -577,13 +596,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
     const int gj = j0 + j;
     const int par = j & 1;
     // 1. this CTA's candidate (the thread's rows in increasing order: first on ties)
-    float best = -1.f;
+    R best = R(-1);
     int brow = INT_MAX;
 #pragma unroll
     for (int rr = 0; rr < RPT; ++rr) {
       const int lr = t + rr * kClusterThreads;
       if (lr < cnt && base + lr >= gj) {
-        const float v = cabs1(tile[(size_t)j * rpc + lr]);
+        const R v = cabs1(tile[(size_t)j * rpc + lr]);
         if (v > best) {
           best = v;
           brow = base + lr;
@@ -592,7 +611,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
       if (ov > best || (ov == best && orow < brow)) {
         best = ov;
@@ -604,11 +623,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
       red_r[par][warp] = brow;
     }
     __syncthreads();
-    best = -1.f;
+    best = R(-1);
     brow = INT_MAX;
 #pragma unroll
     for (int q = 0; q < kClusterThreads / 32; ++q) {
-      const float v = red_v[par][q];
+      const R v = red_v[par][q];
       const int r = red_r[par][q];
       if (v > best || (v == best && r < brow)) {
         best = v;
@@ -616,28 +635,28 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
       }
     }
     // 2. publish it in this CTA's shared memory
-    ClusterPub& my = pub[par];
+    Pub& my = pub[par];
     if (t == 0) {
       my.val = best;
       my.row = brow;
     }
     if (t < w) {
-      if (best >= 0.f) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
+      if (best >= R(0)) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
       if (gj >= base && gj < base + cnt) my.diag[t] = tile[(size_t)t * rpc + (gj - base)];
     }
     // 3. the cluster meets (also orders this CTA's own threads)
     cluster_sync_all();
     // 4. winner over the cluster, computed by every warp from the CTAs' shared memory
-    float v = -1.f;
+    R v = R(-1);
     int r = INT_MAX, q = -1;
     if (lane < (int)cs) {
-      v = ld_cluster_f32(map_rank(&pub[par].val, lane));
+      v = ld_cluster_r(&pub[par].val, map_rank(&pub[par].val, lane));
       r = ld_cluster_s32(map_rank(&pub[par].row, lane));
       q = lane;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const R ov = __shfl_xor_sync(0xffffffffu, v, o);
       const int orow = __shfl_xor_sync(0xffffffffu, r, o);
       const int oq = __shfl_xor_sync(0xffffffffu, q, o);
       if (ov > v || (ov == v && orow < r)) {
@@ -649,13 +668,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
     const int prw = r;
     const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
     if (t < w) {
-      prow[t] = ld_cluster_f2(map_rank(&pub[par].cand[t], (unsigned)q));
-      if (prw != gj) dgr[t] = ld_cluster_f2(map_rank(&pub[par].diag[t], owner_gj));
+      prow[t] = ld_cluster_c(prow, map_rank(&pub[par].cand[t], (unsigned)q));
+      if (prw != gj) dgr[t] = ld_cluster_c(prow, map_rank(&pub[par].diag[t], owner_gj));
     }
     __syncthreads();
     if (rank == 0 && t == 0) ipiv[gj] = prw + 1;
-    const float2 piv = prow[j];
-    const bool zero = piv.x == 0.f && piv.y == 0.f;
+    const C piv = prow[j];
+    const bool zero = piv.x == R(0) && piv.y == R(0);
     if (zero && rank == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
     // 5. this thread's rows: interchange, then scale and rank-1 update below gj
 #pragma unroll
@@ -670,7 +689,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(float
           for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + lr] = prow[c];
       }
       if (gr > gj) {
-        float2 l = tile[(size_t)j * rpc + lr];
+        C l = tile[(size_t)j * rpc + lr];
         if (!zero) {
           l = cmul(l, crecip(piv));
           tile[(size_t)j * rpc + lr] = l;
@@ -977,6 +996,26 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
     const int c = idx / kTrsvB, q = idx - c * kTrsvB;
     Ds[idx] = (c < rows && q < rows) ? A[(size_t)(r0 + c) * lda + r0 + q] : cmake<C>(0, 0);
   }
+  // back substitution divides by the diagonal: Smith's ratio and the reciprocal of
+  // its denominator for every diagonal entry, in parallel and before the waits, so
+  // that the dependent chain below multiplies instead of dividing
+  __shared__ R dg_r[kTrsvB], dg_inv[kTrsvB];
+  __shared__ int dg_sw[kTrsvB];
+  if (UPPER && tid < kTrsvB) {
+    const int c = tid;
+    const C d = (c < rows) ? A[(size_t)(r0 + c) * lda + r0 + c] : cmake<C>(1, 0);
+    if (fabs(d.x) >= fabs(d.y)) {
+      const R q = d.y / d.x;
+      dg_r[c] = q;
+      dg_inv[c] = R(1) / (d.x + d.y * q);
+      dg_sw[c] = 0;
+    } else {
+      const R q = d.x / d.y;
+      dg_r[c] = q;
+      dg_inv[c] = R(1) / (d.y + d.x * q);
+      dg_sw[c] = 1;
+    }
+  }
   C acc = cmake<C>(0, 0);
   const int nsteps = UPPER ? nblk - 1 - b : b;
   // this thread's 16 entries of an off-diagonal 64 x 64 tile: row r, columns g + 4i;
@@ -1051,11 +1090,17 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
         if (tid + 32 > c && tid + 32 < rows) s1 = cfms(s1, D[(size_t)c * lda + tid + 32], xc);
       }
     } else {
+      // a / d_c by Smith's formula with the precomputed ratio and reciprocal
+      auto div_diag = [&](C a, int c) -> C {
+        const R q = dg_r[c], inv = dg_inv[c];
+        return dg_sw[c] ? cmake<C>((a.x * q + a.y) * inv, (a.y * q - a.x) * inv)
+                        : cmake<C>((a.x + a.y * q) * inv, (a.y - a.x * q) * inv);
+      };
       for (int c = rows - 1; c >= 0; --c) {
         if (c < 32) {
-          if (tid == c) s0 = cdiv(s0, D[(size_t)c * lda + c]);
+          if (tid == c) s0 = div_diag(s0, c);
         } else {
-          if (tid + 32 == c) s1 = cdiv(s1, D[(size_t)c * lda + c]);
+          if (tid + 32 == c) s1 = div_diag(s1, c);
         }
         const R xr = __shfl_sync(0xffffffffu, c < 32 ? s0.x : s1.x, c & 31);
         const R xi = __shfl_sync(0xffffffffu, c < 32 ? s0.y : s1.y, c & 31);
@@ -1189,12 +1234,12 @@ int max_cluster_size(const DeviceLimits& lim) {
   if (it != cache.end()) return it->second;
   int best = 0;
   const size_t smem = (size_t)lim.smem_optin - 4096;
-  if (allow_dynamic_smem((const void*)panel_cluster_kernel<1>, smem) == cudaSuccess &&
-      allow_dynamic_smem((const void*)panel_cluster_kernel<2>, smem) == cudaSuccess &&
-      cudaFuncSetAttribute(panel_cluster_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-          cudaSuccess &&
-      cudaFuncSetAttribute(panel_cluster_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-          cudaSuccess) {
+  auto prepare = [&](const void* k) {
+    return allow_dynamic_smem(k, smem) == cudaSuccess &&
+           cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  };
+  if (prepare((const void*)panel_cluster_kernel<float2, 1>) && prepare((const void*)panel_cluster_kernel<float2, 2>) &&
+      prepare((const void*)panel_cluster_kernel<double2, 1>)) {
     for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs, 1, 1);
@@ -1208,7 +1253,8 @@ int max_cluster_size(const DeviceLimits& lim) {
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)panel_cluster_kernel<1>, &cfg) == cudaSuccess &&
+      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)panel_cluster_kernel<float2, 1>, &cfg) ==
+              cudaSuccess &&
           nclusters >= 1)
         best = cs;
     }
@@ -1219,40 +1265,55 @@ int max_cluster_size(const DeviceLimits& lim) {
 }
 
 template <typename C>
-PanelLaunch panel_launch(int m, const DeviceLimits& lim) {
+PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using R = decltype(C{}.x);
   PanelLaunch pl;
   const size_t cap = (size_t)lim.smem_optin - 4096;
-  if (sizeof(R) == 4 && !cluster_panels_disabled()) {
-    // Preference: one row per thread in the smallest cluster (the cluster barrier and
-    // the remote reads cost more per column as the cluster grows); two rows per thread
+  if (!cluster_panels_disabled() && (sizeof(R) == 4 || fp64_cluster)) {
+    // FP32: one row per thread in the smallest cluster (the cluster barrier and the
+    // remote reads cost more per column as the cluster grows); two rows per thread
     // only for panels taller than 16 x 512 rows, which would otherwise need the
     // cooperative kernel.  Two rows per thread in 8 CTAs instead of one in 16 for an
     // N = 8192 batch of 12 was measured: the panel became 40% faster, but its
     // 24-column width cost more in triangular solves, updates and launches.  The panel
     // is 64 columns wide where the rows leave room, else narrower.
+    // FP64 (only with a tensor-core trailing update, fp64_cluster): the rank-1 row
+    // updates run on the FP64 pipe (about 2 FMA per clock per SM), so the cluster
+    // starts at about 256 rows per CTA (more SMs per matrix) and the panel is at most
+    // 32 columns wide (its FP64 work grows with the width; the tensor-core updates
+    // take K = span x width).  The plain FP64 form keeps the cooperative 64-column
+    // panels: its SIMT FP64 update loses more at K = 24-32 than the narrow cluster
+    // panels save (measured 0.64 vs 0.76 freq-solves/s at N = 8192, 24.0 vs 27.3 at
+    // N = 2048).
     const int csmax = max_cluster_size(lim);
-    const size_t head = 2 * sizeof(ClusterPub) + 2 * 64 * sizeof(float2);
+    const size_t head = 2 * sizeof(ClusterPub<C>) + 2 * 64 * sizeof(C);
+    const int wcap = sizeof(R) == 4 ? 64 : 32;
     auto try_shape = [&](int rpt, int cs_lo, int cs_hi, int wmin) -> bool {
       for (int cs = cs_lo; cs <= std::min(cs_hi, csmax); cs *= 2) {
         const int rpc = (m + cs - 1) / cs;
         if (rpc > rpt * kClusterThreads || (rpt > 1 && rpc <= kClusterThreads)) continue;
-        int w = (int)std::min<size_t>(64, (cap - head) / ((size_t)rpc * sizeof(float2)));
-        if (w < 64) w &= ~7;
+        int w = (int)std::min<size_t>(wcap, (cap - head) / ((size_t)rpc * sizeof(C)));
+        if (w < wcap) w &= ~7;
         if (w < wmin) continue;
         pl.cluster = true;
         pl.rpt = rpt;
         pl.P = cs;
         pl.rpc = rpc;
         pl.w = w;
-        pl.smem = head + (size_t)rpc * w * sizeof(float2);
+        pl.smem = head + (size_t)rpc * w * sizeof(C);
         return true;
       }
       return false;
     };
-    if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
+    if (sizeof(R) == 4) {
+      if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
+    } else {
+      int cs0 = 1;
+      while (cs0 < kClusterMax && (m + cs0 - 1) / cs0 > 256) cs0 *= 2;
+      if (try_shape(1, cs0, kClusterMax, 16)) return pl;
+    }
   }
   if (sizeof(R) == 4) {
     const int P = (m + NT - 1) / NT;
@@ -1304,12 +1365,13 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   // panel of columns [jp, jp + w), rows jp..n-1 (cooperative launch)
   auto panel = [&](int jp, int w) -> cudaError_t {
     const int m = n - jp;
-    const PanelLaunch pl = panel_launch<C>(m, lim);
+    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr);
     const int P = pl.P;
-    if constexpr (std::is_same<C, float2>::value) {
+    {
       if (pl.cluster) {
         if (w > pl.w) return cudaErrorInvalidValue;
-        const void* ck = pl.rpt == 2 ? (const void*)panel_cluster_kernel<2> : (const void*)panel_cluster_kernel<1>;
+        const void* ck =
+            pl.rpt == 2 ? (const void*)panel_cluster_kernel<C, 2> : (const void*)panel_cluster_kernel<C, 1>;
         cudaError_t ce = allow_dynamic_smem(ck, pl.smem);
         if (ce != cudaSuccess) return ce;
         cudaLaunchConfig_t cfg = {};
@@ -1325,9 +1387,10 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
-        return pl.rpt == 2
-                   ? cudaLaunchKernelEx(&cfg, panel_cluster_kernel<2>, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride)
-                   : cudaLaunchKernelEx(&cfg, panel_cluster_kernel<1>, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
+        return pl.rpt == 2 ? cudaLaunchKernelEx(&cfg, panel_cluster_kernel<C, 2>, A, lda, n, jp, w, pl.rpc, ipiv, gb,
+                                                astride)
+                           : cudaLaunchKernelEx(&cfg, panel_cluster_kernel<C, 1>, A, lda, n, jp, w, pl.rpc, ipiv, gb,
+                                                astride);
       }
     }
     const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
@@ -1410,7 +1473,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     int np = 0;
     c[0] = j0;
     while (np < S && c[np] < n) {
-      w[np] = std::min(panel_launch<C>(n - c[np], lim).w, n - c[np]);
+      w[np] = std::min(panel_launch<C>(n - c[np], lim, gemm_hook != nullptr).w, n - c[np]);
       c[np + 1] = c[np] + w[np];
       ++np;
     }
@@ -1467,7 +1530,7 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
     if (e != cudaSuccess) return e;
     e = allow_dynamic_smem((const void*)trsv_kernel<C, true>, dsmem);
     if (e != cudaSuccess) return e;
-    stats::Scope sc(stats::kTrsm, s, 8.0 * n * (double)n * batch, 2);
+    stats::Scope sc(stats::kTrsv, s, 8.0 * n * (double)n * batch, 2);
     for (int pass = 0; pass < 2; ++pass) {
       const int ep = ++ws->epoch;
       e = cudaMemsetAsync(ws->ticket, 0, sizeof(unsigned int) * batch, s);
@@ -1518,25 +1581,26 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
 }
 
 template <typename C>
-int lu_max_batch(int n) {
+int lu_max_batch(int n, bool fp64_cluster) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   const DeviceLimits lim = device_limits();
   if (lim.sms <= 0 || n <= 0) return 1;
   static std::mutex mu;
-  static std::map<std::pair<int, int>, int> cache;  // (device, n) -> batch
+  static std::map<std::pair<int, int>, int> cache;  // (device, n, fp64_cluster) -> batch
   int dev = 0;
   cudaGetDevice(&dev);
+  const std::pair<int, int> key{2 * dev + (fp64_cluster ? 1 : 0), n};
   {
     std::lock_guard<std::mutex> lk(mu);
-    auto it = cache.find({dev, n});
+    auto it = cache.find(key);
     if (it != cache.end()) return it->second;
   }
   // every panel's cooperative launch must fit co-resident; shapes change as the
   // panels shrink, so the smallest batch over all of them is the limit
   int best = kMaxLuBatch;
   for (int j0 = 0; j0 < n && best > 1; j0 += NB) {
-    const PanelLaunch pl = panel_launch<C>(n - j0, lim);
+    const PanelLaunch pl = panel_launch<C>(n - j0, lim, fp64_cluster);
     if (pl.cluster) continue;  // clusters are independent of one another
     const void* kern = pl.rows ? (const void*)panel_rows_kernel<C, NB, NT> : (const void*)panel_kernel<C, NB, NT>;
     if (allow_dynamic_smem(kern, pl.smem) != cudaSuccess) return 1;
@@ -1546,12 +1610,12 @@ int lu_max_batch(int n) {
   }
   best = std::max(1, best);
   std::lock_guard<std::mutex> lk(mu);
-  cache[{dev, n}] = best;
+  cache[key] = best;
   return best;
 }
 
-template int lu_max_batch<double2>(int);
-template int lu_max_batch<float2>(int);
+template int lu_max_batch<double2>(int, bool);
+template int lu_max_batch<float2>(int, bool);
 
 template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWorkspace*, cudaStream_t,
                                           GemmHook<double2>, int, long long, int);

@@ -11,29 +11,32 @@
 //     B'^T (2N x 2K) has rows 2n = (Br, -Bi) and 2n+1 = (Bi, Br);
 //   * row m of A' is scaled by 2^-ea[m] (ea = the exponent of its largest entry,
 //     so the scaled entries lie in (-1, 1)), column n of B by 2^-eb[n];
-//   * a scaled entry x is written as NS signed 8-bit digits,
-//       x = sum_t d_t 2^(-8(t+1)) + rest,  d_t = rint(256 x_t), x_(t+1) = 256 x_t - d_t,
-//     every step exact in FP64, |d_0| <= 256, |d_t| <= 128; plane t stores
-//     d_t 2^(-8t), exact in bf16;
+//   * a scaled entry x is rounded once to the 48-bit fixed-point integer
+//     X = rint(x 2^48) and written as NS = 6 balanced base-256 digits,
+//       x = sum_t d_t 2^(-8(t+1)) + rest,  |rest| <= 2^-49,
+//     |d_0| <= 256, d_t in [-128, 127] for t > 0; plane t stores d_t 2^(-8t), exact
+//     in bf16;
 //   * the product of planes i and j has weight 2^(-8(i+j)) ("level" i + j); the
 //     levels 0, 1 and 2 each go to their own TMEM accumulator, where their sums
 //     are exact in FP32 as long as 2K <= 192 (|level-2 sum| <= 192 (2*256*128 +
 //     128^2) 2^-16 < 2^24 2^-16); levels 3..NS-1 share a fourth accumulator,
 //     whose FP32 rounding is below 2^-48 of the leading term;
-//   * the epilogue adds the four accumulators in FP64, scales by 2^(ea + eb - 16)
-//     and subtracts the result from C.
+//   * the epilogue adds the four accumulators error-free in FP32 (a float pair),
+//     scales the pair by 2^(ea + eb - 16) with integer operations on the exponent
+//     and subtracts it from C with two FP64 additions.
 // Dropped levels (i + j >= NS) and the digit remainder are about 2^-45 of
 // K * max|A| * max|B|, so the factorisation this update serves is FP64-grade
 // (backward error near FP64 LU's); the FP64 refinement checks every solution.
 //
-// Kernel: persistent, one CTA (6 warps) per SM, 128 x 128 real output tiles
-// (64 complex columns).  A producer thread streams K in chunks of 32 bf16 (one
-// 64-byte swizzle row) of all 2 x NS planes with 4-D TMA into a 2-stage ring; an
+// Kernel: persistent, one CTA (10 warps) per SM, 128 x 64 real output tiles
+// (32 complex columns).  A producer thread streams K in chunks of 32 bf16 (one
+// 64-byte swizzle row) of all 2 x NS planes with 4-D TMA into a 3-stage ring; an
 // MMA thread issues the 21 plane products (2 K-steps each) of a chunk into the four
-// accumulators; four epilogue warps read their 32-lane quarter with tcgen05.ld and
-// update C.  The accumulators fill TMEM (4 x 128 columns), so the epilogue of a
-// tile and the MMAs of the next one do not overlap.  Every wait is bounded; on
-// timeout the kernel records an error, skips the rest and still frees its TMEM.
+// accumulators of one of two accumulator sets (2 x 4 x 64 columns fill TMEM);
+// eight epilogue warps (two per TMEM lane quarter) prefetch their 16 entries of C
+// while the tile is multiplied, then read the accumulators with tcgen05.ld and
+// update C while the next tile is multiplied.  Every wait is bounded; on timeout
+// the kernel records an error, skips the rest and still frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -54,21 +57,24 @@ namespace emul {
 
 using namespace tc;
 
-constexpr int BM = 128;                           // accumulator lanes = rows of C per tile
-constexpr int BN = 128;                           // real columns = 64 complex columns of C
-constexpr int KC = 32;                            // bf16 of K per chunk (64 bytes)
-constexpr int NS = 6;                             // digit planes per operand
-constexpr int NLEV = 4;                           // accumulators: levels 0, 1, 2, then 3..NS-1
-constexpr int STAGES = 2;
-constexpr int TILE_BYTES = BM * KC * 2;           // one plane's tile (A and B alike)
-constexpr int STAGE_BYTES = 2 * NS * TILE_BYTES;  // 96 KB
+constexpr int BM = 128;                             // accumulator lanes = rows of C per tile
+constexpr int BN = 64;                              // real columns = 32 complex columns of C
+constexpr int KC = 32;                              // bf16 of K per chunk (64 bytes)
+constexpr int NS = 6;                               // digit planes per operand
+constexpr int NLEV = 4;                             // accumulators: levels 0, 1, 2, then 3..NS-1
+constexpr int NBUF = 2;                             // accumulator sets (tile i's epilogue || i+1's MMAs)
+constexpr int STAGES = 3;
+constexpr int A_TILE = BM * KC * 2;                 // one plane's tile of A' (8 KB)
+constexpr int B_TILE = BN * KC * 2;                 // one plane's tile of B'^T (4 KB)
+constexpr int STAGE_BYTES = NS * (A_TILE + B_TILE);  // 72 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
-constexpr int NTHREADS = 192;                     // producer warp, MMA warp, 4 epilogue warps
-constexpr int TMEM_COLS = NLEV * BN;              // 512: all of TMEM
-constexpr int kMaxK = 96;                         // complex K per launch (2K <= 192)
+constexpr int EPI_WARPS = 8;                        // two per TMEM lane quarter, one column half each
+constexpr int NTHREADS = 64 + 32 * EPI_WARPS;       // producer warp, MMA warp, epilogue warps
+constexpr int TMEM_COLS = NBUF * NLEV * BN;         // 512: all of TMEM
+constexpr int kMaxK = 96;                           // complex K per launch (2K <= 192)
 
-static_assert(BN == BM, "A and B tiles share TILE_BYTES");
 static_assert(NS * (NS + 1) / 2 == 21, "plane products per chunk");
+static_assert(TMEM_COLS == 512, "accumulators fill TMEM");
 
 // Instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -89,17 +95,54 @@ __device__ __forceinline__ double pow2(int e) {
   return ldexp(1.0, e);
 }
 
-// Plane values of x in (-1, 1): p[t] = d_t 2^(-8t) with the digits above.
-__device__ __forceinline__ void digit_planes(double x, float p[NS]) {
+// Plane values p[t] = d_t 2^(-8t) of x = v 2^-e in (-1, 1) (sc48 = 2^(48-e)): x is
+// rounded once to the 48-bit fixed-point integer X = rint(x 2^48) (one exact FP64
+// scaling and one conversion), whose balanced base-256 digits follow by integer
+// operations: d_5..d_1 in [-128, 127], d_0 = what is left, |d_0| <= 256.  Then
+// x = sum_t d_t 2^(-8(t+1)) to within 2^-49.
+__device__ __forceinline__ void digit_planes(double v, double sc48, float p[NS]) {
+  long long X = __double2ll_rn(v * sc48);
+  int d[NS];
+#pragma unroll
+  for (int t = NS - 1; t > 0; --t) {
+    d[t] = (int)((X + 128) & 255) - 128;
+    X = (X - d[t]) >> 8;
+  }
+  d[0] = (int)X;
   float w = 1.0f;
 #pragma unroll
   for (int t = 0; t < NS; ++t) {
-    const double y = x * 256.0;
-    const double d = rint(y);
-    p[t] = (float)d * w;
-    x = y - d;
+    p[t] = (float)d[t] * w;
     w *= 0x1p-8f;
   }
+}
+
+// 16 consecutive 32-bit TMEM columns of this warp's lane quarter.
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(addr));
+}
+
+// Error-free sum of two floats: s + e = a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// 2^k x as a double for a float x that is zero or normal, by integer operations on
+// the bit fields (exact; the caller keeps k within [-900, 900], so that the result
+// is a normal double for every accumulator value).
+__device__ __forceinline__ double f32_scaled(float x, int k) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t mag = u & 0x7fffffffu;
+  const uint32_t sign = u & 0x80000000u;
+  const uint32_t hi = sign | ((mag >> 3) + ((uint32_t)(896 + k) << 20));
+  return __hiloint2double((int)(mag ? hi : sign), (int)(mag ? (u << 29) : 0u));
 }
 
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
@@ -109,32 +152,43 @@ __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
 
 // ---------------------------------------------------------------- pack ----
 // A (M x K complex, column-major) -> NS planes of A' (row-major M x K2p bf16,
-// zero beyond 2K) and the row exponents ea.  One thread per row.
-__global__ void emul_pack_a_kernel(const double2* __restrict__ A, long long lda, int M, int K, int K2p,
-                                   __nv_bfloat16* __restrict__ planes, size_t plane_elems,
-                                   int* __restrict__ ea, long long astride) {
+// zero beyond 2K) and the row exponents ea.  A block of 4 warps covers 32 rows:
+// lane = row (coalesced column reads), warp = a quarter of the K2p/2 complex
+// columns; the quarters' row maxima meet in shared memory.
+__global__ void __launch_bounds__(128) emul_pack_a_kernel(const double2* __restrict__ A, long long lda, int M, int K,
+                                                         int K2p, __nv_bfloat16* __restrict__ planes,
+                                                         size_t plane_elems, int* __restrict__ ea,
+                                                         long long astride) {
+  __shared__ double smax[4][32];
   const int b = blockIdx.y;
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= M) return;
+  const int lane = threadIdx.x & 31, part = threadIdx.x >> 5;
+  const int m = blockIdx.x * 32 + lane;
+  const int kq = K2p / 8;  // complex columns per quarter (a multiple of 4)
+  const int k0 = part * kq;
   A += (size_t)b * astride;
   double mx = 0.0;
-  for (int k = 0; k < K; ++k) {
-    const double2 v = A[(size_t)k * lda + m];
-    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
-  }
+  if (m < M)
+    for (int k = k0; k < min(K, k0 + kq); ++k) {
+      const double2 v = A[(size_t)k * lda + m];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+  smax[part][lane] = mx;
+  __syncthreads();
+  mx = fmax(fmax(smax[0][lane], smax[1][lane]), fmax(smax[2][lane], smax[3][lane]));
+  if (m >= M) return;
   int e = 0;
   frexp(mx, &e);  // mx < 2^e; e = 0 for a zero row
-  ea[(size_t)b * M + m] = e;
-  const double sc = pow2(-e);
+  if (part == 0) ea[(size_t)b * M + m] = e;
+  const double sc48 = pow2(48 - e);
   __nv_bfloat16* row = planes + ((size_t)b * M + m) * K2p;
-  for (int k0 = 0; k0 < K2p / 2; k0 += 4) {  // 4 complex = 8 bf16 = 16 bytes per plane
+  for (int kc = k0; kc < k0 + kq; kc += 4) {  // 4 complex = 8 bf16 = 16 bytes per plane
     float pr[4][NS], pi[4][NS];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       double2 v = make_double2(0.0, 0.0);
-      if (k0 + u < K) v = A[(size_t)(k0 + u) * lda + m];
-      digit_planes(v.x * sc, pr[u]);
-      digit_planes(v.y * sc, pi[u]);
+      if (kc + u < K) v = A[(size_t)(kc + u) * lda + m];
+      digit_planes(v.x, sc48, pr[u]);
+      digit_planes(v.y, sc48, pi[u]);
     }
 #pragma unroll
     for (int t = 0; t < NS; ++t) {
@@ -143,7 +197,7 @@ __global__ void emul_pack_a_kernel(const double2* __restrict__ A, long long lda,
       q.y = bf16x2(pr[1][t], pi[1][t]);
       q.z = bf16x2(pr[2][t], pi[2][t]);
       q.w = bf16x2(pr[3][t], pi[3][t]);
-      *reinterpret_cast<uint4*>(row + (size_t)t * plane_elems + 2 * k0) = q;
+      *reinterpret_cast<uint4*>(row + (size_t)t * plane_elems + 2 * kc) = q;
     }
   }
 }
@@ -168,15 +222,15 @@ __global__ void emul_pack_b_kernel(const double2* __restrict__ B, long long ldb,
   int e = 0;
   frexp(mx, &e);
   if (lane == 0) eb[(size_t)b * N + n] = e;
-  const double sc = pow2(-e);
+  const double sc48 = pow2(48 - e);
   __nv_bfloat16* r0 = planes + ((size_t)b * 2 * N + 2 * (size_t)n) * K2p;
   __nv_bfloat16* r1 = r0 + K2p;
   for (int k = lane; k < K2p / 2; k += 32) {
     double2 v = make_double2(0.0, 0.0);
     if (k < K) v = B[k];
     float pr[NS], pi[NS];
-    digit_planes(v.x * sc, pr);
-    digit_planes(v.y * sc, pi);
+    digit_planes(v.x, sc48, pr);
+    digit_planes(v.y, sc48, pi);
 #pragma unroll
     for (int t = 0; t < NS; ++t) {
       *reinterpret_cast<uint32_t*>(r0 + (size_t)t * plane_elems + 2 * k) = bf16x2(pr[t], -pi[t]);
@@ -207,15 +261,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
-  // bars: full[STAGES], empty[STAGES], tfull, tempty
+  // bars: full[STAGES], empty[STAGES], tfull[NBUF], tempty[NBUF]
   __shared__ uint32_t tmem_base;
   __shared__ volatile int s_fail;
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
   auto empty_bar = [&](int s) { return smem_u32(&bars[STAGES + s]); };
-  const uint32_t tfull_bar = smem_u32(&bars[2 * STAGES]);
-  const uint32_t tempty_bar = smem_u32(&bars[2 * STAGES + 1]);
+  auto tfull_bar = [&](int b) { return smem_u32(&bars[2 * STAGES + b]); };
+  auto tempty_bar = [&](int b) { return smem_u32(&bars[2 * STAGES + NBUF + b]); };
 
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -228,8 +282,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), 1);
     }
-    mbar_init(tfull_bar, 1);
-    mbar_init(tempty_bar, NTHREADS / 32 - 2);  // one arrival per epilogue warp
+    for (int b = 0; b < NBUF; ++b) {
+      mbar_init(tfull_bar(b), 1);
+      mbar_init(tempty_bar(b), EPI_WARPS);  // one arrival per epilogue warp
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_fail = *reinterpret_cast<const volatile int*>(err) != 0;
   }
@@ -249,12 +305,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const int s = it % STAGES, use = it / STAGES;
           if (use > 0 && !(ok = role_wait(empty_bar(s), (use - 1) & 1, err, &s_fail))) break;
           const uint32_t a0 = smem_u32(base + s * STAGE_BYTES);
-          const uint32_t b0 = a0 + NS * TILE_BYTES;
+          const uint32_t b0 = a0 + NS * A_TILE;
           mbar_expect_tx(full_bar(s), STAGE_BYTES);
 #pragma unroll
           for (int p = 0; p < NS; ++p) {
-            tma_load_4d(a0 + p * TILE_BYTES, &mapA, c * KC, tc.m0, tc.mat, p, full_bar(s));
-            tma_load_4d(b0 + p * TILE_BYTES, &mapB, c * KC, tc.j0, tc.mat, p, full_bar(s));
+            tma_load_4d(a0 + p * A_TILE, &mapA, c * KC, tc.m0, tc.mat, p, full_bar(s));
+            tma_load_4d(b0 + p * B_TILE, &mapB, c * KC, tc.j0, tc.mat, p, full_bar(s));
           }
           ++it;
         }
@@ -274,17 +330,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int it = 0, tl = 0;
       bool ok = !s_fail;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tl) {
-        if (tl > 0 && !(ok = role_wait(tempty_bar, (tl - 1) & 1, err, &s_fail))) break;
+        const int b = tl % NBUF, use = tl / NBUF;
+        if (use > 0 && !(ok = role_wait(tempty_bar(b), (use - 1) & 1, err, &s_fail))) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t accb = tmem + (uint32_t)(b * NLEV * BN);
         for (int c = 0; c < nchunks; ++c) {
           const int s = it % STAGES;
           if (!(ok = role_wait(full_bar(s), (it / STAGES) & 1, err, &s_fail))) break;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t a0 = smem_u32(base + s * STAGE_BYTES);
-          const uint32_t b0 = a0 + NS * TILE_BYTES;
+          const uint32_t b0 = a0 + NS * A_TILE;
 #pragma unroll
           for (int L = 0; L < NS; ++L) {
-            const uint32_t acc = tmem + (uint32_t)(min(L, NLEV - 1) * BN);
+            const uint32_t acc = accb + (uint32_t)(min(L, NLEV - 1) * BN);
 #pragma unroll
             for (int i = 0; i <= L; ++i) {
               const int j = L - i;
@@ -292,8 +350,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               for (int kk = 0; kk < KC / 16; ++kk) {
                 // the first product into accumulators 0..NLEV-1 of a tile overwrites
                 const uint32_t accum = (c == 0 && i == 0 && kk == 0 && L < NLEV) ? 0u : 1u;
-                mma_bf16(acc, sdesc_sw<64>(a0 + i * TILE_BYTES + kk * 32),
-                         sdesc_sw<64>(b0 + j * TILE_BYTES + kk * 32), accum);
+                mma_bf16(acc, sdesc_sw<64>(a0 + i * A_TILE + kk * 32), sdesc_sw<64>(b0 + j * B_TILE + kk * 32),
+                         accum);
               }
             }
           }
@@ -301,7 +359,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           ++it;
         }
         if (!ok) break;
-        mma_commit(tfull_bar);
+        mma_commit(tfull_bar(b));
       }
       if (!ok) {
         s_fail = 1;
@@ -315,7 +373,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ----------------------------------------------------------- epilogue
-    const int q = warp & 3;  // TMEM lanes 32q..32q+31
+    // warp w >= 2: TMEM lanes 32 (w % 4) .. +31 (the quarter it may read), complex
+    // columns h*16 .. h*16+15 of the tile
+    const int q = warp & 3, h = (warp - 2) >> 2;
     int tl = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
@@ -324,16 +384,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int row = tc.m0 + q * 32 + lane;
       const bool row_ok = row < M;
       const int erow = row_ok ? ea[(size_t)tc.mat * M + row] - 16 : 0;
-      auto load_c_chunk = [&](int cc, double2* dst) {
-        const int n0 = (tc.j0 >> 1) + cc * 8;
+      const int n0 = (tc.j0 >> 1) + h * 16;
+      // this thread's 16 entries of C, in flight while the tile is multiplied
+      double2 cv[16];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-          dst[j] = (row_ok && n0 + j < N) ? Cm[(size_t)(n0 + j) * ldc + row] : make_double2(0.0, 0.0);
-      };
-      double2 cbuf[8], nxt[8];
-      load_c_chunk(0, cbuf);
+      for (int j = 0; j < 16; ++j)
+        cv[j] = (row_ok && n0 + j < N) ? Cm[(size_t)(n0 + j) * ldc + row] : make_double2(0.0, 0.0);
+      const int b = tl % NBUF, use = tl / NBUF;
       int ok = 0;
-      if (lane == 0) ok = role_wait(tfull_bar, tl & 1, err, &s_fail) ? 1 : 0;
+      if (lane == 0) ok = role_wait(tfull_bar(b), use & 1, err, &s_fail) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) {
         if (lane == 0) {
@@ -343,44 +402,59 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
-#pragma unroll 1
-      for (int cc = 0; cc < BN / 16; ++cc) {
-        if (cc + 1 < BN / 16) load_c_chunk(cc + 1, nxt);
-        uint32_t r[NLEV][16];
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NLEV * BN + h * 32);
 #pragma unroll
-        for (int L = 0; L < NLEV; ++L)
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-              : "=r"(r[L][0]), "=r"(r[L][1]), "=r"(r[L][2]), "=r"(r[L][3]), "=r"(r[L][4]), "=r"(r[L][5]),
-                "=r"(r[L][6]), "=r"(r[L][7]), "=r"(r[L][8]), "=r"(r[L][9]), "=r"(r[L][10]), "=r"(r[L][11]),
-                "=r"(r[L][12]), "=r"(r[L][13]), "=r"(r[L][14]), "=r"(r[L][15])
-              : "r"(taddr + (uint32_t)(L * BN + cc * 16)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int cc = 0; cc < 2; ++cc) {
+        // the four levels of 16 real entries (8 complex) summed error-free into float
+        // pairs (s, e), highest level first, one accumulator read at a time
+        float sp[16], ep[16];
+        {
+          uint32_t r3[16], r2[16];
+          tmem_ld16(taddr + (uint32_t)(3 * BN + cc * 16), r3);
+          tmem_ld16(taddr + (uint32_t)(2 * BN + cc * 16), r2);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int x = 0; x < 16; ++x) two_sum(__uint_as_float(r2[x]), __uint_as_float(r3[x]), sp[x], ep[x]);
+        }
+#pragma unroll
+        for (int L = 1; L >= 0; --L) {
+          uint32_t rl[16];
+          tmem_ld16(taddr + (uint32_t)(L * BN + cc * 16), rl);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int x = 0; x < 16; ++x) {
+            float e2;
+            two_sum(__uint_as_float(rl[x]), sp[x], sp[x], e2);
+            ep[x] = __fadd_rn(ep[x], e2);
+          }
+        }
         if (row_ok) {
-          const int n0 = (tc.j0 >> 1) + cc * 8;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            if (n0 + j < N) {
-              double vr = (double)__uint_as_float(r[3][2 * j]) + (double)__uint_as_float(r[2][2 * j]);
-              double vi = (double)__uint_as_float(r[3][2 * j + 1]) + (double)__uint_as_float(r[2][2 * j + 1]);
-              vr = (vr + (double)__uint_as_float(r[1][2 * j])) + (double)__uint_as_float(r[0][2 * j]);
-              vi = (vi + (double)__uint_as_float(r[1][2 * j + 1])) + (double)__uint_as_float(r[0][2 * j + 1]);
-              const double sc = pow2(erow + ebm[n0 + j]);
-              double2 v = cbuf[j];
-              v.x = fma(-vr, sc, v.x);
-              v.y = fma(-vi, sc, v.y);
-              Cm[(size_t)(n0 + j) * ldc + row] = v;
+            const int n = n0 + cc * 8 + j;
+            if (n < N) {
+              // scaled and subtracted with two FP64 additions per real entry (the
+              // SM's FP64 pipe is the epilogue's arithmetic bound; the rest is FP32
+              // and integer work)
+              const int k = erow + ebm[n];
+              double2 v = cv[cc * 8 + j];
+              if (k >= -900 && k <= 900) {
+                v.x = __dsub_rn(__dsub_rn(v.x, f32_scaled(sp[2 * j], k)), f32_scaled(ep[2 * j], k));
+                v.y = __dsub_rn(__dsub_rn(v.y, f32_scaled(sp[2 * j + 1], k)), f32_scaled(ep[2 * j + 1], k));
+              } else {
+                const double sc = pow2(k);
+                v.x = __dsub_rn(__dsub_rn(v.x, (double)sp[2 * j] * sc), (double)ep[2 * j] * sc);
+                v.y = __dsub_rn(__dsub_rn(v.y, (double)sp[2 * j + 1] * sc), (double)ep[2 * j + 1] * sc);
+              }
+              Cm[(size_t)n * ldc + row] = v;
             }
           }
         }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) cbuf[j] = nxt[j];
       }
+      // accumulator set b read out: the MMA issuer may overwrite it
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(tempty_bar);
+      if (lane == 0) mbar_arrive(tempty_bar(b));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -396,13 +470,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 namespace {
 
 // 4-D map over NS planes of `batch` matrices of rows x k2p bf16 (row-major),
-// 32 x 128 boxes with 64-byte swizzle.
-bool make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int k2p, int batch) {
+// 32 x box_rows boxes with 64-byte swizzle.
+bool make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int k2p, int batch, int box_rows) {
   EncodeFn enc = encode_fn();
   if (!enc) return false;
   cuuint64_t dims[4] = {(cuuint64_t)k2p, (cuuint64_t)rows, (cuuint64_t)batch, (cuuint64_t)NS};
   cuuint64_t strides[3] = {(cuuint64_t)k2p * 2, (cuuint64_t)rows * k2p * 2, (cuuint64_t)batch * rows * k2p * 2};
-  cuuint32_t box[4] = {(cuuint32_t)KC, (cuuint32_t)BM, 1, 1};
+  cuuint32_t box[4] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 1, 1};
   cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(ptr), dims, strides, box,
                    estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -441,10 +515,11 @@ cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, con
   int* ea = reinterpret_cast<int*>(pb + NS * b_pl);
   int* eb = ea + (size_t)M * batch;
   stats::count(stats::kMisc, 2);
-  emul_pack_a_kernel<<<dim3((M + 127) / 128, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
+  emul_pack_a_kernel<<<dim3((M + 31) / 32, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
   emul_pack_b_kernel<<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
   CUtensorMap ma, mb;
-  if (!make_map(&ma, pa, M, K2p, batch) || !make_map(&mb, pb, 2 * N, K2p, batch)) return cudaErrorInvalidValue;
+  if (!make_map(&ma, pa, M, K2p, batch, BM) || !make_map(&mb, pb, 2 * N, K2p, batch, BN))
+    return cudaErrorInvalidValue;
   e = allow_dynamic_smem((const void*)zgemm_sub_emul_kernel, SMEM_BYTES);
   if (e != cudaSuccess) return e;
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;

@@ -10,9 +10,11 @@ namespace wmom {
 constexpr int kMaxPanelBlocks = 256;
 constexpr int kMaxLuBatch = 16;  // matrices per batched factorisation
 
-// Largest batch whose first panel launch fits co-resident on this device.
+// Largest batch whose cooperative panel launches all fit co-resident on this device
+// (cluster panels impose no limit).  fp64_cluster: the FP64 factorisation runs with
+// a tensor-core trailing update, whose panels are cluster panels where they fit.
 template <typename C>
-int lu_max_batch(int n);
+int lu_max_batch(int n, bool fp64_cluster = false);
 
 struct GridBarrier;
 

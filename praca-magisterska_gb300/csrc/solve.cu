@@ -283,6 +283,16 @@ int gmres_restart() {
   const int v = env_int("WMOM_GMRES_RESTART", 4, 400);
   return v ? v : 30;
 }
+// GMRES refinement with the FP32 factors before the FP64-grade tiers: on by default
+// only without the tensor-core second tier, which serves a stalled matrix in less
+// time than GMRES (measured on the grid workloads: 6.12 vs 5.83 freq-solves/s at
+// N = 8192, 67.9 vs 57.8 at N = 2048).  WMOM_KRYLOV=1 / 0 forces it on / off.
+bool krylov_enabled() {
+  const char* e = std::getenv("WMOM_KRYLOV");
+  if (e && e[0] == '1') return true;
+  if (e && e[0] == '0') return false;
+  return emul_gemm_hook() == nullptr;
+}
 int gmres_cycles() {
   const int v = env_int("WMOM_GMRES_CYCLES", 1, 20);
   return v ? v : 2;
@@ -705,7 +715,7 @@ namespace {
 wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws, cudaStream_t s, int* info,
                         GemmHook<double2> hook) {
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
-  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, 1);
+  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, 2);
   if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t (tier 2)");
   int err = lu_workspace_read_status(ws, info, s, bg);
   err |= tc::read_and_clear_error(ws, s);
@@ -821,6 +831,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   // barely moved, i.e. kappa * u_fp32 >> 1 -- go straight to the FP64 LU.
   constexpr double kKrylovEntry = 1e-3;
   for (int b = 0; b < bg; ++b) {
+    if (!krylov_enabled()) break;
     if (!fallback[b] || info[b] != 0) continue;
     if (!(rel_best[b] <= kKrylovEntry * rel_first[b])) continue;
     double2* xb = g.x64.as<double2>() + (size_t)b * n;
@@ -900,20 +911,32 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   for (int b = 0; b < bg; ++b)
     if (fallback[b]) fb[nfb++] = b;
   if (nfb == 0) return WMOM_OK;
+  const GemmHook<double2> emul = emul_gemm_hook();
   if (g.fb_cap == 0) {
     size_t fr = 0, tot = 0;
     SWEEP_TRY(cudaMemGetInfo(&fr, &tot));
-    LuConfig c64;
-    const wmom_status cs = choose_lu_config(WMOM_MODE_FP64, n, g.B, nullptr, ws, s, fr / 2, &c64, false);
-    if (cs != WMOM_OK) return cs;
-    const int cap = std::max(1, std::min(c64.batch, g.B));
+    int cap = 1;
+    if (emul) {
+      // with its updates on the tensor cores the second tier's time goes to the FP64
+      // panels, which run side by side across a batch: as wide as co-residency of
+      // the panel, the workspace and a quarter of the free memory allow
+      cap = std::min({g.B, ws->max_batch, kMaxLuBatch, lu_max_batch<double2>(n, true)});
+      const int eb = env_int("WMOM_LU_BATCH", 1, kMaxLuBatch);
+      if (eb) cap = std::min(cap, eb);
+      while (cap > 1 && (size_t)cap * nn * sizeof(double2) > fr / 4) --cap;
+    } else {
+      LuConfig c64;
+      const wmom_status cs = choose_lu_config(WMOM_MODE_FP64, n, g.B, nullptr, ws, s, fr / 2, &c64, false);
+      if (cs != WMOM_OK) return cs;
+      cap = c64.batch;
+    }
+    cap = std::max(1, std::min(cap, g.B));
     SWEEP_TRY(g.fb_lu.alloc(sizeof(double2) * nn * cap, s));
     SWEEP_TRY(g.fb_ipiv.alloc(sizeof(int) * (size_t)n * cap, s));
     SWEEP_TRY(g.fb_x.alloc(sizeof(double2) * (size_t)n * cap, s));
     SWEEP_TRY(g.fb_r.alloc(sizeof(double2) * (size_t)n * cap, s));
     g.fb_cap = cap;
   }
-  const GemmHook<double2> emul = emul_gemm_hook();
   double2* flu = g.fb_lu.as<double2>();
   double2* fx = g.fb_x.as<double2>();
   double2* frr = g.fb_r.as<double2>();

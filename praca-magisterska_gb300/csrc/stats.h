@@ -21,6 +21,7 @@ enum Cls : int {
   kResidual,   // FP64 residual GEMV (work: bytes of Z read)
   kMisc,       // conversions, norms, packing, permutations
   kEmulGemm,   // FP64-grade trailing update on the bf16 tensor cores (8*M*N*K real flops)
+  kTrsv,       // triangular solves of one right-hand side per matrix (the refinement's)
   kNumCls
 };
 

@@ -170,3 +170,24 @@ def test_second_tier_serves_ill_conditioned_grid(cuda, wmom):
         assert rp[k]["tier"] == 3 and rp[k]["status"] == 0
         assert np.array_equal(cp[k], c64[k])
     plan.close()
+
+
+def test_krylov_step_forced_on(cuda, wmom):
+    # GMRES refinement with the FP32 factors runs by default only without the
+    # tensor-core second tier; forced on, every result keeps the contract of the tier
+    # that produced it (two FP64-level solves of these grid systems differ by up to
+    # kappa * eps, bounded by 1e-6 as in the fixture test)
+    topo = wmom.Topology(wmom.geometry.precision_grid(2048))
+    freqs = np.geomspace(0.05, 20.0, 8).astype(np.float32)
+    plan = wmom.Plan(topo)
+    c64, _, r64 = plan.solve(freqs, 1000, mode=0)
+    os.environ["WMOM_KRYLOV"] = "1"
+    try:
+        cm, _, rm = plan.solve(freqs, 1000, mode=1)
+    finally:
+        del os.environ["WMOM_KRYLOV"]
+    assert sum(r["krylov_steps"] for r in rm) > 0, rm
+    for k in range(len(freqs)):
+        assert rm[k]["status"] == 0 and rm[k]["tier"] in (1, 2, 3), rm[k]
+        assert _rel(cm[k], c64[k]) < 1e-6, (k, _rel(cm[k], c64[k]), rm[k])
+    plan.close()
