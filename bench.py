@@ -309,7 +309,8 @@ def run_wmom(args):
     # DRAM traffic per launch: bytes per unit from one ncu capture of a smaller case,
     # scaled by the units this launch processed (traffic grows in proportion)
     units = {"fill": work_per_launch / 384.0,            # Z entries (384 flop-eq each)
-             "tc_gemm": work_per_launch / (8.0 * 96)}.get(dom)  # complex entries of C (K = 96)
+             "tc_gemm": work_per_launch / (8.0 * 96),     # complex entries of C (K = 96)
+             "emul_gemm": work_per_launch / (8.0 * 96)}.get(dom)  # complex entries of C (K = 96)
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             cap = json.load(f).get(roof["kernel"].split("::")[-1])
@@ -479,6 +480,46 @@ def run_geometries(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gemm(args):
+    """One trailing-update kernel alone (profiling cases): C -= A B for complex operands,
+    m = n = --n, k = --k, through the C ABI on device-resident operands; W untimed then K
+    timed calls, each bracketed by CUDA events.  gemm_emul: the FP64-grade digit-plane
+    update (complex128); gemm_tc: the 3xTF32 update of the FP32 factorisation (complex64)."""
+    import ctypes
+    import torch
+    torch.cuda.set_device(0)
+    w = importlib.import_module("praca-magisterska_gb300")
+    m = nn = args.n
+    k = args.k
+    emul = args.workload == "gemm_emul"
+    dt = torch.complex128 if emul else torch.complex64
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    a = torch.randn(k, m, dtype=dt, device="cuda", generator=g)   # column-major m x k
+    b = torch.randn(nn, k, dtype=dt, device="cuda", generator=g)  # column-major k x n
+    c = torch.randn(nn, m, dtype=dt, device="cuda", generator=g)  # column-major m x n
+    f = w._lib.wmom_zgemm_sub_emul if emul else w._lib.wmom_cgemm_sub_tc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_longlong] * 3 + [ctypes.c_void_p]
+    call = lambda: f(m, nn, k, a.data_ptr(), m, b.data_ptr(), k, c.data_ptr(), m, None)
+    for _ in range(args.warmup):
+        assert call() == 0
+    ms = []
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        assert call() == 0
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    med = statistics.median(ms)
+    print(json.dumps({"metric": "trailing-update GEMM, algorithmic complex TFLOP/s (8 m n k)",
+                      "kernel": "zgemm_sub_emul_kernel" if emul else "cgemm_sub_tc_kernel",
+                      "value": 8.0 * m * nn * k / (med / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_call": med,
+                      "steps": args.steps, "warmup": args.warmup, "config": {"m": m, "n": nn, "k": k}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,7 +527,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wmom", choices=["wmom", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--workload", default="sweep", choices=sorted(WORKLOADS) + ["serving", "geometries"])
+    ap.add_argument("--workload", default="sweep",
+                    choices=sorted(WORKLOADS) + ["serving", "geometries", "gemm_emul", "gemm_tc"])
+    ap.add_argument("--k", type=int, default=96, help="inner dimension of the gemm_* workloads")
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--fp64-freqs", type=int, default=2)
@@ -501,7 +544,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "serving":
+    if args.workload in ("gemm_emul", "gemm_tc"):
+        run_gemm(args)
+    elif args.workload == "serving":
         run_serving(args)
     elif args.workload == "geometries":
         run_geometries(args)

@@ -74,24 +74,35 @@ __device__ __forceinline__ float tf32_rna(float x) {
 
 // ---------------------------------------------------------------- pack ----
 // A (M x K complex, col-major) -> hi/lo planes, row-major M x K2p FP32 (re, im
-// interleaved along K, zero padding up to K2p).
-__global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int K2p,
-                              float* __restrict__ hi, float* __restrict__ lo, long long astride) {
+// interleaved along K, zero padding up to K2p).  A block transposes a tile of 32 rows
+// x 32 complex columns through shared memory: column reads and plane writes are both
+// coalesced.
+__global__ void __launch_bounds__(256) pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K,
+                                                     int K2p, float* __restrict__ hi, float* __restrict__ lo,
+                                                     long long astride) {
+  __shared__ float2 tile[32][33];  // [complex column][row]
   // batch: blockIdx.z selects the matrix; its planes follow each other
   A += (size_t)blockIdx.z * astride;
   hi += (size_t)blockIdx.z * M * K2p;
   lo += (size_t)blockIdx.z * M * K2p;
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;  // complex column, K2p/2 of them
-  if (m >= M) return;
-  float2 v = make_float2(0.f, 0.f);
-  if (k < K) v = A[(size_t)k * lda + m];
-  const float hr = tf32_rna(v.x), hi_ = tf32_rna(v.y);
-  const size_t o = (size_t)m * K2p + 2 * k;
-  hi[o] = hr;
-  hi[o + 1] = hi_;
-  lo[o] = tf32_rna(v.x - hr);
-  lo[o + 1] = tf32_rna(v.y - hi_);
+  const int m0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int k = k0 + ty + 8 * i, m = m0 + tx;
+    tile[ty + 8 * i][tx] = (k < K && m < M) ? A[(size_t)k * lda + m] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = ty + 8 * i, m = m0 + r, k = k0 + tx;
+    if (m >= M || 2 * k >= K2p) continue;
+    const float2 v = tile[tx][r];
+    const float hr = tf32_rna(v.x), hi_ = tf32_rna(v.y);
+    const size_t o = (size_t)m * K2p + 2 * k;
+    *reinterpret_cast<float2*>(hi + o) = make_float2(hr, hi_);
+    *reinterpret_cast<float2*>(lo + o) = make_float2(tf32_rna(v.x - hr), tf32_rna(v.y - hi_));
+  }
 }
 
 // B (K x N complex, col-major) -> hi/lo planes of B'^T, row-major 2N x K2p FP32:
@@ -422,7 +433,8 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
   float* bhi = alo + a_pl;
   float* blo = bhi + b_pl;
   stats::count(stats::kMisc, 2);
-  pack_a_kernel<<<dim3((M + 127) / 128, K2p / 2, batch), 128, 0, s>>>(A, lda, M, K, K2p, ahi, alo, bstride);
+  pack_a_kernel<<<dim3((M + 31) / 32, (K2p / 2 + 31) / 32, batch), 256, 0, s>>>(A, lda, M, K, K2p, ahi, alo,
+                                                                                bstride);
   pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
   CUtensorMap mah, mal, mbh, mbl;
   if (!make_map(&mah, ahi, M, K2p, batch) || !make_map(&mal, alo, M, K2p, batch) ||

@@ -715,7 +715,11 @@ namespace {
 wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws, cudaStream_t s, int* info,
                         GemmHook<double2> hook) {
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
-  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, 2);
+  // span: panels per tensor-core update.  3 x a 32-column panel is K = 96, the most
+  // one launch of the digit-plane GEMM takes; measured on the N = 8192 grid workload
+  // at spans 1 / 2 / 3: 6.70 / 8.66 / 9.67 freq-solves/s.  WMOM_EMUL_SPAN overrides.
+  const int es = env_int("WMOM_EMUL_SPAN", 1, kMaxSpan);
+  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, es ? es : 3);
   if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t (tier 2)");
   int err = lu_workspace_read_status(ws, info, s, bg);
   err |= tc::read_and_clear_error(ws, s);
