@@ -158,15 +158,6 @@ cudaError_t get_default_ws(int n, int nrhs, LuWorkspace** out) {
   return cudaSuccess;
 }
 
-struct FreqParamsH {
-  double ka, ka2, cq;
-};
-
-FreqParamsH freq_params(double ka) {
-  const double pi = std::acos(-1.0);
-  const double eta0 = 120. * pi;
-  return FreqParamsH{ka, ka * ka, eta0 / (4.0 * pi * ka)};
-}
 
 }  // namespace
 }  // namespace wmom
@@ -176,7 +167,7 @@ using namespace wmom;
 struct wmom_plan_s {
   Plan p;
   std::mutex mu;
-  FreqParamsH* d_fp = nullptr;
+  FreqParams* d_fp = nullptr;
   int fp_cap = 0;
   LuWorkspace ws{};
   int ws_n = 0;
@@ -341,12 +332,12 @@ wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long l
       cudaFree(h->d_fp);
       h->d_fp = nullptr;
     }
-    WMOM_CUDA_TRY(cudaMalloc(&h->d_fp, sizeof(FreqParamsH) * nk));
+    WMOM_CUDA_TRY(cudaMalloc(&h->d_fp, sizeof(FreqParams) * nk));
     h->fp_cap = nk;
   }
-  std::vector<FreqParamsH> fp(nk);
+  std::vector<FreqParams> fp(nk);
   for (int i = 0; i < nk; ++i) fp[i] = freq_params(ka[i]);
-  WMOM_CUDA_TRY(cudaMemcpyAsync(h->d_fp, fp.data(), sizeof(FreqParamsH) * nk, cudaMemcpyHostToDevice, s));
+  WMOM_CUDA_TRY(cudaMemcpyAsync(h->d_fp, fp.data(), sizeof(FreqParams) * nk, cudaMemcpyHostToDevice, s));
   WMOM_CUDA_TRY(launch_fill(h->p, reinterpret_cast<const double*>(h->d_fp), nk,
                             reinterpret_cast<double2*>(z_dev), ldz, zstride, s));
   // the parameter upload is from pageable memory: finish before the vector dies

@@ -187,18 +187,20 @@ __device__ __forceinline__ void gauss2(double dl, double s[2], double wu[2], dou
 
 // One regular source half of the per-entry kernel: the ramped integral times the
 // projection t (rising ramp for S_n+, falling for S_n-) and the plain integral over
-// dl, i.e. (dl/2) sum g / dl = sum g / 2.
+// dl, i.e. (dl/2) sum g / dl = sum g / 2; the first scaled by kc = k^2 cq, the
+// second by cq (hc = cq / 2), as the pair values are.
 __device__ void regular_half(const double rm[3], const double rs[3], const double dc[3], double dl, double an,
-                             double ka, bool falling, double t, const double2* tab, Cx* At, Cx* Pd) {
+                             double ka, bool falling, double t, double kc, double hc, const double2* tab, Cx* At,
+                             Cx* Pd) {
   double s[2], wu[2], wd[2];
   gauss2(dl, s, wu, wd);
   const double ex[3] = {sub(rm[0], rs[0]), sub(rm[1], rs[1]), sub(rm[2], rs[2])};
   Cx su, sd, sp;
   regular_sums(ex, dc, mul(an, an), s, wu, wd, ka, tab, &su, &sd, &sp);
-  const double ht = mul(mul(dl, 0.5), t);
+  const double htk = mul(mul(mul(dl, 0.5), t), kc);
   const Cx& sw = falling ? sd : su;
-  *At = Cx{mul(sw.re, ht), mul(sw.im, ht)};
-  *Pd = Cx{mul(0.5, sp.re), mul(0.5, sp.im)};
+  *At = Cx{mul(sw.re, htk), mul(sw.im, htk)};
+  *Pd = Cx{mul(hc, sp.re), mul(hc, sp.im)};
 }
 
 // Regularised self kernel bracket (Zmatrix.cpp:695-709) at parameter s.
@@ -259,9 +261,6 @@ __device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
   return add(add(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2]));
 }
 
-struct FreqParams {
-  double ka, ka2, cq;  // k, k^2, eta0/(4*pi*k)
-};
 
 // One thread per entry: blockIdx.x*blockDim.x + threadIdx.x = row m (observation),
 // blockIdx.y = column n (source), blockIdx.z = frequency.  Consecutive threads write
@@ -277,7 +276,7 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
   const int n = blockIdx.y;
   const int k = blockIdx.z;
   if (m >= npls) return;
-  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+  const double ka = fp[k].ka, cq = fp[k].cq, kc = fp[k].kc, hc = fp[k].hc;
   const double senv = (double)sgnenv;
   double acc_re = 0.0, acc_im = 0.0;
 #pragma unroll 1
@@ -295,13 +294,15 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
       if (same) {
         Cx A, P;
         self_half(sh.dl, sh.an, ka, falling, &A, &P);
-        At = Cx{mul(A.re, t), mul(A.im, t)};
-        Pd = Cx{__ddiv_rn(P.re, sh.dl), __ddiv_rn(P.im, sh.dl)};
+        const double tk = mul(t, kc);
+        At = Cx{mul(A.re, tk), mul(A.im, tk)};
+        Pd = Cx{mul(__ddiv_rn(P.re, sh.dl), cq), mul(__ddiv_rn(P.im, sh.dl), cq)};
       } else {
-        regular_half(o.rm, sh.rs, sh.dc, sh.dl, sh.an, ka, falling, t, tab, &At, &Pd);
+        regular_half(o.rm, sh.rs, sh.dc, sh.dl, sh.an, ka, falling, t, kc, hc, tab, &At, &Pd);
       }
-      av_re = add(av_re, At.re);
-      av_im = add(av_im, At.im);
+      // the first term starts the sums (no addition to zero), as in the tile assembly
+      av_re = sgm == 0 ? At.re : add(av_re, At.re);
+      av_im = sgm == 0 ? At.im : add(av_im, At.im);
       Cx Pid = {0.0, 0.0};
       if (ienv == 2) {
         const double ti = mul(dot3(sh.dc_img, o.lm), senv);
@@ -309,16 +310,20 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
         if (same && o.on_ground) {
           Cx Ai, Pi;
           self_half(sh.dl, sh.an, ka, falling, &Ai, &Pi);
-          Ait = Cx{mul(Ai.re, ti), mul(Ai.im, ti)};
-          Pid = Cx{__ddiv_rn(Pi.re, sh.dl), __ddiv_rn(Pi.im, sh.dl)};
+          const double tk = mul(ti, kc);
+          Ait = Cx{mul(Ai.re, tk), mul(Ai.im, tk)};
+          Pid = Cx{mul(__ddiv_rn(Pi.re, sh.dl), cq), mul(__ddiv_rn(Pi.im, sh.dl), cq)};
         } else {
-          regular_half(o.rm, sh.rs_img, sh.dc_img, sh.dl, sh.an, ka, falling, ti, tab, &Ait, &Pid);
+          regular_half(o.rm, sh.rs_img, sh.dc_img, sh.dl, sh.an, ka, falling, ti, kc, hc, tab, &Ait, &Pid);
         }
         av_re = add(av_re, Ait.re);
         av_im = add(av_im, Ait.im);
       }
       // scalar potential: + P(S_n+)/dl - P(S_n-)/dl
-      if (!falling) {
+      if (sgm == 0 && ienv != 2) {
+        sv_re = Pd.re;
+        sv_im = Pd.im;
+      } else if (!falling) {
         sv_re = add(sv_re, Pd.re);
         sv_im = add(sv_im, Pd.im);
       } else {
@@ -337,22 +342,14 @@ __global__ void __launch_bounds__(128) fill_entry_kernel(const ObsHalf* __restri
         }
       }
     }
-    double c_re = mul(av_re, ka2), c_im = mul(av_im, ka2);
-    if (h == 0) {
-      c_re = sub(c_re, sv_re);
-      c_im = sub(c_im, sv_im);
-    } else {
-      c_re = add(c_re, sv_re);
-      c_im = add(c_im, sv_im);
-    }
-    acc_re = add(acc_re, c_re);
-    acc_im = add(acc_im, c_im);
+    // k^2 (A+ + A-) -/+ (Phi+ - Phi-), both already scaled by cq
+    const double c_re = h == 0 ? sub(av_re, sv_re) : add(av_re, sv_re);
+    const double c_im = h == 0 ? sub(av_im, sv_im) : add(av_im, sv_im);
+    acc_re = h == 0 ? c_re : add(acc_re, c_re);
+    acc_im = h == 0 ? c_im : add(acc_im, c_im);
   }
-  // times j*cq
-  double2 out;
-  out.x = -mul(cq, acc_im);
-  out.y = mul(cq, acc_re);
-  Z[(size_t)k * zstride + (size_t)n * ldz + m] = out;
+  // times j (cq is in the terms)
+  Z[(size_t)k * zstride + (size_t)n * ldz + m] = make_double2(-acc_im, acc_re);
 }
 
 // ------------------------------------------------------------------------
@@ -434,33 +431,36 @@ __device__ __forceinline__ bool same_segment(const ObsInst& O, const SrcInst& S)
 }
 
 // Phase A value of a regular pair from its R, 1/R and projection t.
+// The ramped integrals carry k^2 cq (kc), the plain one cq (hc = cq / 2 with the 1/2
+// of the 2-point rule), so that phase B only adds.
 __device__ __forceinline__ PairVal regular_pair_value(const double r[2], const double ri[2], double t,
-                                                      const SrcInst& S, double ka, const double2* tab) {
+                                                      const SrcInst& S, const FreqParams& f, const double2* tab) {
   Cx su, sd, sp;
-  gauss_sums(r, ri, S.w_up, S.w_dn, ka, tab, &su, &sd, &sp);
-  const double ht = mul(S.half, t);
+  gauss_sums(r, ri, S.w_up, S.w_dn, f.ka, tab, &su, &sd, &sp);
+  const double htk = mul(mul(S.half, t), f.kc);
   PairVal v;
-  v.wu = make_double2(mul(su.re, ht), mul(su.im, ht));
-  v.wd = make_double2(mul(sd.re, ht), mul(sd.im, ht));
-  v.ph = make_double2(mul(0.5, sp.re), mul(0.5, sp.im));
+  v.wu = make_double2(mul(su.re, htk), mul(su.im, htk));
+  v.wd = make_double2(mul(sd.re, htk), mul(sd.im, htk));
+  v.ph = make_double2(mul(f.hc, sp.re), mul(f.hc, sp.im));
   return v;
 }
 
-// Phase A value of a self pair (identical segments).
-__device__ __forceinline__ PairVal self_pair_value(double t, const SrcInst& S, double ka) {
+// Phase A value of a self pair (identical segments), scaled as above.
+__device__ __forceinline__ PairVal self_pair_value(double t, const SrcInst& S, const FreqParams& f) {
   Cx Au, Ad, P;
-  self_pair(S.dl, S.an, ka, &Au, &Ad, &P);
+  self_pair(S.dl, S.an, f.ka, &Au, &Ad, &P);
+  const double tk = mul(t, f.kc);
   PairVal v;
-  v.wu = make_double2(mul(Au.re, t), mul(Au.im, t));
-  v.wd = make_double2(mul(Ad.re, t), mul(Ad.im, t));
-  v.ph = make_double2(__ddiv_rn(P.re, S.dl), __ddiv_rn(P.im, S.dl));
+  v.wu = make_double2(mul(Au.re, tk), mul(Au.im, tk));
+  v.wd = make_double2(mul(Ad.re, tk), mul(Ad.im, tk));
+  v.ph = make_double2(mul(__ddiv_rn(P.re, S.dl), f.cq), mul(__ddiv_rn(P.im, S.dl), f.cq));
   return v;
 }
 
 // Phase B: the entries of tile (tr, tc) from the pair values, consecutive threads
 // on consecutive rows (coalesced 16-byte stores), in the reference's order.
 __device__ __forceinline__ void assemble_tile(const PairVal* pt, int nQ, const TileLists& L, int tr, int tc, int npls,
-                                              double ka2, double cq, double2* __restrict__ Zk, long long ldz) {
+                                              double2* __restrict__ Zk, long long ldz) {
   for (int e = threadIdx.x; e < kPairTile * kPairTile; e += blockDim.x) {
     const int r = e % kPairTile, c = e / kPairTile;
     const int m = tr * kPairTile + r, n = tc * kPairTile + c;
@@ -479,21 +479,13 @@ __device__ __forceinline__ void assemble_tile(const PairVal* pt, int nQ, const T
         av_im = -av_im;
       }
       const double sv_re = sub(pu.ph.x, pd.ph.x), sv_im = sub(pu.ph.y, pd.ph.y);
-      double c_re = mul(av_re, ka2), c_im = mul(av_im, ka2);
-      if (h == 0) {
-        c_re = sub(c_re, sv_re);
-        c_im = sub(c_im, sv_im);
-      } else {
-        c_re = add(c_re, sv_re);
-        c_im = add(c_im, sv_im);
-      }
-      acc_re = add(acc_re, c_re);
-      acc_im = add(acc_im, c_im);
+      const double c_re = h == 0 ? sub(av_re, sv_re) : add(av_re, sv_re);
+      const double c_im = h == 0 ? sub(av_im, sv_im) : add(av_im, sv_im);
+      acc_re = h == 0 ? c_re : add(acc_re, c_re);
+      acc_im = h == 0 ? c_im : add(acc_im, c_im);
     }
-    double2 out;
-    out.x = -mul(cq, acc_im);
-    out.y = mul(cq, acc_re);
-    Zk[(size_t)n * ldz + m] = out;
+    // times j (cq is in the pair values)
+    Zk[(size_t)n * ldz + m] = make_double2(-acc_im, acc_re);
   }
 }
 
@@ -520,7 +512,7 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
   for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[L.rt_ids[o0 + i]];
   for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[L.ct_ids[q0 + i]];
   __syncthreads();
-  const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+  const FreqParams f = fp[k];
 
   // phase A: distinct pairs of the tile
   for (int p = tid; p < nO * nQ; p += blockDim.x) {
@@ -532,13 +524,13 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
       const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
       double r[2], ri[2];
       gauss_geometry(ex, S.dc, S.an2, S.s, r, ri);
-      pt[p] = regular_pair_value(r, ri, t, S, ka, tab);
+      pt[p] = regular_pair_value(r, ri, t, S, f, tab);
     } else {
-      pt[p] = self_pair_value(t, S, ka);
+      pt[p] = self_pair_value(t, S, f);
     }
   }
   __syncthreads();
-  assemble_tile(pt, nQ, L, tr, tc, npls, ka2, cq, Z + (size_t)k * zstride, ldz);
+  assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
 }
 
 // Frequency-independent values of a pair, kept in shared memory across frequencies.
@@ -585,15 +577,15 @@ __global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
   }
   __syncthreads();
   for (int k = 0; k < nk; ++k) {
-    const double ka = fp[k].ka, ka2 = fp[k].ka2, cq = fp[k].cq;
+    const FreqParams f = fp[k];
     for (int p = tid; p < nO * nQ; p += blockDim.x) {
       const int o = p / nQ, q = p - o * nQ;
       const SrcInst& S = sq[q];
       const PairGeo& g = geo[p];
-      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, ka) : regular_pair_value(g.r, g.ri, g.t, S, ka, tab);
+      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, f) : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
     }
     __syncthreads();
-    assemble_tile(pt, nQ, L, tr, tc, npls, ka2, cq, Z + (size_t)k * zstride, ldz);
+    assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
     __syncthreads();
   }
 }
@@ -645,6 +637,13 @@ cudaError_t ensure_sin_table() {
 }
 
 }  // namespace
+
+FreqParams freq_params(double ka) {
+  const double pi = std::acos(-1.0);
+  const double eta0 = 120. * pi;
+  const double cq = eta0 / (4.0 * pi * ka);
+  return FreqParams{ka, ka * ka, cq, (ka * ka) * cq, 0.5 * cq};
+}
 
 bool fill_multi_fits(const Plan& p) {
   if (!p.pt.ok) return false;

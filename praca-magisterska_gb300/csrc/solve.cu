@@ -1120,22 +1120,16 @@ wmom_status group_results(GroupScratch& g, int bg, int ngap, const wmom_report* 
 wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cudaStream_t s) {
   const int n = p.npls;
   const size_t nn = (size_t)n * n;
-  const double pi = std::acos(-1.0);
-  std::vector<double> fph(3 * (size_t)nk);
-  for (int i = 0; i < nk; ++i) {
-    const double ka = ka_from_mhz(freq[i]);
-    const double eta0 = 120. * pi;
-    fph[3 * i] = ka;
-    fph[3 * i + 1] = ka * ka;
-    fph[3 * i + 2] = eta0 / (4.0 * pi * ka);
-  }
+  std::vector<FreqParams> fph(nk);
+  for (int i = 0; i < nk; ++i) fph[i] = freq_params(ka_from_mhz(freq[i]));
   DevBuf fpb;
-  SWEEP_TRY(fpb.alloc(sizeof(double) * 3 * nk, s));
-  SWEEP_TRY(cudaMemcpyAsync(fpb.p, fph.data(), sizeof(double) * 3 * nk, cudaMemcpyHostToDevice, s));
+  SWEEP_TRY(fpb.alloc(sizeof(FreqParams) * nk, s));
+  SWEEP_TRY(cudaMemcpyAsync(fpb.p, fph.data(), sizeof(FreqParams) * nk, cudaMemcpyHostToDevice, s));
   SWEEP_TRY(launch_fill(p, fpb.as<double>(), nk, Z, n, (long long)nn, s));
   if (!p.load_idx.empty()) {
     // R + j*2*pi*f[MHz]*L[uH] on the loaded diagonal entries (REF/Wire_MoM.cu:346-363)
     const int nl = (int)p.load_idx.size();
+    const double pi = std::acos(-1.0);
     std::vector<double2> lv((size_t)nk * nl);
     for (int i = 0; i < nk; ++i)
       for (int l = 0; l < nl; ++l)

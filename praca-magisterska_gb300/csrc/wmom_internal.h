@@ -124,6 +124,15 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
 
 double ka_from_mhz(float f);
 
+// Per-frequency constants of the fill kernels (host-built, read on the device): k,
+// k^2, cq = eta0 / (4 pi k), and the two products the pair values carry so that
+// assembling an entry needs additions only: kc = k^2 cq (vector-potential terms) and
+// hc = cq / 2 (scalar-potential terms).
+struct FreqParams {
+  double ka, ka2, cq, kc, hc;
+};
+FreqParams freq_params(double ka);
+
 }  // namespace wmom
 
 #if defined(__CUDACC__) || defined(WMOM_WITH_CUDA_RUNTIME)
