@@ -1252,7 +1252,38 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   return WMOM_OK;
 }
 
+namespace {
+
+// The sweep's buffers (Z of a frequency batch and its factors: about 19 GB at
+// N = 8192 and 12 frequencies) come from the stream-ordered allocator.  With the
+// default pool's release threshold of 0 that memory is handed back at every
+// synchronisation and mapped again by the next sweep; the pool of this process keeps
+// up to an eighth of the device's memory instead (WMOM_POOL_RETAIN_GB overrides, 0
+// keeps the default).
+void retain_pool_memory() {
+  static std::mutex mu;
+  static std::vector<char> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+  if (done[dev]) return;
+  done[dev] = 1;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return;
+  uint64_t thr = tot / 8;
+  const char* e = std::getenv("WMOM_POOL_RETAIN_GB");
+  if (e) thr = (uint64_t)std::max(0.0, std::atof(e)) << 30;
+  cudaMemPool_t pool = nullptr;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  cudaGetLastError();
+}
+
+}  // namespace
+
 wmom_status run_sweep(const SweepArgs& a) {
+  retain_pool_memory();
   const Plan& p = *a.plan;
   const int n = p.npls;
   cudaStream_t s = a.stream;
