@@ -708,6 +708,206 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __
   }
 }
 
+// The same panel with a one-column look-ahead.  After the pivot of column j is
+// known, each thread updates column j + 1 of its rows first; the CTA then finds and
+// publishes its candidate for column j + 1 and arrives at the cluster barrier, and
+// only then updates the rest of its rows (columns j + 2 ..) while the barrier
+// completes.  The published candidate row and diagonal row therefore lag one update
+// behind in their columns j + 2 ..; each CTA that reads them applies that update
+// itself (c - l * p, with the row's own multiplier l and the previous pivot row p,
+// the same cfms the owner applies), so the factors are bit-identical to
+// panel_cluster_kernel's.
+template <typename C, int RPT>
+__global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C* __restrict__ A, long long lda,
+                                                                              int n, int j0, int w, int rpc,
+                                                                              int* __restrict__ ipiv,
+                                                                              GridBarrier* __restrict__ gb,
+                                                                              long long astride) {
+  using R = decltype(C{}.x);
+  using Pub = ClusterPub<C>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Pub* pub = reinterpret_cast<Pub*>(smem_raw);  // [2]
+  C* prw_buf = reinterpret_cast<C*>(pub + 2);   // pivot rows of columns j - 1 and j, 2 x 64
+  C* dgr = prw_buf + 128;                       // diagonal row, 64
+  C* tile = dgr + 64;                           // column-major rpc x w
+  __shared__ R red_v[2][kClusterThreads / 32];
+  __shared__ int red_r[2][kClusterThreads / 32];
+
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
+  gb += blockIdx.y;
+  const unsigned cs = gridDim.x;  // the cluster spans blockIdx.x
+  const unsigned rank = cluster_rank();
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int base = j0 + (int)rank * rpc;
+  const int cnt = max(0, min(rpc, n - base));
+
+#pragma unroll
+  for (int rr = 0; rr < RPT; ++rr) {
+    const int lr = t + rr * kClusterThreads;  // local row
+    if (lr < cnt) {
+      const int gr = base + lr;
+      for (int c0 = 0; c0 < w; c0 += 16) {
+        C v[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+          if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+          if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + lr] = v[u];
+      }
+    }
+  }
+  __syncthreads();
+
+  // this CTA's candidate for column jc among its rows >= j0 + jc (first on ties),
+  // published with the candidate row and, from its owner, row j0 + jc
+  auto publish = [&](int jc) {
+    const int gjc = j0 + jc;
+    const int pc = jc & 1;
+    R best = R(-1);
+    int brow = INT_MAX;
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int lr = t + rr * kClusterThreads;
+      if (lr < cnt && base + lr >= gjc) {
+        const R v = cabs1(tile[(size_t)jc * rpc + lr]);
+        if (v > best) {
+          best = v;
+          brow = base + lr;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      if (ov > best || (ov == best && orow < brow)) {
+        best = ov;
+        brow = orow;
+      }
+    }
+    if (lane == 0) {
+      red_v[pc][warp] = best;
+      red_r[pc][warp] = brow;
+    }
+    __syncthreads();
+    best = R(-1);
+    brow = INT_MAX;
+#pragma unroll
+    for (int q = 0; q < kClusterThreads / 32; ++q) {
+      const R v = red_v[pc][q];
+      const int r = red_r[pc][q];
+      if (v > best || (v == best && r < brow)) {
+        best = v;
+        brow = r;
+      }
+    }
+    Pub& my = pub[pc];
+    if (t == 0) {
+      my.val = best;
+      my.row = brow;
+    }
+    if (t < w) {
+      if (best >= R(0)) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
+      if (gjc >= base && gjc < base + cnt) my.diag[t] = tile[(size_t)t * rpc + (gjc - base)];
+    }
+    // every read of the tile for the publication is done before the rows change
+    __syncthreads();
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  };
+
+  publish(0);
+  C lr_l[RPT];  // the rows' multipliers of the current column
+  for (int j = 0; j < w; ++j) {
+    const int gj = j0 + j;
+    const int par = j & 1;
+    C* prow = prw_buf + 64 * par;               // pivot row of column j
+    const C* pprev = prw_buf + 64 * (par ^ 1);  // pivot row of column j - 1
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    // winner over the cluster, computed by every warp from the CTAs' shared memory
+    R v = R(-1);
+    int r = INT_MAX, q = -1;
+    if (lane < (int)cs) {
+      v = ld_cluster_r(&pub[par].val, map_rank(&pub[par].val, lane));
+      r = ld_cluster_s32(map_rank(&pub[par].row, lane));
+      q = lane;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, r, o);
+      const int oq = __shfl_xor_sync(0xffffffffu, q, o);
+      if (ov > v || (ov == v && orow < r)) {
+        v = ov;
+        r = orow;
+        q = oq;
+      }
+    }
+    const int prw = r;
+    const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
+    if (t < w) {
+      // the published rows lag the update of column j - 1 in their columns > j
+      C pv = ld_cluster_c(prow, map_rank(&pub[par].cand[t], (unsigned)q));
+      if (j > 0 && t > j) pv = cfms(pv, ld_cluster_c(prow, map_rank(&pub[par].cand[j - 1], (unsigned)q)), pprev[t]);
+      prow[t] = pv;
+      if (prw != gj) {
+        C dv = ld_cluster_c(prow, map_rank(&pub[par].diag[t], owner_gj));
+        if (j > 0 && t > j) dv = cfms(dv, ld_cluster_c(prow, map_rank(&pub[par].diag[j - 1], owner_gj)), pprev[t]);
+        dgr[t] = dv;
+      }
+    }
+    __syncthreads();
+    if (rank == 0 && t == 0) ipiv[gj] = prw + 1;
+    const C piv = prow[j];
+    const bool zero = piv.x == R(0) && piv.y == R(0);
+    if (zero && rank == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
+    // this thread's rows: interchange, scale, then column j + 1 only
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int lr = t + rr * kClusterThreads;
+      lr_l[rr] = cmake<C>(0, 0);
+      if (lr >= cnt) continue;
+      const int gr = base + lr;
+      if (prw != gj) {
+        if (gr == prw)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + lr] = dgr[c];
+        else if (gr == gj)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + lr] = prow[c];
+      }
+      if (gr > gj) {
+        C l = tile[(size_t)j * rpc + lr];
+        if (!zero) {
+          l = cmul(l, crecip(piv));
+          tile[(size_t)j * rpc + lr] = l;
+        }
+        lr_l[rr] = l;
+        if (j + 1 < w) tile[(size_t)(j + 1) * rpc + lr] = cfms(tile[(size_t)(j + 1) * rpc + lr], l, prow[j + 1]);
+      }
+    }
+    if (j + 1 < w) {
+      __syncthreads();  // column j + 1 of every row is current
+      publish(j + 1);
+      // the rest of this thread's rows while the cluster meets
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr) {
+        const int lr = t + rr * kClusterThreads;
+        if (lr >= cnt || base + lr <= gj) continue;
+        const C l = lr_l[rr];
+        for (int c = j + 2; c < w; ++c) tile[(size_t)c * rpc + lr] = cfms(tile[(size_t)c * rpc + lr], l, prow[c]);
+      }
+    }
+  }
+  // no CTA leaves while another may still read its shared memory
+  cluster_sync_all();
+#pragma unroll
+  for (int rr = 0; rr < RPT; ++rr) {
+    const int lr = t + rr * kClusterThreads;
+    if (lr < cnt)
+      for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + base + lr] = tile[(size_t)c * rpc + lr];
+  }
+}
+
 // ------------------------------------------------------------- laswp ----
 // Interchanges of pivots [k0, k0+kn) applied to the columns [0, j_skip0) and
 // [j_skip1, ncols) of A: one thread per column, interchanges in order.
@@ -1208,6 +1408,13 @@ size_t panel_smem(int rpc, int P) {
 // least kMinRows rows per block: FP64 rank-1 updates are costly, so many blocks share
 // them; FP32 panels are latency-bound, so fewer blocks make each barrier cheaper.
 // WMOM_NO_CLUSTER_PANEL=1 keeps the FP32 panels on the cooperative kernels.
+// WMOM_PANEL_LOOKAHEAD=0 selects the cluster panel without the one-column look-ahead
+// (same factors bit for bit).
+bool panel_lookahead() {
+  const char* e = std::getenv("WMOM_PANEL_LOOKAHEAD");
+  return !(e && e[0] == '0');
+}
+
 bool cluster_panels_disabled() {
   const char* e = std::getenv("WMOM_NO_CLUSTER_PANEL");
   return e && e[0] == '1';
@@ -1239,7 +1446,10 @@ int max_cluster_size(const DeviceLimits& lim) {
            cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
   };
   if (prepare((const void*)panel_cluster_kernel<float2, 1>) && prepare((const void*)panel_cluster_kernel<float2, 2>) &&
-      prepare((const void*)panel_cluster_kernel<double2, 1>)) {
+      prepare((const void*)panel_cluster_kernel<double2, 1>) &&
+      prepare((const void*)panel_cluster_la_kernel<float2, 1>) &&
+      prepare((const void*)panel_cluster_la_kernel<float2, 2>) &&
+      prepare((const void*)panel_cluster_la_kernel<double2, 1>)) {
     for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs, 1, 1);
@@ -1288,7 +1498,9 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
     // panels save (measured 0.64 vs 0.76 freq-solves/s at N = 8192, 24.0 vs 27.3 at
     // N = 2048).
     const int csmax = max_cluster_size(lim);
-    const size_t head = 2 * sizeof(ClusterPub<C>) + 2 * 64 * sizeof(C);
+    // publication slots, two pivot rows and the diagonal row (the look-ahead kernel's
+    // layout; the other kernel uses one pivot row less)
+    const size_t head = 2 * sizeof(ClusterPub<C>) + 3 * 64 * sizeof(C);
     const int wcap = sizeof(R) == 4 ? 64 : 32;
     auto try_shape = [&](int rpt, int cs_lo, int cs_hi, int wmin) -> bool {
       for (int cs = cs_lo; cs <= std::min(cs_hi, csmax); cs *= 2) {
@@ -1370,8 +1582,11 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     {
       if (pl.cluster) {
         if (w > pl.w) return cudaErrorInvalidValue;
-        const void* ck =
-            pl.rpt == 2 ? (const void*)panel_cluster_kernel<C, 2> : (const void*)panel_cluster_kernel<C, 1>;
+        const bool la = panel_lookahead();
+        const void* ck = la ? (pl.rpt == 2 ? (const void*)panel_cluster_la_kernel<C, 2>
+                                           : (const void*)panel_cluster_la_kernel<C, 1>)
+                            : (pl.rpt == 2 ? (const void*)panel_cluster_kernel<C, 2>
+                                           : (const void*)panel_cluster_kernel<C, 1>);
         cudaError_t ce = allow_dynamic_smem(ck, pl.smem);
         if (ce != cudaSuccess) return ce;
         cudaLaunchConfig_t cfg = {};
@@ -1387,6 +1602,11 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
+        if (la)
+          return pl.rpt == 2 ? cudaLaunchKernelEx(&cfg, panel_cluster_la_kernel<C, 2>, A, lda, n, jp, w, pl.rpc, ipiv,
+                                                  gb, astride)
+                             : cudaLaunchKernelEx(&cfg, panel_cluster_la_kernel<C, 1>, A, lda, n, jp, w, pl.rpc, ipiv,
+                                                  gb, astride);
         return pl.rpt == 2 ? cudaLaunchKernelEx(&cfg, panel_cluster_kernel<C, 2>, A, lda, n, jp, w, pl.rpc, ipiv, gb,
                                                 astride)
                            : cudaLaunchKernelEx(&cfg, panel_cluster_kernel<C, 1>, A, lda, n, jp, w, pl.rpc, ipiv, gb,

@@ -139,3 +139,27 @@ def test_fp32_lu_large_panels(cuda, wmom, n):
     err = np.linalg.norm(pax - lux) / (np.linalg.norm(a.astype(np.complex128)) * np.linalg.norm(x) / np.sqrt(n))
     assert err <= 3e-4, err
     assert np.max(np.abs(np.tril(lu, -1))) <= np.sqrt(2.0) * (1 + 1e-5)
+
+
+@pytest.mark.parametrize("n", [300, 4100, 9000])
+def test_panel_lookahead_is_bit_identical(cuda, wmom, n):
+    """The cluster panel with the one-column look-ahead publishes rows one update
+    behind and each reader applies that update itself with the owner's arithmetic:
+    its factors and pivots must equal the plain cluster panel's bit for bit (one
+    cluster, 16-CTA clusters with 48-column panels, two rows per thread)."""
+    import os
+    rng = np.random.default_rng(77 + n)
+    a = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))).astype(np.complex64)
+    out = {}
+    for la in ("1", "0"):
+        os.environ["WMOM_PANEL_LOOKAHEAD"] = la
+        try:
+            at = cuda.from_numpy(np.ascontiguousarray(a.T)).to("cuda")
+            ipiv = cuda.zeros(n, dtype=cuda.int32, device="cuda")
+            assert wmom.cgetrf_device(at.data_ptr(), n, n, ipiv.data_ptr()) == 0
+            cuda.cuda.synchronize()
+            out[la] = (at.cpu().numpy(), ipiv.cpu().numpy())
+        finally:
+            del os.environ["WMOM_PANEL_LOOKAHEAD"]
+    assert np.array_equal(out["1"][1], out["0"][1])
+    assert np.array_equal(out["1"][0], out["0"][0])

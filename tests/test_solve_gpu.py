@@ -191,3 +191,21 @@ def test_krylov_step_forced_on(cuda, wmom):
         assert rm[k]["status"] == 0 and rm[k]["tier"] in (1, 2, 3), rm[k]
         assert _rel(cm[k], c64[k]) < 1e-6, (k, _rel(cm[k], c64[k]), rm[k])
     plan.close()
+
+
+def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
+    # the second tier's FP64 LU (cluster panels) with and without the panel's
+    # one-column look-ahead: the same currents bit for bit
+    topo = wmom.Topology(wmom.geometry.precision_grid(2048))
+    freqs = np.array([0.01], np.float32)
+    out = {}
+    for la in ("1", "0"):
+        os.environ["WMOM_PANEL_LOOKAHEAD"] = la
+        try:
+            plan = wmom.Plan(topo)
+            out[la] = plan.solve(freqs, 1000, mode=1)
+            plan.close()
+        finally:
+            del os.environ["WMOM_PANEL_LOOKAHEAD"]
+    assert out["1"][2][0]["tier"] == 2
+    assert np.array_equal(out["1"][0], out["0"][0])
