@@ -564,6 +564,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __
   C* tile = dgr + 64;                           // column-major rpc x w
   __shared__ R red_v[2][kClusterThreads / 32];
   __shared__ int red_r[2][kClusterThreads / 32];
+  __shared__ C s_inv;  // 1 / pivot of the current column, computed once per CTA
 
   A += (size_t)blockIdx.y * astride;
   ipiv += (size_t)blockIdx.y * n;
@@ -668,7 +669,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __
     const int prw = r;
     const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
     if (t < w) {
-      prow[t] = ld_cluster_c(prow, map_rank(&pub[par].cand[t], (unsigned)q));
+      const C pv = ld_cluster_c(prow, map_rank(&pub[par].cand[t], (unsigned)q));
+      prow[t] = pv;
+      if (t == j) s_inv = (pv.x == R(0) && pv.y == R(0)) ? pv : crecip(pv);
       if (prw != gj) dgr[t] = ld_cluster_c(prow, map_rank(&pub[par].diag[t], owner_gj));
     }
     __syncthreads();
@@ -691,7 +694,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __
       if (gr > gj) {
         C l = tile[(size_t)j * rpc + lr];
         if (!zero) {
-          l = cmul(l, crecip(piv));
+          l = cmul(l, s_inv);
           tile[(size_t)j * rpc + lr] = l;
         }
         for (int c = j + 1; c < w; ++c) tile[(size_t)c * rpc + lr] = cfms(tile[(size_t)c * rpc + lr], l, prow[c]);
@@ -706,6 +709,21 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_kernel(C* __
     if (lr < cnt)
       for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + base + lr] = tile[(size_t)c * rpc + lr];
   }
+}
+
+// Order keys of non-negative floating-point values (and of -1, below them all):
+// the IEEE bits as a signed integer order like the values.
+__device__ __forceinline__ long long order_key(float v) { return (long long)__float_as_int(v); }
+__device__ __forceinline__ long long order_key(double v) { return __double_as_longlong(v); }
+template <typename R>
+__device__ __forceinline__ R key_value(long long k);
+template <>
+__device__ __forceinline__ float key_value<float>(long long k) {
+  return __int_as_float((int)k);
+}
+template <>
+__device__ __forceinline__ double key_value<double>(long long k) {
+  return __longlong_as_double(k);
 }
 
 // The same panel with a one-column look-ahead.  After the pivot of column j is
@@ -730,8 +748,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
   C* prw_buf = reinterpret_cast<C*>(pub + 2);   // pivot rows of columns j - 1 and j, 2 x 64
   C* dgr = prw_buf + 128;                       // diagonal row, 64
   C* tile = dgr + 64;                           // column-major rpc x w
-  __shared__ R red_v[2][kClusterThreads / 32];
+  // candidates are compared through order keys: for the values compared here
+  // (|re| + |im| >= 0, and -1 for no candidate) the IEEE bits as a signed integer
+  // order like the values, so the pivot search runs on the integer pipe instead of
+  // GB300's narrow FP64 pipe; the pivot chosen is the same
+  __shared__ long long red_k[2][kClusterThreads / 32];
   __shared__ int red_r[2][kClusterThreads / 32];
+  __shared__ C s_inv;  // 1 / pivot of the current column, computed once per CTA
+  __shared__ int s_prw;  // pivot row of the current column
 
   A += (size_t)blockIdx.y * astride;
   ipiv += (size_t)blockIdx.y * n;
@@ -765,13 +789,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
   auto publish = [&](int jc) {
     const int gjc = j0 + jc;
     const int pc = jc & 1;
-    R best = R(-1);
+    long long best = order_key(R(-1));
     int brow = INT_MAX;
 #pragma unroll
     for (int rr = 0; rr < RPT; ++rr) {
       const int lr = t + rr * kClusterThreads;
       if (lr < cnt && base + lr >= gjc) {
-        const R v = cabs1(tile[(size_t)jc * rpc + lr]);
+        const long long v = order_key(cabs1(tile[(size_t)jc * rpc + lr]));
         if (v > best) {
           best = v;
           brow = base + lr;
@@ -780,7 +804,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const long long ov = __shfl_xor_sync(0xffffffffu, best, o);
       const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
       if (ov > best || (ov == best && orow < brow)) {
         best = ov;
@@ -788,28 +812,28 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
       }
     }
     if (lane == 0) {
-      red_v[pc][warp] = best;
+      red_k[pc][warp] = best;
       red_r[pc][warp] = brow;
     }
     __syncthreads();
-    best = R(-1);
-    brow = INT_MAX;
+    if (t < w) {  // only these threads publish
+      best = order_key(R(-1));
+      brow = INT_MAX;
 #pragma unroll
-    for (int q = 0; q < kClusterThreads / 32; ++q) {
-      const R v = red_v[pc][q];
-      const int r = red_r[pc][q];
-      if (v > best || (v == best && r < brow)) {
-        best = v;
-        brow = r;
+      for (int q = 0; q < kClusterThreads / 32; ++q) {
+        const long long v = red_k[pc][q];
+        const int r = red_r[pc][q];
+        if (v > best || (v == best && r < brow)) {
+          best = v;
+          brow = r;
+        }
       }
-    }
-    Pub& my = pub[pc];
-    if (t == 0) {
-      my.val = best;
-      my.row = brow;
-    }
-    if (t < w) {
-      if (best >= R(0)) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
+      Pub& my = pub[pc];
+      if (t == 0) {
+        my.val = key_value<R>(best);
+        my.row = brow;
+      }
+      if (best >= 0) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
       if (gjc >= base && gjc < base + cnt) my.diag[t] = tile[(size_t)t * rpc + (gjc - base)];
     }
     // every read of the tile for the publication is done before the rows change
@@ -825,32 +849,38 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
     C* prow = prw_buf + 64 * par;               // pivot row of column j
     const C* pprev = prw_buf + 64 * (par ^ 1);  // pivot row of column j - 1
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-    // winner over the cluster, computed by every warp from the CTAs' shared memory
-    R v = R(-1);
-    int r = INT_MAX, q = -1;
-    if (lane < (int)cs) {
-      v = ld_cluster_r(&pub[par].val, map_rank(&pub[par].val, lane));
-      r = ld_cluster_s32(map_rank(&pub[par].row, lane));
-      q = lane;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const R ov = __shfl_xor_sync(0xffffffffu, v, o);
-      const int orow = __shfl_xor_sync(0xffffffffu, r, o);
-      const int oq = __shfl_xor_sync(0xffffffffu, q, o);
-      if (ov > v || (ov == v && orow < r)) {
-        v = ov;
-        r = orow;
-        q = oq;
-      }
-    }
-    const int prw = r;
+    // winner over the cluster, from the CTAs' shared memory, by the warps that
+    // fetch the pivot and diagonal rows (the others learn the pivot row below)
     const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
+    int r = INT_MAX, q = -1;
+    if (warp * 32 < w) {
+      long long v = order_key(R(-1));
+      if (lane < (int)cs) {
+        v = order_key(ld_cluster_r(&pub[par].val, map_rank(&pub[par].val, lane)));
+        r = ld_cluster_s32(map_rank(&pub[par].row, lane));
+        q = lane;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, r, o);
+        const int oq = __shfl_xor_sync(0xffffffffu, q, o);
+        if (ov > v || (ov == v && orow < r)) {
+          v = ov;
+          r = orow;
+          q = oq;
+        }
+      }
+      if (t == 0) s_prw = r;
+    }
     if (t < w) {
+      const int prw = r;
       // the published rows lag the update of column j - 1 in their columns > j
       C pv = ld_cluster_c(prow, map_rank(&pub[par].cand[t], (unsigned)q));
       if (j > 0 && t > j) pv = cfms(pv, ld_cluster_c(prow, map_rank(&pub[par].cand[j - 1], (unsigned)q)), pprev[t]);
       prow[t] = pv;
+      // the pivot's reciprocal once for the CTA (Smith's formula divides: costly in FP64)
+      if (t == j) s_inv = (pv.x == R(0) && pv.y == R(0)) ? pv : crecip(pv);
       if (prw != gj) {
         C dv = ld_cluster_c(prow, map_rank(&pub[par].diag[t], owner_gj));
         if (j > 0 && t > j) dv = cfms(dv, ld_cluster_c(prow, map_rank(&pub[par].diag[j - 1], owner_gj)), pprev[t]);
@@ -858,6 +888,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
       }
     }
     __syncthreads();
+    const int prw = s_prw;
     if (rank == 0 && t == 0) ipiv[gj] = prw + 1;
     const C piv = prow[j];
     const bool zero = piv.x == R(0) && piv.y == R(0);
@@ -878,7 +909,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_kernel(C*
       if (gr > gj) {
         C l = tile[(size_t)j * rpc + lr];
         if (!zero) {
-          l = cmul(l, crecip(piv));
+          l = cmul(l, s_inv);
           tile[(size_t)j * rpc + lr] = l;
         }
         lr_l[rr] = l;
@@ -1522,8 +1553,13 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
     if (sizeof(R) == 4) {
       if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
     } else {
+      static const int target = [] {
+        const char* e = std::getenv("WMOM_FP64_PANEL_ROWS");
+        const int v = e ? std::atoi(e) : 0;
+        return v >= 16 && v <= 512 ? v : 256;
+      }();
       int cs0 = 1;
-      while (cs0 < kClusterMax && (m + cs0 - 1) / cs0 > 256) cs0 *= 2;
+      while (cs0 < kClusterMax && (m + cs0 - 1) / cs0 > target) cs0 *= 2;
       if (try_shape(1, cs0, kClusterMax, 16)) return pl;
     }
   }

@@ -757,12 +757,19 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   }
   bool fallback[kMaxLuBatch] = {}, active[kMaxLuBatch] = {};
   int stall[kMaxLuBatch] = {};
-  double prev[kMaxLuBatch], rel_first[kMaxLuBatch], rel_best[kMaxLuBatch];
+  double prev[kMaxLuBatch], last[kMaxLuBatch], rel_first[kMaxLuBatch], rel_best[kMaxLuBatch];
   for (int b = 0; b < bg; ++b) {
     fallback[b] = info[b] != 0;
     active[b] = !fallback[b];
-    prev[b] = rel_first[b] = rel_best[b] = HUGE_VAL;
+    prev[b] = last[b] = rel_first[b] = rel_best[b] = HUGE_VAL;
   }
+  // With the tensor-core second tier, a matrix whose refinement contracts slowly
+  // leaves tier 1 once the steps it still needs (extrapolated from its last step)
+  // would cost more than a second-tier factorisation: a step costs O(N^2) (residual
+  // and two triangular solves), the factorisation O(N^3), so the limit grows with N
+  // (8 steps at N = 2048, 32 at N = 8192).
+  const bool tier2 = emul_gemm_hook() != nullptr;
+  const double step_budget = std::max(8.0, n / 256.0);
   const unsigned vgrid = (unsigned)(((size_t)n * bg + 255) / 256);
   // initial solve in FP32
   stats::count(stats::kMisc, 2);
@@ -799,9 +806,14 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       } else if (it >= max_it) {
         fallback[b] = true;
         active[b] = false;
+      } else if (tier2 && it >= 3 && rel < last[b] &&
+                 std::log(tol / rel) / std::log(rel / last[b]) > step_budget) {
+        fallback[b] = true;
+        active[b] = false;
       } else {
         if (rel <= 0.5 * prev[b]) stall[b] = 0;
         prev[b] = std::min(prev[b], rel);
+        last[b] = rel;
         ++nact;
       }
     }
