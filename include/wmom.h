@@ -94,6 +94,10 @@ long long wmom_plan_upload_bytes(wmom_plan plan);
  * the environment forces the per-entry kernel, WMOM_FILL_SINGLE=1 one CTA per tile
  * and frequency. */
 int wmom_plan_fill_variant(wmom_plan plan);
+/* Distinct (observation point, source half-segment) pairs the pair-tiled fill
+ * evaluates per frequency (each with a 2-point rule), 0 for the per-entry kernel.
+ * Divided by npls^2 it is the pairs per entry; the reference evaluates 4. */
+long long wmom_plan_fill_pairs(wmom_plan plan);
 
 /* Fills nk impedance matrices, one per wave number ka[i] (host array), in FP64.
  * Matrix i starts at z_dev + i*zstride complex elements; ldz >= npls.  The

@@ -84,6 +84,7 @@ _plan_destroy = _sig("wmom_plan_destroy", ctypes.c_int, [_vp])
 _plan_npls = _sig("wmom_plan_npls", ctypes.c_int, [_vp])
 _plan_upload_bytes = _sig("wmom_plan_upload_bytes", ctypes.c_longlong, [_vp])
 _plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
+_plan_fill_pairs = _sig("wmom_plan_fill_pairs", ctypes.c_longlong, [_vp])
 _plan_set_loads = _sig("wmom_plan_set_loads", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
 _zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
@@ -258,6 +259,8 @@ class Plan:
         fv = _plan_fill_variant(h)
         self.fill_variant = "pair" if fv >= 1 else "entry"
         self.multi_frequency_fill = fv == 2
+        # pairs the pair-tiled fill evaluates per frequency (0 for the per-entry fill)
+        self.fill_pairs = int(_plan_fill_pairs(h))
 
     def close(self):
         if self._h:

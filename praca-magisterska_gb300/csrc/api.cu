@@ -318,6 +318,14 @@ long long wmom_plan_upload_bytes(wmom_plan h) {
   return (long long)(sizeof(ObsHalf) * h->p.h_obs.size() + sizeof(SrcHalf) * h->p.h_src.size() + h->tile_bytes);
 }
 
+long long wmom_plan_fill_pairs(wmom_plan h) {
+  if (!h) return -1;
+  if (!h->p.pt.ok) return 0;
+  // distinct (observation, source) instance pairs the pair-tiled fill evaluates per
+  // frequency: every row tile meets every column tile
+  return (long long)h->p.pt.rt_ids.size() * (long long)h->p.pt.ct_ids.size();
+}
+
 wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long long ldz,
                       long long zstride, void* stream) {
   if (!h || !ka || nk <= 0 || !z_dev || ldz < h->p.npls || (nk > 1 && zstride < ldz * h->p.npls))

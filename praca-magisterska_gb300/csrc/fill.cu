@@ -445,15 +445,36 @@ __device__ __forceinline__ PairVal regular_pair_value(const double r[2], const d
   return v;
 }
 
-// Phase A value of a self pair (identical segments), scaled as above.
-__device__ __forceinline__ PairVal self_pair_value(double t, const SrcInst& S, const FreqParams& f) {
+// The self integrals of a source instance at one frequency (ramped up, ramped down,
+// plain): they depend on the segment's length and radius and on k only.
+struct SelfVal {
+  double2 au, ad, p;
+};
+
+// Self integrals of every source instance for every frequency of a launch, ahead of
+// the tile kernels: a self pair costs about thirty regular ones (two 4-point rules,
+// sincos, log, divisions), and where they fall into many tiles (junction grids) the
+// CTA holding one would otherwise wait on that thread.
+__global__ void self_values_kernel(const SrcInst* __restrict__ sinst, int nsrc, const FreqParams* __restrict__ fp,
+                                   SelfVal* __restrict__ out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (q >= nsrc) return;
+  const SrcInst& S = sinst[q];
   Cx Au, Ad, P;
-  self_pair(S.dl, S.an, f.ka, &Au, &Ad, &P);
+  self_pair(S.dl, S.an, fp[k].ka, &Au, &Ad, &P);
+  out[(size_t)k * nsrc + q] = SelfVal{make_double2(Au.re, Au.im), make_double2(Ad.re, Ad.im), make_double2(P.re, P.im)};
+}
+
+// Phase A value of a self pair (identical segments) from its self integrals, scaled
+// as above.
+__device__ __forceinline__ PairVal self_pair_value(double t, const SrcInst& S, const FreqParams& f,
+                                                   const SelfVal& sv) {
   const double tk = mul(t, f.kc);
   PairVal v;
-  v.wu = make_double2(mul(Au.re, tk), mul(Au.im, tk));
-  v.wd = make_double2(mul(Ad.re, tk), mul(Ad.im, tk));
-  v.ph = make_double2(mul(__ddiv_rn(P.re, S.dl), f.cq), mul(__ddiv_rn(P.im, S.dl), f.cq));
+  v.wu = make_double2(mul(sv.au.x, tk), mul(sv.au.y, tk));
+  v.wd = make_double2(mul(sv.ad.x, tk), mul(sv.ad.y, tk));
+  v.ph = make_double2(mul(__ddiv_rn(sv.p.x, S.dl), f.cq), mul(__ddiv_rn(sv.p.y, S.dl), f.cq));
   return v;
 }
 
@@ -496,6 +517,7 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
                                                         int off_ct_off, int off_ct_ids, int off_row_local,
                                                         int off_col_local, int npls, int max_o, int max_q,
                                                         const FreqParams* __restrict__ fp,
+                                                        const SelfVal* __restrict__ selfv, int nsrc,
                                                         double2* __restrict__ Z, long long ldz,
                                                         long long zstride) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -526,7 +548,7 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
       gauss_geometry(ex, S.dc, S.an2, S.s, r, ri);
       pt[p] = regular_pair_value(r, ri, t, S, f, tab);
     } else {
-      pt[p] = self_pair_value(t, S, f);
+      pt[p] = self_pair_value(t, S, f, selfv[(size_t)k * nsrc + L.ct_ids[q0 + q]]);
     }
   }
   __syncthreads();
@@ -546,8 +568,8 @@ constexpr int kMultiThreads = 512;
 __global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
     const ObsInst* __restrict__ oinst, const SrcInst* __restrict__ sinst, const int* __restrict__ tiles,
     int off_rt_ids, int off_ct_off, int off_ct_ids, int off_row_local, int off_col_local, int npls, int max_o,
-    int max_q, const FreqParams* __restrict__ fp, int nk, double2* __restrict__ Z, long long ldz,
-    long long zstride) {
+    int max_q, const FreqParams* __restrict__ fp, const SelfVal* __restrict__ selfv, int nsrc, int nk,
+    double2* __restrict__ Z, long long ldz, long long zstride) {
   extern __shared__ __align__(16) unsigned char sm[];
   const double2* tab = g_sin_tab;
   ObsInst* so = reinterpret_cast<ObsInst*>(sm);
@@ -582,7 +604,8 @@ __global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
       const int o = p / nQ, q = p - o * nQ;
       const SrcInst& S = sq[q];
       const PairGeo& g = geo[p];
-      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, f) : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
+      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, f, selfv[(size_t)k * nsrc + L.ct_ids[q0 + q]])
+                                     : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
     }
     __syncthreads();
     assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
@@ -663,29 +686,38 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
   if (te != cudaSuccess) return te;
   const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
   if (p.pt.ok && p.d_tiles && !(force_entry && force_entry[0] == '1')) {
+    const FreqParams* fpd = reinterpret_cast<const FreqParams*>(d_fp);
+    const int nsrc = (int)p.pt.src.size();
+    SelfVal* selfv = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&selfv), sizeof(SelfVal) * (size_t)nsrc * nk, stream);
+    if (e != cudaSuccess) return e;
+    stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk, 2);
+    self_values_kernel<<<dim3((nsrc + 127) / 128, nk), 128, 0, stream>>>(p.d_si, nsrc, fpd, selfv);
     // several frequencies: one CTA of 16 warps per tile for all of them, when its
     // shared memory fits (the geometry of the pairs is then computed once per tile)
     const size_t msmem = pair_multi_smem_bytes(p.pt);
     if (nk > 1 && fill_multi_fits(p)) {
-      cudaError_t e = allow_dynamic_smem((const void*)fill_pair_multi_kernel, msmem);
-      if (e != cudaSuccess) return e;
-      dim3 grid(p.pt.n_tiles, p.pt.n_tiles, 1);
-      stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
-      fill_pair_multi_kernel<<<grid, kMultiThreads, msmem, stream>>>(
-          p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off, p.off_ct_ids, p.off_row_local, p.off_col_local,
-          p.npls, p.pt.max_o, p.pt.max_q, reinterpret_cast<const FreqParams*>(d_fp), nk, z, ldz, zstride);
-      return cudaGetLastError();
+      e = allow_dynamic_smem((const void*)fill_pair_multi_kernel, msmem);
+      if (e == cudaSuccess) {
+        dim3 grid(p.pt.n_tiles, p.pt.n_tiles, 1);
+        fill_pair_multi_kernel<<<grid, kMultiThreads, msmem, stream>>>(
+            p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off, p.off_ct_ids, p.off_row_local, p.off_col_local,
+            p.npls, p.pt.max_o, p.pt.max_q, fpd, selfv, nsrc, nk, z, ldz, zstride);
+        e = cudaGetLastError();
+      }
+    } else {
+      const size_t smem = pair_smem_bytes(p.pt);
+      e = allow_dynamic_smem((const void*)fill_pair_kernel, smem);
+      if (e == cudaSuccess) {
+        dim3 grid(p.pt.n_tiles, p.pt.n_tiles, nk);
+        fill_pair_kernel<<<grid, 256, smem, stream>>>(p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off,
+                                                      p.off_ct_ids, p.off_row_local, p.off_col_local, p.npls,
+                                                      p.pt.max_o, p.pt.max_q, fpd, selfv, nsrc, z, ldz, zstride);
+        e = cudaGetLastError();
+      }
     }
-    const size_t smem = pair_smem_bytes(p.pt);
-    cudaError_t e = allow_dynamic_smem((const void*)fill_pair_kernel, smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid(p.pt.n_tiles, p.pt.n_tiles, nk);
-    stats::Scope sc(stats::kFill, stream, 384.0 * p.npls * (double)p.npls * nk);
-    fill_pair_kernel<<<grid, 256, smem, stream>>>(p.d_oi, p.d_si, p.d_tiles, p.off_rt_ids, p.off_ct_off,
-                                                  p.off_ct_ids, p.off_row_local, p.off_col_local, p.npls,
-                                                  p.pt.max_o, p.pt.max_q, reinterpret_cast<const FreqParams*>(d_fp),
-                                                  z, ldz, zstride);
-    return cudaGetLastError();
+    const cudaError_t fe = cudaFreeAsync(selfv, stream);
+    return e != cudaSuccess ? e : fe;
   }
   dim3 block(128);
   dim3 grid((p.npls + 127) / 128, p.npls, nk);
