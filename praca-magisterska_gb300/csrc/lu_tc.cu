@@ -13,10 +13,12 @@
 // which keeps the product close to FP32 accuracy; the FP64 refinement of the
 // solver then removes the remaining FP32-level error.
 //
-// Kernel: persistent, one CTA (6 warps) per SM, each walking 128 x 128 real output
-// tiles (128 rows, 64 complex columns).  A producer thread streams K in chunks of 32
-// FP32 (one 128-byte swizzle row) with TMA into a 3-stage ring (head and tail
-// planes of A' and B'); an MMA thread issues 3 x 4 tcgen05.mma (M=128, N=128, K=8)
+// Kernel: persistent, one CTA (6 warps) per SM, each walking 128 x 256 real output
+// tiles (128 rows, 128 complex columns; measured against 128 x 128 tiles: 176 vs 167
+// TFLOP/s at K = 96, 235 vs 209 at K = 192, as each stage's four operand planes then
+// feed twice the MMA work).  A producer thread streams K in chunks of 32
+// FP32 (one 128-byte swizzle row) with TMA into a 2-stage ring (head and tail
+// planes of A' and B'); an MMA thread issues 3 x 4 tcgen05.mma (M=128, N=256, K=8)
 // per chunk into one of two TMEM accumulators; four epilogue warps read their
 // 32-lane quarter of a finished accumulator with tcgen05.ld and subtract it from C
 // with coalesced float2 accesses while the next tile is being multiplied.  All
@@ -41,11 +43,11 @@ namespace wmom {
 namespace tc {
 
 constexpr int BM = 128;  // accumulator lanes = rows of C per CTA
-constexpr int BN = 128;  // accumulator FP32 columns = 64 complex columns of C
+constexpr int BN = 256;  // accumulator FP32 columns = 128 complex columns of C
 constexpr int KC = 32;   // FP32 elements of K per chunk (128 bytes)
-constexpr int STAGES = 3;
+constexpr int STAGES = 2;
 constexpr int A_BYTES = BM * KC * 4;  // 16 KB per plane
-constexpr int B_BYTES = BN * KC * 4;  // 16 KB per plane
+constexpr int B_BYTES = BN * KC * 4;  // 32 KB per plane
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
 constexpr int NTHREADS = 192;         // producer warp, MMA warp, 4 epilogue warps
@@ -362,13 +364,13 @@ EncodeFn encode_fn() {
 
 namespace {
 
-// 3-D map over `batch` planes of rows x k2p FP32 (row-major), 32 x 128 boxes.
-bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch) {
+// 3-D map over `batch` planes of rows x k2p FP32 (row-major), 32 x box_rows boxes.
+bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch, int box_rows) {
   EncodeFn enc = encode_fn();
   if (!enc) return false;
   cuuint64_t dims[3] = {(cuuint64_t)k2p, (cuuint64_t)rows, (cuuint64_t)batch};
   cuuint64_t strides[2] = {(cuuint64_t)k2p * sizeof(float), (cuuint64_t)rows * k2p * sizeof(float)};
-  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)BM, 1};
+  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(ptr), dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -437,8 +439,8 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
                                                                                 bstride);
   pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
   CUtensorMap mah, mal, mbh, mbl;
-  if (!make_map(&mah, ahi, M, K2p, batch) || !make_map(&mal, alo, M, K2p, batch) ||
-      !make_map(&mbh, bhi, 2 * N, K2p, batch) || !make_map(&mbl, blo, 2 * N, K2p, batch))
+  if (!make_map(&mah, ahi, M, K2p, batch, BM) || !make_map(&mal, alo, M, K2p, batch, BM) ||
+      !make_map(&mbh, bhi, 2 * N, K2p, batch, BN) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN))
     return cudaErrorInvalidValue;
   e = allow_dynamic_smem((const void*)cgemm_sub_tc_kernel, SMEM_BYTES);
   if (e != cudaSuccess) return e;
