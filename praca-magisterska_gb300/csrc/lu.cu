@@ -1028,37 +1028,38 @@ __global__ void __launch_bounds__(256) trsm_kernel(const C* __restrict__ T, long
 // both kernels give identical results.  Rows and columns of L beyond nb are zero.
 constexpr int kTrsmColThreads = 128;
 
-__global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const float2* __restrict__ T, long long ldt,
-                                                                         float2* __restrict__ B, long long ldb,
-                                                                         int nb, int ncols, long long tstride,
+template <typename C>
+__global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const C* __restrict__ T, long long ldt,
+                                                                         C* __restrict__ B, long long ldb, int nb,
+                                                                         int ncols, long long tstride,
                                                                          long long bstride) {
   constexpr int kILP = 8;
   constexpr int ldbs = kTrsmColThreads + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* Ls = reinterpret_cast<float2*>(smem_raw);  // [64][64] column-major: Ls[k*64 + r] = l_rk
-  float2* Bs = Ls + 64 * 64;                          // [64][ldbs]: Bs[r*ldbs + c]
+  C* Ls = reinterpret_cast<C*>(smem_raw);  // [64][64] column-major: Ls[k*64 + r] = l_rk
+  C* Bs = Ls + 64 * 64;                     // [64][ldbs]: Bs[r*ldbs + c]
   T += (size_t)blockIdx.y * tstride;
   B += (size_t)blockIdx.y * bstride;
   const int tid = threadIdx.x;
   const int c0 = blockIdx.x * kTrsmColThreads;
   const int nc = min(kTrsmColThreads, ncols - c0);
   for (int i0 = tid; i0 < 64 * 64; i0 += kTrsmColThreads * kILP) {
-    float2 v[kILP];
+    C v[kILP];
 #pragma unroll
     for (int u = 0; u < kILP; ++u) {
       const int idx = i0 + u * kTrsmColThreads, k = idx >> 6, r = idx & 63;
-      v[u] = (idx < 64 * 64 && r < nb && k < nb && r > k) ? T[(size_t)k * ldt + r] : make_float2(0.f, 0.f);
+      v[u] = (idx < 64 * 64 && r < nb && k < nb && r > k) ? T[(size_t)k * ldt + r] : cmake<C>(0, 0);
     }
 #pragma unroll
     for (int u = 0; u < kILP; ++u)
       if (i0 + u * kTrsmColThreads < 64 * 64) Ls[i0 + u * kTrsmColThreads] = v[u];
   }
   for (int i0 = tid; i0 < 64 * nc; i0 += kTrsmColThreads * kILP) {
-    float2 v[kILP];
+    C v[kILP];
 #pragma unroll
     for (int u = 0; u < kILP; ++u) {
       const int idx = i0 + u * kTrsmColThreads, c = idx >> 6, r = idx & 63;
-      v[u] = (idx < 64 * nc && r < nb) ? B[(size_t)(c0 + c) * ldb + r] : make_float2(0.f, 0.f);
+      v[u] = (idx < 64 * nc && r < nb) ? B[(size_t)(c0 + c) * ldb + r] : cmake<C>(0, 0);
     }
 #pragma unroll
     for (int u = 0; u < kILP; ++u) {
@@ -1070,7 +1071,7 @@ __global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const 
   if (tid < nc) {
 #pragma unroll 1
     for (int r0 = 0; r0 < 64; r0 += 16) {
-      float2 x[16];
+      C x[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) x[i] = Bs[(r0 + i) * ldbs + tid];
 #pragma unroll
@@ -1081,7 +1082,7 @@ __global__ void __launch_bounds__(kTrsmColThreads) trsm_lower_cols_kernel(const 
       for (int i = 0; i < 16; ++i) Bs[(r0 + i) * ldbs + tid] = x[i];
 #pragma unroll 1
       for (int r = r0 + 16; r < 64; ++r) {
-        float2 b = Bs[r * ldbs + tid];
+        C b = Bs[r * ldbs + tid];
 #pragma unroll
         for (int k = 0; k < 16; ++k) b = cfms(b, Ls[(r0 + k) * 64 + r], x[k]);
         Bs[r * ldbs + tid] = b;
@@ -1684,13 +1685,18 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     C* Bb = A + (size_t)c0 * lda + jp;
     cudaError_t te;
     if constexpr (std::is_same<C, float2>::value) {
-      const size_t tsmem = (64 * 64 + 64 * (kTrsmColThreads + 1)) * sizeof(float2);
-      te = allow_dynamic_smem((const void*)trsm_lower_cols_kernel, tsmem);
+      // one thread per column, L11 from shared memory, rows in register blocks of 16
+      // (the same per-element order of updates as trsm_kernel, so the same results)
+      const size_t tsmem = (64 * 64 + 64 * (kTrsmColThreads + 1)) * sizeof(C);
+      te = allow_dynamic_smem((const void*)trsm_lower_cols_kernel<C>, tsmem);
       if (te != cudaSuccess) return te;
       stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
-      trsm_lower_cols_kernel<<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads, tsmem,
-                               s>>>(T, lda, Bb, lda, w, nc, astride, astride);
+      trsm_lower_cols_kernel<C><<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads,
+                                  tsmem, s>>>(T, lda, Bb, lda, w, nc, astride, astride);
     } else {
+      // FP64: the work is bound by the SMs' FP64 pipes, so it is spread over many
+      // CTAs of 16 columns (the one-thread-per-column kernel, 128 columns per CTA,
+      // was 4x slower on the second tier's late, narrow panels)
       const size_t tsmem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(C);
       te = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
       if (te != cudaSuccess) return te;
