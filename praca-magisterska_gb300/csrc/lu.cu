@@ -1193,7 +1193,7 @@ __device__ __forceinline__ void st_release_i32(int* p, int v) {
 template <typename C, bool UPPER>
 __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long long lda, int n, C* x,
                                                    int* flags, unsigned int* ticket, int epoch, int* err,
-                                                   long long astride, int flag_stride) {
+                                                   long long astride, int flag_stride, const int* __restrict__ sel) {
   using R = decltype(C{}.x);
   __shared__ C xs[kTrsvB];
   __shared__ C part[4][kTrsvB];
@@ -1214,9 +1214,11 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   __syncthreads();
   const int b = s_b;
   if (b < 0 || b >= nblk) return;
-  // the matrix, its right-hand side and flags
-  A += (size_t)s_m * astride;
-  x += (size_t)s_m * n;
+  // the matrix, its right-hand side (sel: slot s_m of the batch is matrix sel[s_m])
+  // and the slot's flags
+  const int mat = sel ? sel[s_m] : s_m;
+  A += (size_t)mat * astride;
+  x += (size_t)mat * n;
   flags += (size_t)s_m * flag_stride;
   const int r0 = b * kTrsvB;
   const int rows = min(kTrsvB, n - r0);
@@ -1351,9 +1353,11 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
 
 // ------------------------------------------------------- permutation ----
 // perm[i] = original row that ends up in row i after the interchanges ipiv[0..n).
-__global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm) {
+__global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm,
+                                      const int* __restrict__ sel) {
   extern __shared__ int sp[];
-  ipiv += (size_t)blockIdx.x * n;  // one block per matrix of a batch
+  // one block per matrix of a batch (sel: the batch's matrices, else all)
+  ipiv += (size_t)(sel ? sel[blockIdx.x] : (int)blockIdx.x) * n;
   perm += (size_t)blockIdx.x * n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
   __syncthreads();
@@ -1374,12 +1378,23 @@ __global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* 
 template <typename C>
 __global__ void gather_rows_kernel(const C* __restrict__ src, long long lds, C* __restrict__ dst,
                                    long long ldd, const int* __restrict__ perm, int n, int nrhs,
-                                   int perm_stride) {
+                                   int perm_stride, const int* __restrict__ sel) {
   // column c: a right-hand side of one matrix (perm_stride 0) or the right-hand
-  // side of matrix c of a batch (perm_stride n)
+  // side of matrix c of a batch (perm_stride n; with sel, of matrix sel[c], whose
+  // vector is column sel[c] of dst)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
-  if (i < n && c < nrhs) dst[(size_t)c * ldd + i] = src[(size_t)c * lds + perm[(size_t)c * perm_stride + i]];
+  const int cd = sel ? sel[c] : c;
+  if (i < n && c < nrhs) dst[(size_t)cd * ldd + i] = src[(size_t)c * lds + perm[(size_t)c * perm_stride + i]];
+}
+
+// dst[c] = src[sel[c]] for the n-vectors of the selected matrices of a batch
+template <typename C>
+__global__ void gather_vecs_kernel(const C* __restrict__ src, int n, C* __restrict__ dst,
+                                   const int* __restrict__ sel) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i < n) dst[(size_t)c * n + i] = src[(size_t)sel[c] * n + i];
 }
 
 // ----------------------------------------------------------- host side ----
@@ -1765,25 +1780,32 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
-                       LuWorkspace* ws, cudaStream_t s, int batch, long long astride) {
+                       LuWorkspace* ws, cudaStream_t s, int batch, long long astride, const int* sel) {
   constexpr int NB = PanelCfg<C>::NB;
   cudaError_t e;
-  if (batch < 1 || batch > ws->max_batch || (batch > 1 && (nrhs != 1 || ldb != n))) return cudaErrorInvalidValue;
+  if (batch < 1 || batch > ws->max_batch || ((batch > 1 || sel) && (nrhs != 1 || ldb != n)))
+    return cudaErrorInvalidValue;
   if (n > ws->perm_cap) return cudaErrorInvalidValue;
+  if (sel && !(nrhs == 1 && ws->flags)) return cudaErrorInvalidValue;
   // row interchanges: B <- P B through a permutation gather into the scratch copy
   if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
   e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
   if (e != cudaSuccess) return e;
   stats::count(stats::kMisc, 2);
-  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm);
+  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
   C* tmp = reinterpret_cast<C*>(ws->rhs);
-  const int ncol = batch > 1 ? batch : nrhs;  // columns of the gathered block
+  const int ncol = (batch > 1 || sel) ? batch : nrhs;  // columns of the gathered block
   if ((size_t)n * ncol * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
-  e = cudaMemcpy2DAsync(tmp, (size_t)n * sizeof(C), B, (size_t)ldb * sizeof(C), (size_t)n * sizeof(C), ncol,
-                        cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return e;
+  if (sel) {
+    stats::count(stats::kMisc);
+    gather_vecs_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(B, n, tmp, sel);
+  } else {
+    e = cudaMemcpy2DAsync(tmp, (size_t)n * sizeof(C), B, (size_t)ldb * sizeof(C), (size_t)n * sizeof(C), ncol,
+                          cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
   gather_rows_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(tmp, n, B, ldb, ws->perm, n, ncol,
-                                                                     batch > 1 ? n : 0);
+                                                                     (batch > 1 || sel) ? n : 0, sel);
   if (nrhs == 1 && ws->flags) {
     const int nblk = (n + kTrsvB - 1) / kTrsvB;
     if (nblk > ws->flag_cap) return cudaErrorInvalidValue;
@@ -1799,10 +1821,10 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
       if (e != cudaSuccess) return e;
       if (pass == 0)
         trsv_kernel<C, false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                               &ws->barrier->err, astride, ws->flag_cap);
+                                                               &ws->barrier->err, astride, ws->flag_cap, sel);
       else
         trsv_kernel<C, true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                              &ws->barrier->err, astride, ws->flag_cap);
+                                                              &ws->barrier->err, astride, ws->flag_cap, sel);
     }
     return cudaGetLastError();
   }
@@ -1884,8 +1906,8 @@ template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWork
 template cudaError_t lu_factor_t<float2>(float2*, long long, int, int*, LuWorkspace*, cudaStream_t,
                                          GemmHook<float2>, int, long long, int);
 template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const int*, double2*, long long, int,
-                                         LuWorkspace*, cudaStream_t, int, long long);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,
-                                        LuWorkspace*, cudaStream_t, int, long long);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*);
 
 }  // namespace wmom

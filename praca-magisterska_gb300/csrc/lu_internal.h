@@ -64,9 +64,12 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
                         GemmHook<C> gemm_hook, int batch = 1, long long astride = 0, int span = 0);
 
 // Solves with the factors; batch > 1 needs nrhs == 1 and right-hand sides n apart.
+// sel (device, `batch` entries): solve only these matrices of a larger batch (matrix
+// sel[i] at A + sel[i] * astride, its right-hand side at B + sel[i] * n).
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
-                       LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0);
+                       LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0,
+                       const int* sel = nullptr);
 
 // Workspace management (api.cu).
 cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch = 1);

@@ -35,12 +35,16 @@ constexpr int kGemvRows = 128;
 constexpr int kGemvChunk = 512;
 
 // partial[chunk*n + i] = sum over the columns of a chunk of Z[i, j] x[j]; blockIdx.z = matrix
+// (sel: the z-th selected matrix is Z's sel[z]; its vector is x's vsel[z], or sel[z])
 __global__ void __launch_bounds__(kGemvRows) gemv_partial_kernel(const double2* __restrict__ Z, long long ldz,
                                                                  long long zstride, const double2* __restrict__ x,
-                                                                 int n, double2* __restrict__ partial) {
+                                                                 int n, double2* __restrict__ partial,
+                                                                 const int* __restrict__ sel,
+                                                                 const int* __restrict__ vsel) {
   __shared__ double2 xs[kGemvChunk];
-  Z += (size_t)blockIdx.z * zstride;
-  x += (size_t)blockIdx.z * n;
+  const int mat = sel ? sel[blockIdx.z] : (int)blockIdx.z;
+  Z += (size_t)mat * zstride;
+  x += (size_t)(vsel ? vsel[blockIdx.z] : mat) * n;
   partial += (size_t)blockIdx.z * gridDim.y * n;
   const int i = blockIdx.x * kGemvRows + threadIdx.x;
   const int c0 = blockIdx.y * kGemvChunk;
@@ -60,11 +64,13 @@ __global__ void __launch_bounds__(kGemvRows) gemv_partial_kernel(const double2* 
 }
 
 // r = v - sum of the partials in chunk order (deterministic); blockIdx.y = matrix
+// (sel: the y-th selected matrix, sel[y])
 __global__ void residual_finish_kernel(const double2* __restrict__ v, const double2* __restrict__ partial,
-                                       int nchunks, int n, double2* __restrict__ r) {
+                                       int nchunks, int n, double2* __restrict__ r, const int* __restrict__ sel,
+                                       const int* __restrict__ vsel) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   partial += (size_t)blockIdx.y * nchunks * n;
-  r += (size_t)blockIdx.y * n;
+  r += (size_t)(vsel ? vsel[blockIdx.y] : (sel ? sel[blockIdx.y] : (int)blockIdx.y)) * n;
   if (i >= n) return;
   double re = 0.0, im = 0.0;
   for (int c = 0; c < nchunks; ++c) {
@@ -211,12 +217,13 @@ __global__ void add_loads_kernel(double2* __restrict__ Z, long long ldz, long lo
 }
 
 cudaError_t residual_fp64(const double2* Z, long long ldz, long long zstride, const double2* x, const double2* v,
-                          int n, double2* r, double2* partial, int nvec, cudaStream_t s) {
+                          int n, double2* r, double2* partial, int nvec, cudaStream_t s, const int* sel,
+                          const int* vsel) {
   const int nchunks = (n + kGemvChunk - 1) / kGemvChunk;
   stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n * nvec, 2);
-  gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks, nvec), kGemvRows, 0, s>>>(Z, ldz, zstride,
-                                                                                                 x, n, partial);
-  residual_finish_kernel<<<dim3((n + 255) / 256, nvec), 256, 0, s>>>(v, partial, nchunks, n, r);
+  gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks, nvec), kGemvRows, 0, s>>>(
+      Z, ldz, zstride, x, n, partial, sel, vsel);
+  residual_finish_kernel<<<dim3((n + 255) / 256, nvec), 256, 0, s>>>(v, partial, nchunks, n, r, sel, vsel);
   return cudaGetLastError();
 }
 
@@ -304,7 +311,7 @@ int gmres_cycles() {
 struct GroupScratch {
   int n = 0, B = 0;
   cudaStream_t s = nullptr;
-  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, fb_lu, fb_ipiv, fb_x, fb_r;
+  DevBuf vrep, x64, r64, d32, part, sc, scal, actv, sel, fb_lu, fb_ipiv, fb_x, fb_r;
   int fb_cap = 0;          // matrices per batched FP64-grade factorisation (tiers 2, 3)
   std::vector<double> vh;  // excitation on the host
   double vnorm = 0.0;
@@ -329,6 +336,7 @@ wmom_status scratch_init(GroupScratch* g, int n, int B, int ngap, float ampl, fl
   SWEEP_TRY(g->sc.alloc(sizeof(GroupScalars), s));
   SWEEP_TRY(g->scal.alloc(sizeof(double) * 2 * kMaxLuBatch, s));
   SWEEP_TRY(g->actv.alloc(sizeof(int) * kMaxLuBatch, s));
+  SWEEP_TRY(g->sel.alloc(sizeof(int) * 2 * kMaxLuBatch, s));
   for (int b = 0; b < B; ++b)
     SWEEP_TRY(cudaMemcpyAsync(g->vrep.as<double2>() + (size_t)b * n, g->vh.data(), sizeof(double2) * n,
                               cudaMemcpyHostToDevice, s));
@@ -502,7 +510,7 @@ wmom_status gmres_correction(int n, const double2* Z, const float2* lu, const in
       {
         stats::Scope sc(stats::kResidual, s, 16.0 * n * (double)n, 1);
         gemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nchunks, 1), kGemvRows, 0, s>>>(
-            Z, n, 0, Vp + (size_t)j * n, n, part.as<double2>());
+            Z, n, 0, Vp + (size_t)j * n, n, part.as<double2>(), nullptr, nullptr);
       }
       matvec_finish_kernel<<<vb, 256, 0, s>>>(part.as<double2>(), nchunks, n, wp);
       st = precond(wp, wp);
@@ -780,9 +788,23 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
   std::vector<int> hact(kMaxLuBatch, 0);
   const int max_it = 40;
+  // the matrices still refining: residuals and corrections are computed for these
+  // only (one slowly converging matrix no longer keeps its whole batch busy)
+  std::vector<int> hsel(kMaxLuBatch, 0);
+  int nsel = 0;
+  for (int b = 0; b < bg; ++b)
+    if (active[b]) hsel[nsel++] = b;
+  SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
   for (int it = 0;; ++it) {
-    const wmom_status rs = group_residuals(g, Z64, bg);
-    if (rs != WMOM_OK) return rs;
+    if (nsel == 0) break;
+    {
+      GroupScalars* dscr = g.sc.as<GroupScalars>();
+      SWEEP_TRY(residual_fp64(Z64, n, (long long)nn, g.x64.as<double2>(), g.vrep.as<double2>(), n,
+                              g.r64.as<double2>(), g.part.as<double2>(), nsel, s, g.sel.as<int>()));
+      SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dscr->rnorm2, bg, s));
+      SWEEP_TRY(cudaMemcpyAsync(&hs, dscr, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+      SWEEP_TRY(cudaStreamSynchronize(s));
+    }
     int nact = 0;
     for (int b = 0; b < bg; ++b) {
       if (!active[b]) continue;
@@ -826,13 +848,19 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       hscale[kMaxLuBatch + b] = 1.0 / scl;
       hact[b] = active[b] ? 1 : 0;
     }
+    nsel = 0;
+    for (int b = 0; b < bg; ++b)
+      if (active[b]) hsel[nsel++] = b;
     SWEEP_TRY(cudaMemcpyAsync(g.scal.p, hscale.data(), sizeof(double) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice, s));
     SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+    SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
     const double* dscale = g.scal.as<double>();
     const double* dinv = dscale + kMaxLuBatch;
     stats::count(stats::kMisc, 4);
     convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
-    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
+                                 nsel == bg ? nullptr : g.sel.as<int>()));
+
     sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
     sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);
     accumulate_vec_kernel<<<vgrid, 256, 0, s>>>(g.x64.as<double2>(), g.d32.as<float2>(), n, bg, dinv,
@@ -982,11 +1010,22 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         act[j] = inf[j] == 0;
         prev2[j] = HUGE_VAL;
       }
+      // the chunk's active matrices in one residual launch: matrix fb[c0 + j] of Z64,
+      // vector slot j of fx / frr
+      std::vector<int> zsel2(2 * kMaxLuBatch, 0);
       for (int it = 0;; ++it) {
+        int na = 0;
         for (int j = 0; j < cn; ++j)
-          if (act[j])
-            SWEEP_TRY(residual_fp64(Z64 + (size_t)fb[c0 + j] * nn, n, 0, fx + (size_t)j * n, g.vrep.as<double2>(), n,
-                                    frr + (size_t)j * n, g.part.as<double2>(), 1, s));
+          if (act[j]) {
+            zsel2[na] = fb[c0 + j];
+            zsel2[kMaxLuBatch + na] = j;
+            ++na;
+          }
+        if (na > 0) {
+          SWEEP_TRY(cudaMemcpyAsync(g.sel.p, zsel2.data(), sizeof(int) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+          SWEEP_TRY(residual_fp64(Z64, n, (long long)nn, fx, g.vrep.as<double2>(), n, frr, g.part.as<double2>(), na,
+                                  s, g.sel.as<int>(), g.sel.as<int>() + kMaxLuBatch));
+        }
         SWEEP_TRY(sumsq_fp64(frr, n, dsc->rnorm2, cn, s));
         SWEEP_TRY(sumsq_fp64(fx, n, dsc->xnorm2, cn, s));
         SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));

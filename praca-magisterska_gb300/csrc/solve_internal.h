@@ -54,9 +54,12 @@ wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float a
                           double* currents, double* zin, wmom_report* reports, cudaStream_t s);
 
 // Device helpers (solve.cu).
-// r[b] = v - Z[b] x[b] for nvec matrices zstride apart (vectors n apart), FP64.
+// r[b] = v - Z[b] x[b] for nvec matrices zstride apart (vectors n apart), FP64;
+// sel (device, nvec entries): only these matrices b of a larger batch; vsel (device,
+// nvec entries): the vector slots of x and r that go with them, when they differ.
 cudaError_t residual_fp64(const double2* Z, long long ldz, long long zstride, const double2* x, const double2* v,
-                          int n, double2* r, double2* partial, int nvec, cudaStream_t s);
+                          int n, double2* r, double2* partial, int nvec, cudaStream_t s, const int* sel = nullptr,
+                          const int* vsel = nullptr);
 // out[b] = sum |x[b]_i|^2 for nvec vectors n apart (deterministic order).
 cudaError_t sumsq_fp64(const double2* x, int n, double* out, int nvec, cudaStream_t s);
 cudaError_t convert_flat_64_to_32(const double2* src, float2* dst, size_t count, cudaStream_t s);
