@@ -63,3 +63,27 @@ def test_no_device_calls_fail_cleanly_without_gpu(wmom):
     with pytest.raises(wmom.WmomError) as e:
         wmom.Plan(topo)
     assert e.value.status in (2, 8)
+
+
+def test_stats_classes_match_library(wmom):
+    """The Python names of the stats classes and the library's class count agree
+    (wmom_stats_read returns the number of classes and needs no GPU)."""
+    import ctypes
+    f = wmom._lib.wmom_stats_read
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int]
+    assert f(None, None, None, None, 0) == len(wmom.STAT_CLASSES)
+    assert wmom.STAT_CLASSES[8:] == ["emul_gemm", "trsv"]
+
+
+def test_report_layout_matches_header(wmom):
+    """wmom_report: a double and six ints (rel_residual, iterations, fell_back, info,
+    status, krylov_steps, tier), 32 bytes; the ctypes mirror has the same layout."""
+    import ctypes
+    import re
+    from conftest import ROOT
+    hdr = open(f"{ROOT}/include/wmom.h").read()
+    body = re.search(r"typedef struct wmom_report \{(.*?)\} wmom_report;", hdr, re.S).group(1)
+    fields = re.findall(r"^\s*(double|int)\s+(\w+);", body, re.M)
+    assert [n for _, n in fields] == [n for n, _ in wmom._Report._fields_]
+    assert ctypes.sizeof(wmom._Report) == 32
