@@ -145,7 +145,10 @@ __device__ __forceinline__ void gauss_geometry(const double ex[3], const double 
 __device__ __forceinline__ void gauss_sums(const double r[2], const double ri[2], const double wu[2],
                                            const double wd[2], double ka, const double2* tab, Cx* up, Cx* dn,
                                            Cx* pl) {
-  Cx su = {0.0, 0.0}, sd = {0.0, 0.0}, sp = {0.0, 0.0};
+  // the falling ramp is one minus the rising one, so its sum is the plain sum minus
+  // the rising sum (wd is kept in the signature for the instances' layout)
+  (void)wd;
+  Cx su = {0.0, 0.0}, sp = {0.0, 0.0};
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
     double sn, cs;
@@ -153,13 +156,11 @@ __device__ __forceinline__ void gauss_sums(const double r[2], const double ri[2]
     const double gre = mul(cs, ri[g]), gim = -mul(sn, ri[g]);
     su.re = fma(wu[g], gre, su.re);
     su.im = fma(wu[g], gim, su.im);
-    sd.re = fma(wd[g], gre, sd.re);
-    sd.im = fma(wd[g], gim, sd.im);
     sp.re = add(sp.re, gre);
     sp.im = add(sp.im, gim);
   }
   *up = su;
-  *dn = sd;
+  *dn = Cx{sub(sp.re, su.re), sub(sp.im, su.im)};
   *pl = sp;
 }
 

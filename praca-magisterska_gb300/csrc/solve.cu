@@ -1074,10 +1074,16 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
             if (stalled[j] && hs.berr[j] <= 4.0 * std::sqrt((double)n) * eps64) plain[j] = false;
         }
         if (nact == 0) break;
-        // d = LU^-1 r for the chunk; x += d where active
-        for (int j = 0; j < cn; ++j) hact[j] = act[j] ? 1 : 0;
+        // d = LU^-1 r for the chunk's active matrices; x += d where active
+        int nsa = 0;
+        for (int j = 0; j < cn; ++j) {
+          hact[j] = act[j] ? 1 : 0;
+          if (act[j]) zsel2[nsa++] = j;
+        }
         SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
-        SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, cn, (long long)nn));
+        SWEEP_TRY(cudaMemcpyAsync(g.sel.p, zsel2.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+        SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, nsa, (long long)nn,
+                                      nsa == cn ? nullptr : g.sel.as<int>()));
         SWEEP_TRY(sumsq_fp64(frr, n, dsc->dnorm2, cn, s));
         stats::count(stats::kMisc);
         accumulate64_kernel<<<(unsigned)(((size_t)n * cn + 255) / 256), 256, 0, s>>>(fx, frr, n, cn,
