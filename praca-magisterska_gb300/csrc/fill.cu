@@ -566,35 +566,33 @@ constexpr int kMultiThreads = 512;
 // One CTA of 16 warps per tile for all nk frequencies: the pairs' geometry (R, 1/R,
 // projection) is computed once, then for each frequency phase A (phase and ramps
 // only) and phase B.  The arithmetic per pair and entry is fill_pair_kernel's.
-__global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
+__global__ void __launch_bounds__(kMultiThreads, 2) fill_pair_multi_kernel(
     const ObsInst* __restrict__ oinst, const SrcInst* __restrict__ sinst, const int* __restrict__ tiles,
     int off_rt_ids, int off_ct_off, int off_ct_ids, int off_row_local, int off_col_local, int npls, int max_o,
     int max_q, const FreqParams* __restrict__ fp, const SelfVal* __restrict__ selfv, int nsrc, int nk,
     double2* __restrict__ Z, long long ldz, long long zstride) {
+  // shared memory holds only the pairs' values and geometry (two CTAs per SM where a
+  // tile's pairs allow it); the instances are read through the read-only cache
   extern __shared__ __align__(16) unsigned char sm[];
   const double2* tab = g_sin_tab;
-  ObsInst* so = reinterpret_cast<ObsInst*>(sm);
-  SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
-  const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
-  PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
-  PairGeo* geo = reinterpret_cast<PairGeo*>(sm + pt_off + (size_t)max_o * max_q * sizeof(PairVal));
+  PairVal* pt = reinterpret_cast<PairVal*>(sm);
+  PairGeo* geo = reinterpret_cast<PairGeo*>(sm + (size_t)max_o * max_q * sizeof(PairVal));
   const TileLists L = tile_lists(tiles, off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local);
   const int tr = blockIdx.x, tc = blockIdx.y;
   const int tid = threadIdx.x;
   const int o0 = L.rt_off[tr], nO = L.rt_off[tr + 1] - o0;
   const int q0 = L.ct_off[tc], nQ = L.ct_off[tc + 1] - q0;
-  for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[L.rt_ids[o0 + i]];
-  for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[L.ct_ids[q0 + i]];
-  __syncthreads();
   for (int p = tid; p < nO * nQ; p += blockDim.x) {
     const int o = p / nQ, q = p - o * nQ;
-    const ObsInst& O = so[o];
-    const SrcInst& S = sq[q];
+    const ObsInst& O = oinst[L.rt_ids[o0 + o]];
+    const SrcInst& S = sinst[L.ct_ids[q0 + q]];
     PairGeo g;
     g.t = dot3(S.dc, O.u);
     if (!same_segment(O, S)) {
       const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
       gauss_geometry(ex, S.dc, S.an2, S.s, g.r, g.ri);
+    } else {
+      g.r[0] = -1.0;  // self pair (a regular pair's R is at least the radius)
     }
     geo[p] = g;
   }
@@ -602,11 +600,12 @@ __global__ void __launch_bounds__(kMultiThreads, 1) fill_pair_multi_kernel(
   for (int k = 0; k < nk; ++k) {
     const FreqParams f = fp[k];
     for (int p = tid; p < nO * nQ; p += blockDim.x) {
-      const int o = p / nQ, q = p - o * nQ;
-      const SrcInst& S = sq[q];
+      const int q = p - (p / nQ) * nQ;
+      const int qg = L.ct_ids[q0 + q];
+      const SrcInst& S = sinst[qg];
       const PairGeo& g = geo[p];
-      pt[p] = same_segment(so[o], S) ? self_pair_value(g.t, S, f, selfv[(size_t)k * nsrc + L.ct_ids[q0 + q]])
-                                     : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
+      pt[p] = g.r[0] < 0.0 ? self_pair_value(g.t, S, f, selfv[(size_t)k * nsrc + qg])
+                           : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
     }
     __syncthreads();
     assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
@@ -635,7 +634,7 @@ size_t pair_smem_bytes(const PairTiles& t) {
 }
 
 size_t pair_multi_smem_bytes(const PairTiles& t) {
-  return pair_smem_bytes(t) + (size_t)t.max_o * t.max_q * sizeof(PairGeo);
+  return (size_t)t.max_o * t.max_q * (sizeof(PairVal) + sizeof(PairGeo));
 }
 
 // Builds the sin/cos table of the current device once (on its own stream, waited for,
