@@ -323,7 +323,7 @@ def run_wmom(args):
         roof["note"] = ("achieved counts 384 flop-eq per entry (8 Green's-function evaluations, as the reference "
                         "evaluates them); the pair-tiled kernel shares evaluations between neighbouring basis "
                         "functions (about 2.1 per entry) and their geometry between frequencies, so the fraction "
-                        "can exceed 1; the FP64 pipe itself is 81% busy in the ncu capture")
+                        "can exceed 1; the FP64 pipe itself is 85% busy in the ncu capture")
         alg = 16.0 * units  # each complex128 entry written once
         roof["hbm_view"] = {"algorithmic_bytes": alg, "achieved_gbs": alg / (avg_ms / 1e3) / 1e9,
                             "frac_of_hbm": alg / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"]}
