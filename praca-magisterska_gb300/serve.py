@@ -25,6 +25,7 @@ path; its driver solved one fixed deck per run ("wersja referencyjna/Wire_MoM.cu
 """
 import collections
 import hashlib
+import importlib
 import threading
 import time
 from concurrent.futures import Future
@@ -57,12 +58,23 @@ class _Resident:
         self.pins = 0
 
 
+def _cuda_stream():
+    """A CUDA stream for one worker: (owner kept alive by the worker, raw handle)."""
+    import torch
+    s = torch.cuda.Stream()
+    return s, s.cuda_stream
+
+
 class Server:
-    def __init__(self, mode=None, hbm_budget_bytes=None, workers=2, tol=1e-12):
-        import torch
-        self._w = __import__("importlib").import_module("praca-magisterska_gb300")
+    """`lib` and `stream_factory` stand in for the solver package and the worker
+    streams (the host-logic tests run the loop on the CPU against a fake library)."""
+
+    def __init__(self, mode=None, hbm_budget_bytes=None, workers=2, tol=1e-12, lib=None, stream_factory=None):
+        self._w = lib if lib is not None else importlib.import_module("praca-magisterska_gb300")
+        self._new_stream = stream_factory or _cuda_stream
         self.mode = self._w.MODE_MIXED if mode is None else mode
         if hbm_budget_bytes is None:
+            import torch
             free, _ = torch.cuda.mem_get_info()
             hbm_budget_bytes = int(free * 0.6)
         self.budget = int(hbm_budget_bytes)
@@ -150,9 +162,7 @@ class Server:
         return True
 
     def _run(self, wid):
-        import torch
-        stream = torch.cuda.Stream()
-        sp = stream.cuda_stream
+        owner, sp = self._new_stream()  # noqa: F841  (owner keeps the stream alive)
         while True:
             with self._lock:
                 while not self._queue and not self._stop:
@@ -173,20 +183,25 @@ class Server:
             raise ValueError("gap outside the geometry")
         freqs = [float(f) for f in req.freqs]
         with self._lock:
-            # pin what is resident, reserve what must be factored
-            have = {f: self._lookup.get((req.geo_key, f)) for f in freqs}
-            missing = sorted({f for f, r in have.items() if r is None})
-            for r in {id(r): r for r in have.values() if r is not None}.values():
-                r.pins += 1
-                self._sets.move_to_end(id(r))
-            need = len(missing) * self._per_matrix_bytes(n)
-            if need > self.budget:
-                for r in {id(r): r for r in have.values() if r is not None}.values():
+            while True:
+                # pin what is resident, reserve what must be factored
+                have = {f: self._lookup.get((req.geo_key, f)) for f in freqs}
+                missing = sorted({f for f, r in have.items() if r is None})
+                pinned = {id(r): r for r in have.values() if r is not None}
+                need = len(missing) * self._per_matrix_bytes(n)
+                if need > self.budget:
+                    raise MemoryError("request needs more device memory than the serving budget")
+                for r in pinned.values():
+                    r.pins += 1
+                    self._sets.move_to_end(id(r))
+                if not missing or self._admit(need):
+                    break
+                # a waiting request holds no pins: two waiters pinning the sets the
+                # other must evict would wait for each other forever
+                for r in pinned.values():
                     r.pins -= 1
-                raise MemoryError("request needs more device memory than the serving budget")
-            while missing and not self._admit(need):
                 self._lock.wait(timeout=0.05)
-        pinned = {id(r): r for r in have.values() if r is not None}
+        reserved = need
         try:
             if missing:
                 fac = self._w.Factors(plan, np.array(missing, np.float32), mode=self.mode, stream=sp)
@@ -194,6 +209,7 @@ class Server:
                 res.pins = 1
                 with self._lock:
                     self._reserved -= need
+                    reserved = 0
                     self._used += res.bytes
                     self._sets[id(res)] = res
                     for f in missing:
@@ -234,6 +250,7 @@ class Server:
                                    "latency_s": done - req.arrival})
         finally:
             with self._lock:
+                self._reserved -= reserved  # a factorisation that failed returns its reservation
                 for r in pinned.values():
                     r.pins -= 1
                 self._lock.notify_all()
