@@ -339,6 +339,7 @@ wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long l
       cudaStreamSynchronize(s);
       cudaFree(h->d_fp);
       h->d_fp = nullptr;
+      h->fp_cap = 0;  // a failed allocation below leaves no stale capacity
     }
     WMOM_CUDA_TRY(cudaMalloc(&h->d_fp, sizeof(FreqParams) * nk));
     h->fp_cap = nk;
