@@ -469,6 +469,7 @@ def run_geometries(args):
         srv.close()
         runs.append((dt, st, done))
     dt, st, done = min(runs, key=lambda r: r[0])
+    fill_ms = _fill_all_geometries(w, pool, freqs)
     line = {"metric": "freq-solves/s over a set of geometries of uneven size (one frequency each)",
             "unit": "freq-solves/s", "value": args.geometries / dt, "higher_is_better": True, "n_gpus": 1,
             "ms_per_step": 1e3 * dt, "steps": len(runs), "data": "synthetic (seeded random wires)",
@@ -476,9 +477,40 @@ def run_geometries(args):
                                    "frequency each in 1 kHz-30 MHz, precision form", "workers": args.workers,
                        "unknowns_total": int(sizes.sum())},
             "latency_ms": {"p50": st.get("p50_ms"), "p99": st.get("p99_ms")},
+            "fill_ms_all_geometries": fill_ms,
             "fallbacks": int(sum(r["fell_back"] for d in done for r in d["reports"])) if done and
             isinstance(done[0], dict) and "reports" in done[0] else None}
     print(json.dumps(line), flush=True)
+
+
+def _fill_all_geometries(w, pool, freqs, reps=3):
+    """Device time to fill the Z of every geometry of the set at its frequency: one
+    launch per geometry (Plan.fill) against one ragged launch for all of them
+    (fill_geometries); best of `reps`, CUDA events on the current stream."""
+    import torch
+    plans = [w.Plan(w.Topology(g)) for g in pool]
+    fl = [float(f) for f in freqs]
+
+    def timed(fn):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            best = e0.elapsed_time(e1) if best is None else min(best, e0.elapsed_time(e1))
+            del out
+        return best
+
+    try:
+        per = timed(lambda: [p.fill([f]) for p, f in zip(plans, fl)])
+        one = timed(lambda: w.fill_geometries(plans, fl))
+    finally:
+        for p in plans:
+            p.close()
+    return {"one_launch_per_geometry": per, "one_launch_for_all": one}
 
 
 def run_gemm(args):

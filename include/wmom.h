@@ -14,6 +14,8 @@
  *   wmom_fill                zmatrix() REF/Zmatrix.h:7-9 and zmatrix_gpu()
  *                            REF/Wire_MoM.h:49-51, into device memory, many
  *                            frequencies per call
+ *   wmom_fill_geometries     the same for several geometries of uneven size, one
+ *                            frequency each, in one launch
  *   wmom_zgetrf / wmom_zgetrs
  *                            LAPACKE_zgetrf / LAPACKE_zgetrs, REF/Wire_MoM.cu:372,382
  *                            (and cublasZgetrfBatched / cublasZgetrsBatched,
@@ -104,6 +106,16 @@ long long wmom_plan_fill_pairs(wmom_plan plan);
  * j*eta0/(4*pi*k) scale of zmatrix() is included. */
 wmom_status wmom_fill(wmom_plan plan, const double* ka, int nk, void* z_dev, long long ldz,
                       long long zstride, void* stream);
+
+/* Fills the impedance matrices of `count` geometries of any sizes, one wave number
+ * each (host arrays plans[i], ka[i], z_dev[i], ldz[i] >= npls of plans[i]), in one
+ * kernel launch for all free-space geometries (ground-plane geometries are filled by
+ * their own launch).  Each matrix equals wmom_fill's for the same plan and ka, bit
+ * for bit.  The reference fills one geometry per process run (zmatrix_gpu,
+ * REF/Wire_MoM.h:49-51); this is its batched form for sets of uneven geometries.
+ * Synchronises `stream`. */
+wmom_status wmom_fill_geometries(const wmom_plan* plans, int count, const double* ka, void* const* z_dev,
+                                 const long long* ldz, void* stream);
 
 /* ------------------------------------------------------------ FP64 LU ---- */
 /* In-place LU with partial pivoting of an n x n complex128 device matrix

@@ -87,6 +87,9 @@ _plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
 _plan_fill_pairs = _sig("wmom_plan_fill_pairs", ctypes.c_longlong, [_vp])
 _plan_set_loads = _sig("wmom_plan_set_loads", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
+_fill_geometries = _sig("wmom_fill_geometries", ctypes.c_int,
+                        [ctypes.POINTER(_vp), ctypes.c_int, _dp, ctypes.POINTER(_vp),
+                         ctypes.POINTER(ctypes.c_longlong), _vp])
 _zgetrf = _sig("wmom_zgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
 _cgetrf = _sig("wmom_cgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _ip, _vp])
 _zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
@@ -314,6 +317,25 @@ class Plan:
         reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
                         info=r.info, status=r.status, krylov_steps=r.krylov_steps, tier=r.tier) for r in reps]
         return cur, zin, reports
+
+
+def fill_geometries(plans, freqs_mhz):
+    """Impedance matrices of several geometries (plans) of any sizes, one float32 MHz
+    frequency each, filled in one launch: a list of complex128 device tensors, the
+    i-th of shape (npls_i, npls_i) laid out as Plan.fill's [k] (its .T is cz)."""
+    import torch
+    freqs = np.atleast_1d(np.asarray(freqs_mhz, np.float32))
+    if len(freqs) != len(plans) or not plans:
+        raise ValueError("one frequency per plan")
+    zs = [torch.empty((p.npls, p.npls), dtype=torch.complex128, device="cuda") for p in plans]
+    count = len(plans)
+    hs = (_vp * count)(*[p._h for p in plans])
+    kas = np.array([ka(f) for f in freqs], np.float64)
+    ptrs = (_vp * count)(*[z.data_ptr() for z in zs])
+    lds = (ctypes.c_longlong * count)(*[p.npls for p in plans])
+    _check(_fill_geometries(hs, count, _ptr(kas, _dp), ptrs, lds, torch.cuda.current_stream().cuda_stream),
+           "wmom_fill_geometries")
+    return zs
 
 
 class Factors:

@@ -354,6 +354,22 @@ wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long l
   return WMOM_OK;
 }
 
+wmom_status wmom_fill_geometries(const wmom_plan* plans, int count, const double* ka, void* const* z_dev,
+                                 const long long* ldz, void* stream) {
+  if (count <= 0 || !plans || !ka || !z_dev || !ldz) return WMOM_ERR_ARG;
+  std::vector<const Plan*> ps(count);
+  for (int i = 0; i < count; ++i) {
+    if (!plans[i] || !z_dev[i] || ldz[i] < plans[i]->p.npls || !(ka[i] > 0.0) || !std::isfinite(ka[i]))
+      return WMOM_ERR_ARG;
+    ps[i] = &plans[i]->p;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  WMOM_CUDA_TRY(launch_fill_geometries(ps.data(), ka, reinterpret_cast<double2* const*>(z_dev), ldz, count, s));
+  // the job list is uploaded from pageable memory: finish before it dies
+  WMOM_CUDA_TRY(cudaStreamSynchronize(s));
+  return WMOM_OK;
+}
+
 wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream) {
   if (n <= 0 || !a_dev || lda < n || !ipiv_dev) return WMOM_ERR_ARG;
   if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;

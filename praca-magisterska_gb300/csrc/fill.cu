@@ -16,7 +16,9 @@
 // so that the float-derived coordinates give the same doubles as the CPU code.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -511,31 +513,25 @@ __device__ __forceinline__ void assemble_tile(const PairVal* pt, int nQ, const T
   }
 }
 
-// One CTA per tile and frequency (blockIdx.z).
-__global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __restrict__ oinst,
-                                                        const SrcInst* __restrict__ sinst,
-                                                        const int* __restrict__ tiles, int off_rt_ids,
-                                                        int off_ct_off, int off_ct_ids, int off_row_local,
-                                                        int off_col_local, int npls, int max_o, int max_q,
-                                                        const FreqParams* __restrict__ fp,
-                                                        const SelfVal* __restrict__ selfv, int nsrc,
-                                                        double2* __restrict__ Z, long long ldz,
-                                                        long long zstride) {
-  extern __shared__ __align__(16) unsigned char sm[];
+// Tile (tr, tc) of one matrix at one frequency: the tile's instances and then its
+// pair values are staged in shared memory `sm` (layout from max_o, max_q), and the
+// entries are written to Zk.  selfv holds this frequency's self values, indexed by
+// source instance.
+__device__ __forceinline__ void pair_tile(const ObsInst* __restrict__ oinst, const SrcInst* __restrict__ sinst,
+                                          const TileLists& L, int tr, int tc, int npls, int max_o, int max_q,
+                                          const FreqParams& f, const SelfVal* __restrict__ selfv,
+                                          double2* __restrict__ Zk, long long ldz, unsigned char* sm) {
   const double2* tab = g_sin_tab;
   ObsInst* so = reinterpret_cast<ObsInst*>(sm);
   SrcInst* sq = reinterpret_cast<SrcInst*>(sm + (size_t)max_o * sizeof(ObsInst));
   const size_t pt_off = ((size_t)max_o * sizeof(ObsInst) + (size_t)max_q * sizeof(SrcInst) + 15) & ~(size_t)15;
   PairVal* pt = reinterpret_cast<PairVal*>(sm + pt_off);
-  const TileLists L = tile_lists(tiles, off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local);
-  const int tr = blockIdx.x, tc = blockIdx.y, k = blockIdx.z;
   const int tid = threadIdx.x;
   const int o0 = L.rt_off[tr], nO = L.rt_off[tr + 1] - o0;
   const int q0 = L.ct_off[tc], nQ = L.ct_off[tc + 1] - q0;
   for (int i = tid; i < nO; i += blockDim.x) so[i] = oinst[L.rt_ids[o0 + i]];
   for (int i = tid; i < nQ; i += blockDim.x) sq[i] = sinst[L.ct_ids[q0 + i]];
   __syncthreads();
-  const FreqParams f = fp[k];
 
   // phase A: distinct pairs of the tile
   for (int p = tid; p < nO * nQ; p += blockDim.x) {
@@ -549,11 +545,82 @@ __global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __rest
       gauss_geometry(ex, S.dc, S.an2, S.s, r, ri);
       pt[p] = regular_pair_value(r, ri, t, S, f, tab);
     } else {
-      pt[p] = self_pair_value(t, S, f, selfv[(size_t)k * nsrc + L.ct_ids[q0 + q]]);
+      pt[p] = self_pair_value(t, S, f, selfv[L.ct_ids[q0 + q]]);
     }
   }
   __syncthreads();
-  assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
+  assemble_tile(pt, nQ, L, tr, tc, npls, Zk, ldz);
+}
+
+// One CTA per tile and frequency (blockIdx.z).
+__global__ void __launch_bounds__(256, 3) fill_pair_kernel(const ObsInst* __restrict__ oinst,
+                                                        const SrcInst* __restrict__ sinst,
+                                                        const int* __restrict__ tiles, int off_rt_ids,
+                                                        int off_ct_off, int off_ct_ids, int off_row_local,
+                                                        int off_col_local, int npls, int max_o, int max_q,
+                                                        const FreqParams* __restrict__ fp,
+                                                        const SelfVal* __restrict__ selfv, int nsrc,
+                                                        double2* __restrict__ Z, long long ldz,
+                                                        long long zstride) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const TileLists L = tile_lists(tiles, off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local);
+  const int k = blockIdx.z;
+  pair_tile(oinst, sinst, L, blockIdx.x, blockIdx.y, npls, max_o, max_q, fp[k], selfv + (size_t)k * nsrc,
+            Z + (size_t)k * zstride, ldz, sm);
+}
+
+// One matrix of a ragged launch over several geometries (one frequency each).
+struct FillJob {
+  const ObsInst* oi;
+  const SrcInst* si;
+  const int* tiles;
+  int off_rt_ids, off_ct_off, off_ct_ids, off_row_local, off_col_local;
+  int npls, n_tiles, max_o, max_q, nsrc;
+  long long tile0;  // first block of this matrix in the launch (n_tiles^2 blocks)
+  long long self0;  // first of its nsrc self values
+  double2* z;
+  long long ldz;
+  FreqParams f;
+};
+
+// The last job whose first index (tile0 or self0) is <= i; jobs are in increasing
+// order of both and job 0 starts at 0.
+template <bool kSelf>
+__device__ __forceinline__ int job_of(const FillJob* __restrict__ jobs, int njobs, long long i) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((kSelf ? jobs[mid].self0 : jobs[mid].tile0) <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Self values of every job's source instances at its frequency (self_values_kernel
+// over a ragged list).
+__global__ void self_values_ragged_kernel(const FillJob* __restrict__ jobs, int njobs, long long nself,
+                                          SelfVal* __restrict__ out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= nself) return;
+  const FillJob& J = jobs[job_of<true>(jobs, njobs, i)];
+  const SrcInst& S = J.si[i - J.self0];
+  Cx Au, Ad, P;
+  self_pair(S.dl, S.an, J.f.ka, &Au, &Ad, &P);
+  out[i] = SelfVal{make_double2(Au.re, Au.im), make_double2(Ad.re, Ad.im), make_double2(P.re, P.im)};
+}
+
+// One CTA per tile of every job: the matrices of several geometries of any sizes in
+// one launch, each tile computed as fill_pair_kernel computes it.
+__global__ void __launch_bounds__(256, 3) fill_pair_ragged_kernel(const FillJob* __restrict__ jobs, int njobs,
+                                                               const SelfVal* __restrict__ selfv) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const FillJob& J = jobs[job_of<false>(jobs, njobs, blockIdx.x)];
+  const int t = (int)(blockIdx.x - J.tile0);
+  const TileLists L = tile_lists(J.tiles, J.off_rt_ids, J.off_ct_off, J.off_ct_ids, J.off_row_local, J.off_col_local);
+  pair_tile(J.oi, J.si, L, t % J.n_tiles, t / J.n_tiles, J.npls, J.max_o, J.max_q, J.f, selfv + J.self0, J.z, J.ldz,
+            sm);
 }
 
 // Frequency-independent values of a pair, kept in shared memory across frequencies.
@@ -726,6 +793,86 @@ cudaError_t launch_fill(const Plan& p, const double* d_fp, int nk, double2* z, l
                                                 reinterpret_cast<const FreqParams*>(d_fp), z, ldz,
                                                 zstride, p.ienv, p.sgnenv);
   return cudaGetLastError();
+}
+
+cudaError_t launch_fill_geometries(const Plan* const* plans, const double* ka, double2* const* z,
+                                   const long long* ldz, int count, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  cudaError_t e = ensure_sin_table();
+  if (e != cudaSuccess) return e;
+  const char* force_entry = std::getenv("WMOM_FILL_ENTRY");
+  const bool entry_only = force_entry && force_entry[0] == '1';
+  auto pair_tiled = [&](const Plan& p) { return !entry_only && p.pt.ok && p.d_tiles; };
+  std::vector<FillJob> jobs;
+  std::vector<FreqParams> fps(count);
+  long long ntiles = 0, nself = 0;
+  size_t smem = 0;
+  double work = 0.0;
+  for (int i = 0; i < count; ++i) {
+    const Plan& p = *plans[i];
+    fps[i] = freq_params(ka[i]);
+    if (p.npls <= 0 || !pair_tiled(p)) continue;
+    FillJob j{};
+    j.oi = p.d_oi;
+    j.si = p.d_si;
+    j.tiles = p.d_tiles;
+    j.off_rt_ids = p.off_rt_ids;
+    j.off_ct_off = p.off_ct_off;
+    j.off_ct_ids = p.off_ct_ids;
+    j.off_row_local = p.off_row_local;
+    j.off_col_local = p.off_col_local;
+    j.npls = p.npls;
+    j.n_tiles = p.pt.n_tiles;
+    j.max_o = p.pt.max_o;
+    j.max_q = p.pt.max_q;
+    j.nsrc = (int)p.pt.src.size();
+    j.tile0 = ntiles;
+    j.self0 = nself;
+    j.z = z[i];
+    j.ldz = ldz[i];
+    j.f = fps[i];
+    ntiles += (long long)j.n_tiles * j.n_tiles;
+    nself += j.nsrc;
+    smem = std::max(smem, pair_smem_bytes(p.pt));
+    work += 384.0 * p.npls * (double)p.npls;
+    jobs.push_back(j);
+  }
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  // one device block: the jobs, then every matrix's frequency constants
+  const size_t jbytes = sizeof(FillJob) * jobs.size();
+  const size_t bytes = jbytes + sizeof(FreqParams) * count;
+  std::vector<unsigned char> h(bytes);
+  if (jbytes) std::memcpy(h.data(), jobs.data(), jbytes);
+  std::memcpy(h.data() + jbytes, fps.data(), sizeof(FreqParams) * count);
+  unsigned char* d = nullptr;
+  e = cudaMallocAsync(reinterpret_cast<void**>(&d), bytes, stream);
+  if (e != cudaSuccess) return e;
+  SelfVal* selfv = nullptr;
+  e = cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess && nself > 0) e = cudaMallocAsync(reinterpret_cast<void**>(&selfv), sizeof(SelfVal) * nself, stream);
+  if (e == cudaSuccess && !jobs.empty()) {
+    stats::Scope sc(stats::kFill, stream, work, 2);
+    const FillJob* dj = reinterpret_cast<const FillJob*>(d);
+    self_values_ragged_kernel<<<(unsigned)((nself + 127) / 128), 128, 0, stream>>>(dj, (int)jobs.size(), nself, selfv);
+    e = allow_dynamic_smem((const void*)fill_pair_ragged_kernel, smem);
+    if (e == cudaSuccess) {
+      fill_pair_ragged_kernel<<<(unsigned)ntiles, 256, smem, stream>>>(dj, (int)jobs.size(), selfv);
+      e = cudaGetLastError();
+    }
+  }
+  // geometries outside the pair-tiled fill (ground plane) take the per-entry kernel
+  const FreqParams* dfp = reinterpret_cast<const FreqParams*>(d + jbytes);
+  for (int i = 0; i < count && e == cudaSuccess; ++i) {
+    const Plan& p = *plans[i];
+    if (p.npls > 0 && !pair_tiled(p))
+      e = launch_fill(p, reinterpret_cast<const double*>(dfp + i), 1, z[i], ldz[i], 0, stream);
+  }
+  if (selfv) {
+    const cudaError_t fe = cudaFreeAsync(selfv, stream);
+    if (e == cudaSuccess) e = fe;
+  }
+  const cudaError_t fe = cudaFreeAsync(d, stream);
+  return e != cudaSuccess ? e : fe;
 }
 
 }  // namespace wmom

@@ -140,6 +140,11 @@ namespace wmom {
 // Fill launcher (fill.cu).
 cudaError_t launch_fill(const Plan& p, const double* d_ka, int nk, double2* z, long long ldz,
                         long long zstride, cudaStream_t stream);
+// Fills count matrices of as many geometries, one wave number each, z[i] with
+// leading dimension ldz[i]: every pair-tiled geometry in one launch, the others
+// (ground plane) by the per-entry kernel.
+cudaError_t launch_fill_geometries(const Plan* const* plans, const double* ka, double2* const* z,
+                                   const long long* ldz, int count, cudaStream_t stream);
 // True when batches of frequencies are filled with one CTA per tile for all of them.
 bool fill_multi_fits(const Plan& p);
 // Lets `func` launch with up to `bytes` of dynamic shared memory.  The cap is process-

@@ -65,6 +65,19 @@ def test_no_device_calls_fail_cleanly_without_gpu(wmom):
     assert e.value.status in (2, 8)
 
 
+def test_fill_geometries_rejects_bad_arguments(wmom):
+    """Argument checks of wmom_fill_geometries come before any device call."""
+    import ctypes
+    f = wmom._fill_geometries
+    ka = (ctypes.c_double * 1)(1.0)
+    ptr = (ctypes.c_void_p * 1)(1)
+    ld = (ctypes.c_longlong * 1)(4)
+    plans = (ctypes.c_void_p * 1)(None)
+    assert f(plans, 0, ka, ptr, ld, None) == 1          # count 0
+    assert f(None, 1, ka, ptr, ld, None) == 1           # no plan array
+    assert f(plans, 1, ka, ptr, ld, None) == 1          # null plan
+
+
 def test_stats_classes_match_library(wmom):
     """The Python names of the stats classes and the library's class count agree
     (wmom_stats_read returns the number of classes and needs no GPU)."""

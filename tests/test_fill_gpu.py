@@ -93,6 +93,31 @@ def test_pair_tiled_fill_equals_per_entry_fill(cuda, wmom, geo):
     assert np.array_equal(zp, ze)
 
 
+def test_fill_of_uneven_geometries_in_one_call_equals_per_geometry_fill(cuda, wmom):
+    """Geometries of uneven size (free space, and one over a ground plane), one
+    frequency each, filled by one wmom_fill_geometries call: every matrix equals the
+    per-geometry fill bit for bit (same tile arithmetic, one ragged launch)."""
+    import torch
+    g = wmom.geometry
+    d = np.load(os.path.join(GOLDEN, "topology_bent_ground.npz"))
+    topos = [wmom.Topology(g.random_wires(300, seed=3)), wmom.Topology(g.dipole(1.0, 1e-3, 64)),
+             wmom.Topology(str(d["geo"]), ienv=2), wmom.Topology(g.grid(5, 1.0, 1.0, 5e-3, None, 3)),
+             wmom.Topology(g.random_wires(1000, seed=4))]
+    freqs = [3.0, 150.0, 30.0, 10.0, 0.5]
+    plans = [wmom.Plan(t) for t in topos]
+    try:
+        assert [p.fill_variant for p in plans].count("entry") == 1
+        zs = wmom.fill_geometries(plans, freqs)
+        for p, f, z in zip(plans, freqs, zs):
+            zr = p.fill([f])[0]
+            assert z.shape == zr.shape and torch.equal(z, zr), (p.npls, f)
+        with pytest.raises(ValueError):
+            wmom.fill_geometries(plans, freqs[:2])
+    finally:
+        for p in plans:
+            p.close()
+
+
 def test_ground_plane_uses_per_entry_fill(cuda, wmom):
     d = np.load(os.path.join(GOLDEN, "topology_bent_ground.npz"))
     plan = wmom.Plan(wmom.Topology(str(d["geo"]), ienv=2))
