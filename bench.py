@@ -564,7 +564,7 @@ def main():
                     choices=sorted(WORKLOADS) + ["serving", "geometries", "gemm_emul", "gemm_tc"])
     ap.add_argument("--k", type=int, default=96, help="inner dimension of the gemm_* workloads")
     ap.add_argument("--geometries", type=int, default=64)
-    ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--workers", type=int, default=6)  # best of 4/6/8/10 on the 64-geometry set
     ap.add_argument("--fp64-freqs", type=int, default=2)
     ap.add_argument("--nfreq", type=int, default=None,
                     help="use an evenly spaced subset of the workload's frequencies (profiling cases)")

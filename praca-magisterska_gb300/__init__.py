@@ -187,7 +187,8 @@ class Topology:
     """Reference topology arrays (configwire layout: 0-based storage, 1-based values,
     second columns at offset nsmax) built from the text of a .geo file."""
 
-    def __init__(self, geo_text, ienv=1, nsmax=NSMAX, nwmax=NWMAX):
+    def __init__(self, geo_text, ienv=1, nsmax=NSMAX, nwmax=NWMAX, listing=True):
+        """listing=False skips the configwire.txt text (self.listing is then None)."""
         self.nsmax = nsmax
         self.ienv = ienv
         self.x = np.zeros(nsmax, np.float32)
@@ -202,14 +203,14 @@ class Topology:
         t = _Topology(nsmax, 0, 0, 0, 0, _ptr(self.x, _fp), _ptr(self.y, _fp), _ptr(self.z, _fp),
                       _ptr(self.rad, _fp), _ptr(self.ipc, _ip), _ptr(self.ips, _ip), _ptr(self.ise, _ip),
                       _ptr(self.isp, _ip), _ptr(self.iwe, _ip))
-        cap = 1 << 24
-        listing = ctypes.create_string_buffer(cap)
+        cap = (1 << 24) if listing else 0
+        buf = ctypes.create_string_buffer(cap) if listing else None
         err = ctypes.create_string_buffer(512)
-        st = _topology_from_geo(geo_text.encode(), ienv, nsmax, nwmax, ctypes.byref(t), listing, cap, err, 512)
+        st = _topology_from_geo(geo_text.encode(), ienv, nsmax, nwmax, ctypes.byref(t), buf, cap, err, 512)
         if st != WMOM_OK:
             raise WmomError(st, "wmom_topology_from_geo: " + err.value.decode(errors="replace"))
         self.npnt, self.npls, self.nseg, self.nw = t.npnt, t.npls, t.nseg, t.nw
-        self.listing = listing.value.decode()
+        self.listing = buf.value.decode() if listing else None
         if ienv == 1:
             self.sgn = (1.0, 1.0, 1.0, 1.0)
         else:  # PEC ground at z = 0 (Wire_MoM.cu:107-122)

@@ -9,6 +9,7 @@
 // define every Z entry.  Index conventions are the reference's: arrays are stored
 // 0-based but hold 1-based node/segment/basis numbers; the second column of
 // ise/isp/ips/iwe lives at offset nsmax; ipc is negative for junction functions.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -396,9 +397,10 @@ extern "C" wmom_status wmom_topology_from_geo(const char* geo_text, int ienv, in
       topo->npls = t.npls;
       topo->nseg = t.nseg;
       topo->nw = g.nw;
-      if (listing && listing_cap) {
-        std::strncpy(listing, lst.c_str(), listing_cap - 1);
-        listing[listing_cap - 1] = 0;
+      if (listing && listing_cap) {  // truncated to listing_cap - 1 bytes, no padding
+        const size_t len = std::min(lst.size(), listing_cap - 1);
+        std::memcpy(listing, lst.data(), len);
+        listing[len] = 0;
       }
     }
   }

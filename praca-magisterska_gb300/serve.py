@@ -47,6 +47,9 @@ class Request:
         self.future = Future()
 
 
+_BUILDING = object()  # placeholder of a plan under construction
+
+
 class _Resident:
     """One factor set: some frequencies of one geometry."""
 
@@ -134,11 +137,29 @@ class Server:
 
     # ------------------------------------------------------------ internals ----
     def _plan(self, req):
-        ent = self._plans.get(req.geo_key)
-        if ent is None:
-            topo = self._w.Topology(req.geo_text, ienv=req.ienv)
+        """The geometry's (Topology, Plan), built once.  Builds of different geometries
+        run in parallel outside the server lock (parsing and table building are host
+        work of tens of ms); a request for a geometry being built waits for it."""
+        with self._lock:
+            while True:
+                ent = self._plans.get(req.geo_key)
+                if ent is None:
+                    self._plans[req.geo_key] = _BUILDING
+                    break
+                if ent is not _BUILDING:
+                    return ent
+                self._lock.wait(timeout=0.05)
+        try:
+            topo = self._w.Topology(req.geo_text, ienv=req.ienv, listing=False)
             ent = (topo, self._w.Plan(topo))
+        except BaseException:
+            with self._lock:
+                del self._plans[req.geo_key]
+                self._lock.notify_all()
+            raise
+        with self._lock:
             self._plans[req.geo_key] = ent
+            self._lock.notify_all()
         return ent
 
     def _per_matrix_bytes(self, n):
@@ -176,8 +197,7 @@ class Server:
                 req.future.set_exception(e)
 
     def _serve(self, req, sp):
-        with self._lock:
-            topo, plan = self._plan(req)
+        topo, plan = self._plan(req)
         n = topo.npls
         if not 0 < req.ngap <= n:
             raise ValueError("gap outside the geometry")

@@ -34,12 +34,17 @@ class FakeLib:
         self.fail_freq = None
         self.hold = {}        # ampl -> (entered Event, release Event): solve() waits there
         self.mu = threading.Lock()
+        self.topologies = []  # geometry name per Topology built
+        self.parse_s = 0.0    # host time of one Topology build
         lib = self
 
         class Topology:
-            def __init__(self, text, ienv=1):
+            def __init__(self, text, ienv=1, listing=True):
                 self.name, n = text.split()
                 self.npls = int(n)
+                with lib.mu:
+                    lib.topologies.append(self.name)
+                time.sleep(lib.parse_s)
 
         class Plan:
             def __init__(self, topo):
@@ -173,5 +178,23 @@ def test_waiting_requests_do_not_pin_each_others_sets():
         _check(f_d.result(timeout=10), [1.0, 2.0], 1.0)
         st = srv.stats()
         assert st["resident_bytes"] <= st["budget_bytes"] and st["evictions"] >= 1
+    finally:
+        srv.close()
+
+
+def test_plans_build_in_parallel_and_once_per_geometry():
+    """Plans of different geometries build concurrently, outside the server lock; two
+    requests for one geometry share one build."""
+    lib = FakeLib()
+    lib.parse_s = 0.3
+    srv = _server(lib, budget=_per_set(64, 16), workers=4)
+    try:
+        t0 = time.perf_counter()
+        futs = [srv.submit(serve.Request(f"{g} 64", [1.0], 1)) for g in ("a", "b", "c", "a")]
+        for f in futs:
+            _check(f.result(timeout=10), [1.0], 1.0)
+        dt = time.perf_counter() - t0
+        assert sorted(lib.topologies) == ["a", "b", "c"]
+        assert dt < 2 * lib.parse_s, dt   # serial builds would take 3 x 0.3 s
     finally:
         srv.close()
