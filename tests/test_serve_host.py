@@ -36,12 +36,15 @@ class FakeLib:
         self.mu = threading.Lock()
         self.topologies = []  # geometry name per Topology built
         self.parse_s = 0.0    # host time of one Topology build
+        self.bad_geometries = set()
         lib = self
 
         class Topology:
             def __init__(self, text, ienv=1, listing=True):
                 self.name, n = text.split()
                 self.npls = int(n)
+                if self.name in lib.bad_geometries:
+                    raise RuntimeError("bad geometry")
                 with lib.mu:
                     lib.topologies.append(self.name)
                 time.sleep(lib.parse_s)
@@ -196,5 +199,22 @@ def test_plans_build_in_parallel_and_once_per_geometry():
         dt = time.perf_counter() - t0
         assert sorted(lib.topologies) == ["a", "b", "c"]
         assert dt < 2 * lib.parse_s, dt   # serial builds would take 3 x 0.3 s
+    finally:
+        srv.close()
+
+
+def test_failed_plan_build_fails_alone_and_is_retried():
+    """A geometry whose plan build raises fails its request; the next request for it
+    builds again (no placeholder is left behind), and other geometries are served."""
+    lib = FakeLib()
+    lib.bad_geometries.add("x")
+    srv = _server(lib, budget=_per_set(64, 4), workers=2)
+    try:
+        with pytest.raises(RuntimeError):
+            srv.submit(serve.Request("x 64", [1.0], 1)).result(timeout=10)
+        _check(srv.submit(serve.Request("a 64", [1.0], 1)).result(timeout=10), [1.0], 1.0)
+        lib.bad_geometries.clear()
+        _check(srv.submit(serve.Request("x 64", [2.0], 1)).result(timeout=10), [2.0], 1.0)
+        assert lib.topologies == ["x", "a", "x"]
     finally:
         srv.close()
