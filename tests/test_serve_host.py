@@ -43,11 +43,11 @@ class FakeLib:
             def __init__(self, text, ienv=1, listing=True):
                 self.name, n = text.split()
                 self.npls = int(n)
-                if self.name in lib.bad_geometries:
-                    raise RuntimeError("bad geometry")
                 with lib.mu:
                     lib.topologies.append(self.name)
                 time.sleep(lib.parse_s)
+                if self.name in lib.bad_geometries:
+                    raise RuntimeError("bad geometry")
 
         class Plan:
             def __init__(self, topo):
