@@ -39,6 +39,29 @@ def test_library_exports_every_declared_symbol(wmom):
         getattr(lib, n)
 
 
+def _prototypes():
+    """name -> number of parameters of every function prototype in wmom.h."""
+    text = re.sub(r"/\*.*?\*/", " ", open(HDR).read(), flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(wmom_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_header_arity(wmom):
+    """Every ctypes binding of the Python package declares as many arguments as the
+    header's prototype of the same entry point."""
+    protos = _prototypes()
+    bound = {}
+    for v in vars(wmom).values():
+        if isinstance(v, ctypes._CFuncPtr) and v.__name__.startswith("wmom_") and v.argtypes is not None:
+            bound[v.__name__] = len(v.argtypes)
+    assert len(bound) >= 20
+    wrong = {n: (k, protos.get(n)) for n, k in bound.items() if protos.get(n) != k}
+    assert not wrong, wrong
+
+
 def test_dropin_cxx_symbols_have_reference_mangling(wmom):
     # the reference's own declarations mangle to these names (g++ Itanium ABI)
     exp = _exports()
