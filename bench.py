@@ -489,7 +489,7 @@ def _fill_all_geometries(w, pool, freqs, reps=3):
     launch per geometry (Plan.fill) against one ragged launch for all of them
     (fill_geometries); best of `reps`, CUDA events on the current stream."""
     import torch
-    plans = [w.Plan(w.Topology(g)) for g in pool]
+    plans = [w.Plan(w.Topology(g, listing=False)) for g in pool]
     fl = [float(f) for f in freqs]
 
     def timed(fn):
