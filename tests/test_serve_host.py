@@ -189,7 +189,7 @@ def test_plans_build_in_parallel_and_once_per_geometry():
     """Plans of different geometries build concurrently, outside the server lock; two
     requests for one geometry share one build."""
     lib = FakeLib()
-    lib.parse_s = 0.3
+    lib.parse_s = 0.5
     srv = _server(lib, budget=_per_set(64, 16), workers=4)
     try:
         t0 = time.perf_counter()
@@ -198,7 +198,7 @@ def test_plans_build_in_parallel_and_once_per_geometry():
             _check(f.result(timeout=10), [1.0], 1.0)
         dt = time.perf_counter() - t0
         assert sorted(lib.topologies) == ["a", "b", "c"]
-        assert dt < 2 * lib.parse_s, dt   # serial builds would take 3 x 0.3 s
+        assert dt < 2 * lib.parse_s, dt   # serial builds would take 3 x 0.5 s
     finally:
         srv.close()
 
