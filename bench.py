@@ -25,6 +25,7 @@ scaling, no collective in the data path); value = all ranks' solves / max time.
 """
 import argparse
 import importlib
+import importlib.util
 import json
 import os
 import statistics
@@ -36,6 +37,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+PKG = "praca-magisterska_gb300"
 N_DEFAULT = 8192
 SEED = 20261203
 METRIC = "freq-solves/s and p50/p99 latency: mixed+refine vs FP64 LU at rel err <=1e-10"
@@ -119,42 +121,66 @@ WORKLOADS = {
 }
 
 
+def _geometry():
+    """The workload generators: seeded numpy draws written as .geo text (the
+    reference's input format).  Loaded from their file on their own, so that the CPU
+    reference arm reads the same inputs without importing the product package."""
+    spec = importlib.util.spec_from_file_location("wmom_workload_geometry", os.path.join(ROOT, PKG, "geometry.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def workload(n, kind="sweep", nfreq=None):
-    w = importlib.import_module("praca-magisterska_gb300")
+    """(.geo text, float32 MHz frequencies, gap index) of a workload."""
+    import numpy as np
+    g = _geometry()
     if kind == "sweep":
-        topo = w.Topology(w.geometry.random_wires(n, seed=SEED))
-        freqs = w.geometry.sweep_freqs()
+        geo, freqs = g.random_wires(n, seed=SEED), g.sweep_freqs()
     elif kind == "precision":
-        topo = w.Topology(w.geometry.precision_grid(n))
-        freqs = w.geometry.sweep_freqs()
+        geo, freqs = g.precision_grid(n), g.sweep_freqs()
     elif kind == "batching":
-        topo = w.Topology(w.geometry.precision_grid(n))
-        freqs = w.geometry.log_freqs(0.001, 30.0, 256)
+        geo, freqs = g.precision_grid(n), g.log_freqs(0.001, 30.0, 256)
     else:
         raise ValueError(kind)
     if nfreq and nfreq < len(freqs):
         # evenly spaced subset of the sweep (small cases for the profiler)
-        import numpy as np
         freqs = freqs[np.unique(np.linspace(0, len(freqs) - 1, nfreq).round().astype(int))]
-    ngap = n // 2
-    return w, topo, freqs, ngap
+    return geo, freqs, n // 2
+
+
+def config_dict(kind, n, nf, ngap):
+    """The `config` object of both arms' lines: the same workload, the same keys."""
+    return {"workload": WORKLOADS[kind].format(n=n, nf=nf), "unknowns": n, "frequencies": nf, "seed": SEED,
+            "ngap": ngap, "refine_tol": 1e-12,
+            "l2": "inputs larger than L2 (each Z is %.2f GB)" % (16 * n * n / 1e9)}
+
+
+def oracle_topology(geo):
+    """Topology arrays of the CPU reference path (the oracle's restatement of the
+    reference's geoinp + configwire; no product library involved)."""
+    from oracle import build as ob
+    ob.build_port()
+    from oracle import oracle as orc
+    return orc.topology(geo)
 
 
 def cpu_solve_once(topo, freq, ngap, threads):
+    """One frequency of the reference's CPU path: oracle fill + LAPACK zgetrf/zgetrs."""
     from oracle import oracle as orc
     t0 = time.perf_counter()
-    i, zin, _ = orc.solve(topo.arrays(), float(freq), ngap, threads=threads)
+    i, zin, _ = orc.solve(topo, float(freq), ngap, threads=threads)
     return time.perf_counter() - t0, i, zin
 
 
 def run_reference(args):
-    """The reference's CPU path (oracle port: fill threaded over rows + LAPACK)."""
+    """The reference's CPU path (oracle port: fill threaded over rows + LAPACK), built
+    from the oracle alone: this arm never loads the product library."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    from oracle import build as ob
-    ob.build_port()
-    w, topo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
+    geo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
+    topo = oracle_topology(geo)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
     k = 0
@@ -167,13 +193,14 @@ def run_reference(args):
         t += dt
         k += 1
     value = args.steps / t
-    sample = (f"one frequency per step of the {len(freqs)}-frequency sweep (cycling), full N={topo.npls} "
+    n = topo["npls"]
+    sample = (f"one frequency per step of the {len(freqs)}-frequency sweep (cycling), full N={n} "
               "fill + zgetrf + zgetrs")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload].format(n=topo.npls, nf=len(freqs)),
-                       "unknowns": topo.npls, "frequencies": len(freqs), "seed": SEED},
+            "form": "FP64: oracle fill (reference zmatrix restated in C) + LAPACK zgetrf/zgetrs",
+            "config": config_dict(args.workload, n, len(freqs), ngap),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -187,7 +214,9 @@ def run_wmom(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    w, topo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
+    w = importlib.import_module(PKG)
+    geo, freqs, ngap = workload(args.n, args.workload, args.nfreq)
+    topo = w.Topology(geo)
     n = topo.npls
     nf = len(freqs)
     plan = w.Plan(topo)
@@ -265,6 +294,7 @@ def run_wmom(args):
 
     # plain FP64 form on the same systems (2 of the 12 frequencies) + agreement check
     fsub = np.array([freqs[0], freqs[-1]], np.float32) if args.fp64_freqs == 2 else freqs[:args.fp64_freqs]
+    plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=False)  # warm-up (and batch-width tuning)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     cur64, zin64, rep64 = plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=True)
@@ -332,9 +362,8 @@ def run_wmom(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 fill/residual, c64 tensor-core LU", "data": "synthetic (seeded random wires)",
-        "config": {"workload": WORKLOADS[args.workload].format(n=n, nf=nf) + ", mixed+refine",
-                   "unknowns": n, "frequencies": nf, "seed": SEED, "ngap": ngap, "refine_tol": 1e-12,
-                   "l2": "inputs larger than L2 (each Z is %.2f GB)" % (16 * n * n / 1e9)},
+        "form": "mixed+refine (precision form)",
+        "config": config_dict(args.workload, n, nf, ngap),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(sum(v["launches"] for v in launches.values())),
         "roofline": roof,
@@ -355,8 +384,7 @@ def run_wmom(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import build as ob
-        ob.build_port()
+        topo = oracle_topology(geo)  # the CPU path builds its own topology
         threads = os.cpu_count() or 1
         dt, i_cpu, zin_cpu = cpu_solve_once(topo, freqs[-1], ngap, threads)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",

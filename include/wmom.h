@@ -143,10 +143,11 @@ wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const
  * once running.  Same arguments and results as wmom_zgetrf; the factorisation's
  * scratch lives in a fixed 576 KiB __device__ array inside the library, held by every
  * GPU that loads the library until exit.  n above WMOM_NOALLOC_MAX_N returns
- * WMOM_ERR_ARG.  The first call on a device looks up the array's device address
- * (once per device); make that first call before any stream capture.  All calls
- * share the array: calls whose work overlaps on the GPU race and must be serialised
- * by the caller. */
+ * WMOM_ERR_ARG.  Each call looks up the array's device address on the current
+ * device (cudaGetSymbolAddress, which allocates nothing), so calls stay valid after
+ * a cudaDeviceReset.  The call synchronises `stream` to read the pivot status.  All
+ * calls share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller. */
 #define WMOM_NOALLOC_MAX_N 20480
 wmom_status wmom_zgetrf_noalloc(int n, void* a_dev, long long lda, int* ipiv_dev, int* info,
                                 void* stream);

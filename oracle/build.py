@@ -8,6 +8,11 @@
 
 Both use -ffp-contract=off so no multiply-add is fused, which keeps x86-64 and
 aarch64 builds bit-identical to each other.
+
+The reference checkout is found through WMOM_REFERENCE_DIR (or --reference-dir):
+the directory holding the reference's CPU variant ("wersja referencyjna").  Without
+it an existing oracle/_ref build is kept and nothing new is compiled from the
+reference.
 """
 import os
 import platform
@@ -15,7 +20,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("WMOM_REFERENCE_DIR", "/root/reference/wersja referencyjna")
+REF_DIR = os.environ.get("WMOM_REFERENCE_DIR") or None
 CUDA_INC = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/include"
 
 PORT_SO = os.path.join(HERE, "liboracle.so")
@@ -39,23 +44,27 @@ def _stamp(lib):
         f.write(platform.machine())
 
 
+PORT_SOURCES = ["wmom_oracle.c", "topology_oracle.c"]
+
+
 def build_port(force=False):
-    src = os.path.join(HERE, "wmom_oracle.c")
-    if not force and _newer(PORT_SO, [src]) and _arch_ok(PORT_SO):
+    srcs = [os.path.join(HERE, f) for f in PORT_SOURCES]
+    if not force and _newer(PORT_SO, srcs) and _arch_ok(PORT_SO):
         return PORT_SO
-    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", PORT_SO, src, "-lm"]
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", PORT_SO] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     _stamp(PORT_SO)
     return PORT_SO
 
 
 def reference_available():
-    return all(os.path.exists(os.path.join(REF_DIR, f)) for f in ("Zmatrix.cpp", "Configuration.cpp", "Complex.cpp"))
+    return bool(REF_DIR) and all(os.path.exists(os.path.join(REF_DIR, f))
+                                 for f in ("Zmatrix.cpp", "Configuration.cpp", "Complex.cpp"))
 
 
 def build_ref(force=False):
     if not reference_available():
-        return None
+        return REF_SO if os.path.exists(REF_SO) and _arch_ok(REF_SO) else None
     srcs = [os.path.join(REF_DIR, f) for f in ("Configuration.cpp", "Zmatrix.cpp", "Complex.cpp")]
     srcs.append(os.path.join(HERE, "ref_harness.cpp"))
     if not force and _newer(REF_SO, srcs) and _arch_ok(REF_SO):
@@ -69,6 +78,9 @@ def build_ref(force=False):
 
 
 def main():
+    global REF_DIR
+    if "--reference-dir" in sys.argv:
+        REF_DIR = sys.argv[sys.argv.index("--reference-dir") + 1]
     print(build_port(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
 

@@ -12,6 +12,9 @@ as the checker; never by the product library.
   aarch64; in the build container torch's MKL 2024.2 is used instead when
   available, see lapack_backend()).  zgetf2()/zgetrs() restate the unblocked
   algorithm in C for small pinning cases.
+* topology(): the reference's geoinp() + configwire() restated in C
+  (oracle/topology_oracle.c), so that the CPU reference path builds its topology
+  arrays without the product library.
 * ref_*(): the reference's own Configuration.cpp/Zmatrix.cpp compiled unmodified
   (oracle/_ref/libwmomref.so), present only where the reference checkout exists.
 """
@@ -49,6 +52,8 @@ def _load_port():
         _port.oracle_zgetf2.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip]
         _port.oracle_zgetrs.restype = None
         _port.oracle_zgetrs.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _dp]
+        _port.oracle_topology.restype = ctypes.c_int
+        _port.oracle_topology.argtypes = [ctypes.c_char_p] + [ctypes.c_int] * 5 + [_fp] * 4 + [_ip] * 6
     return _port
 
 
@@ -73,6 +78,34 @@ def _load_ref():
 
 def _p(a, t):
     return a.ctypes.data_as(t)
+
+
+# array capacities of the reference driver ("wersja referencyjna/Wire_MoM.cu":43-44)
+NNMAX, NTMAX, NWMAX, NSMAX = 3000, 5000, 10000, 30480
+TOPOLOGY_ERRORS = {1: "parse error", 2: "too many nodes", 3: "too many wires", 4: "too many patches",
+                   5: "node below a PEC ground", 6: "too many segments", 7: "too many basis functions",
+                   8: "out of memory"}
+
+
+def topology(geo_text, ienv=1, nsmax=NSMAX, nwmax=NWMAX):
+    """The reference's geoinp() + configwire() on the text of a .geo file: a dict with
+    x, y, z, rad, ipc (nsmax entries), ips, ise, isp, iwe (2*nsmax) in the reference
+    layout, npnt, npls, nseg, nw, nsmax and the sign quadruple of its environment."""
+    lib = _load_port()
+    out = dict(x=np.zeros(nsmax, np.float32), y=np.zeros(nsmax, np.float32), z=np.zeros(nsmax, np.float32),
+               rad=np.zeros(nsmax, np.float32), ipc=np.zeros(nsmax, np.int32), ips=np.zeros(2 * nsmax, np.int32),
+               ise=np.zeros(2 * nsmax, np.int32), isp=np.zeros(2 * nsmax, np.int32),
+               iwe=np.zeros(2 * nsmax, np.int32))
+    counts = np.zeros(4, np.int32)
+    rc = lib.oracle_topology(geo_text.encode(), ienv, nsmax, nwmax, NNMAX, NTMAX, _p(out["x"], _fp),
+                             _p(out["y"], _fp), _p(out["z"], _fp), _p(out["rad"], _fp), _p(out["ipc"], _ip),
+                             _p(out["ips"], _ip), _p(out["ise"], _ip), _p(out["isp"], _ip), _p(out["iwe"], _ip),
+                             _p(counts, _ip))
+    if rc != 0:
+        raise ValueError("oracle topology: " + TOPOLOGY_ERRORS.get(rc, str(rc)))
+    out.update(npnt=int(counts[0]), npls=int(counts[1]), nseg=int(counts[2]), nw=int(counts[3]), nsmax=nsmax,
+               ienv=ienv, sgn=(1.0, 1.0, 1.0, 1.0) if ienv == 1 else (1.0, 1.0, -1.0, -1.0))
+    return out
 
 
 def ka(freq_mhz):

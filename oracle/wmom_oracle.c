@@ -19,7 +19,7 @@
  *
  * Parity is pinned by tests/test_oracle_golden.py: against the Z_in values the
  * reference printed in its run logs, and against the reference's own zmatrix()
- * compiled from its sources (oracle/Makefile -> oracle/_ref/).
+ * compiled from its sources (recipe oracle/build.py -> oracle/_ref/).
  *
  * Compile with -ffp-contract=off so that x86-64 and aarch64 builds round the
  * same way (no fused multiply-add contraction).

@@ -15,10 +15,15 @@
 // it and must be serialised by the caller.  It keeps the last call's contents; the
 // parts that must start at zero (the barrier word, error flag and pivot info) are
 // cleared by each call with cudaMemsetAsync on the caller's stream.
+//
+// Host code cannot pass the array's name to a kernel (in host code it names a
+// host-side stand-in), so every call asks the runtime for its device address on the
+// current device with cudaGetSymbolAddress, which allocates nothing.  Asking on every
+// call rather than once keeps the address right after a cudaDeviceReset, which may
+// reload the library's device image at another address.
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "lu_common.cuh"
 #include "lu_internal.h"
@@ -30,18 +35,8 @@ namespace {
 // 576 KiB: the barrier header (256 B) plus the FP64 panel kernel's double-buffered
 // candidate staging for up to kMaxPanelBlocks blocks (about 520 KiB).
 constexpr size_t kScratchBytes = 576 * 1024;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_lu_scratch[kScratchBytes];
-
-// Device address of g_lu_scratch per device (host code cannot use the symbol itself:
-// in host code it names a host-side stand-in, not device memory).
-struct ScratchSlot {
-  bool ready;
-  void* addr;
-};
-ScratchSlot g_slots[kMaxDevices];
-std::mutex g_slots_mu;
 
 }  // namespace
 }  // namespace wmom
@@ -57,24 +52,10 @@ extern "C" wmom_status wmom_zgetrf_noalloc(int n, void* a_dev, long long lda, in
     return WMOM_ERR_ARG;
   }
   if (lu_workspace_bytes(16) > kScratchBytes) return WMOM_ERR_UNSUPPORTED;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return wmom_fail_cuda(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) return WMOM_ERR_UNSUPPORTED;
+  // the array's device address on the current device (see the file comment)
   void* scratch = nullptr;
-  {
-    // one-time set-up on this device (the current device): look up the array's
-    // device address; the first call per device does this
-    std::lock_guard<std::mutex> lk(g_slots_mu);
-    if (!g_slots[dev].ready) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_lu_scratch);
-      if (e != cudaSuccess) return wmom_fail_cuda(e, "cudaGetSymbolAddress(g_lu_scratch)");
-      g_slots[dev].addr = p;
-      g_slots[dev].ready = true;
-    }
-    scratch = g_slots[dev].addr;
-  }
+  cudaError_t e = cudaGetSymbolAddress(&scratch, g_lu_scratch);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "cudaGetSymbolAddress(g_lu_scratch)");
   cudaStream_t s = (cudaStream_t)stream;
   LuWorkspace ws{};
   ws.barrier = reinterpret_cast<GridBarrier*>(scratch);

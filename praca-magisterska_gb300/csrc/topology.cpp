@@ -357,6 +357,15 @@ int build_topology(const GeoInput& gin, int nsmax, int nwmax, int ienv, Topology
     out->iwe[i - 1] = iwe[i];
     out->iwe[i - 1 + nsmax] = iwe[i + nsmax];
   }
+  // The reference shifts both columns in place in one loop (Configuration.cpp:497-514):
+  // its first step overwrites the first column's entry nsmax with the second column's
+  // first entry before the last step moves it down, so slot nsmax - 1 of every
+  // two-column array ends up holding that entry.  No basis function or segment number
+  // reaches that slot; it is kept for drop-in callers that read whole arrays.
+  out->ise[nsmax - 1] = ise[nsmax + 1];
+  out->isp[nsmax - 1] = isp[nsmax + 1];
+  out->ips[nsmax - 1] = ips[nsmax + 1];
+  out->iwe[nsmax - 1] = iwe[nsmax + 1];
   return WMOM_OK;
 }
 

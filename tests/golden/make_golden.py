@@ -4,7 +4,7 @@ Run in a checkout that has the reference sources (the oracle's reference build,
 oracle/_ref/libwmomref.so, compiled by oracle/build.py from the reference's own
 Configuration.cpp / Zmatrix.cpp / Complex.cpp):
 
-    python tests/golden/make_golden.py [--reference-dir DIR]
+    python tests/golden/make_golden.py --reference-dir DIR
 
 Writes:
   zin_logs.json     every "Freq = f <re> <im>" line of the reference's run logs
@@ -71,7 +71,8 @@ def mkl_solve(z, v):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-dir", default="/root/reference")
+    ap.add_argument("--reference-dir", required=True,
+                    help="root of the reference checkout (the directory holding 'wersja referencyjna')")
     args = ap.parse_args()
     os.environ["WMOM_REFERENCE_DIR"] = os.path.join(args.reference_dir, "wersja referencyjna")
     from oracle import build as ob

@@ -4,8 +4,11 @@
   results_P_F_N.txt in all four program variants);
 * against the reference's own zmatrix() output and MKL currents (fixtures made by
   tests/golden/make_golden.py from the reference compiled unmodified);
-* the C restatement of LAPACK's unblocked LU against scipy's zgetrf.
+* the C restatement of LAPACK's unblocked LU against scipy's zgetrf;
+* the C restatement of the reference's geoinp + configwire (the topology of the CPU
+  reference path) against the reference's own config() arrays.
 """
+import glob
 import json
 import math
 import os
@@ -117,3 +120,47 @@ def test_ka_matches_reference_formula(orc, wmom):
         lam = c / float(np.float32(f)) * 1e-6
         assert orc.ka(f) == (math.pi + math.pi) / lam
         assert wmom.ka(f) == orc.ka(f)
+
+
+TOPO_NAMES = sorted(os.path.basename(p)[len("topology_"):-4]
+                    for p in glob.glob(os.path.join(GOLDEN, "topology_*.npz")))
+
+
+@pytest.mark.parametrize("name", TOPO_NAMES)
+def test_oracle_topology_matches_reference(orc, name):
+    """The oracle's topology equals the reference's config() output, bit for bit."""
+    d = np.load(os.path.join(GOLDEN, f"topology_{name}.npz"))
+    t = orc.topology(str(d["geo"]), ienv=int(d["ienv"]), nsmax=int(d["nsmax"]))
+    assert (t["npls"], t["nseg"], t["npnt"]) == (int(d["npls"]), int(d["nseg"]), int(d["npnt"]))
+    ns, npl, npnt, S = t["nseg"], t["npls"], t["npnt"], t["nsmax"]
+    for k in ("x", "y", "z"):
+        assert np.array_equal(t[k][:npnt], d[k]), k
+    assert np.array_equal(t["rad"][:ns], d["rad"])
+    assert np.array_equal(t["ipc"][:npl], d["ipc"])
+    assert np.array_equal(t["ips"][:npl], d["ips1"]) and np.array_equal(t["ips"][S:S + npl], d["ips2"])
+    assert np.array_equal(t["ise"][:ns], d["ise1"]) and np.array_equal(t["ise"][S:S + ns], d["ise2"])
+    assert np.array_equal(t["isp"][:ns], d["isp1"]) and np.array_equal(t["isp"][S:S + ns], d["isp2"])
+
+
+@pytest.mark.parametrize("kind", ["random_8192", "grid_8192", "random_14336", "ground"])
+def test_oracle_topology_equals_product_whole_arrays(orc, wmom, kind):
+    """Benchmark geometries: the oracle's arrays (the CPU reference path's) and the
+    product's host builder agree on every slot, so both arms of the benchmark solve
+    the same systems."""
+    g = wmom.geometry
+    text, ienv = {"random_8192": (g.random_wires(8192, seed=20261203), 1),
+                  "grid_8192": (g.precision_grid(8192), 1),
+                  "random_14336": (g.random_wires(14336, seed=20261203), 1),
+                  "ground": (g.geo_text([(0, 0, 0), (0, 0, 1.0), (1.0, 0, 1.0)],
+                                        [(1, 2, 1e-3, 20), (2, 3, 1e-3, 20)]), 2)}[kind]
+    a = wmom.Topology(text, ienv=ienv, listing=False)
+    b = orc.topology(text, ienv=ienv)
+    assert (a.npls, a.nseg, a.npnt) == (b["npls"], b["nseg"], b["npnt"])
+    for k in ("x", "y", "z", "rad", "ipc", "ips", "ise", "isp", "iwe"):
+        assert np.array_equal(getattr(a, k), b[k]), k
+
+
+@pytest.mark.parametrize("text", ["c\nc\n", "c\nc\n2\n0 0 0\n", "c\nc\n4000\n"])
+def test_oracle_topology_rejects_bad_input(orc, text):
+    with pytest.raises(ValueError):
+        orc.topology(text)

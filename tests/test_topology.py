@@ -59,3 +59,21 @@ def test_segment_limit(wmom):
     text = wmom.geometry.dipole(1.0, 1e-3, 200)
     with pytest.raises(wmom.WmomError):
         wmom.Topology(text, nsmax=150, nwmax=10)
+
+
+def test_whole_arrays_match_the_reference_build(wmom, orc):
+    """Every slot of the product's arrays, including the ones no basis function
+    reaches (the reference's in-place shift leaves the second column's first entry in
+    slot nsmax - 1), against the reference's own config() compiled here.  The last
+    slot of each array is left out: the reference reads one entry past its array
+    there."""
+    if not orc.ref_available():
+        pytest.skip("the reference's own build (oracle/_ref) exists only where the reference checkout is")
+    g = wmom.geometry
+    for text, ienv in ((g.precision_grid(2048), 1), (g.random_wires(1024, seed=20261203), 1),
+                       (g.geo_text([(0, 0, 0), (0, 0, 1.0), (1.0, 0, 1.0)],
+                                   [(1, 2, 1e-3, 20), (2, 3, 1e-3, 20)]), 2)):
+        r = orc.ref_geometry(text, ienv=ienv)
+        t = wmom.Topology(text, ienv=ienv, nsmax=r["nsmax"], listing=False)
+        for k in ("x", "y", "z", "rad", "ipc", "ips", "ise", "isp", "iwe"):
+            assert np.array_equal(getattr(t, k)[:-1], r[k][:-1]), k
