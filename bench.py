@@ -206,6 +206,167 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _fixture(kind, n):
+    """Full-size reference results of a workload (tests/golden/large_<kind>_<n>.npz:
+    the reference's own fill + MKL currents, the extended-precision truth and
+    kappa_1), or None."""
+    import numpy as np
+    name = {"sweep": "random", "precision": "precision"}.get(kind)
+    p = os.path.join(ROOT, "tests", "golden", f"large_{name}_{n}.npz")
+    return dict(np.load(p)) if name and os.path.exists(p) else None
+
+
+def _rel(a, b):
+    import numpy as np
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def accuracy_vs_reference(freqs, cur_mixed, cur_fp64_by_freq, reports, fx):
+    """Per fixture frequency: both forms against the reference's fill + MKL currents
+    and against the truth of the reference's FP64 system, with kappa_1 (LAPACK's on
+    the reference's matrix and the device's estimate)."""
+    import numpy as np
+    out = {}
+    if fx is None:
+        return out
+    for k, f in enumerate(fx["freqs"]):
+        i = int(np.argmin(np.abs(freqs - f)))
+        if abs(float(freqs[i]) - float(f)) > 1e-6 * float(f):
+            continue
+        mkl, truth = fx["currents_mkl"][k], fx["truth"][k]
+        e = {"kappa1_lapack": float(fx["kappa1"][k]), "kappa1_device": reports[i].get("cond1"),
+             "tier": reports[i].get("tier"), "refinement_steps": reports[i]["iterations"],
+             "mixed_vs_mkl": _rel(cur_mixed[i], mkl), "mixed_vs_truth": _rel(cur_mixed[i], truth),
+             "mkl_vs_truth": float(fx["mkl_vs_truth"][k])}
+        c64 = cur_fp64_by_freq.get(float(f))
+        if c64 is not None:
+            e["fp64_vs_mkl"] = _rel(c64, mkl)
+            e["fp64_vs_truth"] = _rel(c64, truth)
+        out["%.6g MHz" % float(f)] = e
+    return out
+
+
+def time_sweep(w, plan, freqs, ngap, steps, warmup, mode, currents=False):
+    """Device-timed sweeps (CUDA events on the current stream around `steps` calls
+    after `warmup` untimed ones); returns (ms per step, reports of the last, host
+    latencies of each call)."""
+    import torch
+    for _ in range(warmup):
+        plan.solve(freqs, ngap, mode=mode, currents=False)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    lat, rep = [], None
+    e0.record()
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        _, _, rep = plan.solve(freqs, ngap, mode=mode, currents=currents)
+        lat.append(1e3 * (time.perf_counter() - t0))
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, rep, lat
+
+
+def e2e_sweep(w, topo, freqs, ngap, steps):
+    """End to end through the C ABI: a new plan (geometry tables uploaded), the sweep,
+    currents to the host, per step.  Returns (freq-solves/s, h2d, d2h bytes per step,
+    currents, reports of the last step)."""
+    import torch
+    n, nf = topo.npls, len(freqs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        p2 = w.Plan(topo)
+        cur, _, rep = p2.solve(freqs, ngap, mode=w.MODE_MIXED, currents=True)
+        up = p2.upload_bytes
+        p2.close()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    iters = sum(r["iterations"] for r in rep)
+    h2d = up + 4 * nf + 3 * 8 * nf + 16 * n          # tables, frequencies, k params, excitation
+    d2h = 16 * n * nf + 32 * (iters + nf) + 16 * nf  # currents, residual norms, factor status
+    return nf * steps / dt, h2d, d2h, cur, rep
+
+
+def fp64_leg(w, plan, freqs, ngap):
+    """The plain FP64 form on the lowest and highest frequency, warmed up once (batch
+    width tuned), then timed once; returns (freq-solves/s, {freq: currents}, reports)."""
+    import numpy as np
+    import torch
+    fsub = np.array([freqs[0], freqs[-1]], np.float32)
+    plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cur64, _, rep64 = plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return len(fsub) / dt, {float(f): cur64[j] for j, f in enumerate(fsub)}, rep64
+
+
+def tier_counts(reports):
+    return {str(t): sum(1 for r in reports if r.get("tier") == t) for t in (1, 2, 3)}
+
+
+def fill_roofline(plan, nf, avg_ms, entries, fp64_peak, peaks, cap):
+    """The fill kernel against the FP64 pipe: achieved = the FP64 flops the kernel
+    executes (2 DFMA + DADD + DMUL thread instructions per launch, counted by ncu on a
+    smaller case and scaled by this launch's (observation, source) pairs) / launch
+    time; peak = the FMA-chain probe of this device."""
+    pairs = plan.fill_pairs / float(plan.npls) ** 2
+    flops_per_pair_freq = cap["fp64_flops"] / (cap["units"] * cap["pairs_per_entry"])
+    flops = flops_per_pair_freq * pairs * entries
+    achieved = flops / (avg_ms / 1e3) / 1e12
+    alg = 16.0 * entries  # each complex128 entry written once
+    return {"kernel": "fill_pair_multi_kernel" if plan.multi_frequency_fill and nf > 1 else "fill_pair_kernel",
+            "bound": "fp64", "unit": "TFLOP/s", "achieved": achieved, "peak": fp64_peak,
+            "frac": achieved / fp64_peak,
+            "peak_source": "measured: FP64 FMA-chain probe on this device in this run (wmom_probe_fp64_tflops, "
+                           "2 flop per DFMA); MEASURED_PEAKS.json has no FP64 figure",
+            "work": "executed FP64 flops: %.1f per (pair, frequency) x %.4f pairs per entry x %d entries (2 DFMA "
+                    "+ DADD + DMUL thread instructions from the ncu capture of profiles/dram_traffic.json)"
+                    % (flops_per_pair_freq, pairs, entries),
+            "fp64_pipe_busy_ncu": cap.get("fp64_pipe_busy"),
+            "hbm_view": {"algorithmic_bytes": alg, "achieved_gbs": alg / (avg_ms / 1e3) / 1e9,
+                         "frac_of_hbm": alg / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"]}}
+
+
+def precision_leg(w, args):
+    """The precision configuration (20 x 20 m junction grid, N = 8192, 12 frequencies
+    10 kHz - 10 MHz): device value, e2e, the FP64 form's rate, tiers, and per
+    frequency kappa_1 (device estimate) plus, at the fixture frequencies, the errors
+    against the reference's fill + MKL and against the truth."""
+    import numpy as np
+    n = 8192
+    geo, freqs, ngap = workload(n, "precision")
+    topo = w.Topology(geo, listing=False)
+    plan = w.Plan(topo)
+    steps = max(1, min(args.steps, 3))
+    ms, rep, _ = time_sweep(w, plan, freqs, ngap, steps, 2, w.MODE_MIXED)
+    value = len(freqs) / (ms / 1e3)
+    e2e_value, h2d, d2h, _, _ = e2e_sweep(w, topo, freqs, ngap, 1)
+    cur, _, repc = plan.solve(freqs, ngap, mode=w.MODE_MIXED, currents=True, condest=True)
+    fp64_value, cur64, _ = fp64_leg(w, plan, freqs, ngap)
+    plan.close()
+    per_f = [{"freq_mhz": float(f), "kappa1_device": r["cond1"], "tier": r["tier"],
+              "refinement_steps": r["iterations"], "rel_residual": r["rel_residual"]}
+             for f, r in zip(freqs, repc)]
+    return {"workload": WORKLOADS["precision"].format(n=n, nf=len(freqs)), "value": value, "unit": UNIT,
+            "steps": steps, "warmup": 2, "ms_per_step": ms,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "fp64_path": {"value": fp64_value, "unit": UNIT, "frequencies": 2,
+                          "speedup_mixed_over_fp64": value / fp64_value},
+            "tiers": tier_counts(rep), "per_frequency": per_f,
+            "vs_reference": accuracy_vs_reference(freqs, cur, cur64, repc, _fixture("precision", n))}
+
+
+def serving_leg(args, rate, seconds):
+    """One offered rate of the serving configuration (Poisson requests over seeded
+    random-wire geometries, N in [512, 6144], 1-16 frequencies in 1 kHz - 30 MHz, 30%
+    repeat excitations): p50/p99 latency, throughput and goodput."""
+    st = serve_rates(args, [rate], seconds)[0]
+    return st
+
+
 def run_wmom(args):
     import numpy as np
     import torch
@@ -276,33 +437,16 @@ def run_wmom(args):
     del os.environ["WMOM_NO_GRAPHS"]
 
     # end to end through the C ABI: geometry upload + solves + currents to host
-    e2e_steps = max(1, min(args.steps, 3))
     barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        p2 = w.Plan(topo)
-        cur, zin_e2e, rep_e2e = p2.solve(freqs, ngap, mode=w.MODE_MIXED, currents=True)
-        up = p2.upload_bytes
-        p2.close()
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = ws * nf * e2e_steps / e2e_s
-    iters = sum(r["iterations"] for r in rep_e2e)
-    h2d = up + 4 * nf + 3 * 8 * nf + 16 * n          # tables, frequencies, k params, excitation
-    d2h = 16 * n * nf + 32 * (iters + nf) + 16 * nf  # currents, residual norms, factor status
+    e2e_value, h2d, d2h, cur, rep_e2e = e2e_sweep(w, topo, freqs, ngap, max(1, min(args.steps, 3)))
+    e2e_value = ws * max_over_ranks(1.0 / e2e_value) ** -1
 
-    # plain FP64 form on the same systems (2 of the 12 frequencies) + agreement check
-    fsub = np.array([freqs[0], freqs[-1]], np.float32) if args.fp64_freqs == 2 else freqs[:args.fp64_freqs]
-    plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=False)  # warm-up (and batch-width tuning)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    cur64, zin64, rep64 = plan.solve(fsub, ngap, mode=w.MODE_FP64, currents=True)
-    torch.cuda.synchronize()
-    fp64_s = time.perf_counter() - t0
-    fp64_value = len(fsub) / fp64_s
-    idx = [int(np.argmin(np.abs(freqs - f))) for f in fsub]
-    rel = [float(np.linalg.norm(cur[i] - cur64[j]) / np.linalg.norm(cur64[j])) for j, i in enumerate(idx)]
+    # plain FP64 form on the same systems (lowest and highest frequency) + agreement,
+    # and one more mixed sweep with condition estimates for the accuracy record
+    fp64_value, cur64, rep64 = fp64_leg(w, plan, freqs, ngap)
+    cur_c, _, rep_c = plan.solve(freqs, ngap, mode=w.MODE_MIXED, currents=True, condest=True)
+    idx = {float(f): int(np.argmin(np.abs(freqs - f))) for f in cur64}
+    rel = [_rel(cur[idx[f]], c) for f, c in cur64.items()]
 
     # roofline of the dominant kernel class (per-launch device time from the instrumented step)
     peaks, peak_src = _peaks()
@@ -311,52 +455,47 @@ def run_wmom(args):
     d = st[dom]
     avg_ms = d["ms"] / max(d["timed"], 1)
     work_per_launch = d["work"] / max(d["timed"], 1)
-    if dom == "tc_gemm":
-        achieved = work_per_launch / (avg_ms / 1e3) / 1e12
-        roof = {"kernel": "cgemm_sub_tc_kernel", "bound": "tensor", "unit": "TFLOP/s",
-                "peak": peaks["bf16_tflops"], "peak_source": f"{peak_src} bf16 (TF32 nominal is half of it)"}
-    elif dom == "emul_gemm":
-        # 21 bf16 digit-plane products per complex FP64 product: issued tensor flops
-        achieved = 21.0 * work_per_launch / (avg_ms / 1e3) / 1e12
-        roof = {"kernel": "zgemm_sub_emul_kernel", "bound": "tensor", "unit": "TFLOP/s",
-                "peak": peaks["bf16_tflops"], "peak_source": f"{peak_src} bf16",
-                "note": "achieved counts the 21 bf16 plane products issued per FP64-grade product; the "
-                        "FP64-equivalent rate is achieved / 21"}
-    elif dom == "residual":
-        achieved = work_per_launch / (avg_ms / 1e3) / 1e9
-        roof = {"kernel": "gemv_partial_kernel", "bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"],
-                "peak_source": peak_src}
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            caps = json.load(f)
+    except (OSError, ValueError):
+        caps = {}
+    if dom == "fill":
+        entries = work_per_launch / 384.0  # the library counts the fill's launches in 384 flop-eq per entry
+        roof = fill_roofline(plan, nf, avg_ms, entries, fp64_peak, peaks, caps.get("fill_pair_multi_kernel"))
+        units = entries
     else:
-        achieved = work_per_launch / (avg_ms / 1e3) / 1e12
-        fill_kernel = "fill_pair_multi_kernel" if plan.multi_frequency_fill and nf > 1 else "fill_pair_kernel"
-        roof = {"kernel": {"fill": fill_kernel, "panel": "panel_cluster_kernel"}.get(dom, dom), "bound": "fp64",
-                "unit": "TFLOP/s", "peak": fp64_peak,
-                "peak_source": "FP64 FMA pipe, measured in this run by wmom_probe_fp64_tflops "
-                               "(MEASURED_PEAKS.json has no FP64 figure)"}
-    roof.update({"achieved": achieved, "frac": achieved / roof["peak"], "traffic": None,
-                 "avg_launch_ms": avg_ms, "launches": d["timed"],
+        if dom == "tc_gemm":
+            achieved = work_per_launch / (avg_ms / 1e3) / 1e12
+            roof = {"kernel": "cgemm_sub_tc_kernel", "bound": "tensor", "unit": "TFLOP/s",
+                    "peak": peaks["bf16_tflops"], "peak_source": f"{peak_src} bf16 (TF32 nominal is half of it)"}
+        elif dom == "emul_gemm":
+            # 21 bf16 digit-plane products per complex FP64 product: issued tensor flops
+            achieved = 21.0 * work_per_launch / (avg_ms / 1e3) / 1e12
+            roof = {"kernel": "zgemm_sub_emul_kernel", "bound": "tensor", "unit": "TFLOP/s",
+                    "peak": peaks["bf16_tflops"], "peak_source": f"{peak_src} bf16",
+                    "note": "achieved counts the 21 bf16 plane products issued per FP64-grade product; the "
+                            "FP64-equivalent rate is achieved / 21"}
+        elif dom == "residual":
+            achieved = work_per_launch / (avg_ms / 1e3) / 1e9
+            roof = {"kernel": "gemv_partial_kernel", "bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"],
+                    "peak_source": peak_src}
+        else:
+            achieved = work_per_launch / (avg_ms / 1e3) / 1e12
+            roof = {"kernel": {"panel": "panel_cluster_la_kernel"}.get(dom, dom), "bound": "fp64",
+                    "unit": "TFLOP/s", "peak": fp64_peak,
+                    "peak_source": "FP64 FMA pipe, measured in this run by wmom_probe_fp64_tflops"}
+        roof.update({"achieved": achieved, "frac": achieved / roof["peak"]})
+        units = {"tc_gemm": work_per_launch / (8.0 * 96),     # complex entries of C (K = 96)
+                 "emul_gemm": work_per_launch / (8.0 * 96)}.get(dom)
+    roof.update({"traffic": None, "avg_launch_ms": avg_ms, "launches": d["timed"],
                  "share_of_device_time": d["ms"] / max(sum(v["ms"] for v in st.values()), 1e-9)})
     # DRAM traffic per launch: bytes per unit from one ncu capture of a smaller case,
     # scaled by the units this launch processed (traffic grows in proportion)
-    units = {"fill": work_per_launch / 384.0,            # Z entries (384 flop-eq each)
-             "tc_gemm": work_per_launch / (8.0 * 96),     # complex entries of C (K = 96)
-             "emul_gemm": work_per_launch / (8.0 * 96)}.get(dom)  # complex entries of C (K = 96)
-    try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
-            cap = json.load(f).get(roof["kernel"].split("::")[-1])
-    except (OSError, ValueError):
-        cap = None
+    cap = caps.get(roof["kernel"].split("::")[-1])
     if cap and units:
         roof["traffic"] = cap["dram_bytes"] / cap["units"] * units
         roof["traffic_source"] = "ncu capture of a smaller case (%s), scaled by units" % cap["unit"]
-    if dom == "fill":
-        roof["note"] = ("achieved counts 384 flop-eq per entry (8 Green's-function evaluations, as the reference "
-                        "evaluates them); the pair-tiled kernel shares evaluations between neighbouring basis "
-                        "functions (about 2.1 per entry) and their geometry between frequencies, so the fraction "
-                        "can exceed 1; the FP64 pipe itself is 85% busy in the ncu capture")
-        alg = 16.0 * units  # each complex128 entry written once
-        roof["hbm_view"] = {"algorithmic_bytes": alg, "achieved_gbs": alg / (avg_ms / 1e3) / 1e9,
-                            "frac_of_hbm": alg / (avg_ms / 1e3) / 1e9 / peaks["hbm_gbs"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -367,50 +506,37 @@ def run_wmom(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(sum(v["launches"] for v in launches.values())),
         "roofline": roof,
-        "fp64_path": {"value": fp64_value, "unit": UNIT, "frequencies": len(fsub),
-                      "speedup_mixed_over_fp64": value / ws / fp64_value},
+        "fp64_path": {"value": fp64_value, "unit": UNIT, "frequencies": len(cur64),
+                      "speedup_mixed_over_fp64": value / ws / fp64_value,
+                      "timing": "one warm-up call, then one timed call of both frequencies"},
         "accuracy": {"max_rel_err_mixed_vs_fp64": max(rel),
                      "max_rel_residual": max(r["rel_residual"] for r in reports),
-                     "fallbacks": sum(r["fell_back"] for r in reports),
-                     "tier2_digit_plane_lu": sum(1 for r in reports if r.get("tier") == 2),
-                     "tier3_plain_fp64_lu": sum(1 for r in reports if r.get("tier") == 3),
+                     "tiers": tier_counts(reports),
                      "krylov_refined": sum(1 for r in reports if r.get("krylov_steps", 0) > 0),
-                     "max_krylov_steps": max(r.get("krylov_steps", 0) for r in reports),
-                     "max_refinement_steps": max(r["iterations"] for r in reports)},
+                     "max_refinement_steps": max(r["iterations"] for r in reports),
+                     "kappa1_device": [r["cond1"] for r in rep_c],
+                     "vs_reference": accuracy_vs_reference(freqs, cur_c, cur64, rep_c,
+                                                           _fixture(args.workload, n) if not args.nfreq else None)},
         "latency_ms": {"p50_sweep": statistics.median(step_ms), "p99_sweep": sorted(step_ms)[-1]},
         "kernel_ms_one_instrumented_step": {k: round(v["ms"], 3) for k, v in st.items()},
         "fill_pairs_per_entry": plan.fill_pairs / float(n * n),
         "lu_config": dict(zip(("batch", "span"), w.tuned_config(n, w.MODE_MIXED) or (None, None))),
         "clocks": clocks,
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        topo = oracle_topology(geo)  # the CPU path builds its own topology
-        threads = os.cpu_count() or 1
-        dt, i_cpu, zin_cpu = cpu_solve_once(topo, freqs[-1], ngap, threads)
-        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"1 of the 12 frequencies ({freqs[-1]:.4g} MHz), full N={n} fill + "
-                                          "zgetrf + zgetrs"}
-        j = fsub.tolist().index(freqs[-1]) if freqs[-1] in fsub else None
-        if j is not None:
-            line["accuracy"]["rel_err_fp64_vs_cpu_oracle"] = float(
-                np.linalg.norm(cur64[j] - i_cpu) / np.linalg.norm(i_cpu))
-            line["accuracy"]["rel_err_mixed_vs_cpu_oracle"] = float(
-                np.linalg.norm(cur[nf - 1] - i_cpu) / np.linalg.norm(i_cpu))
-        # every compared frequency against the CPU oracle: where the plain FP64 form and
-        # the oracle (two FP64 LUs in different summation orders) already disagree by
-        # more than 1e-10, the system's conditioning, not the method, sets the floor
-        per_f = {}
-        for jj, f in enumerate(fsub.tolist()):
-            i_ref = i_cpu if f == freqs[-1] else cpu_solve_once(topo, f, ngap, threads)[1]
-            nrm = np.linalg.norm(i_ref)
-            per_f["%.6g MHz" % f] = {
-                "fp64_vs_cpu_oracle": float(np.linalg.norm(cur64[jj] - i_ref) / nrm),
-                "mixed_vs_cpu_oracle": float(np.linalg.norm(cur[idx[jj]] - i_ref) / nrm),
-                "mixed_vs_fp64": rel[jj],
-                "fp64_rel_residual": float(rep64[jj]["rel_residual"]),
-                "mixed_fell_back": int(reports[idx[jj]]["fell_back"])}
-        line["accuracy"]["per_frequency"] = per_f
     plan.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        topo_o = oracle_topology(geo)  # the CPU path builds its own topology
+        threads = os.cpu_count() or 1
+        dt, i_cpu, _ = cpu_solve_once(topo_o, freqs[-1], ngap, threads)
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 of the {nf} frequencies ({freqs[-1]:.4g} MHz), full N={n} fill + "
+                                          "zgetrf + zgetrs"}
+        line["accuracy"]["cpu_oracle_%.6g_MHz" % freqs[-1]] = {
+            "mixed_vs_cpu_oracle": _rel(cur_c[nf - 1], i_cpu),
+            "fp64_vs_cpu_oracle": _rel(cur64[float(freqs[-1])], i_cpu)}
+    if rank == 0 and args.workload == "sweep" and not args.nfreq and not args.no_extra_legs:
+        line["precision_grid"] = precision_leg(w, args)
+        line["serving"] = serving_leg(args, args.serve_default_rate, args.serve_default_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -418,28 +544,29 @@ def run_wmom(args):
         dist.destroy_process_group()
 
 
-def run_serving(args):
-    """Serving configuration: Poisson request stream over a pool of seeded random-wire
-    geometries (N uniform in [nmin, nmax]), 1-16 frequencies per request drawn
-    log-uniformly from 64 values in 1 kHz - 30 MHz, 30% of the requests repeat an
-    earlier (geometry, frequencies) with a new gap/amplitude (resident factors).
-    Reports p50/p99 latency, throughput and goodput for each offered rate."""
+def serve_rates(args, rates, seconds):
+    """Poisson request streams over a pool of seeded random-wire geometries (N uniform
+    in [nmin, nmax]), 1-16 frequencies per request drawn log-uniformly from 64 values
+    in 1 kHz - 30 MHz, 30% of the requests repeating an earlier (geometry,
+    frequencies) with a new gap/amplitude (resident factors): one server per offered
+    rate, `seconds` of arrivals, then drained.  Returns the server's stats per rate
+    (p50/p99 latency, throughput, goodput within a 1 s objective)."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)
-    w = importlib.import_module("praca-magisterska_gb300")
-    serve = importlib.import_module("praca-magisterska_gb300.serve")
+    w = importlib.import_module(PKG)
+    serve = importlib.import_module(PKG + ".serve")
     rng = np.random.default_rng(SEED)
     pool = [w.geometry.random_wires(int(rng.integers(args.serve_nmin, args.serve_nmax + 1)), seed=SEED + i)
             for i in range(args.serve_geometries)]
     grid = w.geometry.log_freqs(0.001, 30.0, 64)
     results = []
-    for rate in args.serve_rates:
+    for rate in rates:
         warm = serve.Server(workers=1)  # warm-up: CUDA context, kernels, batch-width tuner
         warm.submit(serve.Request(pool[0], grid[:2], 1, currents=False)).result()
         warm.close()
         srv = serve.Server(workers=args.serve_workers)
-        t_end = time.perf_counter() + args.serve_seconds
+        t_end = time.perf_counter() + seconds
         history, futs = [], []
         t = time.perf_counter()
         while t < t_end:
@@ -457,8 +584,17 @@ def run_serving(args):
             f.result()
         st = srv.stats()
         srv.close()
-        st.update(offered_req_per_s=rate, submitted=len(futs))
+        st.update(offered_req_per_s=rate, submitted=len(futs), seconds=seconds,
+                  workload=f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}] over "
+                           f"{args.serve_geometries} geometries, 1-16 frequencies in 1 kHz-30 MHz, 30% repeat "
+                           f"excitations, {args.serve_workers} worker streams")
         results.append(st)
+    return results
+
+
+def run_serving(args):
+    """Serving configuration at each offered rate of --serve-rates."""
+    results = serve_rates(args, args.serve_rates, args.serve_seconds)
     line = {"metric": "serving: p50/p99 latency and freq-solves/s under a Poisson request stream",
             "unit": "freq-solves/s", "value": max(r["solves_per_s"] for r in results), "higher_is_better": True,
             "n_gpus": 1, "data": "synthetic (seeded random wires)",
@@ -598,6 +734,10 @@ def main():
     ap.add_argument("--nfreq", type=int, default=None,
                     help="use an evenly spaced subset of the workload's frequencies (profiling cases)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra-legs", action="store_true",
+                    help="skip the precision-grid and serving sub-objects of the default run")
+    ap.add_argument("--serve-default-rate", type=float, default=40.0)
+    ap.add_argument("--serve-default-seconds", type=float, default=8.0)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2.0, 5.0, 10.0])
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-nmin", type=int, default=512)

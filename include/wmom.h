@@ -152,6 +152,21 @@ wmom_status wmom_zgetrs(int n, int nrhs, const void* a_dev, long long lda, const
 wmom_status wmom_zgetrf_noalloc(int n, void* a_dev, long long lda, int* ipiv_dev, int* info,
                                 void* stream);
 
+/* 1-norm of an n x n complex128 device matrix, max_j sum_i |a_ij| (LAPACK zlange
+ * with norm '1'; the moduli are summed in FP32, so the norm is good to about 1e-7,
+ * enough for a condition estimate).  Synchronises `stream`.  No reference
+ * counterpart (the reference estimates no condition number). */
+wmom_status wmom_zlange1(int n, const void* a_dev, long long lda, double* anorm, void* stream);
+
+/* LAPACK zgecon with norm '1' on device factors from wmom_zgetrf: *rcond = 1 /
+ * (anorm * est), est an estimate of ||A^-1||_1 by Higham's method (LAPACK zlacn2:
+ * solves with A and A^H, at most 5 of each plus one), anorm = ||A||_1 of the matrix
+ * before factoring (wmom_zlange1).  *rcond = 0 for anorm = 0.  Synchronises
+ * `stream`.  No reference counterpart (the reference only checks zgetrf's info,
+ * REF/Wire_MoM.cu:372-377). */
+wmom_status wmom_zgecon(int n, const void* a_dev, long long lda, const int* ipiv_dev, double anorm,
+                        double* rcond, void* stream);
+
 /* Host-buffer drop-in for LAPACKE_zgetrf + LAPACKE_zgetrs with one right-hand
  * side: z (n*n, overwritten by the factors), v (n), i_out (n), ipiv (n, 1-based). */
 wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, int* ipiv,
@@ -181,6 +196,13 @@ typedef enum wmom_mode {
                          iterative refinement, FP64 LU fallback when refinement stalls */
 } wmom_mode;
 
+/* OR'd into the mode of wmom_solve_sweep or wmom_factor: every result also carries
+ * an estimate of the 1-norm condition number of its matrix (wmom_report.cond1),
+ * ||Z||_1 times LAPACK zlacn2's estimate of ||Z^-1||_1 from the factors behind the
+ * result (the FP32 factors for tier 1, the FP64-grade ones for tiers 2 and 3).  It
+ * costs up to eleven more triangular-solve pairs per matrix. */
+#define WMOM_SOLVE_CONDEST 0x100
+
 /* Per-frequency result record. */
 typedef struct wmom_report {
   double rel_residual;  /* ||V - Z I||_2 / ||V||_2 of the returned currents (FP64) */
@@ -193,6 +215,8 @@ typedef struct wmom_report {
   int tier;             /* factors behind I: 1 FP32 tensor-core LU + FP64 refinement,
                            2 FP64 LU with tensor-core (digit-plane) trailing updates +
                            FP64 refinement, 3 plain FP64 LU; 0 for WMOM_MODE_FP64 */
+  double cond1;         /* estimated 1-norm condition number of Z with WMOM_SOLVE_CONDEST,
+                           else 0 */
 } wmom_report;
 
 /* Lumped series loads for the sweeps of this plan: Z[k-1, k-1] += r_ohm + j*2*pi*f*l_uh
@@ -271,6 +295,14 @@ wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void
  * WMOM_ERR_ARG when no sweep of that order has been tuned yet.  No reference
  * counterpart. */
 wmom_status wmom_tuned_config(int n, int mode, int* batch, int* span);
+
+/* ---------------------------------------------------------------- testing ---- */
+/* Test hook, not for production use: every grid barrier of the plain FP64 LU's
+ * cooperative panel kernels waits for `count` arrivals more than its blocks send,
+ * so that its bounded wait (2 s) runs out; the factorisation then returns
+ * WMOM_ERR_TIMEOUT without a device fault and the next call with count = 0 works.
+ * No reference counterpart. */
+void wmom_debug_panel_missing_arrivals(int count);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,8 @@
 """Build recipe for the oracle libraries (test infrastructure only).
 
-* oracle/liboracle.so  -- the C restatement in oracle/wmom_oracle.c (always built).
+* oracle/liboracle.so  -- the C restatements in oracle/wmom_oracle.c (fill, unblocked
+  LU) and oracle/topology_oracle.c (geoinp + configwire), and the double-double
+  residual of oracle/refine_oracle.c (always built).
 * oracle/_ref/libwmomref.so -- the reference's own Configuration.cpp, Zmatrix.cpp and
   Complex.cpp, compiled UNMODIFIED where they lie in the reference checkout, plus
   oracle/ref_harness.cpp.  Built only when that checkout is present (it is not on
@@ -44,7 +46,7 @@ def _stamp(lib):
         f.write(platform.machine())
 
 
-PORT_SOURCES = ["wmom_oracle.c", "topology_oracle.c"]
+PORT_SOURCES = ["wmom_oracle.c", "topology_oracle.c", "refine_oracle.c"]
 
 
 def build_port(force=False):
@@ -77,12 +79,37 @@ def build_ref(force=False):
     return REF_SO
 
 
+DRIVER_OBJ = os.path.join(HERE, "_ref", "Wire_MoM.o")
+NVCC = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+
+
+def build_ref_driver(force=False):
+    """The reference's driver, "wersja referencyjna/Wire_MoM.cu" (its main() and GPU
+    fill kernels), compiled UNMODIFIED into oracle/_ref/Wire_MoM.o with the stand-in
+    mkl.h / mpi.h of oracle/shim, for the test that links it against libwmom
+    instead of Configuration.cpp, Zmatrix.cpp and Complex.cpp."""
+    if not reference_available() or not os.path.exists(os.path.join(REF_DIR, "Wire_MoM.cu")):
+        return DRIVER_OBJ if os.path.exists(DRIVER_OBJ) and _arch_ok(DRIVER_OBJ) else None
+    srcs = [os.path.join(REF_DIR, f) for f in ("Wire_MoM.cu", "Wire_MoM.h")] + \
+        [os.path.join(HERE, "shim", f) for f in ("mkl.h", "mpi.h")]
+    if not force and _newer(DRIVER_OBJ, srcs) and _arch_ok(DRIVER_OBJ):
+        return DRIVER_OBJ
+    os.makedirs(os.path.dirname(DRIVER_OBJ), exist_ok=True)
+    cmd = [NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-w", "-Xcompiler", "-fpermissive",
+           "-I", os.path.join(HERE, "shim"), "-I", REF_DIR, "-c", os.path.join(REF_DIR, "Wire_MoM.cu"), "-o",
+           DRIVER_OBJ]
+    subprocess.check_call(cmd)
+    _stamp(DRIVER_OBJ)
+    return DRIVER_OBJ
+
+
 def main():
     global REF_DIR
     if "--reference-dir" in sys.argv:
         REF_DIR = sys.argv[sys.argv.index("--reference-dir") + 1]
     print(build_port(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_driver(force="--force" in sys.argv))
 
 
 if __name__ == "__main__":

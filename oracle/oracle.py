@@ -15,6 +15,10 @@ as the checker; never by the product library.
 * topology(): the reference's geoinp() + configwire() restated in C
   (oracle/topology_oracle.c), so that the CPU reference path builds its topology
   arrays without the product library.
+* residual_dd() / refine_truth(): residuals in about twice double precision
+  (oracle/refine_oracle.c) and iterative refinement with them, an extended-precision
+  "truth" of the solution of a given FP64 system, which separates a solver's own
+  error from the error the system's conditioning imposes on every FP64 solver.
 * ref_*(): the reference's own Configuration.cpp/Zmatrix.cpp compiled unmodified
   (oracle/_ref/libwmomref.so), present only where the reference checkout exists.
 """
@@ -52,6 +56,8 @@ def _load_port():
         _port.oracle_zgetf2.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip]
         _port.oracle_zgetrs.restype = None
         _port.oracle_zgetrs.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _dp]
+        _port.oracle_residual_dd.restype = None
+        _port.oracle_residual_dd.argtypes = [ctypes.c_int] + [_dp] * 6 + [ctypes.c_int]
         _port.oracle_topology.restype = ctypes.c_int
         _port.oracle_topology.argtypes = [ctypes.c_char_p] + [ctypes.c_int] * 5 + [_fp] * 4 + [_ip] * 6
     return _port
@@ -148,14 +154,85 @@ def lapack_backend():
     return "scipy"
 
 
-def lu_solve(z, v):
-    """I = Z^-1 V with LAPACK zgetrf + zgetrs (partial pivoting).  Returns (I, info)."""
+def lu_solve(z, v, return_factors=False):
+    """I = Z^-1 V with LAPACK zgetrf + zgetrs (partial pivoting).  Returns (I, info),
+    or (I, info, (lu, piv)) with return_factors."""
     from scipy.linalg import lapack
     lu, piv, info = lapack.zgetrf(np.asfortranarray(z), overwrite_a=0)
     if info < 0:
         raise ValueError("zgetrf argument error")
     x, info2 = lapack.zgetrs(lu, piv, np.asarray(v, np.complex128))
+    if return_factors:
+        return x, info, (lu, piv)
     return x, info
+
+
+def cond1(z, factors=None):
+    """kappa_1 of Z estimated by LAPACK zgecon from (lu, piv) of scipy's zgetrf, and
+    ||Z||_1 (zlange '1')."""
+    from scipy.linalg import lapack
+    zf = np.asfortranarray(z, np.complex128)
+    anorm = float(np.max(np.sum(np.abs(zf), axis=0)))
+    if factors is None:
+        lu, piv, _ = lapack.zgetrf(zf, overwrite_a=0)
+    else:
+        lu, piv = factors
+    rcond, info = lapack.zgecon(lu, anorm, norm="1")
+    return (1.0 / rcond if rcond > 0 else float("inf")), anorm
+
+
+def residual_dd(z, v, xh, xl=None, threads=1):
+    """(r_hi, r_lo): b - Z (xh + xl) in about twice double precision; Z (n, n)
+    complex128 (any memory order), v, xh, xl complex n-vectors."""
+    lib = _load_port()
+    zf = np.asfortranarray(z, np.complex128)
+    n = zf.shape[0]
+    v = np.ascontiguousarray(v, np.complex128)
+    xh = np.ascontiguousarray(xh, np.complex128)
+    xl = np.zeros(n, np.complex128) if xl is None else np.ascontiguousarray(xl, np.complex128)
+    rh = np.zeros(n, np.complex128)
+    rl = np.zeros(n, np.complex128)
+    lib.oracle_residual_dd(n, zf.ctypes.data_as(_dp), v.ctypes.data_as(_dp), xh.ctypes.data_as(_dp),
+                           xl.ctypes.data_as(_dp), rh.ctypes.data_as(_dp), rl.ctypes.data_as(_dp), threads)
+    return rh, rl
+
+
+def refine_truth(z, v, x0, factors=None, max_steps=30, threads=1):
+    """Solution of the FP64 system Z x = v to about 2^-106 relative: iterative
+    refinement from x0 with residuals in twice double precision (residual_dd), the
+    corrections solved with an FP64 LU (`factors` = scipy zgetrf (lu, piv) of Z or of
+    a matrix close to Z; computed here when None), x carried as a double-double.
+    Returns (x rounded to complex128, list of ||d|| / ||x|| per step)."""
+    from scipy.linalg import lapack
+    zf = np.asfortranarray(z, np.complex128)
+    if factors is None:
+        lu, piv, info = lapack.zgetrf(zf, overwrite_a=0)
+        if info != 0:
+            raise ValueError("zgetrf info %d" % info)
+    else:
+        lu, piv = factors
+    xh = np.array(x0, np.complex128, copy=True)
+    xl = np.zeros_like(xh)
+    hist = []
+    for _ in range(max_steps):
+        rh, _ = residual_dd(zf, v, xh, xl, threads)
+        d, info = lapack.zgetrs(lu, piv, rh)
+        # (xh, xl) += d, componentwise two-sum then renormalisation
+        s = xh + d
+        bb = s - xh
+        e = (xh - (s - bb)) + (d - bb)
+        lo = xl + e
+        hi = s + lo
+        xl = lo - (hi - s)
+        xh = hi
+        rel = float(np.linalg.norm(d) / max(np.linalg.norm(xh), 1e-300))
+        hist.append(rel)
+        # done: the correction is far below double precision, or it no longer
+        # shrinks at the level set by the double-double residual's own rounding
+        # (about kappa * 2^-106)
+        if rel <= 2.0 ** -80 or (len(hist) > 2 and rel > 0.5 * hist[-2] and rel < 2.0 ** -60):
+            break
+    return xh, hist
 
 
 def zin(v, i, ngap):

@@ -35,6 +35,7 @@ STATUS_NAMES = {
 }
 MODE_FP64 = 0
 MODE_MIXED = 1
+SOLVE_CONDEST = 0x100  # OR'd into a mode: estimate kappa_1 of every matrix (report "cond1")
 NSMAX = 30480   # array capacity of the reference driver (Wire_MoM.cu:44)
 NWMAX = 10000
 
@@ -63,7 +64,7 @@ class _Topology(ctypes.Structure):
 class _Report(ctypes.Structure):
     _fields_ = [("rel_residual", ctypes.c_double), ("iterations", ctypes.c_int),
                 ("fell_back", ctypes.c_int), ("info", ctypes.c_int), ("status", ctypes.c_int),
-                ("krylov_steps", ctypes.c_int), ("tier", ctypes.c_int)]
+                ("krylov_steps", ctypes.c_int), ("tier", ctypes.c_int), ("cond1", ctypes.c_double)]
 
 
 def _sig(name, res, args):
@@ -95,6 +96,10 @@ _cgetrf = _sig("wmom_cgetrf", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlon
 _zgetrs = _sig("wmom_zgetrs", ctypes.c_int,
                [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_longlong, _vp, _vp, ctypes.c_longlong, _vp])
 _zgesv_like = _sig("wmom_zgesv_like", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _ip, _ip])
+_zlange1 = _sig("wmom_zlange1", ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _dp, _vp])
+_zgecon = _sig("wmom_zgecon", ctypes.c_int,
+               [ctypes.c_int, _vp, ctypes.c_longlong, _vp, ctypes.c_double, _dp, _vp])
+_debug_missing = _sig("wmom_debug_panel_missing_arrivals", None, [ctypes.c_int])
 _excitation = _sig("wmom_excitation", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, _dp])
 _solve_sweep = _sig("wmom_solve_sweep", ctypes.c_int,
                     [_vp, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int,
@@ -302,9 +307,13 @@ class Plan:
         self.fill_device(kas, z.data_ptr(), n, n * n, torch.cuda.current_stream().cuda_stream)
         return z
 
-    def solve(self, freqs_mhz, ngap, ampl=1.0, phas=0.0, mode=MODE_FP64, tol=1e-12, currents=True, stream=0):
+    def solve(self, freqs_mhz, ngap, ampl=1.0, phas=0.0, mode=MODE_FP64, tol=1e-12, currents=True, stream=0,
+              condest=False):
         """Fill, factor and solve per frequency.  Returns (currents (nfreq, npls) complex128
-        or None, zin (nfreq,) complex128, reports list of dicts)."""
+        or None, zin (nfreq,) complex128, reports list of dicts).  condest=True adds the
+        estimated 1-norm condition number of every matrix to its report ("cond1")."""
+        if condest:
+            mode |= SOLVE_CONDEST
         freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
         nf = len(freqs)
         cur = np.zeros((nf, self.npls), np.complex128) if currents else None
@@ -315,9 +324,12 @@ class Plan:
                           _ptr(zin.view(np.float64), _dp), reps, stream)
         if st not in (WMOM_OK, 3):
             raise WmomError(st, "wmom_solve_sweep")
-        reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
-                        info=r.info, status=r.status, krylov_steps=r.krylov_steps, tier=r.tier) for r in reps]
-        return cur, zin, reports
+        return cur, zin, _reports(reps)
+
+
+def _reports(reps):
+    return [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back, info=r.info,
+                 status=r.status, krylov_steps=r.krylov_steps, tier=r.tier, cond1=r.cond1) for r in reps]
 
 
 def fill_geometries(plans, freqs_mhz):
@@ -343,12 +355,13 @@ class Factors:
     """Z and its LU factors for a list of frequencies of one plan, resident on the
     device: new excitations of those (geometry, frequency) pairs only run solves."""
 
-    def __init__(self, plan, freqs_mhz, mode=MODE_MIXED, stream=0):
+    def __init__(self, plan, freqs_mhz, mode=MODE_MIXED, stream=0, condest=False):
         self.plan = plan  # keeps the plan alive
         self.freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
         self.mode = mode
         h = _vp()
-        _check(_factor(plan._h, _ptr(self.freqs, _fp), len(self.freqs), mode, ctypes.byref(h), stream), "wmom_factor")
+        _check(_factor(plan._h, _ptr(self.freqs, _fp), len(self.freqs), mode | (SOLVE_CONDEST if condest else 0),
+                       ctypes.byref(h), stream), "wmom_factor")
         self._h = h
         self.device_bytes = int(_factors_bytes(h))
 
@@ -363,9 +376,7 @@ class Factors:
                             _ptr(zin.view(np.float64), _dp), reps, stream)
         if st not in (WMOM_OK, 3):
             raise WmomError(st, "wmom_factors_solve")
-        reports = [dict(rel_residual=r.rel_residual, iterations=r.iterations, fell_back=r.fell_back,
-                        info=r.info, status=r.status, krylov_steps=r.krylov_steps, tier=r.tier) for r in reps]
-        return cur, zin, reports
+        return cur, zin, _reports(reps)
 
     def close(self):
         if self._h:
@@ -395,6 +406,27 @@ def cgetrf_device(a_ptr, n, lda, ipiv_ptr, stream=0):
     if st not in (WMOM_OK, 3):
         raise WmomError(st, "wmom_cgetrf")
     return info.value
+
+
+def zlange1_device(a_ptr, n, lda, stream=0):
+    """||A||_1 of an n x n complex128 device matrix (LAPACK zlange '1')."""
+    v = ctypes.c_double(0.0)
+    _check(_zlange1(n, a_ptr, lda, ctypes.byref(v), stream), "wmom_zlange1")
+    return v.value
+
+
+def zgecon_device(a_ptr, n, lda, ipiv_ptr, anorm, stream=0):
+    """LAPACK zgecon ('1' norm) on device factors from zgetrf_device: the reciprocal
+    condition estimate 1 / (anorm * est ||A^-1||_1)."""
+    v = ctypes.c_double(0.0)
+    _check(_zgecon(n, a_ptr, lda, ipiv_ptr, anorm, ctypes.byref(v), stream), "wmom_zgecon")
+    return v.value
+
+
+def debug_panel_missing_arrivals(count):
+    """Test hook: the plain FP64 LU's cooperative panel barriers wait for `count`
+    arrivals that never come (their bounded waits run out); 0 restores normal use."""
+    _debug_missing(int(count))
 
 
 def zgetrs_device(n, nrhs, a_ptr, lda, ipiv_ptr, b_ptr, ldb, stream=0):

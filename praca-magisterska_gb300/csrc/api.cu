@@ -387,6 +387,46 @@ wmom_status wmom_zgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* i
   return inf ? WMOM_ERR_SINGULAR : WMOM_OK;
 }
 
+wmom_status wmom_zlange1(int n, const void* a_dev, long long lda, double* anorm, void* stream) {
+  if (n <= 0 || !a_dev || lda < n || !anorm) return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* d = nullptr;
+  WMOM_CUDA_TRY(cudaMallocAsync(&d, sizeof(double), s));
+  cudaError_t e = norm1_batch(reinterpret_cast<const double2*>(a_dev), n, lda, 0, 1, d, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(anorm, d, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return wmom_fail_cuda(e, "wmom_zlange1");
+  return WMOM_OK;
+}
+
+wmom_status wmom_zgecon(int n, const void* a_dev, long long lda, const int* ipiv_dev, double anorm, double* rcond,
+                        void* stream) {
+  if (n <= 0 || !a_dev || lda < n || !ipiv_dev || !rcond || !(anorm >= 0.0)) return WMOM_ERR_ARG;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;
+  *rcond = 0.0;
+  if (anorm == 0.0) return WMOM_OK;  // LAPACK: rcond = 0 for a zero matrix
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(default_ws().mu);
+  LuWorkspace* ws = nullptr;
+  WMOM_CUDA_TRY(get_default_ws(n, 1, &ws));
+  WMOM_CUDA_TRY(lu_workspace_reset_barrier(ws, s));
+  double2* x = nullptr;
+  WMOM_CUDA_TRY(cudaMallocAsync(&x, sizeof(double2) * n, s));
+  const int slot = 0;
+  double est = 0.0;
+  const wmom_status st = condest_t<double2>(n, reinterpret_cast<const double2*>(a_dev), lda, 0, ipiv_dev, &slot, 1,
+                                            x, ws, s, &est);
+  cudaFreeAsync(x, s);
+  if (st != WMOM_OK) return st;
+  if (est > 0.0) *rcond = (1.0 / est) / anorm;
+  return WMOM_OK;
+}
+
+void wmom_debug_panel_missing_arrivals(int count) {
+  g_panel_missing_arrivals.store(count > 0 ? (unsigned)count : 0u, std::memory_order_relaxed);
+}
+
 wmom_status wmom_cgetrf(int n, void* a_dev, long long lda, int* ipiv_dev, int* info, void* stream) {
   if (n <= 0 || !a_dev || lda < n || !ipiv_dev) return WMOM_ERR_ARG;
   if ((size_t)n * sizeof(int) > 200 * 1024) return WMOM_ERR_ARG;
@@ -455,12 +495,15 @@ wmom_status wmom_zgesv_like(int n, double* z, const double* v, double* i_out, in
 wmom_status wmom_solve_sweep(wmom_plan h, const float* freq_mhz, int nfreq, int ngap, float ampl,
                              float phas_deg, int mode, double tol, double* currents, double* zin,
                              wmom_report* reports, void* stream) {
+  const bool condest = (mode & WMOM_SOLVE_CONDEST) != 0;
+  mode &= ~WMOM_SOLVE_CONDEST;
   if (!h || !freq_mhz || nfreq <= 0 || ngap < 1 || ngap > h->p.npls ||
       (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED))
     return WMOM_ERR_ARG;
   for (int i = 0; i < nfreq; ++i)
     if (!(freq_mhz[i] > 0.f) || !std::isfinite(freq_mhz[i])) return WMOM_ERR_ARG;
   SweepArgs a;
+  a.condest = condest;
   a.plan = &h->p;
   a.freq_mhz = freq_mhz;
   a.nfreq = nfreq;
@@ -500,6 +543,8 @@ extern "C" {
 wmom_status wmom_factor(wmom_plan h, const float* freq_mhz, int nfreq, int mode, wmom_factors* out, void* stream) {
   if (!out) return WMOM_ERR_ARG;
   *out = nullptr;
+  const bool condest = (mode & WMOM_SOLVE_CONDEST) != 0;
+  mode &= ~WMOM_SOLVE_CONDEST;
   if (!h || !freq_mhz || nfreq <= 0 || (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED)) return WMOM_ERR_ARG;
   for (int i = 0; i < nfreq; ++i)
     if (!(freq_mhz[i] > 0.f) || !std::isfinite(freq_mhz[i])) return WMOM_ERR_ARG;
@@ -520,6 +565,7 @@ wmom_status wmom_factor(wmom_plan h, const float* freq_mhz, int nfreq, int mode,
   f->plan = h;
   f->fs.plan = &h->p;
   f->fs.mode = mode;
+  f->fs.condest = condest;
   f->fs.freq.assign(freq_mhz, freq_mhz + nfreq);
   f->fs.ws = &f->ws;
   f->bytes = need + (size_t)nfreq * n * sizeof(int);

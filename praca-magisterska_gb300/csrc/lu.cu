@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstddef>
 #include <cstdlib>
@@ -37,6 +38,10 @@
 #include "wmom_internal.h"
 
 namespace wmom {
+
+// Test hook (wmom_debug_panel_missing_arrivals): extra arrivals every cooperative
+// panel's grid barrier waits for and never gets, so that its bounded wait runs out.
+std::atomic<unsigned int> g_panel_missing_arrivals{0};
 
 // ------------------------------------------------------------- panel ----
 template <typename C, int NB>
@@ -957,7 +962,9 @@ __global__ void laswp_kernel(C* __restrict__ A, long long lda, int ncols, int j_
   C* col = A + (size_t)c * lda;
   for (int i = 0; i < kn; ++i) {
     const int p = piv[i];
-    if (p != k0 + i) {
+    // a pivot outside the matrix is left alone: after a panel gave up on a timed-out
+    // wait its later pivots were never written and hold what the buffer held
+    if (p != k0 + i && p >= 0 && p < n) {
       const C t = col[k0 + i];
       col[k0 + i] = col[p];
       col[p] = t;
@@ -1351,6 +1358,201 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   if (tid == 0) st_release_i32(&flags[b], epoch);
 }
 
+// ------------------------------------------- conjugate-transpose trsv ----
+// Solves with the conjugate transposes of the factors, the second kind of solve of
+// the condition estimator (A^H x = b with P A = L U): U^H y = b by forward
+// substitution (U^H lower, diagonal conj(u_ii)), then L^H z = y by back substitution
+// (unit diagonal); lu_solve_h_t applies x = P^T z.  Row i of U^H or L^H is column i
+// of the factor storage, so a block's off-diagonal tiles are read along the factor's
+// columns (coalesced): thread (column q of the tile, row group g) keeps the partial
+// sums of its 16 rows g + 4i, reduced across the tile's columns once, after the last
+// tile.  Ticket order, ready flags and bounded waits are trsv_kernel's.
+constexpr int kTrsvLd = kTrsvB + 1;  // padded leading dimension of the diagonal tile
+
+template <typename C, bool LH>  // LH = false: U^H (forward); true: L^H (backward)
+__global__ void __launch_bounds__(256) trsv_h_kernel(const C* __restrict__ A, long long lda, int n, C* x,
+                                                     int* flags, unsigned int* ticket, int epoch, int* err,
+                                                     long long astride, int flag_stride,
+                                                     const int* __restrict__ sel) {
+  using R = decltype(C{}.x);
+  __shared__ C xs[kTrsvB];
+  __shared__ C part[2][kTrsvB];
+  __shared__ int s_b, s_m, s_ok;
+  __shared__ R dg_r[kTrsvB], dg_inv[kTrsvB];
+  __shared__ int dg_sw[kTrsvB];
+  const int tid = threadIdx.x;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  const int batch = (int)gridDim.x / nblk;
+  if (tid == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    const int bi = (int)(t / (unsigned)batch);
+    s_m = (int)(t % (unsigned)batch);
+    s_b = LH ? nblk - 1 - bi : bi;
+    s_ok = 1;
+  }
+  __syncthreads();
+  const int b = s_b;
+  if (b < 0 || b >= nblk) return;
+  const int mat = sel ? sel[s_m] : s_m;
+  A += (size_t)mat * astride;
+  x += (size_t)mat * n;
+  flags += (size_t)s_m * flag_stride;
+  const int r0 = b * kTrsvB;
+  const int rows = min(kTrsvB, n - r0);
+  // diagonal tile of T (T = U^H or L^H): Ds[c * kTrsvLd + q] = T[r0 + q][r0 + c]
+  // = conj(A[(r0 + q) * lda + r0 + c]), read along A's columns
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  C* Ds = reinterpret_cast<C*>(trsv_smem);
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int q = idx / kTrsvB, c = idx - q * kTrsvB;
+    C v = cmake<C>(0, 0);
+    if (q < rows && c < rows) {
+      const C a = A[(size_t)(r0 + q) * lda + r0 + c];
+      v = cmake<C>(a.x, -a.y);
+    }
+    Ds[c * kTrsvLd + q] = v;
+  }
+  if (!LH && tid < kTrsvB) {
+    // forward substitution with U^H divides by conj(u_cc): Smith's ratio and
+    // reciprocal of each diagonal entry, ahead of the waits
+    const int c = tid;
+    C d = cmake<C>(1, 0);
+    if (c < rows) {
+      const C a = A[(size_t)(r0 + c) * lda + r0 + c];
+      d = cmake<C>(a.x, -a.y);
+    }
+    if (fabs(d.x) >= fabs(d.y)) {
+      const R q = d.y / d.x;
+      dg_r[c] = q;
+      dg_inv[c] = R(1) / (d.x + d.y * q);
+      dg_sw[c] = 0;
+    } else {
+      const R q = d.x / d.y;
+      dg_r[c] = q;
+      dg_inv[c] = R(1) / (d.y + d.x * q);
+      dg_sw[c] = 1;
+    }
+  }
+  constexpr int kPer = kTrsvB / 4;
+  const int q = tid & (kTrsvB - 1), g = tid >> 6;
+  // this thread's entries of an off-diagonal tile: T[r0 + g + 4i][c0 + q]
+  // = conj(A[(r0 + g + 4i) * lda + c0 + q])
+  auto load_tile = [&](int j, C* dst) {
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int rr = g + 4 * i;
+      dst[i] = (rr < rows && q < cols) ? A[(size_t)(r0 + rr) * lda + c0 + q] : cmake<C>(0, 0);
+    }
+  };
+  C acc[kPer];
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) acc[i] = cmake<C>(0, 0);
+  const int nsteps = LH ? nblk - 1 - b : b;
+  C a_cur[kPer];
+  if (nsteps > 0) load_tile(LH ? nblk - 1 : 0, a_cur);
+  for (int step = 0; step < nsteps; ++step) {
+    const int j = LH ? nblk - 1 - step : step;
+    if (tid == 0) {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_i32(&flags[j]) != epoch) {
+        if (ld_volatile_i32(err) || global_ns() - t0 > kTrsvWaitNs) {
+          atomicExch(err, 1);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+    if (tid < cols) xs[tid] = __ldcg(&x[c0 + tid]);
+    __syncthreads();
+    C a_next[kPer];
+    if (step + 1 < nsteps) load_tile(LH ? j - 1 : j + 1, a_next);
+    if (q < cols) {
+      const C xq = xs[q];
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) acc[i] = cfms(acc[i], cmake<C>(a_cur[i].x, -a_cur[i].y), xq);
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) a_cur[i] = a_next[i];
+    __syncthreads();
+  }
+  // -sum over the tile columns of T x: each warp holds half of the columns for the
+  // rows of its group g
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    R re = acc[i].x, im = acc[i].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if ((tid & 31) == 0) part[q >> 5][g + 4 * i] = cmake<C>(re, im);
+  }
+  __syncthreads();
+  if (tid < 32) {
+    C s0 = cmake<C>(0, 0), s1 = cmake<C>(0, 0);
+    if (tid < rows) {
+      const C b0 = x[r0 + tid];
+      s0 = cmake<C>(b0.x + (part[0][tid].x + part[1][tid].x), b0.y + (part[0][tid].y + part[1][tid].y));
+    }
+    if (tid + 32 < rows) {
+      const int qq = tid + 32;
+      const C b1 = x[r0 + qq];
+      s1 = cmake<C>(b1.x + (part[0][qq].x + part[1][qq].x), b1.y + (part[0][qq].y + part[1][qq].y));
+    }
+    if (!LH) {
+      auto div_diag = [&](C a, int c) -> C {
+        const R qq = dg_r[c], inv = dg_inv[c];
+        return dg_sw[c] ? cmake<C>((a.x * qq + a.y) * inv, (a.y * qq - a.x) * inv)
+                        : cmake<C>((a.x + a.y * qq) * inv, (a.y - a.x * qq) * inv);
+      };
+      for (int c = 0; c < rows; ++c) {
+        if (c < 32) {
+          if (tid == c) s0 = div_diag(s0, c);
+        } else {
+          if (tid + 32 == c) s1 = div_diag(s1, c);
+        }
+        const R xr = __shfl_sync(0xffffffffu, c < 32 ? s0.x : s1.x, c & 31);
+        const R xi = __shfl_sync(0xffffffffu, c < 32 ? s0.y : s1.y, c & 31);
+        const C xc = cmake<C>(xr, xi);
+        if (tid > c && tid < rows) s0 = cfms(s0, Ds[c * kTrsvLd + tid], xc);
+        if (tid + 32 > c && tid + 32 < rows) s1 = cfms(s1, Ds[c * kTrsvLd + tid + 32], xc);
+      }
+    } else {
+      for (int c = rows - 1; c >= 0; --c) {
+        const R xr = __shfl_sync(0xffffffffu, c < 32 ? s0.x : s1.x, c & 31);
+        const R xi = __shfl_sync(0xffffffffu, c < 32 ? s0.y : s1.y, c & 31);
+        const C xc = cmake<C>(xr, xi);
+        if (tid < c && tid < rows) s0 = cfms(s0, Ds[c * kTrsvLd + tid], xc);
+        if (tid + 32 < c && tid + 32 < rows) s1 = cfms(s1, Ds[c * kTrsvLd + tid + 32], xc);
+      }
+    }
+    if (tid < rows) x[r0 + tid] = s0;
+    if (tid + 32 < rows) x[r0 + tid + 32] = s1;
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) st_release_i32(&flags[b], epoch);
+}
+
+// dst[c][perm[c][i]] = src[c][i]: x = P^T z for the vectors of a batch (column c of
+// the compact src goes to vector sel[c] of dst, or c)
+template <typename C>
+__global__ void scatter_rows_kernel(const C* __restrict__ src, C* __restrict__ dst, const int* __restrict__ perm,
+                                    int n, const int* __restrict__ sel) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i >= n) return;
+  const int p = perm[(size_t)c * n + i];
+  if (p >= 0 && p < n) dst[(size_t)(sel ? sel[c] : c) * n + p] = src[(size_t)c * n + i];
+}
+
 // ------------------------------------------------------- permutation ----
 // perm[i] = original row that ends up in row i after the interchanges ipiv[0..n).
 __global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm,
@@ -1676,7 +1878,9 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     long long ldap = lda, astr = astride;
     int np = n, j0p = jp, nbp = w, rpcp = pl.rpc;
     int* ipivp = ipiv;
-    unsigned int basep = bar_base;
+    // a test may make every barrier of this panel wait for arrivals that never come
+    // (bounded: the wait gives up and the factorisation reports a timeout)
+    unsigned int basep = bar_base + g_panel_missing_arrivals.load(std::memory_order_relaxed);
     void* args[] = {&Ap, &ldap, &np, &j0p, &nbp, &rpcp, &ipivp, &st, &gb, &basep, &astr};
     {
       stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
@@ -1865,6 +2069,49 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
 }
 
 template <typename C>
+cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B, LuWorkspace* ws, cudaStream_t s,
+                         int batch, long long astride, const int* sel) {
+  if (batch < 1 || batch > ws->max_batch || !ws->flags || n > ws->perm_cap) return cudaErrorInvalidValue;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
+  if ((size_t)n * batch * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  if (nblk > ws->flag_cap) return cudaErrorInvalidValue;
+  const size_t dsmem = sizeof(C) * kTrsvB * kTrsvLd;
+  cudaError_t e = allow_dynamic_smem((const void*)trsv_h_kernel<C, false>, dsmem);
+  if (e != cudaSuccess) return e;
+  e = allow_dynamic_smem((const void*)trsv_h_kernel<C, true>, dsmem);
+  if (e != cudaSuccess) return e;
+  e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
+  if (e != cudaSuccess) return e;
+  {
+    stats::Scope sc(stats::kTrsv, s, 8.0 * n * (double)n * batch, 2);
+    for (int pass = 0; pass < 2; ++pass) {
+      const int ep = ++ws->epoch;
+      e = cudaMemsetAsync(ws->ticket, 0, sizeof(unsigned int) * batch, s);
+      if (e != cudaSuccess) return e;
+      if (pass == 0)
+        trsv_h_kernel<C, false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                                 &ws->barrier->err, astride, ws->flag_cap, sel);
+      else
+        trsv_h_kernel<C, true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                                &ws->barrier->err, astride, ws->flag_cap, sel);
+    }
+  }
+  // x = P^T z: the row each entry of z came from
+  stats::count(stats::kMisc, 3);
+  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
+  C* tmp = reinterpret_cast<C*>(ws->rhs);
+  if (sel) {
+    gather_vecs_kernel<C><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(B, n, tmp, sel);
+  } else {
+    e = cudaMemcpyAsync(tmp, B, (size_t)n * batch * sizeof(C), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  scatter_rows_kernel<C><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(tmp, B, ws->perm, n, sel);
+  return cudaGetLastError();
+}
+
+template <typename C>
 int lu_max_batch(int n, bool fp64_cluster) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
@@ -1909,5 +2156,10 @@ template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const i
                                          LuWorkspace*, cudaStream_t, int, long long, const int*);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,
                                          LuWorkspace*, cudaStream_t, int, long long, const int*);
+template cudaError_t lu_solve_h_t<double2>(const double2*, long long, int, const int*, double2*, LuWorkspace*,
+                                           cudaStream_t, int, long long, const int*);
+template cudaError_t lu_solve_h_t<float2>(const float2*, long long, int, const int*, float2*, LuWorkspace*,
+                                          cudaStream_t, int, long long, const int*);
+
 
 }  // namespace wmom

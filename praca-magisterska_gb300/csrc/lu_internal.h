@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 
 namespace wmom {
@@ -70,6 +71,17 @@ template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
                        LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0,
                        const int* sel = nullptr);
+
+// Solves A^H x = b with the factors of lu_factor_t (the condition estimator's second
+// kind of solve), one right-hand side per matrix, vectors n apart; batch and sel as
+// lu_solve_t's.
+template <typename C>
+cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B, LuWorkspace* ws, cudaStream_t s,
+                         int batch = 1, long long astride = 0, const int* sel = nullptr);
+
+// Test hook: arrivals every cooperative panel barrier waits for in addition to its
+// blocks' own (0 in normal use).
+extern std::atomic<unsigned int> g_panel_missing_arrivals;
 
 // Workspace management (api.cu).
 cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch = 1);

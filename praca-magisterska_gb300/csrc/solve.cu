@@ -270,6 +270,7 @@ struct GroupScalars {
   double dnorm2[kMaxLuBatch];
   double xnorm2[kMaxLuBatch];
   double berr[kMaxLuBatch];    // componentwise backward errors of the second tier
+  double anorm[kMaxLuBatch];   // ||Z||_1 of the group's matrices (condition estimates)
   double vnorm2;
 };
 
@@ -742,7 +743,7 @@ wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws
 // mask, FP64 LU for the matrices that stall.
 wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float2* lu32, const double2* lu64,
                         const int* ipiv, const int* info, double tol, LuWorkspace* ws, GroupScratch& g,
-                        wmom_report* rep) {
+                        wmom_report* rep, bool condest) {
   const size_t nn = (size_t)n * n;
   cudaStream_t s = g.s;
   GroupScalars& hs = g.hs;
@@ -752,6 +753,19 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     rep[b].rel_residual = -1.0;
     rep[b].info = info[b];
   }
+  // condition estimates: ||Z||_1 now (read back with the next scalars), ||Z^-1||_1
+  // from the factors behind each matrix's solution once it is final
+  if (condest) SWEEP_TRY(norm1_batch(Z64, n, n, (long long)nn, bg, dsc->anorm, s));
+  auto estimate = [&](auto* lu, const int* piv, auto* X, const std::vector<int>& slots,
+                      const std::vector<int>& mats) -> wmom_status {
+    if (!condest || slots.empty()) return WMOM_OK;
+    std::vector<double> est(slots.size(), 0.0);
+    const wmom_status cs = condest_t(n, lu, (long long)n, (long long)nn, piv, slots.data(), (int)slots.size(), X, ws,
+                                     s, est.data());
+    if (cs != WMOM_OK) return cs;
+    for (size_t q = 0; q < slots.size(); ++q) rep[mats[q]].cond1 = hs.anorm[mats[q]] * est[q];
+    return WMOM_OK;
+  };
   if (mode == WMOM_MODE_FP64) {
     SWEEP_TRY(cudaMemcpyAsync(g.x64.p, g.vrep.p, sizeof(double2) * n * bg, cudaMemcpyDeviceToDevice, s));
     SWEEP_TRY(lu_solve_t<double2>(lu64, n, n, ipiv, g.x64.as<double2>(), n, 1, ws, s, bg, (long long)nn));
@@ -761,7 +775,10 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       rep[b].status = info[b] ? WMOM_ERR_SINGULAR : WMOM_OK;
       rep[b].rel_residual = std::sqrt(hs.rnorm2[b]) / g.vnorm;
     }
-    return WMOM_OK;
+    std::vector<int> all;
+    for (int b = 0; b < bg; ++b)
+      if (info[b] == 0) all.push_back(b);
+    return estimate(lu64, ipiv, g.r64.as<double2>(), all, all);
   }
   bool fallback[kMaxLuBatch] = {}, active[kMaxLuBatch] = {};
   int stall[kMaxLuBatch] = {};
@@ -938,6 +955,15 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       rep[b].status = WMOM_OK;
       rep[b].tier = 1;
     }
+  {
+    // tier 1: the FP32 factors (their estimate is kappa of the FP32-rounded Z, which
+    // refinement only reaches when kappa * u_fp32 < 1)
+    std::vector<int> t1;
+    for (int b = 0; b < bg; ++b)
+      if (!fallback[b]) t1.push_back(b);
+    const wmom_status cs = estimate(lu32, ipiv, g.d32.as<float2>(), t1, t1);
+    if (cs != WMOM_OK) return cs;
+  }
   // The matrices the FP32 factors could not serve get FP64-grade factors, batched
   // as wide as the plain FP64 form batches at this order (copies in the scratch
   // factor buffer, so that their panels run side by side).
@@ -1090,13 +1116,19 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
                                                                                    g.actv.as<int>());
         SWEEP_TRY(cudaGetLastError());
       }
+      std::vector<int> s2, m2;
       for (int j = 0; j < cn; ++j)
         if (!plain[j]) {
           const int b = fb[c0 + j];
           rep[b].tier = 2;
           rep[b].info = 0;
           rep[b].status = WMOM_OK;
+          s2.push_back(j);
+          m2.push_back(b);
         }
+      // before tier 3 reuses the scratch factors
+      const wmom_status cs = estimate(flu, fpiv, frr, s2, m2);
+      if (cs != WMOM_OK) return cs;
     }
     // tier 3: the chunk's remaining matrices, compacted into the scratch buffer
     int n3 = 0, idx3[kMaxLuBatch];
@@ -1112,6 +1144,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       if (fst != WMOM_OK) return fst;
       SWEEP_TRY(cudaMemcpyAsync(frr, g.vrep.p, sizeof(double2) * (size_t)n * n3, cudaMemcpyDeviceToDevice, s));
       SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, n3, (long long)nn));
+      std::vector<int> s3, m3;
       for (int i = 0; i < n3; ++i) {
         const int j = idx3[i], b = fb[c0 + j];
         SWEEP_TRY(cudaMemcpyAsync(fx + (size_t)j * n, frr + (size_t)i * n, sizeof(double2) * n,
@@ -1119,7 +1152,13 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         rep[b].tier = 3;
         rep[b].info = inf[i];
         rep[b].status = inf[i] ? WMOM_ERR_SINGULAR : WMOM_OK;
+        if (inf[i] == 0) {
+          s3.push_back(i);
+          m3.push_back(b);
+        }
       }
+      const wmom_status cs = estimate(flu, fpiv, frr, s3, m3);
+      if (cs != WMOM_OK) return cs;
     }
     for (int j = 0; j < cn; ++j)
       SWEEP_TRY(cudaMemcpyAsync(g.x64.as<double2>() + (size_t)fb[c0 + j] * n, fx + (size_t)j * n,
@@ -1388,7 +1427,7 @@ wmom_status run_sweep(const SweepArgs& a) {
                         &graph, cfg.span);
       if (st != WMOM_OK) return st;
       st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                       rep.data());
+                       rep.data(), a.condest);
       if (st != WMOM_OK) return st;
       st = group_results(g, bg, a.ngap, rep.data(), f0 + g0, a.currents, a.zin, a.reports, &overall);
       if (st != WMOM_OK) return st;
@@ -1447,7 +1486,7 @@ wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float a
     const float2* l32 = reinterpret_cast<const float2*>(fs->lu) + (size_t)f * nn;
     const double2* l64 = reinterpret_cast<const double2*>(fs->lu) + (size_t)f * nn;
     st = solve_group(fs->mode, n, fs->z64 + (size_t)f * nn, bg, mixed ? l32 : nullptr, mixed ? nullptr : l64,
-                     fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data());
+                     fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data(), fs->condest);
     if (st != WMOM_OK) return st;
     // results are indexed from `first` in the caller's arrays
     st = group_results(g, bg, ngap, rep.data(), f - first, currents, zin, reports, &overall);

@@ -23,6 +23,7 @@ struct SweepArgs {
   cudaStream_t stream = nullptr;
   LuWorkspace* ws = nullptr;
   size_t mem_budget = 0;  // bytes of device memory the sweep may use; 0 = automatic
+  bool condest = false;   // estimate kappa_1 of every matrix (wmom_report.cond1)
 };
 
 wmom_status run_sweep(const SweepArgs& a);
@@ -47,11 +48,23 @@ struct FactorSet {
   void* lu = nullptr;         // nf factors: float2 (mixed) or double2 (FP64)
   int* ipiv = nullptr;        // nf * n
   std::vector<int> info;
+  bool condest = false;       // estimate kappa_1 with every solve
 };
 
 wmom_status factors_build(FactorSet* fs, cudaStream_t s);
 wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
                           double* currents, double* zin, wmom_report* reports, cudaStream_t s);
+
+// Condition estimates (condest.cu).  condest_t: est[k] = an estimate of
+// ||A^-1||_1 for the factored matrices slots[0..m) (host list; matrix slot at
+// lu + slot * astride, pivots at ipiv + slot * n), by LAPACK zlacn2's algorithm with
+// batched solves; X holds one n-vector per slot (at X + slot * n) as scratch.
+template <typename C>
+wmom_status condest_t(int n, const C* lu, long long lda, long long astride, const int* ipiv, const int* slots, int m,
+                      C* X, LuWorkspace* ws, cudaStream_t s, double* est);
+// out_dev[b] = ||Z_b||_1 (maximum column sum of moduli) for nmat matrices zstride apart.
+cudaError_t norm1_batch(const double2* Z, int n, long long lda, long long zstride, int nmat, double* out_dev,
+                        cudaStream_t s);
 
 // Device helpers (solve.cu).
 // r[b] = v - Z[b] x[b] for nvec matrices zstride apart (vectors n apart), FP64;

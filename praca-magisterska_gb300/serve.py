@@ -91,6 +91,7 @@ class Server:
         self._reserved = 0        # bytes reserved by admitted requests still factoring
         self._stop = False
         self._latency = []
+        self._done_sizes = []     # frequencies of each completed request, in completion order
         self._solves = 0
         self._t0 = None
         self._t1 = None
@@ -124,14 +125,19 @@ class Server:
                 plan.close()
             self._plans.clear()
 
-    def stats(self):
+    def stats(self, slo_ms=1000.0):
+        """Completed requests, frequency-solves, throughput, p50/p99 latency, and
+        goodput: the frequency-solves per second of the requests that completed within
+        slo_ms of their arrival."""
         with self._lock:
             lat = sorted(self._latency)
             span = (self._t1 - self._t0) if self._t0 and self._t1 else 0.0
+            good = sum(nf for t, nf in zip(self._latency, self._done_sizes) if 1e3 * t <= slo_ms)
             out = {"requests": len(lat), "freq_solves": self._solves,
                    "solves_per_s": self._solves / span if span > 0 else 0.0,
                    "p50_ms": 1e3 * lat[len(lat) // 2] if lat else None,
                    "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+                   "slo_ms": slo_ms, "goodput_solves_per_s": good / span if span > 0 else 0.0,
                    "resident_bytes": self._used, "budget_bytes": self.budget, "evictions": self.evictions}
         return out
 
@@ -264,6 +270,7 @@ class Server:
             done = time.perf_counter()
             with self._lock:
                 self._latency.append(done - req.arrival)
+                self._done_sizes.append(len(freqs))
                 self._solves += len(freqs)
                 self._t1 = done
             req.future.set_result({"zin": zin, "currents": cur, "reports": reports,

@@ -113,8 +113,9 @@ def test_stats_classes_match_library(wmom):
 
 
 def test_report_layout_matches_header(wmom):
-    """wmom_report: a double and six ints (rel_residual, iterations, fell_back, info,
-    status, krylov_steps, tier), 32 bytes; the ctypes mirror has the same layout."""
+    """wmom_report: a double, six ints (rel_residual, iterations, fell_back, info,
+    status, krylov_steps, tier) and a double (cond1), 40 bytes; the ctypes mirror has
+    the same layout."""
     import ctypes
     import re
     from conftest import ROOT
@@ -122,4 +123,5 @@ def test_report_layout_matches_header(wmom):
     body = re.search(r"typedef struct wmom_report \{(.*?)\} wmom_report;", hdr, re.S).group(1)
     fields = re.findall(r"^\s*(double|int)\s+(\w+);", body, re.M)
     assert [n for _, n in fields] == [n for n, _ in wmom._Report._fields_]
-    assert ctypes.sizeof(wmom._Report) == 32
+    assert ctypes.sizeof(wmom._Report) == 40
+    assert wmom._Report.cond1.offset == 32

@@ -1,0 +1,83 @@
+"""Parity at the benchmark configurations' full sizes, against the reference itself.
+
+Fixtures (tests/golden/large_*.npz, made by tests/golden/make_golden_large.py): the
+reference's own zmatrix() fill solved by MKL zgetrf/zgetrs, an extended-precision
+truth of that FP64 system, and its kappa_1 (LAPACK zgecon on MKL's factors), for
+  * the 20 x 20 m junction grid at N = 8192 (the precision configuration), 10 kHz
+    and 10 MHz;
+  * the random-wire sweep at N = 4096 and N = 8192, 10 kHz and 10 MHz;
+  * the random-wire sweep at N = 14336, 10 MHz.
+Both forms run on the GPU with condition estimates.  Each result must lie within
+    max(tolerance, KAPPA_FACTOR * kappa_1 * 2^-53)
+of MKL's currents and of the truth, tolerance 1e-10 for the FP64 form and 1e-9 for
+the precision form: two backward-stable FP64 solvers agree only to about kappa * eps,
+so on well-conditioned systems the tolerance binds and on the low-frequency junction
+grid the conditioning does.  Where kappa is large, the truth of the GPU's own matrix
+(refined on the host from the GPU's Z) separates the solver's error from the part that
+the fill's last-bit differences contribute.  The device's condition estimate must be
+within a factor of 2 of LAPACK's on the reference's matrix.
+"""
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+EPS = 2.0 ** -53
+KAPPA_FACTOR = 64
+LARGE = sorted(glob.glob(os.path.join(GOLDEN, "large_*.npz")))
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("path", LARGE, ids=[os.path.basename(p)[6:-4] for p in LARGE])
+def test_full_size_parity_against_reference_and_truth(cuda, wmom, orc, path):
+    w = wmom
+    d = np.load(path)
+    kind, n = os.path.basename(path)[len("large_"):-4].rsplit("_", 1)
+    text = w.geometry.precision_grid(int(n)) if kind == "precision" else \
+        w.geometry.random_wires(int(n), seed=20261203)
+    assert hashlib.sha256(text.encode()).hexdigest() == str(d["geo_sha256"])
+    freqs = np.asarray(d["freqs"], np.float32)
+    ngap = int(d["ngap"])
+    plan = w.Plan(w.Topology(text, listing=False))
+    cur_m, zin_m, rep_m = plan.solve(freqs, ngap, mode=w.MODE_MIXED, tol=1e-12, condest=True)
+    cur_d, zin_d, rep_d = plan.solve(freqs, ngap, mode=w.MODE_FP64, condest=True)
+    threads = os.cpu_count() or 1
+    for k, f in enumerate(freqs):
+        kappa = float(d["kappa1"][k])
+        cond_bound = KAPPA_FACTOR * kappa * EPS
+        mkl, truth = d["currents_mkl"][k], d["truth"][k]
+        line = dict(freq=float(f), kappa1=kappa, kappa1_gpu=rep_d[k]["cond1"], tier=rep_m[k]["tier"])
+        for form, cur, rep, tol in (("mixed", cur_m, rep_m, 1e-9), ("fp64", cur_d, rep_d, 1e-10)):
+            bound = max(tol, cond_bound)
+            e_mkl, e_truth = _rel(cur[k], mkl), _rel(cur[k], truth)
+            line[f"{form}_vs_mkl"], line[f"{form}_vs_truth"] = e_mkl, e_truth
+            assert rep[k]["status"] == 0
+            assert e_mkl <= bound, (form, line)
+            assert e_truth <= bound, (form, line)
+            zref = complex(d["zin_mkl"][k])
+            zgot = complex((zin_m if form == "mixed" else zin_d)[k])
+            assert abs(zgot - zref) / abs(zref) <= bound, (form, zgot, zref)
+        assert kappa / 2.0 <= rep_d[k]["cond1"] <= 2.0 * kappa, line
+        assert kappa / 2.0 <= rep_m[k]["cond1"] <= 2.0 * kappa, line
+        if cond_bound > 1e-10:
+            # ill-conditioned: the truth of the GPU's own matrix, so that the solver's
+            # error and the fill's last-bit contribution are seen apart
+            z = plan.fill([float(f)])[0].cpu().numpy().T  # the GPU's Z, column-major
+            v = orc.excitation(int(n), ngap)
+            tg, _ = orc.refine_truth(z, v, cur_d[k], threads=threads)
+            del z
+            line["truth_gpu_vs_truth"] = _rel(tg, truth)
+            for form, cur, tol in (("mixed", cur_m, 1e-9), ("fp64", cur_d, 1e-10)):
+                line[f"{form}_vs_truth_gpu"] = _rel(cur[k], tg)
+                assert line[f"{form}_vs_truth_gpu"] <= max(tol, cond_bound), (form, line)
+        print(kind, n, line)
+    plan.close()

@@ -122,6 +122,32 @@ def test_dropin_zmatrix_symbol(cuda, wmom, orc):
     assert np.max(np.abs(cz - zr) / np.max(np.abs(zr), axis=0)) < 1e-13
 
 
+@pytest.mark.parametrize("ienv", [1, 2])
+def test_dropin_zmatrix_gpu_symbol(cuda, wmom, orc, ienv):
+    """The reference's GPU entry point (REF/Wire_MoM.h:49-51: host arrays in, host cz
+    out, its own argument order) called through its mangled name; free space and the
+    PEC-ground image terms."""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(wmom.__file__), "libwmom.so"))
+    f = getattr(lib, "_Z11zmatrix_gpuP7double2PfS1_S1_S1_PiS2_S2_idiiffff")
+    fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+    f.restype = None
+    f.argtypes = [ctypes.c_void_p, fp, fp, fp, fp, ip, ip, ip, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+    g = wmom.geometry
+    text = g.grid(4, 1.0, 1.0, 5e-3, None, 3) if ienv == 1 else \
+        g.geo_text([(0, 0, 0), (0, 0, 1.0), (1.0, 0, 1.0)], [(1, 2, 1e-3, 20), (2, 3, 1e-3, 20)])
+    topo = wmom.Topology(text, ienv=ienv)
+    n = topo.npls
+    cz = np.zeros((n, n), np.complex128, order="F")
+    p = lambda a, t: a.ctypes.data_as(t)
+    sg = topo.sgn
+    f(cz.ctypes.data, p(topo.x, fp), p(topo.y, fp), p(topo.z, fp), p(topo.rad, fp), p(topo.ipc, ip),
+      p(topo.ips, ip), p(topo.ise, ip), topo.nsmax, orc.ka(20.0), n, ienv, sg[0], sg[1], sg[2], sg[3])
+    zr = orc.fill(topo.arrays(), 20.0, ienv=ienv, sgn=sg)
+    assert np.max(np.abs(cz - zr) / np.max(np.abs(zr), axis=0)) < 1e-13
+
+
 def test_batch_width_does_not_change_results(cuda, wmom):
     # the same frequencies factored one matrix per launch and four per launch
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
