@@ -682,23 +682,32 @@ def run_gemm(args):
     """One trailing-update kernel alone (profiling cases): C -= A B for complex operands,
     m = n = --n, k = --k, through the C ABI on device-resident operands; W untimed then K
     timed calls, each bracketed by CUDA events.  gemm_emul: the FP64-grade digit-plane
-    update (complex128); gemm_tc: the 3xTF32 update of the FP32 factorisation (complex64)."""
+    update (complex128); gemm_tc: the 3xTF32 update of the FP32 factorisation
+    (complex64); gemm_simt / gemm_dmma: the plain FP64 form's update as SIMT DFMA or as
+    DMMA on the FP64 tensor pipe (complex128)."""
     import ctypes
     import torch
     torch.cuda.set_device(0)
     w = importlib.import_module("praca-magisterska_gb300")
     m = nn = args.n
     k = args.k
-    emul = args.workload == "gemm_emul"
-    dt = torch.complex128 if emul else torch.complex64
+    fp64 = args.workload in ("gemm_emul", "gemm_dmma", "gemm_simt")
+    dt = torch.complex128 if fp64 else torch.complex64
     g = torch.Generator(device="cuda").manual_seed(SEED)
     a = torch.randn(k, m, dtype=dt, device="cuda", generator=g)   # column-major m x k
     b = torch.randn(nn, k, dtype=dt, device="cuda", generator=g)  # column-major k x n
     c = torch.randn(nn, m, dtype=dt, device="cuda", generator=g)  # column-major m x n
-    f = w._lib.wmom_zgemm_sub_emul if emul else w._lib.wmom_cgemm_sub_tc
-    f.restype = ctypes.c_int
-    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_longlong] * 3 + [ctypes.c_void_p]
-    call = lambda: f(m, nn, k, a.data_ptr(), m, b.data_ptr(), k, c.data_ptr(), m, None)
+    if args.workload in ("gemm_dmma", "gemm_simt"):
+        f = w._lib.wmom_zgemm_sub_fp64
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_longlong] * 3 + [ctypes.c_int, ctypes.c_void_p]
+        variant = 1 if args.workload == "gemm_dmma" else 0
+        call = lambda: f(m, nn, k, a.data_ptr(), m, b.data_ptr(), k, c.data_ptr(), m, variant, None)
+    else:
+        f = w._lib.wmom_zgemm_sub_emul if args.workload == "gemm_emul" else w._lib.wmom_cgemm_sub_tc
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_longlong] * 3 + [ctypes.c_void_p]
+        call = lambda: f(m, nn, k, a.data_ptr(), m, b.data_ptr(), k, c.data_ptr(), m, None)
     for _ in range(args.warmup):
         assert call() == 0
     ms = []
@@ -712,8 +721,10 @@ def run_gemm(args):
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
     med = statistics.median(ms)
+    kernel = {"gemm_emul": "zgemm_sub_emul_kernel", "gemm_tc": "cgemm_sub_tc_kernel",
+              "gemm_dmma": "zgemm_sub_dmma_kernel", "gemm_simt": "gemm_sub_kernel<double2>"}[args.workload]
     print(json.dumps({"metric": "trailing-update GEMM, algorithmic complex TFLOP/s (8 m n k)",
-                      "kernel": "zgemm_sub_emul_kernel" if emul else "cgemm_sub_tc_kernel",
+                      "kernel": kernel,
                       "value": 8.0 * m * nn * k / (med / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_call": med,
                       "steps": args.steps, "warmup": args.warmup, "config": {"m": m, "n": nn, "k": k}}), flush=True)
 
@@ -726,7 +737,8 @@ def main():
     ap.add_argument("--impl", default="wmom", choices=["wmom", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--workload", default="sweep",
-                    choices=sorted(WORKLOADS) + ["serving", "geometries", "gemm_emul", "gemm_tc"])
+                    choices=sorted(WORKLOADS) + ["serving", "geometries", "gemm_emul", "gemm_tc", "gemm_dmma",
+                                                 "gemm_simt"])
     ap.add_argument("--k", type=int, default=96, help="inner dimension of the gemm_* workloads")
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--workers", type=int, default=6)  # best of 4/6/8/10 on the 64-geometry set
@@ -747,7 +759,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload in ("gemm_emul", "gemm_tc"):
+    if args.workload in ("gemm_emul", "gemm_tc", "gemm_dmma", "gemm_simt"):
         run_gemm(args)
     elif args.workload == "serving":
         run_serving(args)

@@ -189,6 +189,15 @@ wmom_status wmom_cgemm_sub_tc(int m, int n, int k, const void* a_dev, long long 
 wmom_status wmom_zgemm_sub_emul(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
                                 long long ldb, void* c_dev, long long ldc, void* stream);
 
+/* The plain FP64 form's trailing update: C -= A * B for complex FP64 (double2)
+ * column-major device matrices, C m x n, A m x k, B k x n.  variant 0: SIMT DFMA (the
+ * update the plain form uses by default); variant 1: DMMA, warp-level
+ * mma.m8n8k4.f64 on the FP64 tensor pipe (selected inside the LU by
+ * WMOM_FP64_UPDATE=dmma).  Synchronises `stream`.  No reference counterpart (the
+ * reference factors with MKL / cuBLAS); exposed for testing and timing. */
+wmom_status wmom_zgemm_sub_fp64(int m, int n, int k, const void* a_dev, long long lda, const void* b_dev,
+                                long long ldb, void* c_dev, long long ldc, int variant, void* stream);
+
 /* ----------------------------------------------------------- solver ---- */
 typedef enum wmom_mode {
   WMOM_MODE_FP64 = 0, /* plain form: FP64 fill, FP64 LU, FP64 solves */

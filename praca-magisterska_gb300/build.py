@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CPP_SOURCES = ["topology.cpp", "plan.cpp", "dropin.cpp"]
-CU_SOURCES = ["fill.cu", "lu.cu", "solve.cu", "api.cu", "lu_tc.cu", "lu_emul.cu", "stats.cu", "noalloc.cu", "condest.cu"]
+CU_SOURCES = ["fill.cu", "lu.cu", "solve.cu", "api.cu", "lu_tc.cu", "lu_emul.cu", "stats.cu", "noalloc.cu", "condest.cu", "lu_dmma.cu"]
 HEADERS = ["wmom_internal.h", "lu_common.cuh", "lu_internal.h", "solve_internal.h", "stats.h"]
 
 

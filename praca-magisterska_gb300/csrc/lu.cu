@@ -1177,6 +1177,15 @@ __global__ void __launch_bounds__(256) gemm_sub_kernel(const C* __restrict__ Am,
   }
 }
 
+cudaError_t zgemm_sub_simt(const double2* Am, long long lda, const double2* Bm, long long ldb, double2* Cm,
+                           long long ldc, int M, int N, int K, cudaStream_t s, int batch, long long bstride) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  stats::Scope sc(stats::kGemm, s, 8.0 * M * (double)N * K * batch);
+  dim3 grid((M + kGemmBM - 1) / kGemmBM, (N + kGemmBN - 1) / kGemmBN, batch);
+  gemm_sub_kernel<double2><<<grid, 256, 0, s>>>(Am, lda, Bm, ldb, Cm, ldc, M, N, K, bstride);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------------- trsv ----
 // One right-hand side, the whole triangular solve in ONE launch.  Each CTA owns a
 // block of 64 rows; it takes a ticket (atomicAdd) that fixes its block in
@@ -1932,6 +1941,8 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     const C* Bm = A + (size_t)c0 * lda + k0;
     C* Cm = A + (size_t)c0 * lda + r0;
     if (gemm_hook) return gemm_hook(ws, Am, lda, Bm, lda, Cm, lda, M, N, K, s, batch, astride);
+    if constexpr (std::is_same<C, double2>::value)
+      if (fp64_update_dmma()) return zgemm_sub_dmma(Am, lda, Bm, lda, Cm, lda, M, N, K, s, batch, astride);
     stats::Scope sc(stats::kGemm, s, 8.0 * M * (double)N * K * batch);
     dim3 grid((M + kGemmBM - 1) / kGemmBM, (N + kGemmBN - 1) / kGemmBN, batch);
     gemm_sub_kernel<C><<<grid, 256, 0, s>>>(Am, lda, Bm, lda, Cm, lda, M, N, K, astride);

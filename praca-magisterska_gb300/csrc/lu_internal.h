@@ -79,6 +79,16 @@ template <typename C>
 cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B, LuWorkspace* ws, cudaStream_t s,
                          int batch = 1, long long astride = 0, const int* sel = nullptr);
 
+// The plain FP64 form's trailing update, C -= A B for complex FP64 column-major
+// operands (`batch` matrices bstride apart): SIMT DFMA (gemm_sub_kernel, lu.cu) or
+// DMMA on the FP64 tensor pipe (lu_dmma.cu).  WMOM_FP64_UPDATE=dmma selects the
+// latter inside the plain form's LU.
+cudaError_t zgemm_sub_simt(const double2* Am, long long lda, const double2* Bm, long long ldb, double2* Cm,
+                           long long ldc, int M, int N, int K, cudaStream_t s, int batch, long long bstride);
+cudaError_t zgemm_sub_dmma(const double2* Am, long long lda, const double2* Bm, long long ldb, double2* Cm,
+                           long long ldc, int M, int N, int K, cudaStream_t s, int batch, long long bstride);
+bool fp64_update_dmma();
+
 // Test hook: arrivals every cooperative panel barrier waits for in addition to its
 // blocks' own (0 in normal use).
 extern std::atomic<unsigned int> g_panel_missing_arrivals;

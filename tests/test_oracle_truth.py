@@ -20,7 +20,7 @@ import pytest
 from conftest import GOLDEN
 
 EPS = 2.0 ** -53
-KAPPA_FACTOR = 64  # forward error <= max(tolerance, KAPPA_FACTOR * kappa_1 * eps)
+KAPPA_FACTOR = 8  # forward error <= max(tolerance, KAPPA_FACTOR * kappa_1 * eps)
 
 
 def _integer_system(c=30, n=64, seed=7):

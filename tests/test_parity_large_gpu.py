@@ -12,7 +12,9 @@ Both forms run on the GPU with condition estimates.  Each result must lie within
 of MKL's currents and of the truth, tolerance 1e-10 for the FP64 form and 1e-9 for
 the precision form: two backward-stable FP64 solvers agree only to about kappa * eps,
 so on well-conditioned systems the tolerance binds and on the low-frequency junction
-grid the conditioning does.  Where kappa is large, the truth of the GPU's own matrix
+grid the conditioning does.  KAPPA_FACTOR = 8: measured on GB300, the worst case (the
+grid at 10 kHz, kappa_1 = 2.3e10) sits at 0.07 kappa * eps for every solver, MKL
+included, so the bound keeps a margin of about 100.  Where kappa is large, the truth of the GPU's own matrix
 (refined on the host from the GPU's Z) separates the solver's error from the part that
 the fill's last-bit differences contribute.  The device's condition estimate must be
 within a factor of 2 of LAPACK's on the reference's matrix.
@@ -29,7 +31,7 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 EPS = 2.0 ** -53
-KAPPA_FACTOR = 64
+KAPPA_FACTOR = 8
 LARGE = sorted(glob.glob(os.path.join(GOLDEN, "large_*.npz")))
 
 
