@@ -350,6 +350,21 @@ def precision_leg(w, args):
     per_f = [{"freq_mhz": float(f), "kappa1_device": r["cond1"], "tier": r["tier"],
               "refinement_steps": r["iterations"], "rel_residual": r["rel_residual"]}
              for f, r in zip(freqs, repc)]
+    if args.oracle_all_freqs:
+        # every frequency against the CPU oracle (the reference's fill restated in C +
+        # LAPACK) and against the truth of the oracle's FP64 system
+        from oracle import oracle as orc
+        topo_o = oracle_topology(geo)
+        threads = os.cpu_count() or 1
+        v = orc.excitation(n, ngap)
+        for k, f in enumerate(freqs):
+            z = orc.fill(topo_o, float(f), threads=threads)
+            i_o, _, fac = orc.lu_solve(z, v, return_factors=True)
+            truth, _ = orc.refine_truth(z, v, i_o, factors=fac, threads=threads)
+            kap, _ = orc.cond1(z, fac)
+            per_f[k].update(kappa1_lapack=kap, mixed_vs_oracle=_rel(cur[k], i_o), mixed_vs_truth=_rel(cur[k], truth),
+                            oracle_vs_truth=_rel(i_o, truth))
+            del z, fac
     return {"workload": WORKLOADS["precision"].format(n=n, nf=len(freqs)), "value": value, "unit": UNIT,
             "steps": steps, "warmup": 2, "ms_per_step": ms,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -748,6 +763,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra-legs", action="store_true",
                     help="skip the precision-grid and serving sub-objects of the default run")
+    ap.add_argument("--oracle-all-freqs", action="store_true",
+                    help="precision-grid leg: compare every frequency with the CPU oracle and the truth")
     ap.add_argument("--serve-default-rate", type=float, default=40.0)
     ap.add_argument("--serve-default-seconds", type=float, default=8.0)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2.0, 5.0, 10.0])
