@@ -621,11 +621,44 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def geometries_batched(w, pool, freqs, workers):
+    """The set solved through wmom_factor_geometries: plans built on `workers` host
+    threads (geometry tables are host work; ctypes releases the interpreter lock),
+    one batched fill + factorisation per size class for all pairs, then every pair's
+    solve (precision form, refinement to 1e-12) spread over `workers` streams.
+    Returns (seconds, {phase: ms}, reports)."""
+    import concurrent.futures as cf
+    import torch
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(workers) as ex:
+        plans = list(ex.map(lambda g: w.Plan(w.Topology(g, listing=False)), pool))
+    t1 = time.perf_counter()
+    sets = w.factor_geometries(plans, freqs, mode=w.MODE_MIXED)
+    t2 = time.perf_counter()
+    streams = [torch.cuda.Stream() for _ in range(workers)]
+
+    def solve(i):
+        st = streams[i % workers]
+        return sets[i].solve(1, currents=False, stream=st.cuda_stream)[2][0]
+
+    with cf.ThreadPoolExecutor(workers) as ex:
+        reps = list(ex.map(solve, range(len(sets))))
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    for f in sets:
+        f.close()
+    for p in plans:
+        p.close()
+    return t3 - t0, {"plans": 1e3 * (t1 - t0), "fill_and_factor": 1e3 * (t2 - t1), "solves": 1e3 * (t3 - t2)}, reps
+
+
 def run_geometries(args):
     """Batching over geometries: 64 seeded random-wire geometries with N uniform in
-    [256, 4096] and one frequency each (log-uniform in 1 kHz - 30 MHz), all submitted at
-    once to the serving engine, whose worker streams overlap the solves on the device.
-    Reports freq-solves/s over the whole set and the per-geometry completion latency."""
+    [256, 4096] and one frequency each (log-uniform in 1 kHz - 30 MHz).  `value`: the
+    whole set through wmom_factor_geometries (batched fill + factorisation per size
+    class); beside it the same set submitted at once to the serving engine (one
+    factorisation per request on its worker streams).  Reports freq-solves/s over the
+    whole set, wall-clock from the geometry text to every pair's solution."""
     import numpy as np
     import torch
     torch.cuda.set_device(0)
@@ -650,13 +683,20 @@ def run_geometries(args):
         runs.append((dt, st, done))
     dt, st, done = min(runs, key=lambda r: r[0])
     fill_ms = _fill_all_geometries(w, pool, freqs)
+    geometries_batched(w, pool, freqs, args.workers)  # warm-up (kernels of every class)
+    bruns = [geometries_batched(w, pool, freqs, args.workers) for _ in range(max(1, args.steps))]
+    bdt, phases, breps = min(bruns, key=lambda r: r[0])
     line = {"metric": "freq-solves/s over a set of geometries of uneven size (one frequency each)",
-            "unit": "freq-solves/s", "value": args.geometries / dt, "higher_is_better": True, "n_gpus": 1,
-            "ms_per_step": 1e3 * dt, "steps": len(runs), "data": "synthetic (seeded random wires)",
+            "unit": "freq-solves/s", "value": args.geometries / bdt, "higher_is_better": True, "n_gpus": 1,
+            "ms_per_step": 1e3 * bdt, "steps": len(bruns), "data": "synthetic (seeded random wires)",
             "config": {"workload": f"{args.geometries} random-wire geometries, N uniform in [256, 4096], one "
                                    "frequency each in 1 kHz-30 MHz, precision form", "workers": args.workers,
-                       "unknowns_total": int(sizes.sum())},
-            "latency_ms": {"p50": st.get("p50_ms"), "p99": st.get("p99_ms")},
+                       "unknowns_total": int(sizes.sum()),
+                       "classes": len({w.padded_order(int(n)) for n in sizes})},
+            "batched": {"phases_ms": phases, "tiers": tier_counts(breps),
+                        "max_rel_residual": max(r["rel_residual"] for r in breps)},
+            "serving_engine": {"value": args.geometries / dt, "ms": 1e3 * dt,
+                               "latency_ms": {"p50": st.get("p50_ms"), "p99": st.get("p99_ms")}},
             "fill_ms_all_geometries": fill_ms,
             "fallbacks": int(sum(r["fell_back"] for d in done for r in d["reports"])) if done and
             isinstance(done[0], dict) and "reports" in done[0] else None}

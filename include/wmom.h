@@ -263,6 +263,24 @@ wmom_status wmom_factors_solve(wmom_factors f, int first, int count, int ngap, f
 long long wmom_factors_device_bytes(wmom_factors f);
 wmom_status wmom_factors_destroy(wmom_factors f);
 
+/* Factor sets for `count` (geometry, frequency) pairs of uneven orders -- plans[i] at
+ * freq_mhz[i], the same plan may appear several times -- filled and factored in
+ * batched launches instead of one factorisation each.  Each pair's matrix is stored
+ * at the padded order of its size class, wmom_padded_order(npls) (four classes per
+ * octave, at most 1.25 npls), with an identity block beyond npls; pairs of one class
+ * are filled by one ragged launch and factored by one batched launch sequence.  The
+ * leading block of the factors, and so every solution, is the geometry's own, and
+ * does not depend on the other pairs of the call: a pair's results are the same
+ * alone and in any batch, bit for bit.  out[i] receives a one-frequency factor set
+ * used like wmom_factor's (wmom_factors_solve returns npls entries per frequency;
+ * destroy each set; the sets of a class share one allocation, freed with the last).
+ * mode may include WMOM_SOLVE_CONDEST.  The reference solves one geometry per run
+ * and factors with a batch of one (cublasZgetrfBatched, GPU/Wire_MoM.cu:468). */
+wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const float* freq_mhz, int mode,
+                                   wmom_factors* out, void* stream);
+/* The padded order of an npls-unknown geometry in wmom_factor_geometries. */
+int wmom_padded_order(int npls);
+
 /* Human-readable name of a status code. */
 const char* wmom_status_string(wmom_status s);
 
@@ -287,10 +305,10 @@ void wmom_stats_enable(int on);
 void wmom_stats_reset(void);
 int wmom_stats_read(double* ms, long long* launches, long long* timed, double* work, int n);
 
-/* Measures this device's FP64 fused multiply-add throughput (TFLOP/s, 2 flop per
- * FMA) with a short bounded kernel of independent FMA chains, best of a few launch
- * shapes.  It is the denominator of the FP64-bound rooflines (fill, panel, SIMT
- * GEMM).  No reference counterpart. */
+/* Measures this device's FP64 throughput (TFLOP/s, 2 flop per FMA): the best of
+ * short bounded kernels of independent FMA chains and of the plain form's FP64
+ * complex GEMM on a compute-bound shape (4096 x 4096 x 256).  It is the denominator
+ * of the FP64-bound rooflines (fill, panel, SIMT GEMM).  No reference counterpart. */
 wmom_status wmom_probe_fp64_tflops(double* tflops);
 
 /* Diagnostic: for n device doubles x[i] writes d_out[4i..4i+3] = the fill's

@@ -111,6 +111,9 @@ _factors_solve = _sig("wmom_factors_solve", ctypes.c_int,
                       [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_double,
                        _dp, _dp, ctypes.POINTER(_Report), _vp])
 _factors_bytes = _sig("wmom_factors_device_bytes", ctypes.c_longlong, [_vp])
+_factor_geometries = _sig("wmom_factor_geometries", ctypes.c_int,
+                          [ctypes.POINTER(_vp), ctypes.c_int, _fp, ctypes.c_int, ctypes.POINTER(_vp), _vp])
+_padded_order = _sig("wmom_padded_order", ctypes.c_int, [ctypes.c_int])
 _factors_destroy = _sig("wmom_factors_destroy", ctypes.c_int, [_vp])
 _stats_enable = _sig("wmom_stats_enable", None, [ctypes.c_int])
 _stats_reset = _sig("wmom_stats_reset", None, [])
@@ -365,6 +368,17 @@ class Factors:
         self._h = h
         self.device_bytes = int(_factors_bytes(h))
 
+    @classmethod
+    def _adopt(cls, plan, freqs_mhz, mode, handle):
+        """Wraps a factor set the library made (factor_geometries)."""
+        self = cls.__new__(cls)
+        self.plan = plan
+        self.freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
+        self.mode = mode
+        self._h = _vp(handle)
+        self.device_bytes = int(_factors_bytes(self._h))
+        return self
+
     def solve(self, ngap, ampl=1.0, phas=0.0, first=0, count=None, tol=1e-12, currents=True, stream=0):
         count = len(self.freqs) - first if count is None else count
         n = self.plan.npls
@@ -388,6 +402,28 @@ class Factors:
             self.close()
         except Exception:
             pass
+
+
+def padded_order(npls):
+    """The order at which factor_geometries stores a geometry of npls unknowns (its
+    size class: four per octave, at most 1.25 npls)."""
+    return int(_padded_order(int(npls)))
+
+
+def factor_geometries(plans, freqs_mhz, mode=MODE_MIXED, condest=False, stream=0):
+    """Factor sets for (plans[i], freqs_mhz[i]) pairs of uneven orders, filled and
+    factored in batched launches per size class (wmom_factor_geometries): a list of
+    one-frequency Factors, each used like Factors(plan, [f]).  A pair's results do not
+    depend on the other pairs of the call."""
+    freqs = np.ascontiguousarray(np.atleast_1d(freqs_mhz), np.float32)
+    if len(freqs) != len(plans) or not plans:
+        raise ValueError("one frequency per plan")
+    count = len(plans)
+    hs = (_vp * count)(*[p._h for p in plans])
+    outs = (_vp * count)()
+    _check(_factor_geometries(hs, count, _ptr(freqs, _fp), mode | (SOLVE_CONDEST if condest else 0), outs, stream),
+           "wmom_factor_geometries")
+    return [Factors._adopt(p, [f], mode, outs[i]) for i, (p, f) in enumerate(zip(plans, freqs))]
 
 
 # ----------------------------------------------------------------- LAPACK-ish ----

@@ -7,6 +7,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <set>
@@ -415,8 +417,8 @@ wmom_status wmom_zgecon(int n, const void* a_dev, long long lda, const int* ipiv
   WMOM_CUDA_TRY(cudaMallocAsync(&x, sizeof(double2) * n, s));
   const int slot = 0;
   double est = 0.0;
-  const wmom_status st = condest_t<double2>(n, reinterpret_cast<const double2*>(a_dev), lda, 0, ipiv_dev, &slot, 1,
-                                            x, ws, s, &est);
+  const wmom_status st = condest_t<double2>(n, n, reinterpret_cast<const double2*>(a_dev), lda, 0, ipiv_dev, &slot,
+                                            1, x, ws, s, &est);
   cudaFreeAsync(x, s);
   if (st != WMOM_OK) return st;
   if (est > 0.0) *rcond = (1.0 / est) / anorm;
@@ -536,7 +538,26 @@ struct wmom_factors_s {
   wmom_plan plan = nullptr;
   size_t bytes = 0;
   std::mutex mu;
+  // sets made by one geometry batch share one allocation of their class's matrices,
+  // freed with the last of them
+  std::shared_ptr<void> shared;
 };
+
+namespace {
+
+// Matrices, factors and pivots of one class of a geometry batch.
+struct ClassStore {
+  void* z64 = nullptr;
+  void* lu = nullptr;
+  int* ipiv = nullptr;
+  ~ClassStore() {
+    if (z64) cudaFree(z64);
+    if (lu) cudaFree(lu);
+    if (ipiv) cudaFree(ipiv);
+  }
+};
+
+}  // namespace
 
 extern "C" {
 
@@ -597,11 +618,105 @@ long long wmom_factors_device_bytes(wmom_factors f) { return f ? (long long)f->b
 wmom_status wmom_factors_destroy(wmom_factors f) {
   if (!f) return WMOM_ERR_ARG;
   cudaDeviceSynchronize();
-  if (f->fs.z64) cudaFree(f->fs.z64);
-  if (f->fs.lu) cudaFree(f->fs.lu);
-  if (f->fs.ipiv) cudaFree(f->fs.ipiv);
+  if (f->shared) {
+    f->shared.reset();  // the class's storage goes with its last set
+  } else {
+    if (f->fs.z64) cudaFree(f->fs.z64);
+    if (f->fs.lu) cudaFree(f->fs.lu);
+    if (f->fs.ipiv) cudaFree(f->fs.ipiv);
+  }
   lu_workspace_destroy(&f->ws);
   delete f;
+  return WMOM_OK;
+}
+
+int wmom_padded_order(int npls) { return npls > 0 ? padded_order(npls) : 0; }
+
+wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const float* freq_mhz, int mode,
+                                   wmom_factors* out, void* stream) {
+  if (!out || count <= 0) return WMOM_ERR_ARG;
+  for (int i = 0; i < count; ++i) out[i] = nullptr;
+  const bool condest = (mode & WMOM_SOLVE_CONDEST) != 0;
+  mode &= ~WMOM_SOLVE_CONDEST;
+  if (!plans || !freq_mhz || (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED)) return WMOM_ERR_ARG;
+  for (int i = 0; i < count; ++i)
+    if (!plans[i] || !(freq_mhz[i] > 0.f) || !std::isfinite(freq_mhz[i])) return WMOM_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool mixed = mode == WMOM_MODE_MIXED;
+  const size_t elem = mixed ? sizeof(float2) : sizeof(double2);
+  // size classes, members in input order, batches of up to kMaxLuBatch
+  std::map<int, std::vector<int>> cls;
+  size_t need = 0;
+  for (int i = 0; i < count; ++i) {
+    const int P = padded_order(plans[i]->p.npls);
+    cls[P].push_back(i);
+    need += (size_t)P * P * (sizeof(double2) + elem) + sizeof(int) * (size_t)P;
+  }
+  size_t fr = 0, tot = 0;
+  WMOM_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+  if (need > fr) return WMOM_ERR_NOMEM;
+  // the fill reads every plan's loads: hold each distinct plan's lock, in address order
+  std::set<wmom_plan> uniq(plans, plans + count);
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (wmom_plan h : uniq) locks.emplace_back(h->mu);
+  auto fail = [&](wmom_status st) {
+    for (int i = 0; i < count; ++i)
+      if (out[i]) {
+        wmom_factors_destroy(out[i]);
+        out[i] = nullptr;
+      }
+    return st;
+  };
+  for (auto& kv : cls) {
+    const int P = kv.first;
+    const size_t nn = (size_t)P * P;
+    for (size_t c0 = 0; c0 < kv.second.size(); c0 += kMaxLuBatch) {
+      const int bg = (int)std::min<size_t>(kMaxLuBatch, kv.second.size() - c0);
+      const int* mem = kv.second.data() + c0;
+      auto store = std::make_shared<ClassStore>();
+      cudaError_t e = cudaMalloc(&store->z64, sizeof(double2) * nn * bg);
+      if (e == cudaSuccess) e = cudaMalloc(&store->lu, elem * nn * bg);
+      if (e == cudaSuccess) e = cudaMalloc(&store->ipiv, sizeof(int) * (size_t)P * bg);
+      if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "geometry batch storage"));
+      std::vector<wmom_factors_s*> sets(bg, nullptr);
+      for (int j = 0; j < bg; ++j) {
+        wmom_factors_s* f = new (std::nothrow) wmom_factors_s();
+        if (!f) return fail(WMOM_ERR_NOMEM);
+        out[mem[j]] = f;
+        sets[j] = f;
+        e = lu_workspace_create(&f->ws, P, 1, kMaxLuBatch);
+        if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "factor workspace"));
+        wmom_plan h = plans[mem[j]];
+        f->plan = h;
+        f->shared = store;
+        f->fs.plan = &h->p;
+        f->fs.mode = mode;
+        f->fs.condest = condest;
+        f->fs.freq.assign(1, freq_mhz[mem[j]]);
+        f->fs.ws = &f->ws;
+        f->fs.batch = 1;
+        f->fs.span = tuned_span(P, mode);
+        f->fs.order = P;
+        f->fs.z64 = reinterpret_cast<double2*>(store->z64) + (size_t)j * nn;
+        f->fs.lu = reinterpret_cast<unsigned char*>(store->lu) + elem * nn * j;
+        f->fs.ipiv = store->ipiv + (size_t)j * P;
+        f->fs.info.assign(1, 0);
+        f->bytes = nn * (sizeof(double2) + elem) + sizeof(int) * (size_t)P;
+      }
+      std::vector<const Plan*> ps(bg);
+      std::vector<float> fq(bg);
+      for (int j = 0; j < bg; ++j) {
+        ps[j] = &plans[mem[j]]->p;
+        fq[j] = freq_mhz[mem[j]];
+      }
+      std::vector<int> info(bg, 0);
+      const wmom_status st =
+          factor_class(mode, P, ps.data(), fq.data(), bg, reinterpret_cast<double2*>(store->z64), store->lu,
+                       store->ipiv, info.data(), &sets[0]->ws, sets[0]->fs.span, s);
+      if (st != WMOM_OK) return fail(st);
+      for (int j = 0; j < bg; ++j) sets[j]->fs.info[0] = info[j];
+    }
+  }
   return WMOM_OK;
 }
 

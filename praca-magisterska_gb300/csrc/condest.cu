@@ -31,11 +31,11 @@ namespace {
 
 constexpr int kCondThreads = 256;
 
-// out[4c + 0..3] for the vector of slot c (vector sel[c] of a batch n apart):
-// sum_i |x_i|, the first index of max_i |x_i|, that maximum, |x_jprev[c]|.  |.| is
-// the modulus (LAPACK's dzsum1 / izmax1); fixed reduction order.
+// out[4c + 0..3] for the vector of slot c (vector sel[c] of a batch n apart, its
+// first nreal entries): sum_i |x_i|, the first index of max_i |x_i|, that maximum,
+// |x_jprev[c]|.  |.| is the modulus (LAPACK's dzsum1 / izmax1); fixed reduction order.
 template <typename C>
-__global__ void __launch_bounds__(kCondThreads) cond_stats_kernel(const C* __restrict__ X, int n,
+__global__ void __launch_bounds__(kCondThreads) cond_stats_kernel(const C* __restrict__ X, int n, int nreal,
                                                                   const int* __restrict__ sel,
                                                                   const int* __restrict__ jprev,
                                                                   double* __restrict__ out) {
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kCondThreads) cond_stats_kernel(const C* __res
   const C* x = X + (size_t)sel[c] * n;
   double sum = 0.0, mx = -1.0;
   int mi = 0x7fffffff;
-  for (int i = t; i < n; i += kCondThreads) {
+  for (int i = t; i < nreal; i += kCondThreads) {
     const double a = hypot((double)x[i].x, (double)x[i].y);
     sum += a;
     if (a > mx) {  // increasing i: the first index of a tie stays
@@ -74,14 +74,16 @@ __global__ void __launch_bounds__(kCondThreads) cond_stats_kernel(const C* __res
     out[4 * c + 0] = ssum[0];
     out[4 * c + 1] = (double)sidx[0];
     out[4 * c + 2] = smax[0];
-    out[4 * c + 3] = (jp >= 0 && jp < n) ? hypot((double)x[jp].x, (double)x[jp].y) : 0.0;
+    out[4 * c + 3] = (jp >= 0 && jp < nreal) ? hypot((double)x[jp].x, (double)x[jp].y) : 0.0;
   }
 }
 
-// Sets the vector of slot c: action 0 x_i / |x_i| (1 where |x_i| is below the
-// smallest normal), 1 the unit vector e_arg, 2 (-1)^i (1 + i / (n - 1)), 3 1/n.
+// Sets the first nreal entries of the vector of slot c: action 0 x_i / |x_i| (1 where
+// |x_i| is below the smallest normal), 1 the unit vector e_arg, 2 (-1)^i (1 + i /
+// (nreal - 1)), 3 1/nreal; entries from nreal to n (the padding of a matrix stored at
+// a larger order, an identity block) are 0.
 template <typename C>
-__global__ void cond_setup_kernel(C* __restrict__ X, int n, const int* __restrict__ sel,
+__global__ void cond_setup_kernel(C* __restrict__ X, int n, int nreal, const int* __restrict__ sel,
                                   const int* __restrict__ action, const int* __restrict__ arg) {
   using R = decltype(C{}.x);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -89,6 +91,10 @@ __global__ void cond_setup_kernel(C* __restrict__ X, int n, const int* __restric
   if (i >= n) return;
   C* x = X + (size_t)sel[c] * n;
   double re = 0.0, im = 0.0;
+  if (i >= nreal) {
+    x[i] = cmake<C>((R)0, (R)0);
+    return;
+  }
   switch (action[c]) {
     case 0: {
       const double a = hypot((double)x[i].x, (double)x[i].y);
@@ -104,10 +110,10 @@ __global__ void cond_setup_kernel(C* __restrict__ X, int n, const int* __restric
       re = i == arg[c] ? 1.0 : 0.0;
       break;
     case 2:
-      re = (i & 1 ? -1.0 : 1.0) * (1.0 + (n > 1 ? (double)i / (double)(n - 1) : 0.0));
+      re = (i & 1 ? -1.0 : 1.0) * (1.0 + (nreal > 1 ? (double)i / (double)(nreal - 1) : 0.0));
       break;
     default:
-      re = 1.0 / (double)n;
+      re = 1.0 / (double)nreal;
   }
   x[i] = cmake<C>((R)re, (R)im);
 }
@@ -163,10 +169,10 @@ cudaError_t norm1_batch(const double2* Z, int n, long long lda, long long zstrid
 }
 
 template <typename C>
-wmom_status condest_t(int n, const C* lu, long long lda, long long astride, const int* ipiv, const int* slots, int m,
-                      C* X, LuWorkspace* ws, cudaStream_t s, double* est) {
+wmom_status condest_t(int n, int nreal, const C* lu, long long lda, long long astride, const int* ipiv,
+                      const int* slots, int m, C* X, LuWorkspace* ws, cudaStream_t s, double* est) {
   if (m <= 0) return WMOM_OK;
-  if (m > kMaxLuBatch || n < 1) return WMOM_ERR_ARG;
+  if (m > kMaxLuBatch || n < 1 || nreal < 1 || nreal > n) return WMOM_ERR_ARG;
   // device lists: [0] Z-solves, [1] Z^H-solves, [2] all, [3] previous index,
   // [4] setup slots, [5] actions, [6] unit-vector indices; then 4 doubles per slot
   constexpr int L = kMaxLuBatch;
@@ -195,7 +201,8 @@ wmom_status condest_t(int n, const C* lu, long long lda, long long astride, cons
     }
     COND_TRY(cudaMemcpyAsync(di + 4 * L, hi.data() + 4 * L, sizeof(int) * 3 * L, cudaMemcpyHostToDevice, s));
     stats::count(stats::kMisc);
-    cond_setup_kernel<C><<<dim3(vgrid, (unsigned)ks.size()), 256, 0, s>>>(X, n, di + 4 * L, di + 5 * L, di + 6 * L);
+    cond_setup_kernel<C><<<dim3(vgrid, (unsigned)ks.size()), 256, 0, s>>>(X, n, nreal, di + 4 * L, di + 5 * L,
+                                                                        di + 6 * L);
     COND_TRY(cudaGetLastError());
     // the host lists are reused before the copy above has run
     COND_TRY(cudaStreamSynchronize(s));
@@ -227,7 +234,8 @@ wmom_status condest_t(int n, const C* lu, long long lda, long long astride, cons
     if (!kh.empty())
       COND_TRY(lu_solve_h_t<C>(lu, lda, n, ipiv, X, ws, s, (int)kh.size(), astride, di + L));
     stats::count(stats::kMisc);
-    cond_stats_kernel<C><<<(unsigned)kall.size(), kCondThreads, 0, s>>>(X, n, di + 2 * L, di + 3 * L, dstat);
+    cond_stats_kernel<C><<<(unsigned)kall.size(), kCondThreads, 0, s>>>(X, n, nreal, di + 2 * L, di + 3 * L,
+                                                                        dstat);
     COND_TRY(cudaGetLastError());
     COND_TRY(cudaMemcpyAsync(hstat.data(), dstat, sizeof(double) * 4 * kall.size(), cudaMemcpyDeviceToHost, s));
     COND_TRY(cudaStreamSynchronize(s));
@@ -239,7 +247,7 @@ wmom_status condest_t(int n, const C* lu, long long lda, long long astride, cons
       switch (z.step) {
         case kFirstA:  // x = Z^-1 (1/n, ..., 1/n)
           z.est = sum;
-          if (n == 1) {
+          if (nreal == 1) {
             z.step = kDone;
           } else {
             z.step = kFirstH;
@@ -288,7 +296,7 @@ wmom_status condest_t(int n, const C* lu, long long lda, long long astride, cons
           break;
         }
         case kAltA: {  // x = Z^-1 (alternating test vector)
-          const double temp = 2.0 * (sum / (3.0 * n));
+          const double temp = 2.0 * (sum / (3.0 * nreal));
           if (temp > z.est) z.est = temp;
           z.step = kDone;
           break;
@@ -305,9 +313,9 @@ wmom_status condest_t(int n, const C* lu, long long lda, long long astride, cons
   return WMOM_OK;
 }
 
-template wmom_status condest_t<double2>(int, const double2*, long long, long long, const int*, const int*, int,
-                                        double2*, LuWorkspace*, cudaStream_t, double*);
-template wmom_status condest_t<float2>(int, const float2*, long long, long long, const int*, const int*, int,
+template wmom_status condest_t<double2>(int, int, const double2*, long long, long long, const int*, const int*,
+                                        int, double2*, LuWorkspace*, cudaStream_t, double*);
+template wmom_status condest_t<float2>(int, int, const float2*, long long, long long, const int*, const int*, int,
                                        float2*, LuWorkspace*, cudaStream_t, double*);
 
 }  // namespace wmom

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -743,7 +744,8 @@ wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws
 // mask, FP64 LU for the matrices that stall.
 wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float2* lu32, const double2* lu64,
                         const int* ipiv, const int* info, double tol, LuWorkspace* ws, GroupScratch& g,
-                        wmom_report* rep, bool condest) {
+                        wmom_report* rep, bool condest, int nreal) {
+  if (nreal <= 0) nreal = n;
   const size_t nn = (size_t)n * n;
   cudaStream_t s = g.s;
   GroupScalars& hs = g.hs;
@@ -755,13 +757,13 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   }
   // condition estimates: ||Z||_1 now (read back with the next scalars), ||Z^-1||_1
   // from the factors behind each matrix's solution once it is final
-  if (condest) SWEEP_TRY(norm1_batch(Z64, n, n, (long long)nn, bg, dsc->anorm, s));
+  if (condest) SWEEP_TRY(norm1_batch(Z64, nreal, n, (long long)nn, bg, dsc->anorm, s));
   auto estimate = [&](auto* lu, const int* piv, auto* X, const std::vector<int>& slots,
                       const std::vector<int>& mats) -> wmom_status {
     if (!condest || slots.empty()) return WMOM_OK;
     std::vector<double> est(slots.size(), 0.0);
-    const wmom_status cs = condest_t(n, lu, (long long)n, (long long)nn, piv, slots.data(), (int)slots.size(), X, ws,
-                                     s, est.data());
+    const wmom_status cs = condest_t(n, nreal, lu, (long long)n, (long long)nn, piv, slots.data(),
+                                     (int)slots.size(), X, ws, s, est.data());
     if (cs != WMOM_OK) return cs;
     for (size_t q = 0; q < slots.size(); ++q) rep[mats[q]].cond1 = hs.anorm[mats[q]] * est[q];
     return WMOM_OK;
@@ -1173,16 +1175,22 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
 namespace {
 
 // Currents / Z_in / reports of a solved group to the caller's host arrays.
+// nout (<= g.n, 0 = g.n): the entries of each solution the caller receives -- the
+// geometry's own order when its matrices are stored at a larger padded order.
 wmom_status group_results(GroupScratch& g, int bg, int ngap, const wmom_report* rep, int f, double* currents,
-                          double* zin, wmom_report* reports, wmom_status* overall) {
+                          double* zin, wmom_report* reports, wmom_status* overall, int nout = 0) {
   const int n = g.n;
+  if (nout <= 0) nout = n;
   std::vector<double2> xh((size_t)n * bg);
-  if (currents) {
+  if (currents && nout == n) {
     SWEEP_TRY(cudaMemcpyAsync(currents + 2 * (size_t)f * n, g.x64.p, sizeof(double2) * (size_t)n * bg,
                               cudaMemcpyDeviceToHost, g.s));
     SWEEP_TRY(cudaStreamSynchronize(g.s));
     std::memcpy(xh.data(), currents + 2 * (size_t)f * n, sizeof(double2) * (size_t)n * bg);
   } else {
+    if (currents)
+      SWEEP_TRY(cudaMemcpy2DAsync(currents + 2 * (size_t)f * nout, sizeof(double2) * nout, g.x64.p,
+                                  sizeof(double2) * n, sizeof(double2) * nout, bg, cudaMemcpyDeviceToHost, g.s));
     for (int b = 0; b < bg; ++b)
       SWEEP_TRY(cudaMemcpyAsync(xh.data() + (size_t)b * n + (ngap - 1), g.x64.as<double2>() + (size_t)b * n + (ngap - 1),
                                 sizeof(double2), cudaMemcpyDeviceToHost, g.s));
@@ -1212,8 +1220,11 @@ wmom_status group_results(GroupScratch& g, int bg, int ngap, const wmom_report* 
   return WMOM_OK;
 }
 
-// Fills nk matrices (frequencies freq[0..nk)) into Z and adds the plan's loads.
-wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cudaStream_t s) {
+// Fills nk matrices (frequencies freq[0..nk)) into Z and adds the plan's loads.  The
+// host staging vectors are copied from pageable memory (staged before each copy call
+// returns) and the device ones are freed in stream order, so `sync` = false leaves
+// the work in flight.
+wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cudaStream_t s, bool sync = true) {
   const int n = p.npls;
   const size_t nn = (size_t)n * n;
   std::vector<FreqParams> fph(nk);
@@ -1239,7 +1250,7 @@ wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cud
     add_loads_kernel<<<(nk + 127) / 128, 128, 0, s>>>(Z, n, (long long)nn, li.as<int>(), lvd.as<double2>(), nl, nk);
     SWEEP_TRY(cudaGetLastError());
   }
-  SWEEP_TRY(cudaStreamSynchronize(s));  // host staging vectors end with this scope
+  if (sync) SWEEP_TRY(cudaStreamSynchronize(s));
   return WMOM_OK;
 }
 
@@ -1378,8 +1389,136 @@ void retain_pool_memory() {
 
 }  // namespace
 
+namespace {
+
+// Groups a sweep is split into so that the fill of one group (FP64 pipe) runs while
+// the previous group factors (tensor pipe): WMOM_PIPELINE = 1 (off) .. 8; default 2.
+int pipeline_groups() {
+  const int v = env_int("WMOM_PIPELINE", 1, 8);
+  return v ? v : 2;
+}
+
+// The cached factorisation shape for (n, mode), if a sweep of that order was tuned.
+bool cached_lu_config(int mode, int n, LuConfig* out) {
+  if (env_int("WMOM_LU_BATCH", 1, kMaxLuBatch)) return false;  // an override goes through the tuner path
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find({(n + 255) / 256, mode});
+  if (it == g_tuned.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+struct StreamPair {
+  cudaStream_t hi = nullptr, lo = nullptr;
+  ~StreamPair() {
+    if (hi) cudaStreamDestroy(hi);
+    if (lo) cudaStreamDestroy(lo);
+  }
+};
+
+// Pipelined sweep: the frequencies are split into G groups of width Bp; group g + 1 is
+// filled on a second stream while group g is factored and solved on a
+// higher-priority one, whose kernels the block scheduler serves first.  Results are
+// those of the plain sweep bit for bit: the same fill per matrix and factorisations
+// that do not depend on the batch width.
+wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) {
+  const Plan& p = *a.plan;
+  const int n = p.npls;
+  const bool mixed = a.mode == WMOM_MODE_MIXED;
+  const size_t nn = (size_t)n * n;
+  const size_t mat64 = sizeof(double2) * nn;
+  const int Bp = std::min(cfg.batch, (a.nfreq + G - 1) / G);
+  StreamPair sp;
+  int lo_pri = 0, hi_pri = 0;
+  SWEEP_TRY(cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri));
+  SWEEP_TRY(cudaStreamCreateWithPriority(&sp.hi, cudaStreamNonBlocking, hi_pri));
+  SWEEP_TRY(cudaStreamCreateWithPriority(&sp.lo, cudaStreamNonBlocking, lo_pri));
+  cudaEvent_t start = nullptr;
+  SWEEP_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  std::vector<cudaEvent_t> filled((a.nfreq + Bp - 1) / Bp, nullptr);
+  auto cleanup = [&]() {
+    if (start) cudaEventDestroy(start);
+    for (cudaEvent_t e : filled)
+      if (e) cudaEventDestroy(e);
+  };
+  struct Guard {
+    std::function<void()> f;
+    ~Guard() { f(); }
+  } guard{cleanup};
+  for (auto& e : filled) SWEEP_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // both internal streams start after the caller's stream work so far
+  SWEEP_TRY(cudaEventRecord(start, a.stream));
+  SWEEP_TRY(cudaStreamWaitEvent(sp.hi, start, 0));
+  SWEEP_TRY(cudaStreamWaitEvent(sp.lo, start, 0));
+  DevBuf zall, lu, piv;
+  SWEEP_TRY(zall.alloc(mat64 * a.nfreq, sp.hi));
+  SWEEP_TRY(lu.alloc((mixed ? sizeof(float2) : sizeof(double2)) * nn * Bp, sp.hi));
+  SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * Bp, sp.hi));
+  // the buffers come from the high-priority stream's pool: the fill stream waits for them
+  cudaEvent_t alloc_done = nullptr;
+  SWEEP_TRY(cudaEventCreateWithFlags(&alloc_done, cudaEventDisableTiming));
+  SWEEP_TRY(cudaEventRecord(alloc_done, sp.hi));
+  SWEEP_TRY(cudaStreamWaitEvent(sp.lo, alloc_done, 0));
+  cudaEventDestroy(alloc_done);
+  const int ngroups = (int)filled.size();
+  auto launch_fill = [&](int gi) -> wmom_status {
+    const int f0 = gi * Bp, nb = std::min(Bp, a.nfreq - f0);
+    const wmom_status st = fill_batch(p, a.freq_mhz + f0, nb, zall.as<double2>() + (size_t)f0 * nn, sp.lo, false);
+    if (st != WMOM_OK) return st;
+    SWEEP_TRY(cudaEventRecord(filled[gi], sp.lo));
+    return WMOM_OK;
+  };
+  wmom_status st = launch_fill(0);
+  if (st != WMOM_OK) return st;
+  GroupScratch g;
+  st = scratch_init(&g, n, Bp, a.ngap, a.ampl, a.phas_deg, sp.hi);
+  if (st != WMOM_OK) return st;
+  FactorGraph graph;
+  std::vector<wmom_report> rep(kMaxLuBatch);
+  wmom_status overall = WMOM_OK;
+  for (int gi = 0; gi < ngroups; ++gi) {
+    // the next group's fill goes in before this group's factorisation: it runs on the
+    // SMs the factorisation leaves
+    if (gi + 1 < ngroups) {
+      st = launch_fill(gi + 1);
+      if (st != WMOM_OK) return st;
+    }
+    const int f0 = gi * Bp, bg = std::min(Bp, a.nfreq - f0);
+    SWEEP_TRY(cudaStreamWaitEvent(sp.hi, filled[gi], 0));
+    const double2* Zg = zall.as<double2>() + (size_t)f0 * nn;
+    int info[kMaxLuBatch] = {};
+    st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, sp.hi, info,
+                      nullptr, &graph, cfg.span);
+    if (st != WMOM_OK) return st;
+    st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
+                     rep.data(), a.condest, n);
+    if (st != WMOM_OK) return st;
+    st = group_results(g, bg, a.ngap, rep.data(), f0, a.currents, a.zin, a.reports, &overall);
+    if (st != WMOM_OK) return st;
+  }
+  SWEEP_TRY(cudaStreamSynchronize(sp.lo));
+  SWEEP_TRY(cudaStreamSynchronize(sp.hi));
+  return overall;
+}
+
+}  // namespace
+
 wmom_status run_sweep(const SweepArgs& a) {
   retain_pool_memory();
+  {
+    // pipelined when the shape is already tuned, the sweep has more than one group
+    // and all its matrices fit
+    LuConfig cfg;
+    const int G = pipeline_groups();
+    size_t fr = 0, tot = 0;
+    if (G > 1 && a.nfreq >= 2 * G && cached_lu_config(a.mode, a.plan->npls, &cfg) &&
+        cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+      const size_t nn = (size_t)a.plan->npls * a.plan->npls;
+      const size_t need = nn * (sizeof(double2) * a.nfreq + sizeof(double2) * cfg.batch);
+      const size_t budget = a.mem_budget ? a.mem_budget : fr / 2;
+      if (need < budget) return run_sweep_pipelined(a, cfg, G);
+    }
+  }
   const Plan& p = *a.plan;
   const int n = p.npls;
   cudaStream_t s = a.stream;
@@ -1427,7 +1566,7 @@ wmom_status run_sweep(const SweepArgs& a) {
                         &graph, cfg.span);
       if (st != WMOM_OK) return st;
       st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                       rep.data(), a.condest);
+                       rep.data(), a.condest, n);
       if (st != WMOM_OK) return st;
       st = group_results(g, bg, a.ngap, rep.data(), f0 + g0, a.currents, a.zin, a.reports, &overall);
       if (st != WMOM_OK) return st;
@@ -1435,6 +1574,91 @@ wmom_status run_sweep(const SweepArgs& a) {
   }
   SWEEP_TRY(cudaStreamSynchronize(s));
   return overall;
+}
+
+// ----------------------------------------------- geometries of uneven order ----
+// A batch of geometries of different orders is factored in size classes: each
+// matrix is stored at the padded order of its class, padded_order(n), with an
+// identity block beyond n.  Z_pad = [[Z, 0], [0, I]] factors as the LU of Z beside an
+// identity (the padding rows are zero in Z's columns and never become pivots), so the
+// leading n x n block of the factors and the first n entries of every solution are
+// those of Z.  The class depends on n alone, so a geometry's factors are the same
+// alone and in any batch: the same order, panel widths and reduction orders.  The
+// classes are four per octave (P <= 1.25 n).
+
+int padded_order(int n) {
+  if (n <= 256) return ((n + 63) / 64) * 64;
+  int p2 = 256;
+  while (2 * p2 <= n) p2 *= 2;
+  const int step = p2 / 4;
+  return ((n + step - 1) / step) * step;
+}
+
+namespace {
+
+// Z of matrix b (order P, zstride apart): rows nreal[b].. of its first nreal[b]
+// columns and every other column set to the identity's
+__global__ void pad_identity_kernel(double2* __restrict__ Z, int P, long long zstride,
+                                    const int* __restrict__ nreal) {
+  const int j = blockIdx.y, b = blockIdx.z;
+  const int nb = nreal[b];
+  double2* col = Z + (size_t)b * zstride + (size_t)j * P;
+  const int i0 = j < nb ? nb : 0;
+  for (int i = i0 + threadIdx.x; i < P; i += blockDim.x)
+    col[i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+}
+
+}  // namespace
+
+int tuned_span(int n, int mode) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find({(n + 255) / 256, mode});
+  return it != g_tuned.end() && it->second.span > 0 ? it->second.span : 2;
+}
+
+wmom_status factor_class(int mode, int P, const Plan* const* plans, const float* freq, int count, double2* z64,
+                         void* lu, int* ipiv, int* info, LuWorkspace* ws, int span, cudaStream_t s) {
+  const size_t nn = (size_t)P * P;
+  std::vector<double> ka(count);
+  std::vector<double2*> zp(count);
+  std::vector<long long> ld(count, P);
+  std::vector<int> nreal(count);
+  for (int i = 0; i < count; ++i) {
+    ka[i] = ka_from_mhz(freq[i]);
+    zp[i] = z64 + (size_t)i * nn;
+    nreal[i] = plans[i]->npls;
+  }
+  SWEEP_TRY(launch_fill_geometries(plans, ka.data(), zp.data(), ld.data(), count, s));
+  for (int i = 0; i < count; ++i) {
+    const Plan& p = *plans[i];
+    if (p.load_idx.empty()) continue;
+    // R + j*2*pi*f[MHz]*L[uH] on the loaded diagonal entries (REF/Wire_MoM.cu:346-363)
+    const int nl = (int)p.load_idx.size();
+    const double pi = std::acos(-1.0);
+    std::vector<double2> lv(nl);
+    for (int l = 0; l < nl; ++l) lv[l] = make_double2(p.load_r[l], 2. * pi * freq[i] * p.load_l_uh[l]);
+    DevBuf li, lvd;
+    SWEEP_TRY(li.alloc(sizeof(int) * nl, s));
+    SWEEP_TRY(lvd.alloc(sizeof(double2) * nl, s));
+    SWEEP_TRY(cudaMemcpyAsync(li.p, p.load_idx.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, s));
+    SWEEP_TRY(cudaMemcpyAsync(lvd.p, lv.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, s));
+    stats::count(stats::kMisc);
+    add_loads_kernel<<<1, 128, 0, s>>>(zp[i], P, (long long)nn, li.as<int>(), lvd.as<double2>(), nl, 1);
+    SWEEP_TRY(cudaGetLastError());
+    SWEEP_TRY(cudaStreamSynchronize(s));  // the host staging vectors end with this scope
+  }
+  DevBuf dn;
+  SWEEP_TRY(dn.alloc(sizeof(int) * count, s));
+  SWEEP_TRY(cudaMemcpyAsync(dn.p, nreal.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  stats::count(stats::kMisc);
+  pad_identity_kernel<<<dim3(1, P, count), 256, 0, s>>>(z64, P, (long long)nn, dn.as<int>());
+  SWEEP_TRY(cudaGetLastError());
+  const bool mixed = mode == WMOM_MODE_MIXED;
+  const wmom_status st = factor_group(mode, P, z64, count, mixed ? reinterpret_cast<float2*>(lu) : nullptr,
+                                      mixed ? nullptr : reinterpret_cast<double2*>(lu), ipiv, ws, s, info, nullptr,
+                                      nullptr, span);
+  SWEEP_TRY(cudaStreamSynchronize(s));
+  return st;
 }
 
 // ------------------------------------------------------- resident factors ----
@@ -1471,7 +1695,8 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
 
 wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
                           double* currents, double* zin, wmom_report* reports, cudaStream_t s) {
-  const int n = fs->plan->npls;
+  const int nreal = fs->plan->npls;
+  const int n = fs->order > 0 ? fs->order : nreal;  // storage order (padded for geometry batches)
   const size_t nn = (size_t)n * n;
   const bool mixed = fs->mode == WMOM_MODE_MIXED;
   const int B = std::max(1, fs->batch);
@@ -1486,10 +1711,11 @@ wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float a
     const float2* l32 = reinterpret_cast<const float2*>(fs->lu) + (size_t)f * nn;
     const double2* l64 = reinterpret_cast<const double2*>(fs->lu) + (size_t)f * nn;
     st = solve_group(fs->mode, n, fs->z64 + (size_t)f * nn, bg, mixed ? l32 : nullptr, mixed ? nullptr : l64,
-                     fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data(), fs->condest);
+                     fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data(), fs->condest,
+                     nreal);
     if (st != WMOM_OK) return st;
     // results are indexed from `first` in the caller's arrays
-    st = group_results(g, bg, ngap, rep.data(), f - first, currents, zin, reports, &overall);
+    st = group_results(g, bg, ngap, rep.data(), f - first, currents, zin, reports, &overall, nreal);
     if (st != WMOM_OK) return st;
     f += bg;
   }

@@ -49,19 +49,37 @@ struct FactorSet {
   int* ipiv = nullptr;        // nf * n
   std::vector<int> info;
   bool condest = false;       // estimate kappa_1 with every solve
+  // order of the stored matrices: the plan's npls, or the padded order of the
+  // geometry's size class when the set was factored in a batch of uneven geometries
+  // (identity block beyond npls; factors_solve pads the excitation and returns npls
+  // entries)
+  int order = 0;
 };
 
 wmom_status factors_build(FactorSet* fs, cudaStream_t s);
+
+// Geometries of uneven order (solve.cu): the padded order of n's size class (four
+// classes per octave, P <= 1.25 n); the span a factorisation of order n uses (the
+// tuned one, else 2); and the batched fill + factorisation of `count` geometries of
+// one class, one frequency each, into z64 (count matrices of order P) and lu / ipiv
+// (complex64 or complex128 factors by mode), with an identity block beyond each
+// geometry's order.
+int padded_order(int n);
+int tuned_span(int n, int mode);
+wmom_status factor_class(int mode, int P, const Plan* const* plans, const float* freq, int count, double2* z64,
+                         void* lu, int* ipiv, int* info, LuWorkspace* ws, int span, cudaStream_t s);
 wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
                           double* currents, double* zin, wmom_report* reports, cudaStream_t s);
 
 // Condition estimates (condest.cu).  condest_t: est[k] = an estimate of
 // ||A^-1||_1 for the factored matrices slots[0..m) (host list; matrix slot at
 // lu + slot * astride, pivots at ipiv + slot * n), by LAPACK zlacn2's algorithm with
-// batched solves; X holds one n-vector per slot (at X + slot * n) as scratch.
+// batched solves; X holds one n-vector per slot (at X + slot * n) as scratch.  nreal
+// <= n: the matrices' own order when they are stored at the padded order n with an
+// identity block beyond nreal (the estimate is then that of the leading block).
 template <typename C>
-wmom_status condest_t(int n, const C* lu, long long lda, long long astride, const int* ipiv, const int* slots, int m,
-                      C* X, LuWorkspace* ws, cudaStream_t s, double* est);
+wmom_status condest_t(int n, int nreal, const C* lu, long long lda, long long astride, const int* ipiv,
+                      const int* slots, int m, C* X, LuWorkspace* ws, cudaStream_t s, double* est);
 // out_dev[b] = ||Z_b||_1 (maximum column sum of moduli) for nmat matrices zstride apart.
 cudaError_t norm1_batch(const double2* Z, int n, long long lda, long long zstride, int nmat, double* out_dev,
                         cudaStream_t s);

@@ -1,4 +1,5 @@
 // stats.cu -- see stats.h.
+#include "lu_internal.h"
 #include "stats.h"
 
 #include <algorithm>
@@ -179,6 +180,36 @@ wmom_status wmom_probe_fp64_tflops(double* tflops) {
   best = std::max(best, probe_once<16>(buf, nsm * 4, 256, s, e0, e1));
   best = std::max(best, probe_once<16>(buf, nsm * 8, 128, s, e0, e1));
   best = std::max(best, probe_once<32>(buf, nsm * 2, 256, s, e0, e1));
+  // FMA chains stop short of the pipe's rate on this GPU (about 1.05 against the
+  // 1.24 TFLOP/s a register-tiled GEMM sustains with the FP64 pipe 99% busy, ncu), so
+  // the FP64 complex GEMM of the plain form is timed as well, on a compute-bound shape
+  // (C 4096 x 4096 += A 4096 x 256 B: 64 flops per byte of C), and the faster wins --
+  // as the bf16 denominator is a measured GEMM
+  {
+    const int m = 4096, k = 256;
+    double2 *a = nullptr, *bm = nullptr, *c = nullptr;
+    if (cudaMalloc(&a, sizeof(double2) * (size_t)m * k) == cudaSuccess &&
+        cudaMalloc(&bm, sizeof(double2) * (size_t)m * k) == cudaSuccess &&
+        cudaMalloc(&c, sizeof(double2) * (size_t)m * m) == cudaSuccess) {
+      cudaMemsetAsync(a, 0, sizeof(double2) * (size_t)m * k, s);
+      cudaMemsetAsync(bm, 0, sizeof(double2) * (size_t)m * k, s);
+      cudaMemsetAsync(c, 0, sizeof(double2) * (size_t)m * m, s);
+      for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, s);
+        const cudaError_t ge = wmom::zgemm_sub_simt(a, m, bm, k, c, m, m, m, k, s, 1, 0);
+        cudaEventRecord(e1, s);
+        float ms = 0.f;
+        if (ge == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0.f && rep > 0)
+          best = std::max(best, 8.0 * m * (double)m * k / (ms * 1e-3) / 1e12);
+      }
+    }
+    cudaStreamSynchronize(s);
+    if (a) cudaFree(a);
+    if (bm) cudaFree(bm);
+    if (c) cudaFree(c);
+    cudaGetLastError();
+  }
   const cudaError_t err = cudaStreamSynchronize(s);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -29,3 +29,16 @@ def test_sweep_frequencies():
     f = g.sweep_freqs()
     assert len(f) == 12 and abs(f[0] - 0.01) < 1e-9 and abs(f[-1] - 10.0) < 1e-6
     assert np.all(np.diff(f) > 0)
+
+
+def test_padded_order_classes(wmom):
+    """Size classes of wmom_factor_geometries: at least n, at most 1.25 n above 256 (four
+    classes per octave), a multiple of 64, and the class of the class is itself."""
+    prev = 0
+    for n in range(1, 20481, 7):
+        p = wmom.padded_order(n)
+        assert p >= n and p % 64 == 0 and p >= prev
+        if n > 256:
+            assert p <= 1.25 * n
+        assert wmom.padded_order(p) == p
+        prev = p

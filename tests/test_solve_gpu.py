@@ -235,3 +235,27 @@ def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
             del os.environ["WMOM_PANEL_LOOKAHEAD"]
     assert out["1"][2][0]["tier"] == 2
     assert np.array_equal(out["1"][0], out["0"][0])
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_pipelined_sweep_is_bit_identical(cuda, wmom, mode):
+    """With the factorisation shape tuned, a sweep is split into groups whose fills run
+    on a second stream while the previous group factors (WMOM_PIPELINE groups,
+    default 2); the currents, input impedances and reports must not depend on the
+    number of groups."""
+    topo = wmom.Topology(wmom.geometry.precision_grid(2048))
+    plan = wmom.Plan(topo)
+    freqs = np.array([0.003, 0.02, 0.2, 1.0, 3.0, 7.0, 12.0, 25.0], np.float32)
+    out = {}
+    try:
+        for groups in ("1", "1", "2", "3"):  # the first call tunes the shape
+            os.environ["WMOM_PIPELINE"] = groups
+            out[groups] = plan.solve(freqs, 1000, mode=mode)
+    finally:
+        os.environ.pop("WMOM_PIPELINE", None)
+    c1, z1, r1 = out["1"]
+    for g in ("2", "3"):
+        c, z, r = out[g]
+        assert np.array_equal(c, c1) and np.array_equal(z, z1), g
+        assert r == r1, g
+    plan.close()
