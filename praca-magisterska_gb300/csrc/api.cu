@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -12,6 +13,7 @@
 #include <mutex>
 #include <new>
 #include <set>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -667,55 +669,101 @@ wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const floa
       }
     return st;
   };
+  // every class chunk's storage and sets first (allocations on this thread), then the
+  // chunks' fills and factorisations concurrently: one host thread and stream each,
+  // so that one chunk's fill overlaps another's latency-bound panels
+  struct Chunk {
+    int P = 0, bg = 0;
+    std::vector<int> mem;
+    std::shared_ptr<ClassStore> store;
+    std::vector<wmom_factors_s*> sets;
+    std::vector<int> info;
+    wmom_status st = WMOM_OK;
+  };
+  std::vector<Chunk> chunks;
   for (auto& kv : cls) {
     const int P = kv.first;
     const size_t nn = (size_t)P * P;
     for (size_t c0 = 0; c0 < kv.second.size(); c0 += kMaxLuBatch) {
-      const int bg = (int)std::min<size_t>(kMaxLuBatch, kv.second.size() - c0);
-      const int* mem = kv.second.data() + c0;
-      auto store = std::make_shared<ClassStore>();
-      cudaError_t e = cudaMalloc(&store->z64, sizeof(double2) * nn * bg);
-      if (e == cudaSuccess) e = cudaMalloc(&store->lu, elem * nn * bg);
-      if (e == cudaSuccess) e = cudaMalloc(&store->ipiv, sizeof(int) * (size_t)P * bg);
+      Chunk ch;
+      ch.P = P;
+      ch.bg = (int)std::min<size_t>(kMaxLuBatch, kv.second.size() - c0);
+      ch.mem.assign(kv.second.begin() + c0, kv.second.begin() + c0 + ch.bg);
+      ch.store = std::make_shared<ClassStore>();
+      cudaError_t e = cudaMalloc(&ch.store->z64, sizeof(double2) * nn * ch.bg);
+      if (e == cudaSuccess) e = cudaMalloc(&ch.store->lu, elem * nn * ch.bg);
+      if (e == cudaSuccess) e = cudaMalloc(&ch.store->ipiv, sizeof(int) * (size_t)P * ch.bg);
       if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "geometry batch storage"));
-      std::vector<wmom_factors_s*> sets(bg, nullptr);
-      for (int j = 0; j < bg; ++j) {
+      ch.sets.assign(ch.bg, nullptr);
+      ch.info.assign(ch.bg, 0);
+      for (int j = 0; j < ch.bg; ++j) {
         wmom_factors_s* f = new (std::nothrow) wmom_factors_s();
         if (!f) return fail(WMOM_ERR_NOMEM);
-        out[mem[j]] = f;
-        sets[j] = f;
+        out[ch.mem[j]] = f;
+        ch.sets[j] = f;
         e = lu_workspace_create(&f->ws, P, 1, kMaxLuBatch);
         if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "factor workspace"));
-        wmom_plan h = plans[mem[j]];
+        wmom_plan h = plans[ch.mem[j]];
         f->plan = h;
-        f->shared = store;
+        f->shared = ch.store;
         f->fs.plan = &h->p;
         f->fs.mode = mode;
         f->fs.condest = condest;
-        f->fs.freq.assign(1, freq_mhz[mem[j]]);
+        f->fs.freq.assign(1, freq_mhz[ch.mem[j]]);
         f->fs.ws = &f->ws;
         f->fs.batch = 1;
         f->fs.span = tuned_span(P, mode);
         f->fs.order = P;
-        f->fs.z64 = reinterpret_cast<double2*>(store->z64) + (size_t)j * nn;
-        f->fs.lu = reinterpret_cast<unsigned char*>(store->lu) + elem * nn * j;
-        f->fs.ipiv = store->ipiv + (size_t)j * P;
+        f->fs.z64 = reinterpret_cast<double2*>(ch.store->z64) + (size_t)j * nn;
+        f->fs.lu = reinterpret_cast<unsigned char*>(ch.store->lu) + elem * nn * j;
+        f->fs.ipiv = ch.store->ipiv + (size_t)j * P;
         f->fs.info.assign(1, 0);
         f->bytes = nn * (sizeof(double2) + elem) + sizeof(int) * (size_t)P;
       }
-      std::vector<const Plan*> ps(bg);
-      std::vector<float> fq(bg);
-      for (int j = 0; j < bg; ++j) {
-        ps[j] = &plans[mem[j]]->p;
-        fq[j] = freq_mhz[mem[j]];
-      }
-      std::vector<int> info(bg, 0);
-      const wmom_status st =
-          factor_class(mode, P, ps.data(), fq.data(), bg, reinterpret_cast<double2*>(store->z64), store->lu,
-                       store->ipiv, info.data(), &sets[0]->ws, sets[0]->fs.span, s);
-      if (st != WMOM_OK) return fail(st);
-      for (int j = 0; j < bg; ++j) sets[j]->fs.info[0] = info[j];
+      chunks.push_back(std::move(ch));
     }
+  }
+  cudaEvent_t start = nullptr;
+  WMOM_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  cudaError_t se = cudaEventRecord(start, s);  // the chunks' streams follow the caller's
+  if (se != cudaSuccess) {
+    cudaEventDestroy(start);
+    return fail(wmom_fail_cuda(se, "cudaEventRecord"));
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess || cudaStreamWaitEvent(cs, start, 0)) {
+      for (int c; (c = next.fetch_add(1)) < (int)chunks.size();) chunks[c].st = WMOM_ERR_CUDA;
+      if (cs) cudaStreamDestroy(cs);
+      return;
+    }
+    for (int c; (c = next.fetch_add(1)) < (int)chunks.size();) {
+      Chunk& ch = chunks[c];
+      std::vector<const Plan*> ps(ch.bg);
+      std::vector<float> fq(ch.bg);
+      for (int j = 0; j < ch.bg; ++j) {
+        ps[j] = &plans[ch.mem[j]]->p;
+        fq[j] = freq_mhz[ch.mem[j]];
+      }
+      ch.st = factor_class(mode, ch.P, ps.data(), fq.data(), ch.bg, reinterpret_cast<double2*>(ch.store->z64),
+                           ch.store->lu, ch.store->ipiv, ch.info.data(), &ch.sets[0]->ws, ch.sets[0]->fs.span, cs);
+    }
+    cudaStreamSynchronize(cs);
+    cudaStreamDestroy(cs);
+  };
+  const int nthreads = std::min<int>((int)chunks.size(), 6);
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  cudaEventDestroy(start);
+  for (Chunk& ch : chunks) {
+    if (ch.st != WMOM_OK) return fail(ch.st);
+    for (int j = 0; j < ch.bg; ++j) ch.sets[j]->fs.info[0] = ch.info[j];
   }
   return WMOM_OK;
 }

@@ -1392,10 +1392,14 @@ void retain_pool_memory() {
 namespace {
 
 // Groups a sweep is split into so that the fill of one group (FP64 pipe) runs while
-// the previous group factors (tensor pipe): WMOM_PIPELINE = 1 (off) .. 8; default 2.
+// the previous group factors (tensor pipe): WMOM_PIPELINE = 1 .. 8, default 1 (off).
+// Measured on the 12-frequency N = 8192 sweep: 42.5 / 39.3 / 35.5 freq-solves/s for
+// 1 / 2 / 3 groups -- splitting the batch halves the parallelism of the
+// latency-bound panels (40 -> 68 ms per sweep), and the concurrent fill contends with
+// the factorisation for the SMs.
 int pipeline_groups() {
   const int v = env_int("WMOM_PIPELINE", 1, 8);
-  return v ? v : 2;
+  return v ? v : 1;
 }
 
 // The cached factorisation shape for (n, mode), if a sweep of that order was tuned.

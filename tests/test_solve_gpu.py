@@ -241,7 +241,7 @@ def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
 def test_pipelined_sweep_is_bit_identical(cuda, wmom, mode):
     """With the factorisation shape tuned, a sweep is split into groups whose fills run
     on a second stream while the previous group factors (WMOM_PIPELINE groups,
-    default 2); the currents, input impedances and reports must not depend on the
+    default 1, i.e. off); the currents, input impedances and reports must not depend on the
     number of groups."""
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
     plan = wmom.Plan(topo)
