@@ -1392,14 +1392,17 @@ void retain_pool_memory() {
 namespace {
 
 // Groups a sweep is split into so that the fill of one group (FP64 pipe) runs while
-// the previous group factors (tensor pipe): WMOM_PIPELINE = 1 .. 8, default 1 (off).
-// Measured on the 12-frequency N = 8192 sweep: 42.5 / 39.3 / 35.5 freq-solves/s for
-// 1 / 2 / 3 groups -- splitting the batch halves the parallelism of the
-// latency-bound panels (40 -> 68 ms per sweep), and the concurrent fill contends with
-// the factorisation for the SMs.
-int pipeline_groups() {
+// the previous group factors (tensor pipe).  By default only a sweep of at least two
+// groups of the tuned batch width is pipelined, at that width: splitting a batch
+// narrower costs more than the overlap saves (12-frequency N = 8192 sweep, batch 12:
+// 42.5 / 39.3 / 35.5 freq-solves/s for 1 / 2 / 3 groups -- half the parallelism of
+// the latency-bound panels, 40 -> 68 ms per sweep), while full-width groups gain
+// (256-frequency N = 2048 grid, batch 16: 209.5 -> 214.7).  WMOM_PIPELINE = 1 .. 8
+// forces that many groups (1 = off).
+int pipeline_groups(int nfreq, int batch) {
   const int v = env_int("WMOM_PIPELINE", 1, 8);
-  return v ? v : 1;
+  if (v) return v;
+  return nfreq >= 2 * batch ? (nfreq + batch - 1) / batch : 1;
 }
 
 // The cached factorisation shape for (n, mode), if a sweep of that order was tuned.
@@ -1513,10 +1516,10 @@ wmom_status run_sweep(const SweepArgs& a) {
     // pipelined when the shape is already tuned, the sweep has more than one group
     // and all its matrices fit
     LuConfig cfg;
-    const int G = pipeline_groups();
     size_t fr = 0, tot = 0;
-    if (G > 1 && a.nfreq >= 2 * G && cached_lu_config(a.mode, a.plan->npls, &cfg) &&
-        cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+    int G = 1;
+    if (cached_lu_config(a.mode, a.plan->npls, &cfg)) G = pipeline_groups(a.nfreq, cfg.batch);
+    if (G > 1 && a.nfreq >= 2 * G && cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
       const size_t nn = (size_t)a.plan->npls * a.plan->npls;
       const size_t need = nn * (sizeof(double2) * a.nfreq + sizeof(double2) * cfg.batch);
       const size_t budget = a.mem_budget ? a.mem_budget : fr / 2;

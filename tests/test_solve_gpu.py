@@ -240,9 +240,9 @@ def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
 @pytest.mark.parametrize("mode", [0, 1])
 def test_pipelined_sweep_is_bit_identical(cuda, wmom, mode):
     """With the factorisation shape tuned, a sweep is split into groups whose fills run
-    on a second stream while the previous group factors (WMOM_PIPELINE groups,
-    default 1, i.e. off); the currents, input impedances and reports must not depend on the
-    number of groups."""
+    on a second stream while the previous group factors (WMOM_PIPELINE groups; by
+    default only sweeps of two or more full-width groups); the currents, input
+    impedances and reports must not depend on the number of groups."""
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
     plan = wmom.Plan(topo)
     freqs = np.array([0.003, 0.02, 0.2, 1.0, 3.0, 7.0, 12.0, 25.0], np.float32)
