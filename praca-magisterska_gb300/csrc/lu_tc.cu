@@ -26,11 +26,14 @@
 // still frees its TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -45,9 +48,10 @@ namespace tc {
 constexpr int BM = 128;  // accumulator lanes = rows of C per CTA
 constexpr int BN = 256;  // accumulator FP32 columns = 128 complex columns of C
 constexpr int KC = 32;   // FP32 elements of K per chunk (128 bytes)
+constexpr int KC16 = 64; // FP16 elements of K per chunk (128 bytes)
 constexpr int STAGES = 2;
-constexpr int A_BYTES = BM * KC * 4;  // 16 KB per plane
-constexpr int B_BYTES = BN * KC * 4;  // 32 KB per plane
+constexpr int A_BYTES = BM * 128;  // 16 KB per plane (one 128-byte row of K per row)
+constexpr int B_BYTES = BN * 128;  // 32 KB per plane
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
 constexpr int NTHREADS = 192;         // producer warp, MMA warp, 4 epilogue warps
@@ -65,6 +69,18 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+// Instruction descriptor of the FP16-plane variant: D = F32, A = B = F16, both K-major.
+constexpr uint32_t kIdescF16 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdescF16), "r"(accumulate)
       : "memory");
 }
 
@@ -133,6 +149,117 @@ __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K
   lo[r1 + 1] = lr;
 }
 
+// ------------------------------------------------------- FP16 planes ----
+// The FP16-plane variant scales every row of A' and every complex column of B by a
+// power of two that brings its largest |re| or |im| into [2^14, 2^15) -- inside the
+// FP16 range (65504) with room for the rounding of the head -- and splits each scaled
+// value x into an FP16 head and tail, hi = fp16(x), lo = fp16(x - hi) (x - hi is exact
+// in FP32): 22 significant bits, as the TF32 head and tail.  Entries far below their
+// row's or column's maximum lose relative bits in the FP16 subnormal range, never more
+// than 2^-39 of that maximum, i.e. the split is accurate normwise.  The epilogue
+// multiplies each accumulator by 2^-(e_row + e_col).
+
+__device__ __forceinline__ int fp16_scale_exp(float mx) {
+  if (!(mx > 0.f) || !(mx < 3.0e38f)) return 0;  // zero (or not finite): no scaling
+  int e;
+  frexpf(mx, &e);  // mx in [2^(e-1), 2^e)
+  return 15 - e;
+}
+
+// ea[m] for the rows of A (M x K complex, column-major): one thread per row.
+__global__ void rowexp_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int* __restrict__ ea,
+                                long long astride) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  A += (size_t)blockIdx.y * astride;
+  float mx = 0.f;
+  for (int k = 0; k < K; ++k) {
+    const float2 v = A[(size_t)k * lda + m];
+    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  ea[(size_t)blockIdx.y * M + m] = fp16_scale_exp(mx);
+}
+
+// eb[n] for the columns of B (K x N complex, column-major): one warp per column.
+__global__ void colexp_b_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int* __restrict__ eb,
+                                long long bstride) {
+  const int n = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (n >= N) return;
+  B += (size_t)blockIdx.y * bstride + (size_t)n * ldb;
+  float mx = 0.f;
+  for (int k = lane; k < K; k += 32) mx = fmaxf(mx, fmaxf(fabsf(B[k].x), fabsf(B[k].y)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) eb[(size_t)blockIdx.y * N + n] = fp16_scale_exp(mx);
+}
+
+__device__ __forceinline__ void split_f16(float x, __half* hi, __half* lo) {
+  const __half h = __float2half_rn(x);
+  *hi = h;
+  *lo = __float2half_rn(x - __half2float(h));
+}
+
+// pack_a_kernel's transpose with FP16 planes of the scaled rows.
+__global__ void __launch_bounds__(256) pack_a_f16_kernel(const float2* __restrict__ A, long long lda, int M, int K,
+                                                         int K2p, __half* __restrict__ hi, __half* __restrict__ lo,
+                                                         const int* __restrict__ ea, long long astride) {
+  __shared__ float2 tile[32][33];  // [complex column][row]
+  A += (size_t)blockIdx.z * astride;
+  hi += (size_t)blockIdx.z * M * K2p;
+  lo += (size_t)blockIdx.z * M * K2p;
+  ea += (size_t)blockIdx.z * M;
+  const int m0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int k = k0 + ty + 8 * i, m = m0 + tx;
+    tile[ty + 8 * i][tx] = (k < K && m < M) ? A[(size_t)k * lda + m] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = ty + 8 * i, m = m0 + r, k = k0 + tx;
+    if (m >= M || 2 * k >= K2p) continue;
+    const float2 v = tile[tx][r];
+    const int e = ea[m];
+    __half2 h, l;
+    split_f16(ldexpf(v.x, e), &h.x, &l.x);
+    split_f16(ldexpf(v.y, e), &h.y, &l.y);
+    const size_t o = (size_t)m * K2p + 2 * k;
+    *reinterpret_cast<__half2*>(hi + o) = h;
+    *reinterpret_cast<__half2*>(lo + o) = l;
+  }
+}
+
+// pack_b_kernel with FP16 planes of the scaled columns.
+__global__ void pack_b_f16_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int K2p,
+                                  __half* __restrict__ hi, __half* __restrict__ lo, const int* __restrict__ eb,
+                                  long long bstride) {
+  B += (size_t)blockIdx.z * bstride;
+  hi += (size_t)blockIdx.z * 2 * N * K2p;
+  lo += (size_t)blockIdx.z * 2 * N * K2p;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // complex row of B, K2p/2 of them
+  const int n = blockIdx.y;
+  if (2 * k >= K2p) return;
+  const int e = eb[(size_t)blockIdx.z * N + n];
+  float2 v = make_float2(0.f, 0.f);
+  if (k < K) v = B[(size_t)n * ldb + k];
+  __half hr, lr, hi_, li;
+  split_f16(ldexpf(v.x, e), &hr, &lr);
+  split_f16(ldexpf(v.y, e), &hi_, &li);
+  const size_t r0 = (size_t)(2 * n) * K2p + 2 * k;
+  const size_t r1 = (size_t)(2 * n + 1) * K2p + 2 * k;
+  hi[r0] = hr;
+  hi[r0 + 1] = __hneg(hi_);
+  hi[r1] = hi_;
+  hi[r1 + 1] = hr;
+  lo[r0] = lr;
+  lo[r0 + 1] = __hneg(li);
+  lo[r1] = li;
+  lo[r1 + 1] = lr;
+}
+
 // ---------------------------------------------------------------- gemm ----
 // Persistent, warp-specialised: CTA b takes output tiles b, b + grid, ... (tiles
 // ordered rows fastest, then columns, then matrices of the batch).
@@ -159,11 +286,16 @@ __device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n)
   return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
 }
 
+// F16: FP16 planes of scaled operands (kind::f16, 64 elements of K per chunk; ea / eb
+// hold the rows' and columns' exponents), else TF32 planes (kind::tf32, 32 per chunk).
+template <bool F16>
 __global__ void __launch_bounds__(NTHREADS, 1)
     cgemm_sub_tc_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                         const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
                         float2* __restrict__ C, long long ldc, int M, int N, int nchunks, int tiles_m,
-                        int tiles_n, int ntiles, int* __restrict__ err, long long cstride) {
+                        int tiles_n, int ntiles, int* __restrict__ err, long long cstride,
+                        const int* __restrict__ ea, const int* __restrict__ eb) {
+  constexpr int kChunk = F16 ? KC16 : KC;  // K elements per chunk (128 bytes)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -214,10 +346,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t a_hi = smem_u32(base + s * STAGE_BYTES), a_lo = a_hi + A_BYTES;
           const uint32_t b_hi = a_hi + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
           mbar_expect_tx(full_bar(s), STAGE_BYTES);
-          tma_load_3d(a_hi, &mapAhi, c * KC, tc.m0, tc.mat, full_bar(s));
-          tma_load_3d(a_lo, &mapAlo, c * KC, tc.m0, tc.mat, full_bar(s));
-          tma_load_3d(b_hi, &mapBhi, c * KC, tc.j0, tc.mat, full_bar(s));
-          tma_load_3d(b_lo, &mapBlo, c * KC, tc.j0, tc.mat, full_bar(s));
+          tma_load_3d(a_hi, &mapAhi, c * kChunk, tc.m0, tc.mat, full_bar(s));
+          tma_load_3d(a_lo, &mapAlo, c * kChunk, tc.m0, tc.mat, full_bar(s));
+          tma_load_3d(b_hi, &mapBhi, c * kChunk, tc.j0, tc.mat, full_bar(s));
+          tma_load_3d(b_lo, &mapBlo, c * kChunk, tc.j0, tc.mat, full_bar(s));
           ++it;
         }
       }
@@ -250,11 +382,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           // tail terms first, head product last
           const uint32_t as[3] = {a_lo, a_hi, a_hi};
           const uint32_t bs[3] = {b_hi, b_lo, b_hi};
+          // 4 MMAs of 32 bytes of K each per plane product (K = 8 TF32 or 16 FP16)
 #pragma unroll
           for (int sp = 0; sp < 3; ++sp)
 #pragma unroll
-            for (int kk = 0; kk < KC / 8; ++kk)
-              mma_tf32(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), (c | sp | kk) != 0 ? 1u : 0u);
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t accum = (c | sp | kk) != 0 ? 1u : 0u;
+              if constexpr (F16)
+                mma_f16(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
+              else
+                mma_tf32(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
+            }
           mma_commit(empty_bar(s));
           ++it;
         }
@@ -281,6 +419,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       float2* Cm = C + (size_t)tc.mat * cstride;
       const int row = tc.m0 + q * 32 + lane;
       const bool row_ok = row < M;
+      // FP16 planes: the row's exponent (the columns' are read per chunk)
+      const int erow = F16 && row_ok ? ea[(size_t)tc.mat * M + row] : 0;
       auto load_c_chunk = [&](int cc, float2* dst) {
         const int n0 = (tc.j0 >> 1) + cc * 16;
 #pragma unroll
@@ -323,8 +463,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int j = 0; j < 16; ++j) {
             if (n0 + j < N) {
               float2 v = cbuf[j];
-              v.x -= __uint_as_float(r[2 * j]);
-              v.y -= __uint_as_float(r[2 * j + 1]);
+              float pr = __uint_as_float(r[2 * j]), pi = __uint_as_float(r[2 * j + 1]);
+              if constexpr (F16) {
+                const int e = -(erow + eb[(size_t)tc.mat * N + n0 + j]);
+                pr = ldexpf(pr, e);
+                pi = ldexpf(pi, e);
+              }
+              v.x -= pr;
+              v.y -= pi;
               Cm[(size_t)(n0 + j) * ldc + row] = v;
             }
           }
@@ -364,18 +510,31 @@ EncodeFn encode_fn() {
 
 namespace {
 
-// 3-D map over `batch` planes of rows x k2p FP32 (row-major), 32 x box_rows boxes.
-bool make_map(CUtensorMap* map, const float* ptr, int rows, int k2p, int batch, int box_rows) {
+// 3-D map over `batch` planes of rows x k2p elements (row-major; FP32 or FP16),
+// boxes of one 128-byte row of K x box_rows.
+bool make_map(CUtensorMap* map, const void* ptr, int rows, int k2p, int batch, int box_rows, bool f16) {
   EncodeFn enc = encode_fn();
   if (!enc) return false;
+  const size_t elem = f16 ? 2 : 4;
   cuuint64_t dims[3] = {(cuuint64_t)k2p, (cuuint64_t)rows, (cuuint64_t)batch};
-  cuuint64_t strides[2] = {(cuuint64_t)k2p * sizeof(float), (cuuint64_t)rows * k2p * sizeof(float)};
-  cuuint32_t box[3] = {(cuuint32_t)KC, (cuuint32_t)box_rows, 1};
+  cuuint64_t strides[2] = {(cuuint64_t)k2p * elem, (cuuint64_t)rows * k2p * elem};
+  cuuint32_t box[3] = {(cuuint32_t)(f16 ? KC16 : KC), (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(ptr), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+  CUresult r = enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                   const_cast<void*>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
+}
+
+// Operand planes of the tensor-core update: FP16 (scaled, kind::f16) when
+// WMOM_TC_PLANES=f16, TF32 when tf32 (the default).
+bool f16_planes() {
+  static const bool on = [] {
+    const char* e = std::getenv("WMOM_TC_PLANES");
+    return e && std::strcmp(e, "f16") == 0;
+  }();
+  return on;
 }
 
 }  // namespace
@@ -426,23 +585,50 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
                          long long bstride) {
   if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
   if (!ws || batch < 1 || batch > 65535 || N > 65535) return cudaErrorInvalidValue;
-  const int K2p = ((2 * K + KC - 1) / KC) * KC;
+  const bool f16 = f16_planes();
+  const int kc = f16 ? KC16 : KC;
+  const int K2p = ((2 * K + kc - 1) / kc) * kc;
+  // planes in elements; the FP16 variant's row and column exponents follow its planes
   const size_t a_pl = (size_t)M * K2p * batch, b_pl = (size_t)2 * N * K2p * batch;
-  cudaError_t e = tc_scratch(ws, 2 * a_pl + 2 * b_pl, s);
+  const size_t plane_floats = f16 ? (a_pl + b_pl) : 2 * a_pl + 2 * b_pl;
+  const size_t exp_ints = f16 ? ((size_t)M + (size_t)N) * batch : 0;
+  cudaError_t e = tc_scratch(ws, plane_floats + exp_ints, s);
   if (e != cudaSuccess) return e;
-  float* ahi = ws->tc_buf;
-  float* alo = ahi + a_pl;
-  float* bhi = alo + a_pl;
-  float* blo = bhi + b_pl;
-  stats::count(stats::kMisc, 2);
-  pack_a_kernel<<<dim3((M + 31) / 32, (K2p / 2 + 31) / 32, batch), 256, 0, s>>>(A, lda, M, K, K2p, ahi, alo,
-                                                                                bstride);
-  pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
   CUtensorMap mah, mal, mbh, mbl;
-  if (!make_map(&mah, ahi, M, K2p, batch, BM) || !make_map(&mal, alo, M, K2p, batch, BM) ||
-      !make_map(&mbh, bhi, 2 * N, K2p, batch, BN) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN))
-    return cudaErrorInvalidValue;
-  e = allow_dynamic_smem((const void*)cgemm_sub_tc_kernel, SMEM_BYTES);
+  const void* kern = f16 ? (const void*)cgemm_sub_tc_kernel<true> : (const void*)cgemm_sub_tc_kernel<false>;
+  int* ea = nullptr;
+  int* eb = nullptr;
+  if (f16) {
+    __half* ahi = reinterpret_cast<__half*>(ws->tc_buf);
+    __half* alo = ahi + a_pl;
+    __half* bhi = alo + a_pl;
+    __half* blo = bhi + b_pl;
+    ea = reinterpret_cast<int*>(ws->tc_buf + plane_floats);
+    eb = ea + (size_t)M * batch;
+    stats::count(stats::kMisc, 4);
+    rowexp_a_kernel<<<dim3((M + 255) / 256, batch), 256, 0, s>>>(A, lda, M, K, ea, bstride);
+    colexp_b_kernel<<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, eb, bstride);
+    pack_a_f16_kernel<<<dim3((M + 31) / 32, (K2p / 2 + 31) / 32, batch), 256, 0, s>>>(A, lda, M, K, K2p, ahi, alo,
+                                                                                      ea, bstride);
+    pack_b_f16_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, eb,
+                                                                           bstride);
+    if (!make_map(&mah, ahi, M, K2p, batch, BM, true) || !make_map(&mal, alo, M, K2p, batch, BM, true) ||
+        !make_map(&mbh, bhi, 2 * N, K2p, batch, BN, true) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN, true))
+      return cudaErrorInvalidValue;
+  } else {
+    float* ahi = ws->tc_buf;
+    float* alo = ahi + a_pl;
+    float* bhi = alo + a_pl;
+    float* blo = bhi + b_pl;
+    stats::count(stats::kMisc, 2);
+    pack_a_kernel<<<dim3((M + 31) / 32, (K2p / 2 + 31) / 32, batch), 256, 0, s>>>(A, lda, M, K, K2p, ahi, alo,
+                                                                                  bstride);
+    pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
+    if (!make_map(&mah, ahi, M, K2p, batch, BM, false) || !make_map(&mal, alo, M, K2p, batch, BM, false) ||
+        !make_map(&mbh, bhi, 2 * N, K2p, batch, BN, false) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN, false))
+      return cudaErrorInvalidValue;
+  }
+  e = allow_dynamic_smem(kern, SMEM_BYTES);
   if (e != cudaSuccess) return e;
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
   const long long ntiles = (long long)tiles_m * tiles_n * batch;
@@ -456,8 +642,14 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
   }
   const int grid = (int)std::min<long long>(ntiles, nsm);
   stats::Scope sc(stats::kTcGemm, s, 8.0 * M * (double)N * K * batch);
-  cgemm_sub_tc_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / KC, tiles_m,
-                                                          tiles_n, (int)ntiles, ws->tc_err, bstride);
+  if (f16)
+    cgemm_sub_tc_kernel<true><<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
+                                                                 tiles_m, tiles_n, (int)ntiles, ws->tc_err,
+                                                                 bstride, ea, eb);
+  else
+    cgemm_sub_tc_kernel<false><<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
+                                                                  tiles_m, tiles_n, (int)ntiles, ws->tc_err,
+                                                                  bstride, nullptr, nullptr);
   return cudaGetLastError();
 }
 
