@@ -194,6 +194,11 @@ __global__ void colexp_b_kernel(const float2* __restrict__ B, long long ldb, int
   if (lane == 0) eb[(size_t)blockIdx.y * N + n] = fp16_scale_exp(mx);
 }
 
+// 2^k as a float, exactly: built from its exponent field where that is normal
+__device__ __forceinline__ float pow2f(int k) {
+  return (k >= -126 && k <= 127) ? __int_as_float((k + 127) << 23) : ldexpf(1.0f, k);
+}
+
 __device__ __forceinline__ void split_f16(float x, __half* hi, __half* lo) {
   const __half h = __float2half_rn(x);
   *hi = h;
@@ -419,8 +424,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       float2* Cm = C + (size_t)tc.mat * cstride;
       const int row = tc.m0 + q * 32 + lane;
       const bool row_ok = row < M;
-      // FP16 planes: the row's exponent (the columns' are read per chunk)
-      const int erow = F16 && row_ok ? ea[(size_t)tc.mat * M + row] : 0;
+      // FP16 planes: the row's scale (the columns' are read per chunk)
+      const float srow = F16 && row_ok ? pow2f(-ea[(size_t)tc.mat * M + row]) : 1.0f;
       auto load_c_chunk = [&](int cc, float2* dst) {
         const int n0 = (tc.j0 >> 1) + cc * 16;
 #pragma unroll
@@ -465,9 +470,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               float2 v = cbuf[j];
               float pr = __uint_as_float(r[2 * j]), pi = __uint_as_float(r[2 * j + 1]);
               if constexpr (F16) {
-                const int e = -(erow + eb[(size_t)tc.mat * N + n0 + j]);
-                pr = ldexpf(pr, e);
-                pi = ldexpf(pi, e);
+                // the scaled product times 2^-e_row, then 2^-e_col: exact unless the
+                // true product is below FP32's normal range
+                const float scol = pow2f(-eb[(size_t)tc.mat * N + n0 + j]);
+                pr = (pr * srow) * scol;
+                pi = (pi * srow) * scol;
               }
               v.x -= pr;
               v.y -= pi;
