@@ -580,7 +580,7 @@ def serve_rates(args, rates, seconds):
         warm = serve.Server(workers=1)  # warm-up: CUDA context, kernels, batch-width tuner
         warm.submit(serve.Request(pool[0], grid[:2], 1, currents=False)).result()
         warm.close()
-        srv = serve.Server(workers=args.serve_workers)
+        srv = serve.Server(workers=args.serve_workers, coalesce_freqs=args.serve_coalesce)
         t_end = time.perf_counter() + seconds
         history, futs = [], []
         t = time.perf_counter()
@@ -602,7 +602,8 @@ def serve_rates(args, rates, seconds):
         st.update(offered_req_per_s=rate, submitted=len(futs), seconds=seconds,
                   workload=f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}] over "
                            f"{args.serve_geometries} geometries, 1-16 frequencies in 1 kHz-30 MHz, 30% repeat "
-                           f"excitations, {args.serve_workers} worker streams")
+                           f"excitations, {args.serve_workers} worker streams, waiting requests of one "
+                           f"geometry factored together up to {args.serve_coalesce} frequencies")
         results.append(st)
     return results
 
@@ -616,7 +617,7 @@ def run_serving(args):
             "config": {"workload": f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}], 1-16 "
                                    "frequencies in 1 kHz-30 MHz, 30% repeat excitations",
                        "geometries": args.serve_geometries, "seconds_per_rate": args.serve_seconds,
-                       "workers": args.serve_workers},
+                       "workers": args.serve_workers, "coalesce_freqs": args.serve_coalesce},
             "rates": results}
     print(json.dumps(line), flush=True)
 
@@ -813,6 +814,8 @@ def main():
     ap.add_argument("--serve-nmax", type=int, default=6144)
     ap.add_argument("--serve-geometries", type=int, default=8)
     ap.add_argument("--serve-workers", type=int, default=4)  # 4 beat 2 at the saturated rates
+    ap.add_argument("--serve-coalesce", type=int, default=32,
+                    help="distinct frequencies of one geometry factored together (0: one request at a time)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

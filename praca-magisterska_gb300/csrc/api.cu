@@ -60,46 +60,75 @@ cudaError_t allow_dynamic_smem(const void* func, size_t bytes) {
 }
 
 // ---------------------------------------------------------- workspace ----
-cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch) {
+namespace {
+
+cudaError_t ws_alloc(const LuWorkspace* ws, void** p, size_t bytes, cudaStream_t s) {
+  return ws->pooled ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+}
+
+cudaError_t ws_zero(const LuWorkspace* ws, void* p, size_t bytes, cudaStream_t s) {
+  return ws->pooled ? cudaMemsetAsync(p, 0, bytes, s) : cudaMemset(p, 0, bytes);
+}
+
+cudaError_t workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch, bool pooled, cudaStream_t s) {
   *ws = LuWorkspace{};
+  ws->pooled = pooled;
   max_batch = std::max(max_batch, 1);
   const size_t off = lu_stage_offset(max_batch);
   const size_t bytes = off + lu_stage_bytes(max_batch);
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes);
-  if (e != cudaSuccess) return e;
-  e = cudaMemset(p, 0, bytes);
+  cudaError_t e = ws_alloc(ws, &p, bytes, s);
   if (e != cudaSuccess) return e;
   ws->max_batch = max_batch;
   ws->barrier = reinterpret_cast<GridBarrier*>(p);
   ws->stage = reinterpret_cast<char*>(p) + off;
-  e = cudaMalloc(&ws->perm, sizeof(int) * (size_t)std::max(nmax, 1) * max_batch);
+  e = ws_zero(ws, p, bytes, s);
+  if (e != cudaSuccess) return e;
+  e = ws_alloc(ws, reinterpret_cast<void**>(&ws->perm), sizeof(int) * (size_t)std::max(nmax, 1) * max_batch, s);
   if (e != cudaSuccess) return e;
   ws->perm_cap = nmax;
   ws->rhs_bytes =
       sizeof(double2) * (size_t)std::max(nmax, 1) * (size_t)std::max(std::max(nrhs_max, 1), max_batch);
-  e = cudaMalloc(&ws->rhs, ws->rhs_bytes);
+  e = ws_alloc(ws, &ws->rhs, ws->rhs_bytes, s);
   if (e != cudaSuccess) return e;
   ws->flag_cap = (std::max(nmax, 1) + 63) / 64 + 1;
   const size_t fbytes = sizeof(int) * ((size_t)ws->flag_cap * max_batch + max_batch);
-  e = cudaMalloc(&ws->flags, fbytes);
+  e = ws_alloc(ws, reinterpret_cast<void**>(&ws->flags), fbytes, s);
   if (e != cudaSuccess) return e;
-  e = cudaMemset(ws->flags, 0, fbytes);
+  e = ws_zero(ws, ws->flags, fbytes, s);
   if (e != cudaSuccess) return e;
   ws->ticket = reinterpret_cast<unsigned int*>(ws->flags + (size_t)ws->flag_cap * max_batch);
   ws->epoch = 0;
-  e = cudaMalloc(&ws->tc_err, sizeof(int));
+  e = ws_alloc(ws, reinterpret_cast<void**>(&ws->tc_err), sizeof(int), s);
   if (e != cudaSuccess) return e;
-  return cudaMemset(ws->tc_err, 0, sizeof(int));
+  return ws_zero(ws, ws->tc_err, sizeof(int), s);
+}
+
+}  // namespace
+
+cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch) {
+  return workspace_create(ws, nmax, nrhs_max, max_batch, false, nullptr);
+}
+
+cudaError_t lu_workspace_create_async(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch, cudaStream_t s) {
+  return workspace_create(ws, nmax, nrhs_max, max_batch, true, s);
 }
 
 void lu_workspace_destroy(LuWorkspace* ws) {
-  if (ws->barrier) cudaFree(ws->barrier);
-  if (ws->perm) cudaFree(ws->perm);
-  if (ws->rhs) cudaFree(ws->rhs);
-  if (ws->flags) cudaFree(ws->flags);
-  if (ws->tc_buf) cudaFree(ws->tc_buf);
-  if (ws->tc_err) cudaFree(ws->tc_err);
+  const bool pooled = ws->pooled;
+  auto release = [pooled](void* p) {
+    if (!p) return;
+    if (pooled)
+      cudaFreeAsync(p, cudaStreamPerThread);
+    else
+      cudaFree(p);
+  };
+  release(ws->barrier);
+  release(ws->perm);
+  release(ws->rhs);
+  release(ws->flags);
+  release(ws->tc_buf);
+  release(ws->tc_err);
   *ws = LuWorkspace{};
 }
 
@@ -548,14 +577,16 @@ struct wmom_factors_s {
 namespace {
 
 // Matrices, factors and pivots of one class of a geometry batch.
+// They come from the stream-ordered pool and go back to it on the releasing thread's
+// default stream, after every call that used them has synchronised its stream.
 struct ClassStore {
   void* z64 = nullptr;
   void* lu = nullptr;
   int* ipiv = nullptr;
   ~ClassStore() {
-    if (z64) cudaFree(z64);
-    if (lu) cudaFree(lu);
-    if (ipiv) cudaFree(ipiv);
+    if (z64) cudaFreeAsync(z64, cudaStreamPerThread);
+    if (lu) cudaFreeAsync(lu, cudaStreamPerThread);
+    if (ipiv) cudaFreeAsync(ipiv, cudaStreamPerThread);
   }
 };
 
@@ -579,8 +610,9 @@ wmom_status wmom_factor(wmom_plan h, const float* freq_mhz, int nfreq, int mode,
   if (need > fr) return WMOM_ERR_NOMEM;
   wmom_factors_s* f = new (std::nothrow) wmom_factors_s();
   if (!f) return WMOM_ERR_NOMEM;
-  cudaError_t e = lu_workspace_create(&f->ws, n, 1, kMaxLuBatch);
+  cudaError_t e = lu_workspace_create_async(&f->ws, n, 1, kMaxLuBatch, (cudaStream_t)stream);
   if (e != cudaSuccess) {
+    cudaStreamSynchronize((cudaStream_t)stream);
     lu_workspace_destroy(&f->ws);
     delete f;
     return wmom_fail_cuda(e, "factor workspace");
@@ -598,6 +630,7 @@ wmom_status wmom_factor(wmom_plan h, const float* freq_mhz, int nfreq, int mode,
     st = factors_build(&f->fs, (cudaStream_t)stream);
   }
   if (st != WMOM_OK) {
+    cudaStreamSynchronize((cudaStream_t)stream);  // nothing of the set still queued
     wmom_factors_destroy(f);
     return st;
   }
@@ -619,9 +652,15 @@ long long wmom_factors_device_bytes(wmom_factors f) { return f ? (long long)f->b
 
 wmom_status wmom_factors_destroy(wmom_factors f) {
   if (!f) return WMOM_ERR_ARG;
-  cudaDeviceSynchronize();
+  // Every call on the set synchronised its stream before it returned, so nothing of
+  // the set is still queued: its pooled memory goes back to the pool in the order of
+  // this thread's default stream, without waiting for other streams' work.
   if (f->shared) {
     f->shared.reset();  // the class's storage goes with its last set
+  } else if (f->fs.pooled) {
+    if (f->fs.z64) cudaFreeAsync(f->fs.z64, cudaStreamPerThread);
+    if (f->fs.lu) cudaFreeAsync(f->fs.lu, cudaStreamPerThread);
+    if (f->fs.ipiv) cudaFreeAsync(f->fs.ipiv, cudaStreamPerThread);
   } else {
     if (f->fs.z64) cudaFree(f->fs.z64);
     if (f->fs.lu) cudaFree(f->fs.lu);
@@ -661,7 +700,9 @@ wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const floa
   std::set<wmom_plan> uniq(plans, plans + count);
   std::vector<std::unique_lock<std::mutex>> locks;
   for (wmom_plan h : uniq) locks.emplace_back(h->mu);
+  retain_pool_memory();
   auto fail = [&](wmom_status st) {
+    cudaStreamSynchronize(s);  // allocations and clears of the sets queued on s
     for (int i = 0; i < count; ++i)
       if (out[i]) {
         wmom_factors_destroy(out[i]);
@@ -690,9 +731,9 @@ wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const floa
       ch.bg = (int)std::min<size_t>(kMaxLuBatch, kv.second.size() - c0);
       ch.mem.assign(kv.second.begin() + c0, kv.second.begin() + c0 + ch.bg);
       ch.store = std::make_shared<ClassStore>();
-      cudaError_t e = cudaMalloc(&ch.store->z64, sizeof(double2) * nn * ch.bg);
-      if (e == cudaSuccess) e = cudaMalloc(&ch.store->lu, elem * nn * ch.bg);
-      if (e == cudaSuccess) e = cudaMalloc(&ch.store->ipiv, sizeof(int) * (size_t)P * ch.bg);
+      cudaError_t e = cudaMallocAsync(&ch.store->z64, sizeof(double2) * nn * ch.bg, s);
+      if (e == cudaSuccess) e = cudaMallocAsync(&ch.store->lu, elem * nn * ch.bg, s);
+      if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&ch.store->ipiv), sizeof(int) * (size_t)P * ch.bg, s);
       if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "geometry batch storage"));
       ch.sets.assign(ch.bg, nullptr);
       ch.info.assign(ch.bg, 0);
@@ -701,7 +742,7 @@ wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const floa
         if (!f) return fail(WMOM_ERR_NOMEM);
         out[ch.mem[j]] = f;
         ch.sets[j] = f;
-        e = lu_workspace_create(&f->ws, P, 1, kMaxLuBatch);
+        e = lu_workspace_create_async(&f->ws, P, 1, kMaxLuBatch, s);
         if (e != cudaSuccess) return fail(wmom_fail_cuda(e, "factor workspace"));
         wmom_plan h = plans[ch.mem[j]];
         f->plan = h;

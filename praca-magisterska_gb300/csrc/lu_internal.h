@@ -43,6 +43,9 @@ struct LuWorkspace {
   size_t tc_cap = 0;  // floats
   unsigned tc_gen = 0;
   int* tc_err = nullptr;
+  // allocated from the device's stream-ordered pool (lu_workspace_create_async):
+  // growing and freeing it never waits for work on other streams
+  bool pooled = false;
 };
 
 size_t lu_workspace_bytes(int elem_bytes);  // one matrix: barrier + staging
@@ -95,6 +98,13 @@ extern std::atomic<unsigned int> g_panel_missing_arrivals;
 
 // Workspace management (api.cu).
 cudaError_t lu_workspace_create(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch = 1);
+// The same workspace from the device's stream-ordered pool, allocated and cleared in
+// the order of `s`.  Factor sets that a serving loop creates and evicts while other
+// streams run use it: cudaMalloc / cudaFree may wait for the whole device.
+cudaError_t lu_workspace_create_async(LuWorkspace* ws, int nmax, int nrhs_max, int max_batch, cudaStream_t s);
+// Frees a workspace.  A pooled one is returned to the pool on the calling thread's
+// default stream: every call that used it must have finished (the library's entry
+// points synchronise their stream before returning).
 void lu_workspace_destroy(LuWorkspace* ws);
 cudaError_t lu_workspace_reset_barrier(LuWorkspace* ws, cudaStream_t s);
 // Returns nonzero when a wait of the last factorisation timed out; info[b] = the

@@ -548,7 +548,8 @@ bool f16_planes() {
 
 // Grows ws->tc_buf to `floats`.  Inside a stream capture it refuses (the capture
 // then fails and the caller launches directly, which grows the buffer); otherwise
-// the old buffer is released only after the work queued on `s` has finished.
+// the old buffer is released only after the work queued on `s` has finished (in
+// stream order for a pooled workspace, else by waiting for `s`).
 cudaError_t tc_scratch(LuWorkspace* ws, size_t floats, cudaStream_t s) {
   if (!ws->tc_err) {
     cudaError_t e = cudaMalloc(&ws->tc_err, sizeof(int));
@@ -562,13 +563,18 @@ cudaError_t tc_scratch(LuWorkspace* ws, size_t floats, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   if (cs != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
   if (ws->tc_buf) {
-    e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
-    cudaFree(ws->tc_buf);
+    if (ws->pooled) {
+      e = cudaFreeAsync(ws->tc_buf, s);
+    } else {
+      e = cudaStreamSynchronize(s);
+      if (e == cudaSuccess) e = cudaFree(ws->tc_buf);
+    }
     ws->tc_buf = nullptr;
     ws->tc_cap = 0;
+    if (e != cudaSuccess) return e;
   }
-  e = cudaMalloc(&ws->tc_buf, floats * sizeof(float));
+  e = ws->pooled ? cudaMallocAsync(reinterpret_cast<void**>(&ws->tc_buf), floats * sizeof(float), s)
+                 : cudaMalloc(&ws->tc_buf, floats * sizeof(float));
   if (e != cudaSuccess) {
     ws->tc_buf = nullptr;
     return e;

@@ -1359,14 +1359,12 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   return WMOM_OK;
 }
 
-namespace {
-
 // The sweep's buffers (Z of a frequency batch and its factors: about 19 GB at
-// N = 8192 and 12 frequencies) come from the stream-ordered allocator.  With the
-// default pool's release threshold of 0 that memory is handed back at every
-// synchronisation and mapped again by the next sweep; the pool of this process keeps
-// up to an eighth of the device's memory instead (WMOM_POOL_RETAIN_GB overrides, 0
-// keeps the default).
+// N = 8192 and 12 frequencies) and resident factor sets come from the stream-ordered
+// allocator.  With the default pool's release threshold of 0 that memory is handed
+// back at every synchronisation and mapped again by the next sweep; the pool of this
+// process keeps up to an eighth of the device's memory instead (WMOM_POOL_RETAIN_GB
+// overrides, 0 keeps the default).
 void retain_pool_memory() {
   static std::mutex mu;
   static std::vector<char> done;
@@ -1386,8 +1384,6 @@ void retain_pool_memory() {
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   cudaGetLastError();
 }
-
-}  // namespace
 
 namespace {
 
@@ -1675,9 +1671,13 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
   const size_t nn = (size_t)n * n;
   const bool mixed = fs->mode == WMOM_MODE_MIXED;
   const int nf = (int)fs->freq.size();
-  SWEEP_TRY(cudaMalloc(&fs->z64, sizeof(double2) * nn * nf));
-  SWEEP_TRY(cudaMalloc(&fs->lu, (mixed ? sizeof(float2) : sizeof(double2)) * nn * nf));
-  SWEEP_TRY(cudaMalloc(&fs->ipiv, sizeof(int) * (size_t)n * nf));
+  // from the stream-ordered pool: a serving loop creates and evicts sets while other
+  // streams run, and cudaMalloc / cudaFree may wait for the whole device
+  retain_pool_memory();
+  fs->pooled = true;
+  SWEEP_TRY(cudaMallocAsync(reinterpret_cast<void**>(&fs->z64), sizeof(double2) * nn * nf, s));
+  SWEEP_TRY(cudaMallocAsync(&fs->lu, (mixed ? sizeof(float2) : sizeof(double2)) * nn * nf, s));
+  SWEEP_TRY(cudaMallocAsync(reinterpret_cast<void**>(&fs->ipiv), sizeof(int) * (size_t)n * nf, s));
   fs->info.assign(nf, 0);
   wmom_status st = fill_batch(p, fs->freq.data(), nf, fs->z64, s);
   if (st != WMOM_OK) return st;

@@ -54,9 +54,16 @@ struct FactorSet {
   // (identity block beyond npls; factors_solve pads the excitation and returns npls
   // entries)
   int order = 0;
+  // z64, lu and ipiv come from the stream-ordered pool (freed without waiting for
+  // other streams)
+  bool pooled = false;
 };
 
 wmom_status factors_build(FactorSet* fs, cudaStream_t s);
+
+// Keeps up to an eighth of the device's memory (WMOM_POOL_RETAIN_GB) in the default
+// stream-ordered pool between synchronisations; once per device.
+void retain_pool_memory();
 
 // Geometries of uneven order (solve.cu): the padded order of n's size class (four
 // classes per octave, P <= 1.25 n); the span a factorisation of order n uses (the

@@ -9,7 +9,9 @@ requests as they arrive:
   device (libwmom wmom_factor), so a repeat excitation of a resident pair runs only
   the solves and refinement (wmom_factors_solve);
 * the frequencies a request still needs are filled and factored together, i.e.
-  batched on the device;
+  batched on the device, with those of the requests for the same geometry that are
+  waiting in the queue when a worker takes it (a frequency batch of one geometry:
+  its results do not depend on the batch's composition);
 * admission is by device-memory footprint: the bytes of the factor sets a request
   must create (Z + factors, nf * (16 + 8) * N^2 bytes in the precision form) are
   reserved against a budget; idle resident sets are evicted least-recently-used
@@ -72,7 +74,8 @@ class Server:
     """`lib` and `stream_factory` stand in for the solver package and the worker
     streams (the host-logic tests run the loop on the CPU against a fake library)."""
 
-    def __init__(self, mode=None, hbm_budget_bytes=None, workers=2, tol=1e-12, lib=None, stream_factory=None):
+    def __init__(self, mode=None, hbm_budget_bytes=None, workers=2, tol=1e-12, lib=None, stream_factory=None,
+                 coalesce_freqs=32):
         self._w = lib if lib is not None else importlib.import_module("praca-magisterska_gb300")
         self._new_stream = stream_factory or _cuda_stream
         self.mode = self._w.MODE_MIXED if mode is None else mode
@@ -82,6 +85,9 @@ class Server:
             hbm_budget_bytes = int(free * 0.6)
         self.budget = int(hbm_budget_bytes)
         self.tol = tol
+        # a worker serves, with the request it takes, the queued requests of the same
+        # geometry, up to this many distinct frequencies together (0: one at a time)
+        self.coalesce_freqs = int(coalesce_freqs)
         self._lock = threading.Condition()
         self._queue = collections.deque()
         self._plans = {}          # geo key -> (Topology, Plan)
@@ -96,6 +102,7 @@ class Server:
         self._t0 = None
         self._t1 = None
         self.evictions = 0
+        self.coalesced = 0        # requests served in a group of two or more
         self._workers = [threading.Thread(target=self._run, args=(i,), daemon=True) for i in range(workers)]
         for t in self._workers:
             t.start()
@@ -138,7 +145,8 @@ class Server:
                    "p50_ms": 1e3 * lat[len(lat) // 2] if lat else None,
                    "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
                    "slo_ms": slo_ms, "goodput_solves_per_s": good / span if span > 0 else 0.0,
-                   "resident_bytes": self._used, "budget_bytes": self.budget, "evictions": self.evictions}
+                   "resident_bytes": self._used, "budget_bytes": self.budget, "evictions": self.evictions,
+                   "coalesced_requests": self.coalesced}
         return out
 
     # ------------------------------------------------------------ internals ----
@@ -171,9 +179,11 @@ class Server:
     def _per_matrix_bytes(self, n):
         return n * n * (16 + (8 if self.mode == self._w.MODE_MIXED else 16)) + 4 * n
 
-    def _admit(self, need):
+    def _admit(self, need, evicted):
         """Reserve `need` bytes, evicting idle sets LRU-first; caller holds the lock.
-        Returns False when it does not fit yet."""
+        Evicted sets leave the books here and are appended to `evicted`, which the
+        caller closes after releasing the lock (freeing device memory must not hold up
+        the other workers).  Returns False when it does not fit yet."""
         while self._used + self._reserved + need > self.budget:
             victim = next((k for k, r in self._sets.items() if r.pins == 0), None)
             if victim is None:
@@ -183,10 +193,31 @@ class Server:
                 if self._lookup.get((r.key, f)) is r:
                     del self._lookup[(r.key, f)]
             self._used -= r.bytes
-            r.factors.close()
+            evicted.append(r)
             self.evictions += 1
         self._reserved += need
         return True
+
+    def _take_group(self, req):
+        """Queued requests for req's geometry that join it (caller holds the lock):
+        taken in arrival order while their frequencies together stay within
+        coalesce_freqs; the others keep their places in the queue."""
+        group = [req]
+        if self.coalesce_freqs <= 0:
+            return group
+        freqs = set(float(f) for f in req.freqs)
+        keep = collections.deque()
+        while self._queue:
+            r = self._queue.popleft()
+            if r.geo_key == req.geo_key:
+                more = freqs | set(float(f) for f in r.freqs)
+                if len(more) <= self.coalesce_freqs:
+                    group.append(r)
+                    freqs = more
+                    continue
+            keep.append(r)
+        self._queue = keep
+        return group
 
     def _run(self, wid):
         owner, sp = self._new_stream()  # noqa: F841  (owner keeps the stream alive)
@@ -196,23 +227,49 @@ class Server:
                     self._lock.wait()
                 if self._stop and not self._queue:
                     return
-                req = self._queue.popleft()
+                group = self._take_group(self._queue.popleft())
+                if len(group) > 1:
+                    self.coalesced += len(group)
             try:
-                self._serve(req, sp)
-            except Exception as e:  # the request fails, the loop goes on
-                req.future.set_exception(e)
+                self._serve(group, sp)
+            except Exception as e:  # the group's requests fail, the loop goes on
+                if len(group) == 1:
+                    group[0].future.set_exception(e)
+                    continue
+                # one request may have caused it: each is retried alone, so that only
+                # that request fails
+                for r in group:
+                    if r.future.done():
+                        continue
+                    try:
+                        self._serve([r], sp)
+                    except Exception as e1:
+                        r.future.set_exception(e1)
 
-    def _serve(self, req, sp):
-        topo, plan = self._plan(req)
+    def _serve(self, group, sp):
+        """Serves requests of one geometry: one admission and one factorisation of the
+        frequencies they need that are not resident (a frequency batch of the
+        geometry, whose results do not depend on its composition), then each
+        request's solves."""
+        topo, plan = self._plan(group[0])
         n = topo.npls
-        if not 0 < req.ngap <= n:
-            raise ValueError("gap outside the geometry")
-        freqs = [float(f) for f in req.freqs]
-        with self._lock:
-            while True:
+        key = group[0].geo_key
+        ok = []
+        for r in group:
+            if 0 < r.ngap <= n:
+                ok.append(r)
+            else:
+                r.future.set_exception(ValueError("gap outside the geometry"))
+        if not ok:
+            return
+        group = ok
+        freqs = sorted(set(float(f) for r in group for f in r.freqs))
+        while True:
+            evicted = []
+            with self._lock:
                 # pin what is resident, reserve what must be factored
-                have = {f: self._lookup.get((req.geo_key, f)) for f in freqs}
-                missing = sorted({f for f, r in have.items() if r is None})
+                have = {f: self._lookup.get((key, f)) for f in freqs}
+                missing = sorted(f for f, r in have.items() if r is None)
                 pinned = {id(r): r for r in have.values() if r is not None}
                 need = len(missing) * self._per_matrix_bytes(n)
                 if need > self.budget:
@@ -220,18 +277,23 @@ class Server:
                 for r in pinned.values():
                     r.pins += 1
                     self._sets.move_to_end(id(r))
-                if not missing or self._admit(need):
-                    break
-                # a waiting request holds no pins: two waiters pinning the sets the
-                # other must evict would wait for each other forever
-                for r in pinned.values():
-                    r.pins -= 1
+                admitted = not missing or self._admit(need, evicted)
+                if not admitted:
+                    # a waiting request holds no pins: two waiters pinning the sets the
+                    # other must evict would wait for each other forever
+                    for r in pinned.values():
+                        r.pins -= 1
+            for r in evicted:  # unpinned and off the books: no request can reach them
+                r.factors.close()
+            if admitted:
+                break
+            with self._lock:
                 self._lock.wait(timeout=0.05)
         reserved = need
         try:
             if missing:
                 fac = self._w.Factors(plan, np.array(missing, np.float32), mode=self.mode, stream=sp)
-                res = _Resident(fac, req.geo_key, missing)
+                res = _Resident(fac, key, missing)
                 res.pins = 1
                 with self._lock:
                     self._reserved -= need
@@ -239,45 +301,50 @@ class Server:
                     self._used += res.bytes
                     self._sets[id(res)] = res
                     for f in missing:
-                        self._lookup[(req.geo_key, f)] = res
+                        self._lookup[(key, f)] = res
                         have[f] = res
                     self._lock.notify_all()
                 pinned[id(res)] = res
-            # solve every frequency from its resident set
-            cur = np.zeros((len(freqs), n), np.complex128) if req.currents else None
-            zin = np.zeros(len(freqs), np.complex128)
-            reports = [None] * len(freqs)
-            by_set = collections.defaultdict(list)
-            for k, f in enumerate(freqs):
-                by_set[id(have[f])].append((have[f].index[f], k))
-            for sid, items in by_set.items():
-                res = pinned[sid]
-                items.sort()
-                # contiguous runs of set indices solve in one call
-                run = [items[0]]
-                for it in items[1:] + [None]:
-                    if it is not None and it[0] == run[-1][0] + 1:
-                        run.append(it)
-                        continue
-                    c, z, rp = res.factors.solve(req.ngap, req.ampl, req.phas, first=run[0][0], count=len(run),
-                                                 tol=self.tol, currents=req.currents, stream=sp)
-                    for j, (_, k) in enumerate(run):
-                        zin[k] = z[j]
-                        reports[k] = rp[j]
-                        if cur is not None:
-                            cur[k] = c[j]
-                    run = [it] if it is not None else []
-            done = time.perf_counter()
-            with self._lock:
-                self._latency.append(done - req.arrival)
-                self._done_sizes.append(len(freqs))
-                self._solves += len(freqs)
-                self._t1 = done
-            req.future.set_result({"zin": zin, "currents": cur, "reports": reports,
-                                   "latency_s": done - req.arrival})
+            for req in group:
+                self._solve_request(req, n, have, pinned, sp)
         finally:
             with self._lock:
                 self._reserved -= reserved  # a factorisation that failed returns its reservation
                 for r in pinned.values():
                     r.pins -= 1
                 self._lock.notify_all()
+
+    def _solve_request(self, req, n, have, pinned, sp):
+        """Solves every frequency of req from its resident set (contiguous runs of a
+        set's frequencies in one call) and completes its future."""
+        freqs = [float(f) for f in req.freqs]
+        cur = np.zeros((len(freqs), n), np.complex128) if req.currents else None
+        zin = np.zeros(len(freqs), np.complex128)
+        reports = [None] * len(freqs)
+        by_set = collections.defaultdict(list)
+        for k, f in enumerate(freqs):
+            by_set[id(have[f])].append((have[f].index[f], k))
+        for sid, items in by_set.items():
+            res = pinned[sid]
+            items.sort()
+            run = [items[0]]
+            for it in items[1:] + [None]:
+                if it is not None and it[0] == run[-1][0] + 1:
+                    run.append(it)
+                    continue
+                c, z, rp = res.factors.solve(req.ngap, req.ampl, req.phas, first=run[0][0], count=len(run),
+                                             tol=self.tol, currents=req.currents, stream=sp)
+                for j, (_, k) in enumerate(run):
+                    zin[k] = z[j]
+                    reports[k] = rp[j]
+                    if cur is not None:
+                        cur[k] = c[j]
+                run = [it] if it is not None else []
+        done = time.perf_counter()
+        with self._lock:
+            self._latency.append(done - req.arrival)
+            self._done_sizes.append(len(freqs))
+            self._solves += len(freqs)
+            self._t1 = done
+        req.future.set_result({"zin": zin, "currents": cur, "reports": reports,
+                               "latency_s": done - req.arrival})

@@ -2,8 +2,9 @@
 fake solver library: resident factor sets are reused by repeat excitations, admission
 evicts idle sets least-recently-used first and never a pinned one, an oversized or a
 failing request fails alone and returns its memory reservation, and requests waiting
-for memory do not block each other.  The device path of the same loop is covered by
-test_serve_gpu.py."""
+for memory do not block each other, and waiting requests of one geometry are
+factored together, a failing one failing alone.  The device path of the same loop is
+covered by test_serve_gpu.py."""
 import importlib
 import threading
 import time
@@ -216,5 +217,82 @@ def test_failed_plan_build_fails_alone_and_is_retried():
         lib.bad_geometries.clear()
         _check(srv.submit(serve.Request("x 64", [2.0], 1)).result(timeout=10), [2.0], 1.0)
         assert lib.topologies == ["x", "a", "x"]
+    finally:
+        srv.close()
+
+
+def test_waiting_requests_of_one_geometry_are_factored_together():
+    """While the only worker is busy, three requests for geometry a and one for b
+    queue up.  The worker then takes the a requests together: one factorisation of
+    the union of their missing frequencies (a frequency that is resident or shared is
+    factored once), and b on its own.  Every request gets its own answers."""
+    lib = FakeLib()
+    srv = _server(lib, budget=_per_set(64, 16), workers=1)
+    try:
+        srv.submit(serve.Request("a 64", [1.0], 1)).result(timeout=10)
+        entered, release = threading.Event(), threading.Event()
+        lib.hold[9.0] = (entered, release)
+        f_hold = srv.submit(serve.Request("a 64", [1.0], 2, ampl=9.0))
+        assert entered.wait(10)
+        f1 = srv.submit(serve.Request("a 64", [2.0, 3.0], 1, ampl=2.0))
+        f2 = srv.submit(serve.Request("b 64", [2.0], 1, ampl=3.0))
+        f3 = srv.submit(serve.Request("a 64", [3.0, 1.0, 4.0], 5, ampl=4.0))
+        f4 = srv.submit(serve.Request("a 64", [5.0], 5, ampl=5.0))
+        release.set()
+        _check(f_hold.result(timeout=10), [1.0], 9.0)
+        _check(f1.result(timeout=10), [2.0, 3.0], 2.0)
+        _check(f2.result(timeout=10), [2.0], 3.0)
+        _check(f3.result(timeout=10), [3.0, 1.0, 4.0], 4.0)
+        _check(f4.result(timeout=10), [5.0], 5.0)
+        assert lib.created == [("a", (1.0,)), ("a", (2.0, 3.0, 4.0, 5.0)), ("b", (2.0,))]
+        st = srv.stats()
+        assert st["requests"] == 6 and st["coalesced_requests"] == 3
+    finally:
+        srv.close()
+
+
+def test_coalescing_respects_its_frequency_limit():
+    lib = FakeLib()
+    srv = serve.Server(hbm_budget_bytes=_per_set(64, 16), workers=1, lib=lib,
+                       stream_factory=lambda: (None, "stream"), coalesce_freqs=3)
+    try:
+        entered, release = threading.Event(), threading.Event()
+        lib.hold[9.0] = (entered, release)
+        f_hold = srv.submit(serve.Request("a 64", [1.0], 2, ampl=9.0))
+        assert entered.wait(10)
+        futs = [srv.submit(serve.Request("a 64", fs, 1)) for fs in ([2.0, 3.0], [4.0, 5.0], [3.0])]
+        release.set()
+        f_hold.result(timeout=10)
+        for f, fs in zip(futs, ([2.0, 3.0], [4.0, 5.0], [3.0])):
+            _check(f.result(timeout=10), fs, 1.0)
+        # [2, 3] + [4, 5] would be 4 frequencies: the second request waits for the
+        # next round, the third (frequency 3) joins the first
+        assert lib.created == [("a", (1.0,)), ("a", (2.0, 3.0)), ("a", (4.0, 5.0))]
+    finally:
+        srv.close()
+
+
+def test_failing_request_in_a_group_fails_alone():
+    """A group's factorisation fails because of one request's frequency: the
+    requests are retried one by one, and only that request fails."""
+    lib = FakeLib()
+    srv = _server(lib, budget=_per_set(64, 16), workers=1)
+    try:
+        entered, release = threading.Event(), threading.Event()
+        lib.hold[9.0] = (entered, release)
+        f_hold = srv.submit(serve.Request("a 64", [1.0], 2, ampl=9.0))
+        assert entered.wait(10)
+        lib.fail_freq = 7.0
+        f_ok1 = srv.submit(serve.Request("a 64", [2.0], 1))
+        f_bad = srv.submit(serve.Request("a 64", [7.0, 3.0], 1))
+        f_ok2 = srv.submit(serve.Request("a 64", [3.0], 1))
+        release.set()
+        f_hold.result(timeout=10)
+        _check(f_ok1.result(timeout=10), [2.0], 1.0)
+        _check(f_ok2.result(timeout=10), [3.0], 1.0)
+        with pytest.raises(RuntimeError):
+            f_bad.result(timeout=10)
+        st = srv.stats()
+        assert st["requests"] == 3 and st["resident_bytes"] <= st["budget_bytes"]
     finally:
         srv.close()
