@@ -535,7 +535,9 @@ def run_wmom(args):
         "latency_ms": {"p50_sweep": statistics.median(step_ms), "p99_sweep": sorted(step_ms)[-1]},
         "kernel_ms_one_instrumented_step": {k: round(v["ms"], 3) for k, v in st.items()},
         "fill_pairs_per_entry": plan.fill_pairs / float(n * n),
-        "lu_config": dict(zip(("batch", "span"), w.tuned_config(n, w.MODE_MIXED) or (None, None))),
+        "lu_config": dict(zip(("batch", "span", "tile_n", "panel_w"),
+                              (w.tuned_config(n, w.MODE_MIXED) or (None, None)) +
+                              (w.tuned_shape(n, w.MODE_MIXED) or (None, None)))),
         "clocks": clocks,
     }
     plan.close()

@@ -322,6 +322,11 @@ wmom_status wmom_diag_sincos(const double* d_x, long long n, double* d_out, void
  * WMOM_ERR_ARG when no sweep of that order has been tuned yet.  No reference
  * counterpart. */
 wmom_status wmom_tuned_config(int n, int mode, int* batch, int* span);
+/* The rest of that shape: FP32 columns of the precision form's tensor-core update tile
+ * (256 or 128) and its widest FP32 panel (0 = as wide as shared memory allows, else
+ * 48 or 32 columns); WMOM_ERR_ARG when order n has not been tuned.  No reference
+ * counterpart (the reference's kernels use a fixed BLOCK_SIZE, REF/Wire_MoM.h:21). */
+wmom_status wmom_tuned_shape(int n, int mode, int* tile_n, int* panel_w);
 
 /* ---------------------------------------------------------------- testing ---- */
 /* Test hook, not for production use: every grid barrier of the plain FP64 LU's

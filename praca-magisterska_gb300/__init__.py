@@ -123,6 +123,7 @@ _stats_read = _sig("wmom_stats_read", ctypes.c_int,
 _probe_fp64 = _sig("wmom_probe_fp64_tflops", ctypes.c_int, [_dp])
 _diag_sincos = _sig("wmom_diag_sincos", ctypes.c_int, [_vp, ctypes.c_longlong, _vp, _vp])
 _tuned_config = _sig("wmom_tuned_config", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip])
+_tuned_shape = _sig("wmom_tuned_shape", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _ip, _ip])
 
 STAT_CLASSES = ["fill", "panel", "tc_gemm", "gemm", "trsm", "laswp", "residual", "misc", "emul_gemm", "trsv"]
 
@@ -171,6 +172,16 @@ def tuned_config(n, mode):
     if _tuned_config(n, mode, ctypes.byref(b), ctypes.byref(sp)) != WMOM_OK:
         return None
     return b.value, sp.value
+
+
+def tuned_shape(n, mode):
+    """(tile columns, widest panel) the autotuner chose for order n in this process:
+    FP32 columns of a tensor-core update tile (256 or 128) and the widest FP32 panel
+    (0 = as wide as shared memory allows); None before order n was tuned."""
+    t, pw = ctypes.c_int(0), ctypes.c_int(0)
+    if _tuned_shape(n, mode, ctypes.byref(t), ctypes.byref(pw)) != WMOM_OK:
+        return None
+    return t.value, pw.value
 
 
 def _check(st, what):

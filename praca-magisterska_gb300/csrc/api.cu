@@ -753,7 +753,9 @@ wmom_status wmom_factor_geometries(const wmom_plan* plans, int count, const floa
         f->fs.freq.assign(1, freq_mhz[ch.mem[j]]);
         f->fs.ws = &f->ws;
         f->fs.batch = 1;
-        f->fs.span = tuned_span(P, mode);
+        const LuConfig shape = tuned_shape(P, mode);
+        f->fs.span = shape.span;
+        use_shape(&f->ws, shape);
         f->fs.order = P;
         f->fs.z64 = reinterpret_cast<double2*>(ch.store->z64) + (size_t)j * nn;
         f->fs.lu = reinterpret_cast<unsigned char*>(ch.store->lu) + elem * nn * j;

@@ -1733,7 +1733,7 @@ int max_cluster_size(const DeviceLimits& lim) {
 }
 
 template <typename C>
-PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false) {
+PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false, int wmax = 0) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using R = decltype(C{}.x);
@@ -1759,7 +1759,8 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
     // publication slots, two pivot rows and the diagonal row (the look-ahead kernel's
     // layout; the other kernel uses one pivot row less)
     const size_t head = 2 * sizeof(ClusterPub<C>) + 3 * 64 * sizeof(C);
-    const int wcap = sizeof(R) == 4 ? 64 : 32;
+    // FP32 panels: at most wmax columns when the tuner chose narrower ones
+    const int wcap = sizeof(R) == 4 ? (wmax >= 16 && wmax < 64 ? wmax : 64) : 32;
     auto try_shape = [&](int rpt, int cs_lo, int cs_hi, int wmin) -> bool {
       for (int cs = cs_lo; cs <= std::min(cs_hi, csmax); cs *= 2) {
         const int rpc = (m + cs - 1) / cs;
@@ -1840,7 +1841,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   // panel of columns [jp, jp + w), rows jp..n-1 (cooperative launch)
   auto panel = [&](int jp, int w) -> cudaError_t {
     const int m = n - jp;
-    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr);
+    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w);
     const int P = pl.P;
     {
       if (pl.cluster) {
@@ -1965,7 +1966,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     int np = 0;
     c[0] = j0;
     while (np < S && c[np] < n) {
-      w[np] = std::min(panel_launch<C>(n - c[np], lim, gemm_hook != nullptr).w, n - c[np]);
+      w[np] = std::min(panel_launch<C>(n - c[np], lim, gemm_hook != nullptr, ws->panel_w).w, n - c[np]);
       c[np + 1] = c[np] + w[np];
       ++np;
     }

@@ -46,6 +46,11 @@ struct LuWorkspace {
   // allocated from the device's stream-ordered pool (lu_workspace_create_async):
   // growing and freeing it never waits for work on other streams
   bool pooled = false;
+  // shape of the precision form's factorisation, set from the autotuner's choice
+  // for the order: FP32 columns of a tensor-core update tile (256 or 128; 0 = 256)
+  // and the widest FP32 panel (0 = as wide as the panel's shared memory allows)
+  int tile_n = 0;
+  int panel_w = 0;
 };
 
 size_t lu_workspace_bytes(int elem_bytes);  // one matrix: barrier + staging

@@ -14,9 +14,11 @@
 // solver then removes the remaining FP32-level error.
 //
 // Kernel: persistent, one CTA (6 warps) per SM, each walking 128 x 256 real output
-// tiles (128 rows, 128 complex columns; measured against 128 x 128 tiles: 176 vs 167
-// TFLOP/s at K = 96, 235 vs 209 at K = 192, as each stage's four operand planes then
-// feed twice the MMA work).  A producer thread streams K in chunks of 32
+// tiles (128 rows, 128 complex columns; measured against 128 x 128 tiles on one large
+// update: 176 vs 167 TFLOP/s at K = 96, 235 vs 209 at K = 192, as each stage's four
+// operand planes then feed twice the MMA work).  The narrow 128 x 128 tile is the
+// other instantiation: a factorisation's late trailing matrices have few wide tiles
+// for 152 SMs, so the autotuner times both per order (LuWorkspace::tile_n).  A producer thread streams K in chunks of 32
 // FP32 (one 128-byte swizzle row) with TMA into a 2-stage ring (head and tail
 // planes of A' and B'); an MMA thread issues 3 x 4 tcgen05.mma (M=128, N=256, K=8)
 // per chunk into one of two TMEM accumulators; four epilogue warps read their
@@ -46,24 +48,28 @@ namespace wmom {
 namespace tc {
 
 constexpr int BM = 128;  // accumulator lanes = rows of C per CTA
-constexpr int BN = 256;  // accumulator FP32 columns = 128 complex columns of C
+// accumulator FP32 columns per tile (BN: 256 = 128 complex columns of C, or 128 = 64;
+// the factorisation's autotuner picks one per order, LuWorkspace::tile_n)
+constexpr int kTileWide = 256, kTileNarrow = 128;
 constexpr int KC = 32;   // FP32 elements of K per chunk (128 bytes)
 constexpr int KC16 = 64; // FP16 elements of K per chunk (128 bytes)
 constexpr int STAGES = 2;
 constexpr int A_BYTES = BM * 128;  // 16 KB per plane (one 128-byte row of K per row)
-constexpr int B_BYTES = BN * 128;  // 32 KB per plane
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
+__host__ __device__ constexpr int b_bytes(int bn) { return bn * 128; }  // 32 or 16 KB per plane
+__host__ __device__ constexpr int stage_bytes(int bn) { return 2 * A_BYTES + 2 * b_bytes(bn); }
+__host__ __device__ constexpr int smem_bytes(int bn) { return STAGES * stage_bytes(bn) + 1024 + 128; }
 constexpr int NTHREADS = 192;         // producer warp, MMA warp, 4 epilogue warps
-constexpr int TMEM_COLS = 2 * BN;     // two accumulators
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle.
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) { return sdesc_sw<128>(addr); }
 
-// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = BN, M = BM.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = bn, M = BM.
+__host__ __device__ constexpr uint32_t idesc_tf32(int bn) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
 
+template <int BN>
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  constexpr uint32_t kIdesc = idesc_tf32(BN);
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
@@ -73,9 +79,13 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b
 }
 
 // Instruction descriptor of the FP16-plane variant: D = F32, A = B = F16, both K-major.
-constexpr uint32_t kIdescF16 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+__host__ __device__ constexpr uint32_t idesc_f16(int bn) {
+  return (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
 
+template <int BN>
 __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  constexpr uint32_t kIdescF16 = idesc_f16(BN);
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
@@ -283,6 +293,7 @@ struct TileCoord {
   int mat, m0, j0;
 };
 
+template <int BN>
 __device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n) {
   const int per_mat = tiles_m * tiles_n;
   const int mat = t / per_mat;
@@ -293,7 +304,8 @@ __device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n)
 
 // F16: FP16 planes of scaled operands (kind::f16, 64 elements of K per chunk; ea / eb
 // hold the rows' and columns' exponents), else TF32 planes (kind::tf32, 32 per chunk).
-template <bool F16>
+// BN: FP32 columns of an output tile (256 or 128).
+template <bool F16, int BN>
 __global__ void __launch_bounds__(NTHREADS, 1)
     cgemm_sub_tc_kernel(const __grid_constant__ CUtensorMap mapAhi, const __grid_constant__ CUtensorMap mapAlo,
                         const __grid_constant__ CUtensorMap mapBhi, const __grid_constant__ CUtensorMap mapBlo,
@@ -301,6 +313,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         int tiles_n, int ntiles, int* __restrict__ err, long long cstride,
                         const int* __restrict__ ea, const int* __restrict__ eb) {
   constexpr int kChunk = F16 ? KC16 : KC;  // K elements per chunk (128 bytes)
+  constexpr int B_BYTES = b_bytes(BN), STAGE_BYTES = stage_bytes(BN);
+  constexpr int TMEM_COLS = 2 * BN;  // two accumulators
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -344,7 +358,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int it = 0;  // chunks issued
       bool ok = !s_fail;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+        const TileCoord tc = tile_coord<BN>(t, tiles_m, tiles_n);
         for (int c = 0; c < nchunks; ++c) {
           const int s = it % STAGES, use = it / STAGES;
           if (use > 0 && !(ok = role_wait(empty_bar(s), (use - 1) & 1, err, &s_fail))) break;
@@ -394,9 +408,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int kk = 0; kk < 4; ++kk) {
               const uint32_t accum = (c | sp | kk) != 0 ? 1u : 0u;
               if constexpr (F16)
-                mma_f16(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
+                mma_f16<BN>(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
               else
-                mma_tf32(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
+                mma_tf32<BN>(acc, sdesc(as[sp] + kk * 32), sdesc(bs[sp] + kk * 32), accum);
             }
           mma_commit(empty_bar(s));
           ++it;
@@ -420,7 +434,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int q = warp & 3;  // TMEM lanes 32q..32q+31 are the ones this warp may read
     int tl = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
-      const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+      const TileCoord tc = tile_coord<BN>(t, tiles_m, tiles_n);
       float2* Cm = C + (size_t)tc.mat * cstride;
       const int row = tc.m0 + q * 32 + lane;
       const bool row_ok = row < M;
@@ -608,7 +622,12 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
   cudaError_t e = tc_scratch(ws, plane_floats + exp_ints, s);
   if (e != cudaSuccess) return e;
   CUtensorMap mah, mal, mbh, mbl;
-  const void* kern = f16 ? (const void*)cgemm_sub_tc_kernel<true> : (const void*)cgemm_sub_tc_kernel<false>;
+  // tile width: the one the factorisation's tuner chose for this workspace (the
+  // FP16-plane variant always runs the wide tile)
+  const int bn = (!f16 && ws->tile_n == kTileNarrow) ? kTileNarrow : kTileWide;
+  const void* kern = f16 ? (const void*)cgemm_sub_tc_kernel<true, kTileWide>
+                         : (bn == kTileNarrow ? (const void*)cgemm_sub_tc_kernel<false, kTileNarrow>
+                                              : (const void*)cgemm_sub_tc_kernel<false, kTileWide>);
   int* ea = nullptr;
   int* eb = nullptr;
   if (f16) {
@@ -626,7 +645,7 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
     pack_b_f16_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, eb,
                                                                            bstride);
     if (!make_map(&mah, ahi, M, K2p, batch, BM, true) || !make_map(&mal, alo, M, K2p, batch, BM, true) ||
-        !make_map(&mbh, bhi, 2 * N, K2p, batch, BN, true) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN, true))
+        !make_map(&mbh, bhi, 2 * N, K2p, batch, bn, true) || !make_map(&mbl, blo, 2 * N, K2p, batch, bn, true))
       return cudaErrorInvalidValue;
   } else {
     float* ahi = ws->tc_buf;
@@ -638,12 +657,13 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
                                                                                   bstride);
     pack_b_kernel<<<dim3((K2p / 2 + 127) / 128, N, batch), 128, 0, s>>>(B, ldb, K, N, K2p, bhi, blo, bstride);
     if (!make_map(&mah, ahi, M, K2p, batch, BM, false) || !make_map(&mal, alo, M, K2p, batch, BM, false) ||
-        !make_map(&mbh, bhi, 2 * N, K2p, batch, BN, false) || !make_map(&mbl, blo, 2 * N, K2p, batch, BN, false))
+        !make_map(&mbh, bhi, 2 * N, K2p, batch, bn, false) || !make_map(&mbl, blo, 2 * N, K2p, batch, bn, false))
       return cudaErrorInvalidValue;
   }
-  e = allow_dynamic_smem(kern, SMEM_BYTES);
+  const int smem = smem_bytes(bn);
+  e = allow_dynamic_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + bn - 1) / bn;
   const long long ntiles = (long long)tiles_m * tiles_n * batch;
   if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
   static int nsm = 0;
@@ -656,13 +676,17 @@ cudaError_t cgemm_sub_tc(LuWorkspace* ws, const float2* A, long long lda, const 
   const int grid = (int)std::min<long long>(ntiles, nsm);
   stats::Scope sc(stats::kTcGemm, s, 8.0 * M * (double)N * K * batch);
   if (f16)
-    cgemm_sub_tc_kernel<true><<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
-                                                                 tiles_m, tiles_n, (int)ntiles, ws->tc_err,
-                                                                 bstride, ea, eb);
+    cgemm_sub_tc_kernel<true, kTileWide><<<grid, NTHREADS, smem, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
+                                                                      tiles_m, tiles_n, (int)ntiles, ws->tc_err,
+                                                                      bstride, ea, eb);
+  else if (bn == kTileNarrow)
+    cgemm_sub_tc_kernel<false, kTileNarrow><<<grid, NTHREADS, smem, s>>>(mah, mal, mbh, mbl, C, ldc, M, N,
+                                                                         K2p / kc, tiles_m, tiles_n, (int)ntiles,
+                                                                         ws->tc_err, bstride, nullptr, nullptr);
   else
-    cgemm_sub_tc_kernel<false><<<grid, NTHREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
-                                                                  tiles_m, tiles_n, (int)ntiles, ws->tc_err,
-                                                                  bstride, nullptr, nullptr);
+    cgemm_sub_tc_kernel<false, kTileWide><<<grid, NTHREADS, smem, s>>>(mah, mal, mbh, mbl, C, ldc, M, N, K2p / kc,
+                                                                       tiles_m, tiles_n, (int)ntiles, ws->tc_err,
+                                                                       bstride, nullptr, nullptr);
   return cudaGetLastError();
 }
 

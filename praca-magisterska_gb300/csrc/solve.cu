@@ -611,6 +611,7 @@ struct FactorGraph {
   const void* lu = nullptr;
   const int* ipiv = nullptr;
   int span = 0;
+  int tile_n = 0, panel_w = 0;    // shape of the captured factorisation
   const float* tc_buf = nullptr;  // tensor-core scratch the capture used
   unsigned tc_gen = 0;
   bool failed = false;  // capture unsupported here: launch directly
@@ -653,12 +654,18 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
     cudaGraphExecDestroy(graph->exec);
     graph->exec = nullptr;
   }
+  const bool same_shape = graph && graph->tile_n == ws->tile_n && graph->panel_w == ws->panel_w;
+  if (graph && graph->exec && !same_shape) {
+    // the workspace's factorisation shape changed since the capture
+    cudaGraphExecDestroy(graph->exec);
+    graph->exec = nullptr;
+  }
   if (graph && graph->exec && graph->mode == mode && graph->n == n && graph->bg == bg && graph->lu == lu &&
       graph->ipiv == ipiv && graph->span == span) {
     stats::add_counts(graph->launches);
     fe = cudaGraphLaunch(graph->exec, s);
-  } else if (graph && !graph->failed && graphs_enabled() && graph->mode == mode && graph->n == n &&
-             graph->bg == bg && graph->lu == lu && graph->ipiv == ipiv && graph->span == span) {
+  } else if (graph && !graph->failed && graphs_enabled() && same_shape && graph->mode == mode &&
+             graph->n == n && graph->bg == bg && graph->lu == lu && graph->ipiv == ipiv && graph->span == span) {
     // second use of these buffers: capture the sequence, then replay it from now on
     cudaGraph_t g = nullptr;
     long long before[stats::kNumCls], after[stats::kNumCls];
@@ -698,6 +705,8 @@ wmom_status factor_group(int mode, int n, const double2* Z64, int bg, float2* lu
       graph->lu = lu;
       graph->ipiv = ipiv;
       graph->span = span;
+      graph->tile_n = ws->tile_n;
+      graph->panel_w = ws->panel_w;
     }
     fe = direct();
   }
@@ -1256,17 +1265,19 @@ wmom_status fill_batch(const Plan& p, const float* freq, int nk, double2* Z, cud
 
 }  // namespace
 
-// Batch width: env override, else the autotuned value for (order bucket, form),
-// else tuned now on Z64 (the first matrix of the work) by timing 1, 2, 4, ...
 // Picks the factorisation shape for order n: the batch width (matrices per launch,
 // up to what the cooperative panel keeps co-resident and a quarter of `budget`) and,
-// for the precision form, the span (panels per tensor-core trailing update).  It times
-// factorisations of copies of the first matrix -- spans 1, 2, 4 at width 1, then
-// widths 1, 2, 4, ... at the best span -- and keeps the best time per matrix.
-// Results are cached per (n / 256, form); WMOM_LU_BATCH and WMOM_LU_SPAN override.
-// Without `timing` (requests on a serving path, where trial factorisations would add
-// to a request's latency) a cached result is used if there is one, else the widest
-// batch up to `limit` at span 2, and nothing is cached.
+// for the precision form, the span (panels per tensor-core trailing update), the
+// tensor-core tile (128 x 256 or 128 x 128 real outputs) and the widest FP32 panel
+// (64 columns or as many as shared memory allows, 48 or 32).  It times factorisations
+// of copies of the first matrix: widths 1, 2, 4, ... and the widest at span 2, then
+// spans 1, 2, 4 at the chosen width, then the narrow tile, then the narrower panels;
+// a change is kept only when it is clearly faster (3%).  Results are cached per
+// (n / 256, form); WMOM_LU_BATCH, WMOM_LU_SPAN, WMOM_TC_TILE (128 or 256) and
+// WMOM_PANEL_W (16-64) override.  Without `timing` (requests on a serving path, where
+// trial factorisations would add to a request's latency) a cached result is used if
+// there is one, else the widest batch up to `limit` at span 2 with the default tile
+// and panels, and nothing is cached.
 wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuWorkspace* ws, cudaStream_t s,
                              size_t budget, LuConfig* out, bool timing) {
   const size_t nn = (size_t)n * n;
@@ -1276,6 +1287,8 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   while (bmax > 1 && (size_t)bmax * mat > budget / 4) bmax /= 2;
   bmax = std::max(bmax, 1);
   const int eb = env_int("WMOM_LU_BATCH", 1, kMaxLuBatch), es = env_int("WMOM_LU_SPAN", 1, kMaxSpan);
+  const int et = env_int("WMOM_TC_TILE", 128, 256), ep = env_int("WMOM_PANEL_W", 16, 64);
+  const int etile = et == 128 || et == 256 ? et : 0;
   if (mode != WMOM_MODE_MIXED) {
     // the FP64 form is bound by the FP64 pipe at every width worth batching
     *out = LuConfig{eb ? std::min(eb, bmax) : (n <= 2048 ? bmax : 1), 1};
@@ -1284,7 +1297,7 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     return WMOM_OK;
   }
   if (eb && es) {
-    *out = LuConfig{std::min(eb, bmax), es};
+    *out = LuConfig{std::min(eb, bmax), es, etile, ep};
     return WMOM_OK;
   }
   const std::pair<int, int> key{(n + 255) / 256, mode};
@@ -1292,13 +1305,14 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
-      *out = LuConfig{eb ? std::min(eb, bmax) : std::min(it->second.batch, bmax), es ? es : it->second.span};
+      *out = LuConfig{eb ? std::min(eb, bmax) : std::min(it->second.batch, bmax), es ? es : it->second.span,
+                      etile ? etile : it->second.tile_n, ep ? ep : it->second.panel_w};
       return WMOM_OK;
     }
   }
   const int bcap = eb ? std::min(eb, bmax) : bmax;
   if (!timing) {
-    *out = LuConfig{bcap, es ? es : 2};
+    *out = LuConfig{bcap, es ? es : 2, etile, ep};
     return WMOM_OK;
   }
   DevBuf rep64, lu, piv;
@@ -1308,17 +1322,20 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   for (int b = 0; b < bcap; ++b)
     SWEEP_TRY(cudaMemcpyAsync(rep64.as<double2>() + (size_t)b * nn, Z64, sizeof(double2) * nn,
                               cudaMemcpyDeviceToDevice, s));
-  auto time_one = [&](int batch, int span, float* per) -> wmom_status {
+  const LuConfig saved{0, 0, ws->tile_n, ws->panel_w};
+  auto time_one = [&](const LuConfig& c, float* per) -> wmom_status {
     float ms = 0.f;
     int info[kMaxLuBatch];
-    const wmom_status st = factor_group(mode, n, rep64.as<double2>(), batch, lu.as<float2>(), nullptr,
-                                        piv.as<int>(), ws, s, info, &ms, nullptr, span);
-    *per = ms / batch;
+    use_shape(ws, c);
+    const wmom_status st = factor_group(mode, n, rep64.as<double2>(), c.batch, lu.as<float2>(), nullptr,
+                                        piv.as<int>(), ws, s, info, &ms, nullptr, c.span);
+    use_shape(ws, saved);
+    *per = ms / c.batch;
     return st;
   };
   // widths first (at the default span), then spans at the chosen width: the span's
   // saving is trailing-matrix traffic, which only shows at the width that will run
-  LuConfig best{eb ? bcap : 1, es ? es : 2};
+  LuConfig best{eb ? bcap : 1, es ? es : 2, etile, ep};
   float best_t = 1e30f;
   if (!eb) {
     // widths 1, 2, 4, ... and the widest one allowed (e.g. a whole 12-frequency sweep in
@@ -1328,7 +1345,9 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     if (cands.back() != bcap) cands.push_back(bcap);
     for (int cand : cands) {
       float per = 0.f;
-      const wmom_status st = time_one(cand, best.span, &per);
+      LuConfig c = best;
+      c.batch = cand;
+      const wmom_status st = time_one(c, &per);
       if (st != WMOM_OK) return st;
       if (per < best_t * 0.95f) {
         best_t = per;
@@ -1341,13 +1360,43 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
     int cur = best.span;
     for (int span = 1; span <= kMaxSpan; span *= 2) {
       float per = 0.f;
-      const wmom_status st = time_one(best.batch, span, &per);
+      LuConfig c = best;
+      c.span = span;
+      const wmom_status st = time_one(c, &per);
       if (st != WMOM_OK) return st;
       // keep the default unless another span is clearly faster
       const float margin = span == cur ? 1.0f : 0.97f;
       if (per < best_t * margin) {
         best_t = per;
         best.span = span;
+      }
+    }
+  } else {
+    const wmom_status st = time_one(best, &best_t);
+    if (st != WMOM_OK) return st;
+  }
+  // best_t is now the time of `best`; the narrow tile, then narrower panels
+  if (!etile) {
+    float per = 0.f;
+    LuConfig c = best;
+    c.tile_n = 128;
+    const wmom_status st = time_one(c, &per);
+    if (st != WMOM_OK) return st;
+    if (per < best_t * 0.97f) {
+      best_t = per;
+      best.tile_n = 128;
+    }
+  }
+  if (!ep) {
+    for (int pw : {48, 32}) {
+      float per = 0.f;
+      LuConfig c = best;
+      c.panel_w = pw;
+      const wmom_status st = time_one(c, &per);
+      if (st != WMOM_OK) return st;
+      if (per < best_t * 0.97f) {
+        best_t = per;
+        best.panel_w = pw;
       }
     }
   }
@@ -1425,6 +1474,7 @@ struct StreamPair {
 // those of the plain sweep bit for bit: the same fill per matrix and factorisations
 // that do not depend on the batch width.
 wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) {
+  use_shape(a.ws, cfg);
   const Plan& p = *a.plan;
   const int n = p.npls;
   const bool mixed = a.mode == WMOM_MODE_MIXED;
@@ -1555,6 +1605,7 @@ wmom_status run_sweep(const SweepArgs& a) {
     if (B == 0) {
       st = choose_lu_config(a.mode, n, a.nfreq, zall.as<double2>(), a.ws, s, budget, &cfg, true);
       if (st != WMOM_OK) return st;
+      use_shape(a.ws, cfg);
       B = cfg.batch;
       SWEEP_TRY(lu.alloc((mixed ? mat32 : mat64) * B, s));
       SWEEP_TRY(piv.alloc(sizeof(int) * (size_t)n * B, s));
@@ -1613,10 +1664,15 @@ __global__ void pad_identity_kernel(double2* __restrict__ Z, int P, long long zs
 
 }  // namespace
 
-int tuned_span(int n, int mode) {
+LuConfig tuned_shape(int n, int mode) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tuned.find({(n + 255) / 256, mode});
-  return it != g_tuned.end() && it->second.span > 0 ? it->second.span : 2;
+  LuConfig c{1, 2, 0, 0};
+  if (it != g_tuned.end()) {
+    c = it->second;
+    if (c.span <= 0) c.span = 2;
+  }
+  return c;
 }
 
 wmom_status factor_class(int mode, int P, const Plan* const* plans, const float* freq, int count, double2* z64,
@@ -1686,6 +1742,7 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s) {
   LuConfig cfg;
   st = choose_lu_config(fs->mode, n, nf, fs->z64, fs->ws, s, fr / 2, &cfg, false);
   if (st != WMOM_OK) return st;
+  use_shape(fs->ws, cfg);
   fs->batch = cfg.batch;
   fs->span = cfg.span;
   for (int g0 = 0; g0 < nf; g0 += fs->batch) {
@@ -1739,5 +1796,15 @@ extern "C" wmom_status wmom_tuned_config(int n, int mode, int* batch, int* span)
   if (it == wmom::g_tuned.end()) return WMOM_ERR_ARG;
   if (batch) *batch = it->second.batch;
   if (span) *span = it->second.span;
+  return WMOM_OK;
+}
+
+extern "C" wmom_status wmom_tuned_shape(int n, int mode, int* tile_n, int* panel_w) {
+  if (n <= 0 || (mode != WMOM_MODE_FP64 && mode != WMOM_MODE_MIXED)) return WMOM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(wmom::g_tune_mu);
+  auto it = wmom::g_tuned.find({(n + 255) / 256, mode});
+  if (it == wmom::g_tuned.end()) return WMOM_ERR_ARG;
+  if (tile_n) *tile_n = it->second.tile_n ? it->second.tile_n : 256;
+  if (panel_w) *panel_w = it->second.panel_w;
   return WMOM_OK;
 }

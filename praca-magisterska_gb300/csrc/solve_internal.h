@@ -35,7 +35,15 @@ wmom_status run_sweep(const SweepArgs& a);
 struct LuConfig {
   int batch = 1;
   int span = 0;
+  int tile_n = 0;   // tensor-core update tile: FP32 columns (256 or 128; 0 = 256)
+  int panel_w = 0;  // widest FP32 panel (0 = as wide as shared memory allows)
 };
+
+// The factorisation shape of cfg on the workspace that the factorisation uses.
+inline void use_shape(LuWorkspace* ws, const LuConfig& cfg) {
+  ws->tile_n = cfg.tile_n;
+  ws->panel_w = cfg.panel_w;
+}
 
 struct FactorSet {
   const Plan* plan = nullptr;
@@ -66,13 +74,14 @@ wmom_status factors_build(FactorSet* fs, cudaStream_t s);
 void retain_pool_memory();
 
 // Geometries of uneven order (solve.cu): the padded order of n's size class (four
-// classes per octave, P <= 1.25 n); the span a factorisation of order n uses (the
-// tuned one, else 2); and the batched fill + factorisation of `count` geometries of
+// classes per octave, P <= 1.25 n); the factorisation shape of order n (the tuned
+// span, tile and panels, else span 2 with the default tile and panels); and the
+// batched fill + factorisation of `count` geometries of
 // one class, one frequency each, into z64 (count matrices of order P) and lu / ipiv
 // (complex64 or complex128 factors by mode), with an identity block beyond each
 // geometry's order.
 int padded_order(int n);
-int tuned_span(int n, int mode);
+LuConfig tuned_shape(int n, int mode);
 wmom_status factor_class(int mode, int P, const Plan* const* plans, const float* freq, int count, double2* z64,
                          void* lu, int* ipiv, int* info, LuWorkspace* ws, int span, cudaStream_t s);
 wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float ampl, float phas, double tol,
