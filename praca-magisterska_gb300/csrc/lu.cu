@@ -1673,6 +1673,19 @@ bool panel_lookahead() {
   return !(e && e[0] == '0');
 }
 
+// Widest FP64 cluster panel: WMOM_FP64_PANEL_W (16 .. 32, a multiple of 8) if set,
+// else the workspace's choice (LuWorkspace::panel_w64), else 32 columns.  The panel's
+// rank-1 updates run on GB300's narrow FP64 pipe, and their work grows with the width.
+int fp64_panel_width(int ws_choice) {
+  static const int env = [] {
+    const char* e = std::getenv("WMOM_FP64_PANEL_W");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 16 && v <= 32 ? (v & ~7) : 0;
+  }();
+  if (env) return env;
+  return ws_choice >= 16 && ws_choice <= 32 ? (ws_choice & ~7) : 32;
+}
+
 bool cluster_panels_disabled() {
   const char* e = std::getenv("WMOM_NO_CLUSTER_PANEL");
   return e && e[0] == '1';
@@ -1733,7 +1746,8 @@ int max_cluster_size(const DeviceLimits& lim) {
 }
 
 template <typename C>
-PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false, int wmax = 0) {
+PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false, int wmax = 0,
+                         int wmax64 = 0) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using R = decltype(C{}.x);
@@ -1760,7 +1774,7 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
     // layout; the other kernel uses one pivot row less)
     const size_t head = 2 * sizeof(ClusterPub<C>) + 3 * 64 * sizeof(C);
     // FP32 panels: at most wmax columns when the tuner chose narrower ones
-    const int wcap = sizeof(R) == 4 ? (wmax >= 16 && wmax < 64 ? wmax : 64) : 32;
+    const int wcap = sizeof(R) == 4 ? (wmax >= 16 && wmax < 64 ? wmax : 64) : fp64_panel_width(wmax64);
     auto try_shape = [&](int rpt, int cs_lo, int cs_hi, int wmin) -> bool {
       for (int cs = cs_lo; cs <= std::min(cs_hi, csmax); cs *= 2) {
         const int rpc = (m + cs - 1) / cs;
@@ -1841,7 +1855,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   // panel of columns [jp, jp + w), rows jp..n-1 (cooperative launch)
   auto panel = [&](int jp, int w) -> cudaError_t {
     const int m = n - jp;
-    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w);
+    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w, ws->panel_w64);
     const int P = pl.P;
     {
       if (pl.cluster) {
@@ -1966,7 +1980,8 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     int np = 0;
     c[0] = j0;
     while (np < S && c[np] < n) {
-      w[np] = std::min(panel_launch<C>(n - c[np], lim, gemm_hook != nullptr, ws->panel_w).w, n - c[np]);
+      w[np] = std::min(panel_launch<C>(n - c[np], lim, gemm_hook != nullptr, ws->panel_w, ws->panel_w64).w,
+                       n - c[np]);
       c[np + 1] = c[np] + w[np];
       ++np;
     }

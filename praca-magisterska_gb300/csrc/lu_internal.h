@@ -51,6 +51,8 @@ struct LuWorkspace {
   // and the widest FP32 panel (0 = as wide as the panel's shared memory allows)
   int tile_n = 0;
   int panel_w = 0;
+  // widest FP64 cluster panel of the precision form's second tier (0 = 32)
+  int panel_w64 = 0;
 };
 
 size_t lu_workspace_bytes(int elem_bytes);  // one matrix: barrier + staging
@@ -67,7 +69,7 @@ using GemmHook = cudaError_t (*)(LuWorkspace* ws, const C* Am, long long lda, co
 // In-place LU of `batch` n x n matrices astride elements apart (pivots n apart).
 // With a GEMM hook, `span` panels (1..kMaxSpan, 0 = default 2) share one trailing
 // update.
-constexpr int kMaxSpan = 4;
+constexpr int kMaxSpan = 8;
 template <typename C>
 cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, cudaStream_t s,
                         GemmHook<C> gemm_hook, int batch = 1, long long astride = 0, int span = 0);

@@ -734,11 +734,22 @@ namespace {
 wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws, cudaStream_t s, int* info,
                         GemmHook<double2> hook) {
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
-  // span: panels per tensor-core update.  3 x a 32-column panel is K = 96, the most
-  // one launch of the digit-plane GEMM takes; measured on the N = 8192 grid workload
-  // at spans 1 / 2 / 3: 6.70 / 8.66 / 9.67 freq-solves/s.  WMOM_EMUL_SPAN overrides.
+  // Shape: span panels per tensor-core update, of at most w columns, K = span w <= 96
+  // (the most one launch of the digit-plane GEMM takes).  Measured per 12-frequency
+  // step (instrumented):
+  //   N = 8192 grid: spans 1 / 2 / 3 of 32 columns 6.70 / 8.66 / 9.67 freq-solves/s;
+  //     then w / span 32/3, 24/4, 16/6, 16/4: 946, 918, 932, 1032 ms;
+  //   N = 2048 grid, 256 frequencies: 32/3, 24/4, 16/6, 16/4: 1192, 1201, 1239, 1213 ms.
+  // Narrower panels cut the panels' and the triangular solves' FP64 work, at the
+  // price of more, thinner launches, which only pays at large orders.
+  // WMOM_EMUL_SPAN and WMOM_FP64_PANEL_W override.
+  const bool large = n > 4096;
   const int es = env_int("WMOM_EMUL_SPAN", 1, kMaxSpan);
-  const cudaError_t fe = lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, es ? es : 3);
+  const int saved_w64 = ws->panel_w64;
+  ws->panel_w64 = large ? 24 : 32;
+  const cudaError_t fe =
+      lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, es ? es : (large ? 4 : 3));
+  ws->panel_w64 = saved_w64;
   if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t (tier 2)");
   int err = lu_workspace_read_status(ws, info, s, bg);
   err |= tc::read_and_clear_error(ws, s);
@@ -1358,7 +1369,7 @@ wmom_status choose_lu_config(int mode, int n, int limit, const double2* Z64, LuW
   if (!es) {
     best_t = 1e30f;
     int cur = best.span;
-    for (int span = 1; span <= kMaxSpan; span *= 2) {
+    for (int span = 1; span <= 4; span *= 2) {
       float per = 0.f;
       LuConfig c = best;
       c.span = span;
