@@ -73,7 +73,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-dir", required=True,
                     help="root of the reference checkout (the directory holding 'wersja referencyjna')")
+    ap.add_argument("--only", nargs="*", default=None,
+                    help="write only the fixtures of these case names (default: all)")
     args = ap.parse_args()
+    want = (lambda name: True) if not args.only else (lambda name: name in args.only)
     os.environ["WMOM_REFERENCE_DIR"] = os.path.join(args.reference_dir, "wersja referencyjna")
     from oracle import build as ob
     ob.REF_DIR = os.environ["WMOM_REFERENCE_DIR"]
@@ -83,10 +86,11 @@ def main():
     from oracle import oracle as orc
     geo = importlib.import_module("praca-magisterska_gb300.geometry")
 
-    logs = parse_logs(args.reference_dir)
-    with open(os.path.join(HERE, "zin_logs.json"), "w") as f:
-        json.dump(logs, f, indent=0)
-    print("log lines", len(logs))
+    if want("zin_logs"):
+        logs = parse_logs(args.reference_dir)
+        with open(os.path.join(HERE, "zin_logs.json"), "w") as f:
+            json.dump(logs, f, indent=0)
+        print("log lines", len(logs))
 
     cases = {
         "dipole1m_512": (geo.dipole(1.0, 1e-3, 512), 1),
@@ -99,11 +103,19 @@ def main():
         "mixed_junctions": (geo.geo_text([(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1), (0.5, 0.5, 2)],
                                          [(1, 2, 2e-3, 4), (2, 3, 2e-3, 3), (4, 3, 2e-3, 4), (1, 4, 2e-3, 2),
                                           (5, 1, 1e-3, 5), (3, 5, 1e-3, 1), (2, 4, 1e-3, 6)]), 1),
+        # PEC ground (ienv = 2): a monopole standing on the ground, a frame whose two
+        # legs stand on it, and a grid held 0.5 m above it (no wire touching it)
+        "ground_monopole": (geo.geo_text([(0, 0, 0), (0, 0, 1.0)], [(1, 2, 1e-3, 40)]), 2),
+        "ground_frame": (geo.geo_text([(0, 0, 0), (0, 0, 0.5), (1.5, 0, 0.5), (1.5, 0, 0)],
+                                      [(1, 2, 1e-3, 10), (2, 3, 1e-3, 30), (3, 4, 1e-3, 10)]), 2),
+        "ground_grid": (geo.grid(4, 1.0, 0.5, 5e-3, None, 4), 2),
     }
     topos = {}
     for name, (text, ienv) in cases.items():
         r = orc.ref_geometry(text, ienv=ienv)
         topos[name] = r
+        if not want(name):
+            continue
         np.savez_compressed(os.path.join(HERE, f"topology_{name}.npz"), geo=np.array(text), ienv=ienv,
                             **trimmed_topology(r))
         print("topology", name, r["npls"])
@@ -112,8 +124,13 @@ def main():
     small = [("dipole64", geo.dipole(1.0, 1e-3, 64), 1, 150.0), ("grid5_ns3", cases["grid5_ns3"][0], 1, 30.0),
              ("bent_ground", cases["bent_ground"][0], 2, 100.0),
              ("mixed_junctions", cases["mixed_junctions"][0], 1, 60.0),
-             ("dipole25m_lowf", geo.dipole(25.0, 5e-4, 96), 1, 0.01)]
+             ("dipole25m_lowf", geo.dipole(25.0, 5e-4, 96), 1, 0.01),
+             ("ground_monopole", cases["ground_monopole"][0], 2, 75.0),
+             ("ground_frame", cases["ground_frame"][0], 2, 40.0),
+             ("ground_grid", cases["ground_grid"][0], 2, 20.0)]
     for name, text, ienv, f in small:
+        if not want(name):
+            continue
         r = orc.ref_geometry(text, ienv=ienv)
         z = orc.ref_fill(r, f, ienv=ienv, sgn=sg[ienv])
         np.savez_compressed(os.path.join(HERE, f"zfill_{name}.npz"), geo=np.array(text), ienv=ienv,
@@ -122,8 +139,12 @@ def main():
 
     cur_cases = [("dipole1m_512", [150.0], 256), ("dipole25m_512", [100., 200., 300., 400., 500., 600.], 100),
                  ("grid21_2048", [0.01, 1.0, 10.0], 1000), ("random_1024", list(geo.sweep_freqs()), 500),
-                 ("mixed_junctions", [30.0, 60.0], 3)]
+                 ("mixed_junctions", [30.0, 60.0], 3),
+                 ("ground_monopole", [37.5, 75.0, 150.0], 1), ("ground_frame", [20.0, 40.0, 80.0], 5),
+                 ("ground_grid", [5.0, 20.0], 7)]
     for name, freqs, ngap in cur_cases:
+        if not want(name):
+            continue
         r = topos[name]
         ienv = cases[name][1]
         cur = []

@@ -22,7 +22,8 @@ def _gpu_fill(wmom, topo, freqs):
     return out
 
 
-@pytest.mark.parametrize("name", ["dipole64", "grid5_ns3", "bent_ground", "mixed_junctions", "dipole25m_lowf"])
+@pytest.mark.parametrize("name", ["dipole64", "grid5_ns3", "bent_ground", "mixed_junctions", "dipole25m_lowf",
+                                  "ground_monopole", "ground_frame", "ground_grid"])
 def test_fill_matches_reference_fixture(cuda, wmom, name):
     d = np.load(os.path.join(GOLDEN, f"zfill_{name}.npz"))
     topo = wmom.Topology(str(d["geo"]), ienv=int(d["ienv"]))

@@ -61,7 +61,8 @@ def test_oracle_reproduces_logged_zin(orc, wmom, nsw):
     assert nbad == 0
 
 
-@pytest.mark.parametrize("name", ["dipole64", "grid5_ns3", "bent_ground", "mixed_junctions", "dipole25m_lowf"])
+@pytest.mark.parametrize("name", ["dipole64", "grid5_ns3", "bent_ground", "mixed_junctions", "dipole25m_lowf",
+                                  "ground_monopole", "ground_frame", "ground_grid"])
 def test_oracle_fill_matches_reference_zmatrix(orc, wmom, name):
     d = np.load(os.path.join(GOLDEN, f"zfill_{name}.npz"))
     ienv = int(d["ienv"])
@@ -72,7 +73,8 @@ def test_oracle_fill_matches_reference_zmatrix(orc, wmom, name):
     assert np.max(np.abs(z - zr) / scale) < 1e-14
 
 
-@pytest.mark.parametrize("name", ["dipole1m_512", "dipole25m_512", "mixed_junctions", "random_1024"])
+@pytest.mark.parametrize("name", ["dipole1m_512", "dipole25m_512", "mixed_junctions", "random_1024", "ground_monopole",
+                                  "ground_frame", "ground_grid"])
 def test_oracle_currents_match_reference_mkl(orc, wmom, name):
     d = np.load(os.path.join(GOLDEN, f"currents_{name}.npz"))
     ienv = int(d["ienv"])

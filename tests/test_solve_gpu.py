@@ -35,7 +35,8 @@ def _fixture(name):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
-@pytest.mark.parametrize("name", ["dipole1m_512", "dipole25m_512", "mixed_junctions", "random_1024"])
+@pytest.mark.parametrize("name", ["dipole1m_512", "dipole25m_512", "mixed_junctions", "random_1024", "ground_monopole",
+                                  "ground_frame", "ground_grid"])
 def test_currents_match_reference_fixtures(cuda, wmom, name, mode):
     d, geo = _fixture(name)
     topo = wmom.Topology(geo, ienv=int(d["ienv"]))
