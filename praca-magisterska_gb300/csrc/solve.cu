@@ -764,7 +764,7 @@ wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws
 // mask, FP64 LU for the matrices that stall.
 wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float2* lu32, const double2* lu64,
                         const int* ipiv, const int* info, double tol, LuWorkspace* ws, GroupScratch& g,
-                        wmom_report* rep, bool condest, int nreal) {
+                        wmom_report* rep, bool condest, int nreal, bool direct_t2) {
   if (nreal <= 0) nreal = n;
   const size_t nn = (size_t)n * n;
   cudaStream_t s = g.s;
@@ -806,7 +806,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   int stall[kMaxLuBatch] = {};
   double prev[kMaxLuBatch], last[kMaxLuBatch], rel_first[kMaxLuBatch], rel_best[kMaxLuBatch];
   for (int b = 0; b < bg; ++b) {
-    fallback[b] = info[b] != 0;
+    fallback[b] = direct_t2 || info[b] != 0;
     active[b] = !fallback[b];
     prev[b] = last[b] = rel_first[b] = rel_best[b] = HUGE_VAL;
   }
@@ -818,173 +818,177 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   const bool tier2 = emul_gemm_hook() != nullptr;
   const double step_budget = std::max(8.0, n / 256.0);
   const unsigned vgrid = (unsigned)(((size_t)n * bg + 255) / 256);
-  // initial solve in FP32
-  stats::count(stats::kMisc, 2);
-  convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
-  SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
-  widen_vec_kernel<<<vgrid, 256, 0, s>>>(g.d32.as<float2>(), g.x64.as<double2>(), (size_t)n * bg);
-  SWEEP_TRY(cudaGetLastError());
-  std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
   std::vector<int> hact(kMaxLuBatch, 0);
   const int max_it = 40;
-  // the matrices still refining: residuals and corrections are computed for these
-  // only (one slowly converging matrix no longer keeps its whole batch busy)
-  std::vector<int> hsel(kMaxLuBatch, 0);
-  int nsel = 0;
-  for (int b = 0; b < bg; ++b)
-    if (active[b]) hsel[nsel++] = b;
-  SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
-  for (int it = 0;; ++it) {
-    if (nsel == 0) break;
-    {
-      GroupScalars* dscr = g.sc.as<GroupScalars>();
-      SWEEP_TRY(residual_fp64(Z64, n, (long long)nn, g.x64.as<double2>(), g.vrep.as<double2>(), n,
-                              g.r64.as<double2>(), g.part.as<double2>(), nsel, s, g.sel.as<int>()));
-      SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dscr->rnorm2, bg, s));
-      SWEEP_TRY(cudaMemcpyAsync(&hs, dscr, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
-      SWEEP_TRY(cudaStreamSynchronize(s));
-    }
-    int nact = 0;
-    for (int b = 0; b < bg; ++b) {
-      if (!active[b]) continue;
-      const double rel = std::sqrt(hs.rnorm2[b]) / g.vnorm;
-      rep[b].rel_residual = rel;
-      rep[b].iterations = it;
-      if (it == 0) rel_first[b] = rel;
-      if (rel < rel_best[b]) rel_best[b] = rel;
-      // converged: the target is met, or the last correction no longer changes the
-      // solution at FP64 resolution (systems whose FP64 residual floor lies above
-      // the target); stalled or diverged: FP64 fallback
-      const double corr = it > 0 ? std::sqrt(hs.dnorm2[b] / hs.xnorm2[b]) : HUGE_VAL;
-      if (!(rel == rel)) {
-        fallback[b] = true;
-        active[b] = false;
-      } else if (rel <= tol || corr <= 0x1p-48) {
-        active[b] = false;
-      } else if (rel > 0.5 * prev[b] && ++stall[b] >= 2) {
-        fallback[b] = true;
-        active[b] = false;
-      } else if (it >= max_it) {
-        fallback[b] = true;
-        active[b] = false;
-      } else if (tier2 && it >= 3 && rel < last[b] &&
-                 std::log(tol / rel) / std::log(rel / last[b]) > step_budget) {
-        fallback[b] = true;
-        active[b] = false;
-      } else {
-        if (rel <= 0.5 * prev[b]) stall[b] = 0;
-        prev[b] = std::min(prev[b], rel);
-        last[b] = rel;
-        ++nact;
-      }
-    }
-    if (nact == 0) break;
-    // correction d = (LU32)^-1 r per active matrix, scaled by a power of two
-    for (int b = 0; b < bg; ++b) {
-      const double rn = std::sqrt(hs.rnorm2[b]);
-      const double scl = (active[b] && rn > 0 && std::isfinite(rn)) ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
-      hscale[b] = scl;
-      hscale[kMaxLuBatch + b] = 1.0 / scl;
-      hact[b] = active[b] ? 1 : 0;
-    }
-    nsel = 0;
+  // direct_t2: the caller predicts that no matrix of the group is served by its FP32
+  // factors (none were computed); the group goes straight to the second tier
+  if (!direct_t2) {
+    // initial solve in FP32
+    stats::count(stats::kMisc, 2);
+    convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
+    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+    widen_vec_kernel<<<vgrid, 256, 0, s>>>(g.d32.as<float2>(), g.x64.as<double2>(), (size_t)n * bg);
+    SWEEP_TRY(cudaGetLastError());
+    std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
+    // the matrices still refining: residuals and corrections are computed for these
+    // only (one slowly converging matrix no longer keeps its whole batch busy)
+    std::vector<int> hsel(kMaxLuBatch, 0);
+    int nsel = 0;
     for (int b = 0; b < bg; ++b)
       if (active[b]) hsel[nsel++] = b;
-    SWEEP_TRY(cudaMemcpyAsync(g.scal.p, hscale.data(), sizeof(double) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice, s));
-    SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
     SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
-    const double* dscale = g.scal.as<double>();
-    const double* dinv = dscale + kMaxLuBatch;
-    stats::count(stats::kMisc, 4);
-    convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
-    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
-                                 nsel == bg ? nullptr : g.sel.as<int>()));
+    for (int it = 0;; ++it) {
+      if (nsel == 0) break;
+      {
+        GroupScalars* dscr = g.sc.as<GroupScalars>();
+        SWEEP_TRY(residual_fp64(Z64, n, (long long)nn, g.x64.as<double2>(), g.vrep.as<double2>(), n,
+                                g.r64.as<double2>(), g.part.as<double2>(), nsel, s, g.sel.as<int>()));
+        SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dscr->rnorm2, bg, s));
+        SWEEP_TRY(cudaMemcpyAsync(&hs, dscr, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+        SWEEP_TRY(cudaStreamSynchronize(s));
+      }
+      int nact = 0;
+      for (int b = 0; b < bg; ++b) {
+        if (!active[b]) continue;
+        const double rel = std::sqrt(hs.rnorm2[b]) / g.vnorm;
+        rep[b].rel_residual = rel;
+        rep[b].iterations = it;
+        if (it == 0) rel_first[b] = rel;
+        if (rel < rel_best[b]) rel_best[b] = rel;
+        // converged: the target is met, or the last correction no longer changes the
+        // solution at FP64 resolution (systems whose FP64 residual floor lies above
+        // the target); stalled or diverged: FP64 fallback
+        const double corr = it > 0 ? std::sqrt(hs.dnorm2[b] / hs.xnorm2[b]) : HUGE_VAL;
+        if (!(rel == rel)) {
+          fallback[b] = true;
+          active[b] = false;
+        } else if (rel <= tol || corr <= 0x1p-48) {
+          active[b] = false;
+        } else if (rel > 0.5 * prev[b] && ++stall[b] >= 2) {
+          fallback[b] = true;
+          active[b] = false;
+        } else if (it >= max_it) {
+          fallback[b] = true;
+          active[b] = false;
+        } else if (tier2 && it >= 3 && rel < last[b] &&
+                   std::log(tol / rel) / std::log(rel / last[b]) > step_budget) {
+          fallback[b] = true;
+          active[b] = false;
+        } else {
+          if (rel <= 0.5 * prev[b]) stall[b] = 0;
+          prev[b] = std::min(prev[b], rel);
+          last[b] = rel;
+          ++nact;
+        }
+      }
+      if (nact == 0) break;
+      // correction d = (LU32)^-1 r per active matrix, scaled by a power of two
+      for (int b = 0; b < bg; ++b) {
+        const double rn = std::sqrt(hs.rnorm2[b]);
+        const double scl = (active[b] && rn > 0 && std::isfinite(rn)) ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
+        hscale[b] = scl;
+        hscale[kMaxLuBatch + b] = 1.0 / scl;
+        hact[b] = active[b] ? 1 : 0;
+      }
+      nsel = 0;
+      for (int b = 0; b < bg; ++b)
+        if (active[b]) hsel[nsel++] = b;
+      SWEEP_TRY(cudaMemcpyAsync(g.scal.p, hscale.data(), sizeof(double) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+      SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+      SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+      const double* dscale = g.scal.as<double>();
+      const double* dinv = dscale + kMaxLuBatch;
+      stats::count(stats::kMisc, 4);
+      convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
+      SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
+                                   nsel == bg ? nullptr : g.sel.as<int>()));
 
-    sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
-    sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);
-    accumulate_vec_kernel<<<vgrid, 256, 0, s>>>(g.x64.as<double2>(), g.d32.as<float2>(), n, bg, dinv,
-                                                g.actv.as<int>());
-    SWEEP_TRY(cudaGetLastError());
-  }
-  int tmp_info[kMaxLuBatch];
-  if (lu_workspace_read_status(ws, tmp_info, s, 1)) return WMOM_ERR_TIMEOUT;
-  // GMRES-IR for the matrices whose plain refinement made progress (at least a
-  // factor kKrylovEntry below the first residual) before it stalled: their FP32
-  // factors are still a usable preconditioner.  The others -- refinement diverged or
-  // barely moved, i.e. kappa * u_fp32 >> 1 -- go straight to the FP64 LU.
-  constexpr double kKrylovEntry = 1e-3;
-  for (int b = 0; b < bg; ++b) {
-    if (!krylov_enabled()) break;
-    if (!fallback[b] || info[b] != 0) continue;
-    if (!(rel_best[b] <= kKrylovEntry * rel_first[b])) continue;
-    double2* xb = g.x64.as<double2>() + (size_t)b * n;
-    const double2* Zb = Z64 + (size_t)b * nn;
-    const float2* lub = lu32 + (size_t)b * nn;
-    const int* ipb = ipiv + (size_t)b * n;
-    DevBuf dv;
-    SWEEP_TRY(dv.alloc(sizeof(double2) * n, s));
-    // budget: a correction must cut the residual by kKrylovGain, else the FP32
-    // factors are too poor a preconditioner here and the FP64 LU takes over
-    constexpr double kKrylovGain = 1e-2;
-    double prevr = HUGE_VAL, corr = HUGE_VAL;
-    bool ok = false;
-    for (int outer = 0; outer < 6; ++outer) {
-      SWEEP_TRY(residual_fp64(Zb, n, 0, xb, g.vrep.as<double2>(), n, g.r64.as<double2>(), g.part.as<double2>(), 1,
-                              s));
-      SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dsc->rnorm2, 1, s));
-      SWEEP_TRY(sumsq_fp64(xb, n, dsc->xnorm2, 1, s));
-      SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
-      SWEEP_TRY(cudaStreamSynchronize(s));
-      const double rel = std::sqrt(hs.rnorm2[0]) / g.vnorm;
-      if (!(rel == rel)) {
-        // diverged plain refinement: start the Krylov refinement from zero
-        SWEEP_TRY(cudaMemsetAsync(xb, 0, sizeof(double2) * n, s));
-        prevr = HUGE_VAL;
-        continue;
-      }
-      rep[b].rel_residual = rel;
-      if (rel <= tol || corr <= 0x1p-48) {
-        ok = true;
-        break;
-      }
-      if (rel > kKrylovGain * prevr) break;
-      prevr = rel;
-      int steps = 0;
-      const wmom_status gs = gmres_correction(n, Zb, lub, ipb, g.r64.as<double2>(), dv.as<double2>(), ws, s,
-                                              gmres_restart(), gmres_cycles(), 1e-10, &steps);
-      if (gs != WMOM_OK) return gs;
-      rep[b].krylov_steps += steps;
-      rep[b].iterations += 1;
-      const double xn = std::sqrt(hs.xnorm2[0]);
-      SWEEP_TRY(sumsq_fp64(dv.as<double2>(), n, dsc->dnorm2, 1, s));
-      SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
-      SWEEP_TRY(cudaStreamSynchronize(s));
-      corr = xn > 0 ? std::sqrt(hs.dnorm2[0]) / xn : HUGE_VAL;
-      // x += d
-      stats::count(stats::kMisc);
-      std::vector<double2> onec(1, make_double2(1.0, 0.0));
-      DevBuf cbuf;
-      SWEEP_TRY(cbuf.alloc(sizeof(double2), s));
-      SWEEP_TRY(cudaMemcpyAsync(cbuf.p, onec.data(), sizeof(double2), cudaMemcpyHostToDevice, s));
-      caxpy_many_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(xb, dv.as<double2>(), 1, n, cbuf.as<double2>(),
-                                                                    +1.0);
-      SWEEP_TRY(cudaStreamSynchronize(s));
+      sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
+      sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);
+      accumulate_vec_kernel<<<vgrid, 256, 0, s>>>(g.x64.as<double2>(), g.d32.as<float2>(), n, bg, dinv,
+                                                  g.actv.as<int>());
+      SWEEP_TRY(cudaGetLastError());
     }
-    if (ok) fallback[b] = false;
-  }
-  for (int b = 0; b < bg; ++b)
-    if (!fallback[b]) {
-      rep[b].status = WMOM_OK;
-      rep[b].tier = 1;
+    int tmp_info[kMaxLuBatch];
+    if (lu_workspace_read_status(ws, tmp_info, s, 1)) return WMOM_ERR_TIMEOUT;
+    // GMRES-IR for the matrices whose plain refinement made progress (at least a
+    // factor kKrylovEntry below the first residual) before it stalled: their FP32
+    // factors are still a usable preconditioner.  The others -- refinement diverged or
+    // barely moved, i.e. kappa * u_fp32 >> 1 -- go straight to the FP64 LU.
+    constexpr double kKrylovEntry = 1e-3;
+    for (int b = 0; b < bg; ++b) {
+      if (!krylov_enabled()) break;
+      if (!fallback[b] || info[b] != 0) continue;
+      if (!(rel_best[b] <= kKrylovEntry * rel_first[b])) continue;
+      double2* xb = g.x64.as<double2>() + (size_t)b * n;
+      const double2* Zb = Z64 + (size_t)b * nn;
+      const float2* lub = lu32 + (size_t)b * nn;
+      const int* ipb = ipiv + (size_t)b * n;
+      DevBuf dv;
+      SWEEP_TRY(dv.alloc(sizeof(double2) * n, s));
+      // budget: a correction must cut the residual by kKrylovGain, else the FP32
+      // factors are too poor a preconditioner here and the FP64 LU takes over
+      constexpr double kKrylovGain = 1e-2;
+      double prevr = HUGE_VAL, corr = HUGE_VAL;
+      bool ok = false;
+      for (int outer = 0; outer < 6; ++outer) {
+        SWEEP_TRY(residual_fp64(Zb, n, 0, xb, g.vrep.as<double2>(), n, g.r64.as<double2>(), g.part.as<double2>(), 1,
+                                s));
+        SWEEP_TRY(sumsq_fp64(g.r64.as<double2>(), n, dsc->rnorm2, 1, s));
+        SWEEP_TRY(sumsq_fp64(xb, n, dsc->xnorm2, 1, s));
+        SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+        SWEEP_TRY(cudaStreamSynchronize(s));
+        const double rel = std::sqrt(hs.rnorm2[0]) / g.vnorm;
+        if (!(rel == rel)) {
+          // diverged plain refinement: start the Krylov refinement from zero
+          SWEEP_TRY(cudaMemsetAsync(xb, 0, sizeof(double2) * n, s));
+          prevr = HUGE_VAL;
+          continue;
+        }
+        rep[b].rel_residual = rel;
+        if (rel <= tol || corr <= 0x1p-48) {
+          ok = true;
+          break;
+        }
+        if (rel > kKrylovGain * prevr) break;
+        prevr = rel;
+        int steps = 0;
+        const wmom_status gs = gmres_correction(n, Zb, lub, ipb, g.r64.as<double2>(), dv.as<double2>(), ws, s,
+                                                gmres_restart(), gmres_cycles(), 1e-10, &steps);
+        if (gs != WMOM_OK) return gs;
+        rep[b].krylov_steps += steps;
+        rep[b].iterations += 1;
+        const double xn = std::sqrt(hs.xnorm2[0]);
+        SWEEP_TRY(sumsq_fp64(dv.as<double2>(), n, dsc->dnorm2, 1, s));
+        SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+        SWEEP_TRY(cudaStreamSynchronize(s));
+        corr = xn > 0 ? std::sqrt(hs.dnorm2[0]) / xn : HUGE_VAL;
+        // x += d
+        stats::count(stats::kMisc);
+        std::vector<double2> onec(1, make_double2(1.0, 0.0));
+        DevBuf cbuf;
+        SWEEP_TRY(cbuf.alloc(sizeof(double2), s));
+        SWEEP_TRY(cudaMemcpyAsync(cbuf.p, onec.data(), sizeof(double2), cudaMemcpyHostToDevice, s));
+        caxpy_many_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(xb, dv.as<double2>(), 1, n, cbuf.as<double2>(),
+                                                                      +1.0);
+        SWEEP_TRY(cudaStreamSynchronize(s));
+      }
+      if (ok) fallback[b] = false;
     }
-  {
-    // tier 1: the FP32 factors (their estimate is kappa of the FP32-rounded Z, which
-    // refinement only reaches when kappa * u_fp32 < 1)
-    std::vector<int> t1;
     for (int b = 0; b < bg; ++b)
-      if (!fallback[b]) t1.push_back(b);
-    const wmom_status cs = estimate(lu32, ipiv, g.d32.as<float2>(), t1, t1);
-    if (cs != WMOM_OK) return cs;
+      if (!fallback[b]) {
+        rep[b].status = WMOM_OK;
+        rep[b].tier = 1;
+      }
+    {
+      // tier 1: the FP32 factors (their estimate is kappa of the FP32-rounded Z, which
+      // refinement only reaches when kappa * u_fp32 < 1)
+      std::vector<int> t1;
+      for (int b = 0; b < bg; ++b)
+        if (!fallback[b]) t1.push_back(b);
+      const wmom_status cs = estimate(lu32, ipiv, g.d32.as<float2>(), t1, t1);
+      if (cs != WMOM_OK) return cs;
+    }
   }
   // The matrices the FP32 factors could not serve get FP64-grade factors, batched
   // as wide as the plain FP64 form batches at this order (copies in the scratch
@@ -1462,6 +1466,32 @@ int pipeline_groups(int nfreq, int batch) {
 }
 
 // The cached factorisation shape for (n, mode), if a sweep of that order was tuned.
+// Second-tier prediction inside one sweep.  The sweep's groups run from the highest
+// frequency down (run_sweep orders them so).  The conditioning of these wire
+// structures grows as the frequency falls (kappa ~ 1 / (ka)^2 below resonance), so
+// once every matrix of a group has needed FP64-grade factors, the groups after it
+// (lower frequencies) skip the FP32 factorisation and the refinement attempt that
+// would fail, and go straight to the second tier.  A matrix's second-tier result does
+// not depend on that attempt, so a predicted matrix gets the same answer, bit for
+// bit, as it would after failing in tier 1; only its reported refinement steps
+// differ.  A wrong prediction (a matrix that tier 1 would have served) costs time,
+// not accuracy.  WMOM_TIER_PREDICT=0 turns it off.
+struct TierPrediction {
+  bool on;
+  bool all_fell_back = false;
+  explicit TierPrediction(int mode) {
+    const char* e = std::getenv("WMOM_TIER_PREDICT");
+    on = mode == WMOM_MODE_MIXED && !(e && e[0] == '0') && emul_gemm_hook() != nullptr;
+  }
+  bool direct() const { return on && all_fell_back; }
+  void record(const wmom_report* rep, int bg) {
+    bool all = bg > 0;
+    for (int b = 0; b < bg; ++b)
+      if (rep[b].tier < 2) all = false;
+    all_fell_back = all;
+  }
+};
+
 bool cached_lu_config(int mode, int n, LuConfig* out) {
   if (env_int("WMOM_LU_BATCH", 1, kMaxLuBatch)) return false;  // an override goes through the tuner path
   std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1540,6 +1570,7 @@ wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) 
   FactorGraph graph;
   std::vector<wmom_report> rep(kMaxLuBatch);
   wmom_status overall = WMOM_OK;
+  TierPrediction predict(a.mode);
   for (int gi = 0; gi < ngroups; ++gi) {
     // the next group's fill goes in before this group's factorisation: it runs on the
     // SMs the factorisation leaves
@@ -1551,12 +1582,16 @@ wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) 
     SWEEP_TRY(cudaStreamWaitEvent(sp.hi, filled[gi], 0));
     const double2* Zg = zall.as<double2>() + (size_t)f0 * nn;
     int info[kMaxLuBatch] = {};
-    st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, sp.hi, info,
-                      nullptr, &graph, cfg.span);
-    if (st != WMOM_OK) return st;
+    const bool direct = predict.direct();
+    if (!direct) {
+      st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, sp.hi, info,
+                        nullptr, &graph, cfg.span);
+      if (st != WMOM_OK) return st;
+    }
     st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                     rep.data(), a.condest, n);
+                     rep.data(), a.condest, n, direct);
     if (st != WMOM_OK) return st;
+    predict.record(rep.data(), bg);
     st = group_results(g, bg, a.ngap, rep.data(), f0, a.currents, a.zin, a.reports, &overall);
     if (st != WMOM_OK) return st;
   }
@@ -1567,7 +1602,9 @@ wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) 
 
 }  // namespace
 
-wmom_status run_sweep(const SweepArgs& a) {
+namespace {
+
+wmom_status run_sweep_ordered(const SweepArgs& a) {
   retain_pool_memory();
   {
     // pipelined when the shape is already tuned, the sweep has more than one group
@@ -1609,6 +1646,7 @@ wmom_status run_sweep(const SweepArgs& a) {
   DevBuf lu, piv;
   GroupScratch g;
   FactorGraph graph;
+  TierPrediction predict(a.mode);
   for (int f0 = 0; f0 < a.nfreq; f0 += nbf) {
     const int nb = std::min(nbf, a.nfreq - f0);
     wmom_status st = fill_batch(p, a.freq_mhz + f0, nb, zall.as<double2>(), s);
@@ -1627,18 +1665,61 @@ wmom_status run_sweep(const SweepArgs& a) {
       const int bg = std::min(B, nb - g0);
       const double2* Zg = zall.as<double2>() + (size_t)g0 * nn;
       int info[kMaxLuBatch] = {};
-      st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, s, info, nullptr,
-                        &graph, cfg.span);
-      if (st != WMOM_OK) return st;
+      const bool direct = predict.direct();
+      if (!direct) {
+        st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, s, info,
+                          nullptr, &graph, cfg.span);
+        if (st != WMOM_OK) return st;
+      }
       st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                       rep.data(), a.condest, n);
+                       rep.data(), a.condest, n, direct);
       if (st != WMOM_OK) return st;
+      predict.record(rep.data(), bg);
       st = group_results(g, bg, a.ngap, rep.data(), f0 + g0, a.currents, a.zin, a.reports, &overall);
       if (st != WMOM_OK) return st;
     }
   }
   SWEEP_TRY(cudaStreamSynchronize(s));
   return overall;
+}
+
+}  // namespace
+
+// The sweep in the order its second-tier prediction wants: frequencies from the
+// highest down (TierPrediction).  The frequencies are permuted into that order, the
+// sweep runs, and currents, Z_in and reports go back to the caller's order.  Each
+// matrix is factored and solved on its own (batched launches keep the matrices
+// independent), so the order changes no result.
+wmom_status run_sweep(const SweepArgs& a) {
+  const TierPrediction predict(a.mode);
+  if (!predict.on || a.nfreq < 2) return run_sweep_ordered(a);
+  std::vector<int> ord(a.nfreq);
+  for (int i = 0; i < a.nfreq; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return a.freq_mhz[x] > a.freq_mhz[y]; });
+  bool same = true;
+  for (int i = 0; i < a.nfreq; ++i) same = same && ord[i] == i;
+  if (same) return run_sweep_ordered(a);
+  const size_t n = (size_t)a.plan->npls;
+  std::vector<float> f(a.nfreq);
+  for (int i = 0; i < a.nfreq; ++i) f[i] = a.freq_mhz[ord[i]];
+  std::vector<double> cur(a.currents ? 2 * n * a.nfreq : 0), zin(a.zin ? 2 * (size_t)a.nfreq : 0);
+  std::vector<wmom_report> rep(a.reports ? a.nfreq : 0);
+  SweepArgs b = a;
+  b.freq_mhz = f.data();
+  b.currents = a.currents ? cur.data() : nullptr;
+  b.zin = a.zin ? zin.data() : nullptr;
+  b.reports = a.reports ? rep.data() : nullptr;
+  const wmom_status st = run_sweep_ordered(b);
+  for (int i = 0; i < a.nfreq; ++i) {
+    const int k = ord[i];
+    if (a.currents) std::copy(cur.begin() + 2 * n * i, cur.begin() + 2 * n * (i + 1), a.currents + 2 * n * k);
+    if (a.zin) {
+      a.zin[2 * k] = zin[2 * i];
+      a.zin[2 * k + 1] = zin[2 * i + 1];
+    }
+    if (a.reports) a.reports[k] = rep[i];
+  }
+  return st;
 }
 
 // ----------------------------------------------- geometries of uneven order ----
@@ -1787,7 +1868,7 @@ wmom_status factors_solve(FactorSet* fs, int first, int count, int ngap, float a
     const double2* l64 = reinterpret_cast<const double2*>(fs->lu) + (size_t)f * nn;
     st = solve_group(fs->mode, n, fs->z64 + (size_t)f * nn, bg, mixed ? l32 : nullptr, mixed ? nullptr : l64,
                      fs->ipiv + (size_t)f * n, fs->info.data() + f, tol, fs->ws, g, rep.data(), fs->condest,
-                     nreal);
+                     nreal, false);
     if (st != WMOM_OK) return st;
     // results are indexed from `first` in the caller's arrays
     st = group_results(g, bg, ngap, rep.data(), f - first, currents, zin, reports, &overall, nreal);

@@ -159,12 +159,14 @@ def test_dropin_zmatrix_gpu_symbol(cuda, wmom, orc, ienv):
 
 
 def test_batch_width_does_not_change_results(cuda, wmom):
-    # the same frequencies factored one matrix per launch and four per launch
+    # the same frequencies factored one matrix per launch and four per launch (without
+    # the second-tier prediction, whose decisions follow the group boundaries)
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
     freqs = np.array([0.002, 0.05, 1.0, 7.0, 20.0], np.float32)
     out = {}
     for width in ("1", "4"):
         os.environ["WMOM_LU_BATCH"] = width
+        os.environ["WMOM_TIER_PREDICT"] = "0"
         try:
             plan = wmom.Plan(topo)
             for mode in (0, 1):
@@ -172,6 +174,7 @@ def test_batch_width_does_not_change_results(cuda, wmom):
             plan.close()
         finally:
             del os.environ["WMOM_LU_BATCH"]
+            del os.environ["WMOM_TIER_PREDICT"]
     for mode in (0, 1):
         c1, z1, r1 = out[("1", mode)]
         c4, z4, r4 = out[("4", mode)]
@@ -257,15 +260,55 @@ def test_pipelined_sweep_is_bit_identical(cuda, wmom, mode):
     plan = wmom.Plan(topo)
     freqs = np.array([0.003, 0.02, 0.2, 1.0, 3.0, 7.0, 12.0, 25.0], np.float32)
     out = {}
+    os.environ["WMOM_TIER_PREDICT"] = "0"  # its decisions follow the group boundaries
     try:
         for groups in ("1", "1", "2", "3"):  # the first call tunes the shape
             os.environ["WMOM_PIPELINE"] = groups
             out[groups] = plan.solve(freqs, 1000, mode=mode)
     finally:
         os.environ.pop("WMOM_PIPELINE", None)
+        os.environ.pop("WMOM_TIER_PREDICT", None)
     c1, z1, r1 = out["1"]
     for g in ("2", "3"):
         c, z, r = out[g]
         assert np.array_equal(c, c1) and np.array_equal(z, z1), g
         assert r == r1, g
     plan.close()
+
+
+def test_second_tier_prediction(cuda, wmom):
+    """A sweep runs its groups from the highest frequency down; once a whole group
+    has fallen back to the second tier, the lower-frequency groups go there directly,
+    without FP32 factors.  A predicted matrix must get the answer it gets after
+    failing in tier 1, bit for bit; the sweep must factor fewer FP32 matrices; and
+    the results come back in the caller's frequency order."""
+    w = wmom
+    topo = w.Topology(w.geometry.precision_grid(2048))
+    plan = w.Plan(topo)
+    freqs = np.array([0.003, 30.0, 0.001, 0.01, 10.0, 0.03, 1.0, 0.1], np.float32)  # not sorted
+    out = {}
+    os.environ["WMOM_LU_BATCH"] = "2"
+    os.environ["WMOM_LU_SPAN"] = "2"
+    try:
+        for pred in ("0", "1"):
+            os.environ["WMOM_TIER_PREDICT"] = pred
+            w.stats_reset()
+            out[pred] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True) + (w.stats_read(),)
+    finally:
+        for k in ("WMOM_LU_BATCH", "WMOM_LU_SPAN", "WMOM_TIER_PREDICT"):
+            os.environ.pop(k, None)
+    c0, z0, r0, st0 = out["0"]
+    c1, z1, r1, st1 = out["1"]
+    cfp, _, _ = plan.solve(freqs, 1000, mode=w.MODE_FP64)
+    plan.close()
+    predicted = 0
+    for k, f in enumerate(freqs):
+        assert r1[k]["status"] == 0 and r0[k]["status"] == 0
+        if r0[k]["tier"] >= 2 and r1[k]["tier"] >= 2:
+            assert np.array_equal(c1[k], c0[k]) and z1[k] == z0[k], float(f)
+            predicted += r1[k]["iterations"] < r0[k]["iterations"]
+        bound = max(1e-9, 8 * r1[k]["cond1"] * 2.0 ** -53)
+        assert _rel(c1[k], cfp[k]) <= bound, (float(f), r1[k])
+    # the lowest frequencies sit in groups after a fully fallen-back one
+    assert predicted >= 2, [(r["tier"], r["iterations"]) for r in r1]
+    assert st1["tc_gemm"]["launches"] < st0["tc_gemm"]["launches"]
