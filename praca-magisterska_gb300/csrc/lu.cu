@@ -1026,6 +1026,55 @@ __global__ void __launch_bounds__(256) trsm_kernel(const C* __restrict__ T, long
   }
 }
 
+// FP64 unit-lower TRSM of the second tier's narrow panels, B <- L^-1 B for an NB x NB
+// unit lower L (NB = 8, 16, 24, 32: the FP64 cluster panels' widths), one thread per
+// column of B holding the whole column in registers, one warp per block.  Every
+// element receives its updates in increasing k, as in trsm_kernel, so the results are
+// identical; but no barrier separates the rows, and no padded row costs FP64 work.
+// The FP64 pipe bounds it (4 NB (NB - 1) / 2 FP64 FMAs per column).  trsm_kernel, with
+// a barrier per row of the triangle, ran at about a third of that rate.
+template <typename C, int NB>
+__global__ void __launch_bounds__(32) trsm_lower_reg_kernel(const C* __restrict__ T, long long ldt,
+                                                            C* __restrict__ B, long long ldb, int ncols,
+                                                            long long tstride, long long bstride) {
+  __shared__ C Ls[NB * NB];  // column-major, strictly lower part (the rest zero, never read)
+  T += (size_t)blockIdx.y * tstride;
+  B += (size_t)blockIdx.y * bstride;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < NB * NB; idx += 32) {
+    const int k = idx / NB, r = idx - k * NB;
+    Ls[idx] = r > k ? T[(size_t)k * ldt + r] : cmake<C>(0, 0);
+  }
+  __syncthreads();
+  const int c = blockIdx.x * 32 + tid;
+  if (c >= ncols) return;
+  C* col = B + (size_t)c * ldb;
+  C x[NB];
+#pragma unroll
+  for (int r = 0; r < NB; ++r) x[r] = col[r];
+#pragma unroll
+  for (int k = 0; k < NB - 1; ++k)
+#pragma unroll
+    for (int r = k + 1; r < NB; ++r) x[r] = cfms(x[r], Ls[k * NB + r], x[k]);
+#pragma unroll
+  for (int r = 0; r < NB; ++r) col[r] = x[r];
+}
+
+template <typename C>
+cudaError_t trsm_lower_reg(const C* T, long long ldt, C* B, long long ldb, int nb, int ncols, long long tstride,
+                           long long bstride, int batch, cudaStream_t s, bool* done) {
+  *done = true;
+  const dim3 grid((ncols + 31) / 32, batch);
+  switch (nb) {
+    case 8: trsm_lower_reg_kernel<C, 8><<<grid, 32, 0, s>>>(T, ldt, B, ldb, ncols, tstride, bstride); break;
+    case 16: trsm_lower_reg_kernel<C, 16><<<grid, 32, 0, s>>>(T, ldt, B, ldb, ncols, tstride, bstride); break;
+    case 24: trsm_lower_reg_kernel<C, 24><<<grid, 32, 0, s>>>(T, ldt, B, ldb, ncols, tstride, bstride); break;
+    case 32: trsm_lower_reg_kernel<C, 32><<<grid, 32, 0, s>>>(T, ldt, B, ldb, ncols, tstride, bstride); break;
+    default: *done = false; return cudaSuccess;
+  }
+  return cudaGetLastError();
+}
+
 // FP32 unit-lower TRSM of the factorisation, B <- L^-1 B for an nb x nb unit lower L
 // (nb <= 64), one thread per column of B.  L and the B block are staged once per
 // block in shared memory (loads batched, kILP in flight per thread); L is read by
@@ -1937,9 +1986,17 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       trsm_lower_cols_kernel<C><<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads,
                                   tsmem, s>>>(T, lda, Bb, lda, w, nc, astride, astride);
     } else {
-      // FP64: the work is bound by the SMs' FP64 pipes, so it is spread over many
-      // CTAs of 16 columns (the one-thread-per-column kernel, 128 columns per CTA,
-      // was 4x slower on the second tier's late, narrow panels)
+      // FP64: the work is bound by the SMs' FP64 pipes.  Panels of 8 .. 32 columns
+      // (the second tier's) take the one-warp, column-in-registers kernel; wider ones
+      // (the plain form's cooperative 64-column panels) spread their columns over
+      // many CTAs of 16 (the FP32 one-thread-per-column kernel, 128 columns per CTA,
+      // pads to 64 rows and was 4x slower on the second tier's late panels)
+      if (w == 8 || w == 16 || w == 24 || w == 32) {
+        bool done = false;
+        stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
+        te = trsm_lower_reg<C>(T, lda, Bb, lda, w, nc, astride, astride, batch, s, &done);
+        if (done) return te;
+      }
       const size_t tsmem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(C);
       te = allow_dynamic_smem((const void*)trsm_kernel<C, false>, tsmem);
       if (te != cudaSuccess) return te;
