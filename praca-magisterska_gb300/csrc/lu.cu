@@ -1987,11 +1987,18 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
                                   tsmem, s>>>(T, lda, Bb, lda, w, nc, astride, astride);
     } else {
       // FP64: the work is bound by the SMs' FP64 pipes.  Panels of 8 .. 32 columns
-      // (the second tier's) take the one-warp, column-in-registers kernel; wider ones
-      // (the plain form's cooperative 64-column panels) spread their columns over
-      // many CTAs of 16 (the FP32 one-thread-per-column kernel, 128 columns per CTA,
-      // pads to 64 rows and was 4x slower on the second tier's late panels)
-      if (w == 8 || w == 16 || w == 24 || w == 32) {
+      // (the second tier's) take the one-warp, column-in-registers kernel when their
+      // columns give every SM at least two warps; narrower right-hand sides (the
+      // in-group solves of `span` panels, the late trailing columns) and wider
+      // panels (the plain form's cooperative 64-column ones) spread their rows over
+      // CTAs of 16 columns (the FP32 one-thread-per-column kernel, 128 columns per
+      // CTA, pads to 64 rows and was 4x slower on the second tier's late panels).
+      // Measured on the N = 8192 grid (9 second-tier matrices) and the 256-frequency
+      // N = 2048 grid, trsm class: 71 / 172 ms with trsm_kernel alone, 66 / 196 with
+      // the register kernel on every solve (a one-warp block is too little FP64 work
+      // for the 24-column in-group solves), 51 / 143 with this choice.
+      const long long warps = (long long)((nc + 31) / 32) * batch;
+      if ((w == 8 || w == 16 || w == 24 || w == 32) && warps >= 2LL * lim.sms) {
         bool done = false;
         stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
         te = trsm_lower_reg<C>(T, lda, Bb, lda, w, nc, astride, astride, batch, s, &done);
