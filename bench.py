@@ -582,7 +582,8 @@ def serve_rates(args, rates, seconds):
         warm = serve.Server(workers=1)  # warm-up: CUDA context, kernels, batch-width tuner
         warm.submit(serve.Request(pool[0], grid[:2], 1, currents=False)).result()
         warm.close()
-        srv = serve.Server(workers=args.serve_workers, coalesce_freqs=args.serve_coalesce)
+        srv = serve.Server(workers=args.serve_workers, coalesce_freqs=args.serve_coalesce,
+                           max_wait_s=args.serve_max_wait)
         t_end = time.perf_counter() + seconds
         history, futs = [], []
         t = time.perf_counter()
@@ -598,14 +599,19 @@ def serve_rates(args, rates, seconds):
             t += rng.exponential(1.0 / rate)
             time.sleep(max(0.0, t - time.perf_counter()))
         for f in futs:
-            f.result()
+            try:
+                f.result()
+            except serve.Shed:
+                pass  # counted by the server (shed_requests)
         st = srv.stats()
         srv.close()
         st.update(offered_req_per_s=rate, submitted=len(futs), seconds=seconds,
                   workload=f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}] over "
                            f"{args.serve_geometries} geometries, 1-16 frequencies in 1 kHz-30 MHz, 30% repeat "
                            f"excitations, {args.serve_workers} worker streams, waiting requests of one "
-                           f"geometry factored together up to {args.serve_coalesce} frequencies")
+                           f"geometry factored together up to {args.serve_coalesce} frequencies"
+                           + (f", requests that waited over {args.serve_max_wait} s shed"
+                              if args.serve_max_wait is not None else ""))
         results.append(st)
     return results
 
@@ -619,7 +625,8 @@ def run_serving(args):
             "config": {"workload": f"Poisson requests, N in [{args.serve_nmin}, {args.serve_nmax}], 1-16 "
                                    "frequencies in 1 kHz-30 MHz, 30% repeat excitations",
                        "geometries": args.serve_geometries, "seconds_per_rate": args.serve_seconds,
-                       "workers": args.serve_workers, "coalesce_freqs": args.serve_coalesce},
+                       "workers": args.serve_workers, "coalesce_freqs": args.serve_coalesce,
+                       "max_wait_s": args.serve_max_wait},
             "rates": results}
     print(json.dumps(line), flush=True)
 
@@ -816,6 +823,8 @@ def main():
     ap.add_argument("--serve-nmax", type=int, default=6144)
     ap.add_argument("--serve-geometries", type=int, default=8)
     ap.add_argument("--serve-workers", type=int, default=4)  # 4 beat 2 at the saturated rates
+    ap.add_argument("--serve-max-wait", type=float, default=None,
+                    help="load shedding: requests that waited longer (s) when a worker takes them are turned away")
     ap.add_argument("--serve-coalesce", type=int, default=32,
                     help="distinct frequencies of one geometry factored together (0: one request at a time)")
     args = ap.parse_args()

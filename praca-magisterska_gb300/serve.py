@@ -19,7 +19,10 @@ requests as they arrive:
   memory;
 * requests that arrive while others run are admitted as soon as a worker and
   memory are free, and their GPU work overlaps with the running ones (separate
-  streams).
+  streams);
+* optional load shedding (max_wait_s): a request that has already waited longer
+  when a worker takes it fails with Shed, so that under overload the served
+  requests keep a bounded latency.
 
 Each completed request records its latency (arrival to completion); Server.stats()
 reports p50/p99 latency, throughput and goodput.  The reference has no serving
@@ -33,6 +36,11 @@ import time
 from concurrent.futures import Future
 
 import numpy as np
+
+
+class Shed(Exception):
+    """The request waited in the queue longer than the server's max_wait_s and was
+    turned away without being served."""
 
 
 class Request:
@@ -75,7 +83,7 @@ class Server:
     streams (the host-logic tests run the loop on the CPU against a fake library)."""
 
     def __init__(self, mode=None, hbm_budget_bytes=None, workers=2, tol=1e-12, lib=None, stream_factory=None,
-                 coalesce_freqs=32):
+                 coalesce_freqs=32, max_wait_s=None):
         self._w = lib if lib is not None else importlib.import_module("praca-magisterska_gb300")
         self._new_stream = stream_factory or _cuda_stream
         self.mode = self._w.MODE_MIXED if mode is None else mode
@@ -88,6 +96,10 @@ class Server:
         # a worker serves, with the request it takes, the queued requests of the same
         # geometry, up to this many distinct frequencies together (0: one at a time)
         self.coalesce_freqs = int(coalesce_freqs)
+        # load shedding: a request that has waited longer than this when a worker
+        # takes it fails with Shed instead of being served (None: never)
+        self.max_wait_s = max_wait_s
+        self.shed = 0
         self._lock = threading.Condition()
         self._queue = collections.deque()
         self._plans = {}          # geo key -> (Topology, Plan)
@@ -146,7 +158,7 @@ class Server:
                    "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
                    "slo_ms": slo_ms, "goodput_solves_per_s": good / span if span > 0 else 0.0,
                    "resident_bytes": self._used, "budget_bytes": self.budget, "evictions": self.evictions,
-                   "coalesced_requests": self.coalesced}
+                   "coalesced_requests": self.coalesced, "shed_requests": self.shed}
         return out
 
     # ------------------------------------------------------------ internals ----
@@ -228,8 +240,19 @@ class Server:
                 if self._stop and not self._queue:
                     return
                 group = self._take_group(self._queue.popleft())
+                if self.max_wait_s is not None:
+                    now = time.perf_counter()
+                    late = [r for r in group if now - r.arrival > self.max_wait_s]
+                    group = [r for r in group if now - r.arrival <= self.max_wait_s]
+                    self.shed += len(late)
+                else:
+                    late = []
                 if len(group) > 1:
                     self.coalesced += len(group)
+            for r in late:
+                r.future.set_exception(Shed(f"waited more than {self.max_wait_s} s in the queue"))
+            if not group:
+                continue
             try:
                 self._serve(group, sp)
             except Exception as e:  # the group's requests fail, the loop goes on

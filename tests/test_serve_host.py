@@ -296,3 +296,27 @@ def test_failing_request_in_a_group_fails_alone():
         assert st["requests"] == 3 and st["resident_bytes"] <= st["budget_bytes"]
     finally:
         srv.close()
+
+
+def test_load_shedding_turns_away_requests_that_waited_too_long():
+    """With max_wait_s set, a request that has waited longer than that when a worker
+    takes it fails with Shed and is counted; the others are served."""
+    lib = FakeLib()
+    srv = serve.Server(hbm_budget_bytes=_per_set(64, 16), workers=1, lib=lib,
+                       stream_factory=lambda: (None, "stream"), max_wait_s=0.2)
+    try:
+        entered, release = threading.Event(), threading.Event()
+        lib.hold[9.0] = (entered, release)
+        f_hold = srv.submit(serve.Request("a 64", [1.0], 2, ampl=9.0))
+        assert entered.wait(10)
+        f_late = srv.submit(serve.Request("b 64", [1.0], 1))
+        time.sleep(0.4)
+        release.set()
+        _check(f_hold.result(timeout=10), [1.0], 9.0)
+        with pytest.raises(serve.Shed):
+            f_late.result(timeout=10)
+        _check(srv.submit(serve.Request("b 64", [2.0], 1)).result(timeout=10), [2.0], 1.0)
+        st = srv.stats()
+        assert st["shed_requests"] == 1 and st["requests"] == 2
+    finally:
+        srv.close()
