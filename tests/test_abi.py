@@ -101,6 +101,27 @@ def test_fill_geometries_rejects_bad_arguments(wmom):
     assert f(plans, 1, ka, ptr, ld, None) == 1          # null plan
 
 
+def test_geometry_batch_and_tuner_queries_reject_bad_arguments(wmom):
+    """wmom_factor_geometries checks its arguments before any device call;
+    wmom_tuned_config / wmom_tuned_shape report an order that was never tuned (or a
+    bad one) as WMOM_ERR_ARG; wmom_padded_order is the size-class ladder."""
+    import ctypes
+    f = wmom._factor_geometries
+    freqs = (ctypes.c_float * 1)(10.0)
+    outs = (ctypes.c_void_p * 1)()
+    plans = (ctypes.c_void_p * 1)(None)
+    assert f(plans, 0, freqs, wmom.MODE_MIXED, outs, None) == 1   # count 0
+    assert f(plans, 1, freqs, wmom.MODE_MIXED, None, None) == 1   # no output array
+    assert f(plans, 1, freqs, wmom.MODE_MIXED, outs, None) == 1   # null plan
+    assert f(plans, 1, freqs, 7, outs, None) == 1                  # unknown mode
+    assert wmom.tuned_config(4096, wmom.MODE_MIXED) is None
+    assert wmom.tuned_shape(4096, wmom.MODE_MIXED) is None
+    assert wmom._tuned_shape(0, wmom.MODE_MIXED, None, None) == 1
+    assert wmom._tuned_shape(4096, 5, None, None) == 1
+    assert [wmom.padded_order(n) for n in (1, 64, 65, 256, 257, 320, 321, 1000, 4096, 4097)] == \
+        [64, 64, 128, 256, 320, 320, 384, 1024, 4096, 5120]
+
+
 def test_stats_classes_match_library(wmom):
     """The Python names of the stats classes and the library's class count agree
     (wmom_stats_read returns the number of classes and needs no GPU)."""
