@@ -693,14 +693,15 @@ def run_geometries(args):
         runs.append((dt, st, done))
     dt, st, done = min(runs, key=lambda r: r[0])
     fill_ms = _fill_all_geometries(w, pool, freqs)
-    geometries_batched(w, pool, freqs, args.workers)  # warm-up (kernels of every class)
-    bruns = [geometries_batched(w, pool, freqs, args.workers) for _ in range(max(1, args.steps))]
+    geometries_batched(w, pool, freqs, args.batch_workers)  # warm-up (kernels of every class)
+    bruns = [geometries_batched(w, pool, freqs, args.batch_workers) for _ in range(max(1, args.steps))]
     bdt, phases, breps = min(bruns, key=lambda r: r[0])
     line = {"metric": "freq-solves/s over a set of geometries of uneven size (one frequency each)",
             "unit": "freq-solves/s", "value": args.geometries / bdt, "higher_is_better": True, "n_gpus": 1,
             "ms_per_step": 1e3 * bdt, "steps": len(bruns), "data": "synthetic (seeded random wires)",
             "config": {"workload": f"{args.geometries} random-wire geometries, N uniform in [256, 4096], one "
                                    "frequency each in 1 kHz-30 MHz, precision form", "workers": args.workers,
+                       "batch_workers": args.batch_workers,
                        "unknowns_total": int(sizes.sum()),
                        "classes": len({w.padded_order(int(n)) for n in sizes})},
             "batched": {"phases_ms": phases, "tiers": tier_counts(breps),
@@ -807,6 +808,8 @@ def main():
     ap.add_argument("--k", type=int, default=96, help="inner dimension of the gemm_* workloads")
     ap.add_argument("--geometries", type=int, default=64)
     ap.add_argument("--workers", type=int, default=6)  # best of 4/6/8/10 on the 64-geometry set
+    ap.add_argument("--batch-workers", type=int, default=6,
+                    help="host threads and streams of the geometry batch's plan builds and solves")
     ap.add_argument("--fp64-freqs", type=int, default=2)
     ap.add_argument("--nfreq", type=int, default=None,
                     help="use an evenly spaced subset of the workload's frequencies (profiling cases)")
