@@ -1416,6 +1416,235 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   if (tid == 0) st_release_i32(&flags[b], epoch);
 }
 
+// ------------------------------------------------- float-float trsv ----
+// The second tier's corrections solve with FP64-grade factors held as float-float
+// values: every entry of the factors is hi + lo, two complex64 values with |lo| at
+// most half an FP32 ulp of hi, stored as one float4 (hi.re, hi.im, lo.re, lo.im) in
+// place of the complex128 entry (split_ff_inplace; the same 16 bytes, so the factors'
+// layout and strides are unchanged).  The arithmetic is compensated FP32 (Dekker's and Knuth's error-free
+// products and sums), about 2^-48 relative per operation, on the FP32 pipe, which
+// GB300 runs 64 times as fast as its FP64 pipe.  Inside iterative refinement with
+// FP64 residuals that accuracy is enough: it is below the second tier's own
+// factorisation error (about 2^-45), so the corrections contract as fast as with FP64
+// solves, and the FP64 residual still sets the final accuracy.  Block structure,
+// ticket order, ready flags and bounded waits are trsv_kernel's.
+struct Ff {
+  float h, l;
+};
+struct Ffc {
+  Ff re, im;
+};
+
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// acc - a * b
+__device__ __forceinline__ Ff ff_fms(Ff acc, Ff a, Ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);  // the head product's rounding error, exactly
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  float s, t;
+  ff_two_sum(acc.h, -p, s, t);
+  t = __fadd_rn(t, __fsub_rn(acc.l, e));
+  const float h = __fadd_rn(s, t);
+  return Ff{h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ Ff ff_add(Ff a, Ff b) {
+  float s, e;
+  ff_two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return Ff{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ Ff ff_neg(Ff a) { return Ff{-a.h, -a.l}; }
+
+// acc - a * b, complex
+__device__ __forceinline__ Ffc ffc_fms(Ffc acc, const Ffc& a, const Ffc& b) {
+  acc.re = ff_fms(acc.re, a.re, b.re);
+  acc.re = ff_fms(acc.re, ff_neg(a.im), b.im);
+  acc.im = ff_fms(acc.im, a.re, b.im);
+  acc.im = ff_fms(acc.im, a.im, b.re);
+  return acc;
+}
+
+__device__ __forceinline__ Ffc ffc_add(const Ffc& a, const Ffc& b) { return Ffc{ff_add(a.re, b.re), ff_add(a.im, b.im)}; }
+
+// a * b, complex: 0 - (-a) * b
+__device__ __forceinline__ Ffc ffc_mul(const Ffc& a, const Ffc& b) {
+  return ffc_fms(Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}}, Ffc{ff_neg(a.re), ff_neg(a.im)}, b);
+}
+
+__device__ __forceinline__ Ff ff_of(double v) {
+  const float h = __double2float_rn(v);
+  return Ff{h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double ff_dbl(Ff a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ Ffc ffc_of(double2 v) { return Ffc{ff_of(v.x), ff_of(v.y)}; }
+__device__ __forceinline__ double2 ffc_dbl(const Ffc& a) { return make_double2(ff_dbl(a.re), ff_dbl(a.im)); }
+__device__ __forceinline__ Ffc ffc_ld(const float4* a, size_t i) {
+  const float4 v = a[i];
+  return Ffc{Ff{v.x, v.z}, Ff{v.y, v.w}};
+}
+
+template <bool UPPER>
+__global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__ A, long long lda, int n,
+                                                      double2* x, int* flags,
+                                                      unsigned int* ticket, int epoch, int* err, long long astride,
+                                                      int flag_stride, const int* __restrict__ sel) {
+  __shared__ Ffc xs[kTrsvB];
+  __shared__ Ffc part[4][kTrsvB];
+  __shared__ Ffc dinv[kTrsvB];  // 1 / u_cc (back substitution)
+  __shared__ int s_b, s_m, s_ok;
+  const int tid = threadIdx.x;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  const int batch = (int)gridDim.x / nblk;
+  if (tid == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    const int bi = (int)(t / (unsigned)batch);
+    s_m = (int)(t % (unsigned)batch);
+    s_b = UPPER ? nblk - 1 - bi : bi;
+    s_ok = 1;
+  }
+  __syncthreads();
+  const int b = s_b;
+  if (b < 0 || b >= nblk) return;
+  const int mat = sel ? sel[s_m] : s_m;
+  A += (size_t)mat * astride;
+  x += (size_t)mat * n;
+  flags += (size_t)s_m * flag_stride;
+  const int r0 = b * kTrsvB;
+  const int rows = min(kTrsvB, n - r0);
+  const int r = tid & (kTrsvB - 1), g = tid >> 6;
+  // the diagonal block in shared memory, and (back substitution) the reciprocals of
+  // its diagonal, in FP64 once per entry, before the waits
+  extern __shared__ __align__(16) unsigned char trsv_ff_smem[];
+  Ffc* Ds = reinterpret_cast<Ffc*>(trsv_ff_smem);  // kTrsvB x kTrsvB, column-major
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int c = idx / kTrsvB, q = idx - c * kTrsvB;
+    Ds[idx] = (c < rows && q < rows) ? ffc_ld(A, (size_t)(r0 + c) * lda + r0 + q)
+                                     : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+  }
+  if (UPPER && tid < kTrsvB) {
+    const int c = tid;
+    double2 d = make_double2(1.0, 0.0);
+    if (c < rows) {
+      const Ffc dd = ffc_ld(A, (size_t)(r0 + c) * lda + r0 + c);
+      d = ffc_dbl(dd);
+    }
+    dinv[c] = ffc_of(crecip(d));
+  }
+  Ffc acc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+  const int nsteps = UPPER ? nblk - 1 - b : b;
+  constexpr int kPer = kTrsvB / 4;
+  auto load_tile = [&](int j, Ffc* dst) {
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+    const size_t base = (size_t)c0 * lda + r0 + r;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int c = g + 4 * i;
+      dst[i] = (r < rows && c < cols) ? ffc_ld(A, base + (size_t)c * lda) : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+    }
+  };
+  Ffc a_cur[kPer];
+  if (nsteps > 0) load_tile(UPPER ? nblk - 1 : 0, a_cur);
+  for (int step = 0; step < nsteps; ++step) {
+    const int j = UPPER ? nblk - 1 - step : step;
+    if (tid == 0) {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_i32(&flags[j]) != epoch) {
+        if (ld_volatile_i32(err) || global_ns() - t0 > kTrsvWaitNs) {
+          atomicExch(err, 1);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const int c0 = j * kTrsvB;
+    const int cols = min(kTrsvB, n - c0);
+    if (tid < cols) xs[tid] = ffc_of(__ldcg(&x[c0 + tid]));
+    __syncthreads();
+    Ffc a_next[kPer];
+    if (step + 1 < nsteps) load_tile(UPPER ? j - 1 : j + 1, a_next);
+    if (r < rows) {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i)
+        if (g + 4 * i < cols) acc = ffc_fms(acc, a_cur[i], xs[g + 4 * i]);
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) a_cur[i] = a_next[i];
+    __syncthreads();
+  }
+  part[g][r] = acc;
+  __syncthreads();
+  if (tid < 32) {
+    // lane l holds rows l and l + 32 of the block; part[] holds -sum(T x) per group
+    Ffc s0{Ff{0.f, 0.f}, Ff{0.f, 0.f}}, s1 = s0;
+    if (tid < rows)
+      s0 = ffc_add(ffc_add(ffc_of(x[r0 + tid]), ffc_add(part[0][tid], part[1][tid])),
+                   ffc_add(part[2][tid], part[3][tid]));
+    if (tid + 32 < rows) {
+      const int q = tid + 32;
+      s1 = ffc_add(ffc_add(ffc_of(x[r0 + q]), ffc_add(part[0][q], part[1][q])), ffc_add(part[2][q], part[3][q]));
+    }
+    const Ffc* D = Ds;
+    constexpr int ld = kTrsvB;
+    auto shfl = [&](const Ffc& v, int src) {
+      return Ffc{Ff{__shfl_sync(0xffffffffu, v.re.h, src), __shfl_sync(0xffffffffu, v.re.l, src)},
+                 Ff{__shfl_sync(0xffffffffu, v.im.h, src), __shfl_sync(0xffffffffu, v.im.l, src)}};
+    };
+    if (!UPPER) {
+      for (int c = 0; c < rows; ++c) {
+        const Ffc xc = shfl(c < 32 ? s0 : s1, c & 31);
+        if (tid > c && tid < rows) s0 = ffc_fms(s0, D[(size_t)c * ld + tid], xc);
+        if (tid + 32 > c && tid + 32 < rows) s1 = ffc_fms(s1, D[(size_t)c * ld + tid + 32], xc);
+      }
+    } else {
+      for (int c = rows - 1; c >= 0; --c) {
+        // x_c = s_c / u_cc = s_c * (1 / u_cc), by its owner lane
+        if (c < 32) {
+          if (tid == c) s0 = ffc_mul(s0, dinv[c]);
+        } else {
+          if (tid + 32 == c) s1 = ffc_mul(s1, dinv[c]);
+        }
+        const Ffc xc = shfl(c < 32 ? s0 : s1, c & 31);
+        if (tid < c && tid < rows) s0 = ffc_fms(s0, D[(size_t)c * ld + tid], xc);
+        if (tid + 32 < c && tid + 32 < rows) s1 = ffc_fms(s1, D[(size_t)c * ld + tid + 32], xc);
+      }
+    }
+    if (tid < rows) x[r0 + tid] = ffc_dbl(s0);
+    if (tid + 32 < rows) x[r0 + tid + 32] = ffc_dbl(s1);
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) st_release_i32(&flags[b], epoch);
+}
+
+// Complex128 entries to float-float in place, (re, im) -> (hi.re, hi.im, lo.re,
+// lo.im) with hi = fp32(v), lo = fp32(v - hi); and back (hi + lo is exact in FP64).
+__global__ void split_ff_kernel(double2* a, size_t count) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 v = a[i];
+    const Ff re = ff_of(v.x), im = ff_of(v.y);
+    reinterpret_cast<float4*>(a)[i] = make_float4(re.h, im.h, re.l, im.l);
+  }
+}
+
+__global__ void merge_ff_kernel(double2* a, size_t count) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 v = reinterpret_cast<const float4*>(a)[i];
+    a[i] = make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+  }
+}
+
 // ------------------------------------------- conjugate-transpose trsv ----
 // Solves with the conjugate transposes of the factors, the second kind of solve of
 // the condition estimator (A^H x = b with P A = L U): U^H y = b by forward
@@ -2156,6 +2385,63 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
       gemm_sub_kernel<C><<<grid, 256, 0, s>>>(A + (size_t)k0 * lda, lda, B + k0, ldb, B, ldb, k0, nrhs, kb, 0);
     }
   }
+  return cudaGetLastError();
+}
+
+cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
+                        cudaStream_t s, int batch, long long astride, const int* sel) {
+  if (batch < 1 || batch > ws->max_batch || !ws->flags || n > ws->perm_cap) return cudaErrorInvalidValue;
+  if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
+  if ((size_t)n * batch * sizeof(double2) > ws->rhs_bytes) return cudaErrorInvalidValue;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  if (nblk > ws->flag_cap) return cudaErrorInvalidValue;
+  cudaError_t e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
+  if (e != cudaSuccess) return e;
+  // B <- P B, as lu_solve_t's single-right-hand-side path
+  stats::count(stats::kMisc, 2);
+  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
+  double2* tmp = reinterpret_cast<double2*>(ws->rhs);
+  if (sel) {
+    stats::count(stats::kMisc);
+    gather_vecs_kernel<double2><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(B, n, tmp, sel);
+  } else {
+    e = cudaMemcpyAsync(tmp, B, sizeof(double2) * (size_t)n * batch, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  gather_rows_kernel<double2><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(tmp, n, B, n, ws->perm, n, batch, n, sel);
+  const size_t dsmem = sizeof(Ffc) * kTrsvB * kTrsvB;
+  e = allow_dynamic_smem((const void*)trsv_ff_kernel<false>, dsmem);
+  if (e != cudaSuccess) return e;
+  e = allow_dynamic_smem((const void*)trsv_ff_kernel<true>, dsmem);
+  if (e != cudaSuccess) return e;
+  stats::Scope sc(stats::kTrsv, s, 8.0 * n * (double)n * batch, 2);
+  for (int pass = 0; pass < 2; ++pass) {
+    const int ep = ++ws->epoch;
+    e = cudaMemsetAsync(ws->ticket, 0, sizeof(unsigned int) * batch, s);
+    if (e != cudaSuccess) return e;
+    if (pass == 0)
+      trsv_ff_kernel<false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                             &ws->barrier->err, astride, ws->flag_cap, sel);
+    else
+      trsv_ff_kernel<true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
+                                                            &ws->barrier->err, astride, ws->flag_cap, sel);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t split_ff_inplace(double2* a, size_t count, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  stats::count(stats::kMisc);
+  const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  split_ff_kernel<<<blocks, 256, 0, s>>>(a, count);
+  return cudaGetLastError();
+}
+
+cudaError_t merge_ff_inplace(double2* a, size_t count, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  stats::count(stats::kMisc);
+  const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 152 * 16);
+  merge_ff_kernel<<<blocks, 256, 0, s>>>(a, count);
   return cudaGetLastError();
 }
 

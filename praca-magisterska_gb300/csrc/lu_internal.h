@@ -89,6 +89,18 @@ template <typename C>
 cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B, LuWorkspace* ws, cudaStream_t s,
                          int batch = 1, long long astride = 0, const int* sel = nullptr);
 
+// lu_solve_t with one right-hand side per matrix, for FP64-grade factors held as
+// float-float entries (split_ff_inplace: float4 (hi.re, hi.im, lo.re, lo.im) in
+// place of each complex128 entry, same layout), in compensated FP32 arithmetic
+// (about 2^-48 relative per operation): the second tier's solves inside its FP64
+// refinement.
+cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
+                        cudaStream_t s, int batch = 1, long long astride = 0, const int* sel = nullptr);
+// `count` complex128 values to float-float in place (hi = fp32(v), lo = fp32(v - hi)),
+// and back (exact).
+cudaError_t split_ff_inplace(double2* a, size_t count, cudaStream_t s);
+cudaError_t merge_ff_inplace(double2* a, size_t count, cudaStream_t s);
+
 // The plain FP64 form's trailing update, C -= A B for complex FP64 column-major
 // operands (`batch` matrices bstride apart): SIMT DFMA (gemm_sub_kernel, lu.cu) or
 // DMMA on the FP64 tensor pipe (lu_dmma.cu).  WMOM_FP64_UPDATE=dmma selects the

@@ -144,6 +144,15 @@ __global__ void accumulate_vec_kernel(double2* __restrict__ x, const float2* __r
   x[i].y += (double)d[i].y * inv[b];
 }
 
+// v[b] *= scale[b] (powers of two: exact), every vector of the batch
+__global__ void scale_vec64_kernel(double2* __restrict__ v, int n, int nvec, const double* __restrict__ scale) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * nvec) return;
+  const double sc = scale[i / n];
+  v[i].x *= sc;
+  v[i].y *= sc;
+}
+
 // x[b] += d[b] where active[b] (FP64 corrections of the second tier)
 __global__ void accumulate64_kernel(double2* __restrict__ x, const double2* __restrict__ d, int n, int nvec,
                                     const int* __restrict__ active) {
@@ -819,6 +828,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   const double step_budget = std::max(8.0, n / 256.0);
   const unsigned vgrid = (unsigned)(((size_t)n * bg + 255) / 256);
   std::vector<int> hact(kMaxLuBatch, 0);
+  std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
   const int max_it = 40;
   // direct_t2: the caller predicts that no matrix of the group is served by its FP32
   // factors (none were computed); the group goes straight to the second tier
@@ -829,7 +839,6 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
     widen_vec_kernel<<<vgrid, 256, 0, s>>>(g.d32.as<float2>(), g.x64.as<double2>(), (size_t)n * bg);
     SWEEP_TRY(cudaGetLastError());
-    std::vector<double> hscale(2 * kMaxLuBatch, 1.0);
     // the matrices still refining: residuals and corrections are computed for these
     // only (one slowly converging matrix no longer keeps its whole batch busy)
     std::vector<int> hsel(kMaxLuBatch, 0);
@@ -1052,9 +1061,44 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       int inf[kMaxLuBatch] = {};
       const wmom_status fst = factor_emul(n, flu, cn, fpiv, ws, s, inf, emul);
       if (fst != WMOM_OK) return fst;
+      // The solves run in compensated FP32 on these factors split to float-float in
+      // place (lu_solve_ff: about 2^-48 per operation, below the factors' own error),
+      // with every right-hand side scaled by a power of two to a norm near 1, inside
+      // FP32's range.  The condition estimate merges them back to FP64 first.
+      SWEEP_TRY(split_ff_inplace(flu, nn * cn, s));
+      const float4* fff = reinterpret_cast<const float4*>(flu);
+      double* dscale = g.scal.as<double>();
+      auto scale_slots = [&](double2* v, const double* norm, int cnt) -> wmom_status {
+        for (int j = 0; j < kMaxLuBatch; ++j) {
+          const double rn = j < cnt ? norm[j] : 0.0;
+          const double sc = (rn > 0 && std::isfinite(rn)) ? std::ldexp(1.0, -std::ilogb(rn)) : 1.0;
+          hscale[j] = sc;
+          hscale[kMaxLuBatch + j] = 1.0 / sc;
+        }
+        SWEEP_TRY(cudaMemcpyAsync(g.scal.p, hscale.data(), sizeof(double) * 2 * kMaxLuBatch, cudaMemcpyHostToDevice,
+                                  s));
+        stats::count(stats::kMisc);
+        scale_vec64_kernel<<<(unsigned)(((size_t)n * cnt + 255) / 256), 256, 0, s>>>(v, n, cnt, dscale);
+        SWEEP_TRY(cudaGetLastError());
+        return WMOM_OK;
+      };
+      auto unscale_slots = [&](double2* v, int cnt) -> wmom_status {
+        stats::count(stats::kMisc);
+        scale_vec64_kernel<<<(unsigned)(((size_t)n * cnt + 255) / 256), 256, 0, s>>>(v, n, cnt,
+                                                                                    dscale + kMaxLuBatch);
+        SWEEP_TRY(cudaGetLastError());
+        return WMOM_OK;
+      };
       // x = LU^-1 V (every slot of vrep holds the excitation)
       SWEEP_TRY(cudaMemcpyAsync(fx, g.vrep.p, sizeof(double2) * (size_t)n * cn, cudaMemcpyDeviceToDevice, s));
-      SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, fx, n, 1, ws, s, cn, (long long)nn));
+      {
+        std::vector<double> vn(kMaxLuBatch, g.vnorm);
+        wmom_status ss = scale_slots(fx, vn.data(), cn);
+        if (ss != WMOM_OK) return ss;
+        SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, fx, ws, s, cn, (long long)nn));
+        ss = unscale_slots(fx, cn);
+        if (ss != WMOM_OK) return ss;
+      }
       bool act[kMaxLuBatch];
       int stall2[kMaxLuBatch] = {};
       double prev2[kMaxLuBatch];
@@ -1134,8 +1178,16 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         }
         SWEEP_TRY(cudaMemcpyAsync(g.actv.p, hact.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
         SWEEP_TRY(cudaMemcpyAsync(g.sel.p, zsel2.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
-        SWEEP_TRY(lu_solve_t<double2>(flu, n, n, fpiv, frr, n, 1, ws, s, nsa, (long long)nn,
-                                      nsa == cn ? nullptr : g.sel.as<int>()));
+        {
+          std::vector<double> rn(kMaxLuBatch, 0.0);
+          for (int j = 0; j < cn; ++j) rn[j] = act[j] ? std::sqrt(hs.rnorm2[j]) : 0.0;
+          wmom_status ss = scale_slots(frr, rn.data(), cn);
+          if (ss != WMOM_OK) return ss;
+          SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, frr, ws, s, nsa, (long long)nn,
+                                nsa == cn ? nullptr : g.sel.as<int>()));
+          ss = unscale_slots(frr, cn);
+          if (ss != WMOM_OK) return ss;
+        }
         SWEEP_TRY(sumsq_fp64(frr, n, dsc->dnorm2, cn, s));
         stats::count(stats::kMisc);
         accumulate64_kernel<<<(unsigned)(((size_t)n * cn + 255) / 256), 256, 0, s>>>(fx, frr, n, cn,
@@ -1152,7 +1204,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
           s2.push_back(j);
           m2.push_back(b);
         }
-      // before tier 3 reuses the scratch factors
+      // before tier 3 reuses the scratch factors, with the factors back in FP64
+      if (condest && !s2.empty()) SWEEP_TRY(merge_ff_inplace(flu, nn * cn, s));
       const wmom_status cs = estimate(flu, fpiv, frr, s2, m2);
       if (cs != WMOM_OK) return cs;
     }
