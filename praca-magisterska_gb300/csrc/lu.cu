@@ -1431,7 +1431,7 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
 struct Ff {
   float h, l;
 };
-struct Ffc {
+struct __align__(16) Ffc {
   Ff re, im;
 };
 
@@ -1643,6 +1643,214 @@ __global__ void merge_ff_kernel(double2* a, size_t count) {
     const float4 v = reinterpret_cast<const float4*>(a)[i];
     a[i] = make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
   }
+}
+
+// ------------------------------------------- float-float cluster panel ----
+// The second tier's panels (FP64-grade factors under the digit-plane tensor-core
+// updates) in float-float arithmetic: panel_cluster_la_kernel's cluster, look-ahead,
+// publication and bounded barriers, with the rows held as float-float values in
+// shared memory (16 bytes each, as complex128), read from and written back to the
+// complex128 matrix.  Its rank-1 updates, the bulk of the panel's work, run on the
+// FP32 pipe instead of GB300's narrow FP64 pipe, at about 2^-48 per operation, below
+// the second tier's factorisation error (about 2^-45).  The pivot of a column is the
+// row with the largest |re| + |im| of the heads (within 2^-24 of the FP64 choice; on
+// a near tie either row is a valid partial pivot); its reciprocal is computed once
+// per CTA in FP64.
+struct ClusterPubFf {
+  float val;
+  int row;
+  int pad[2];  // cand starts 16-byte aligned
+  Ffc cand[64];
+  Ffc diag[64];
+};
+static_assert(sizeof(ClusterPubFf) == sizeof(ClusterPub<double2>), "same layout as the FP64 panel's");
+
+__device__ __forceinline__ Ffc ld_cluster_ffc(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(a)
+               : "memory");
+  return Ffc{Ff{v.x, v.y}, Ff{v.z, v.w}};
+}
+
+__device__ __forceinline__ float ffc_abs1(const Ffc& a) { return fabsf(a.re.h) + fabsf(a.im.h); }
+
+__global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_ff_kernel(double2* __restrict__ A,
+                                                                                 long long lda, int n, int j0,
+                                                                                 int w, int rpc,
+                                                                                 int* __restrict__ ipiv,
+                                                                                 GridBarrier* __restrict__ gb,
+                                                                                 long long astride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ClusterPubFf* pub = reinterpret_cast<ClusterPubFf*>(smem_raw);  // [2]
+  Ffc* prw_buf = reinterpret_cast<Ffc*>(pub + 2);  // pivot rows of columns j - 1 and j, 2 x 64
+  Ffc* dgr = prw_buf + 128;                        // diagonal row, 64
+  Ffc* tile = dgr + 64;                            // column-major rpc x w
+  __shared__ long long red_k[2][kClusterThreads / 32];
+  __shared__ int red_r[2][kClusterThreads / 32];
+  __shared__ Ffc s_inv;  // 1 / pivot of the current column, computed once per CTA
+  __shared__ int s_prw;  // pivot row of the current column
+
+  A += (size_t)blockIdx.y * astride;
+  ipiv += (size_t)blockIdx.y * n;
+  gb += blockIdx.y;
+  const unsigned cs = gridDim.x;  // the cluster spans blockIdx.x
+  const unsigned rank = cluster_rank();
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int base = j0 + (int)rank * rpc;
+  const int cnt = max(0, min(rpc, n - base));
+  const Ffc fzero{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+
+  if (t < cnt) {
+    const int gr = base + t;
+    for (int c0 = 0; c0 < w; c0 += 16) {
+      double2 v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + t] = ffc_of(v[u]);
+    }
+  }
+  __syncthreads();
+
+  // this CTA's candidate for column jc among its rows >= j0 + jc (first on ties),
+  // published with the candidate row and, from its owner, row j0 + jc
+  auto publish = [&](int jc) {
+    const int gjc = j0 + jc;
+    const int pc = jc & 1;
+    long long best = order_key(-1.0f);
+    int brow = INT_MAX;
+    if (t < cnt && base + t >= gjc) {
+      best = order_key(ffc_abs1(tile[(size_t)jc * rpc + t]));
+      brow = base + t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int orow = __shfl_xor_sync(0xffffffffu, brow, o);
+      if (ov > best || (ov == best && orow < brow)) {
+        best = ov;
+        brow = orow;
+      }
+    }
+    if (lane == 0) {
+      red_k[pc][warp] = best;
+      red_r[pc][warp] = brow;
+    }
+    __syncthreads();
+    if (t < w) {  // only these threads publish
+      best = order_key(-1.0f);
+      brow = INT_MAX;
+#pragma unroll
+      for (int q = 0; q < kClusterThreads / 32; ++q) {
+        const long long v = red_k[pc][q];
+        const int r = red_r[pc][q];
+        if (v > best || (v == best && r < brow)) {
+          best = v;
+          brow = r;
+        }
+      }
+      ClusterPubFf& my = pub[pc];
+      if (t == 0) {
+        my.val = key_value<float>(best);
+        my.row = brow;
+      }
+      if (best >= 0) my.cand[t] = tile[(size_t)t * rpc + (brow - base)];
+      if (gjc >= base && gjc < base + cnt) my.diag[t] = tile[(size_t)t * rpc + (gjc - base)];
+    }
+    // every read of the tile for the publication is done before the rows change
+    __syncthreads();
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  };
+
+  publish(0);
+  Ffc lr_l = fzero;  // this row's multiplier of the current column
+  for (int j = 0; j < w; ++j) {
+    const int gj = j0 + j;
+    const int par = j & 1;
+    Ffc* prow = prw_buf + 64 * par;               // pivot row of column j
+    const Ffc* pprev = prw_buf + 64 * (par ^ 1);  // pivot row of column j - 1
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    const unsigned owner_gj = (unsigned)((gj - j0) / rpc);  // the CTA holding row gj
+    int r = INT_MAX, q = -1;
+    if (warp * 32 < w) {
+      long long v = order_key(-1.0f);
+      if (lane < (int)cs) {
+        v = order_key(ld_cluster_f32(map_rank(&pub[par].val, lane)));
+        r = ld_cluster_s32(map_rank(&pub[par].row, lane));
+        q = lane;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, r, o);
+        const int oq = __shfl_xor_sync(0xffffffffu, q, o);
+        if (ov > v || (ov == v && orow < r)) {
+          v = ov;
+          r = orow;
+          q = oq;
+        }
+      }
+      if (t == 0) s_prw = r;
+    }
+    if (t < w) {
+      const int prw = r;
+      // the published rows lag the update of column j - 1 in their columns > j
+      Ffc pv = ld_cluster_ffc(map_rank(&pub[par].cand[t], (unsigned)q));
+      if (j > 0 && t > j) pv = ffc_fms(pv, ld_cluster_ffc(map_rank(&pub[par].cand[j - 1], (unsigned)q)), pprev[t]);
+      prow[t] = pv;
+      // the pivot's reciprocal once for the CTA, in FP64
+      if (t == j) {
+        const double2 d = ffc_dbl(pv);
+        s_inv = (d.x == 0.0 && d.y == 0.0) ? fzero : ffc_of(crecip(d));
+      }
+      if (prw != gj) {
+        Ffc dv = ld_cluster_ffc(map_rank(&pub[par].diag[t], owner_gj));
+        if (j > 0 && t > j) dv = ffc_fms(dv, ld_cluster_ffc(map_rank(&pub[par].diag[j - 1], owner_gj)), pprev[t]);
+        dgr[t] = dv;
+      }
+    }
+    __syncthreads();
+    const int prw = s_prw;
+    if (rank == 0 && t == 0) ipiv[gj] = prw + 1;
+    const Ffc piv = prow[j];
+    const bool zero = piv.re.h == 0.f && piv.im.h == 0.f;
+    if (zero && rank == 0 && t == 0) atomicCAS(&gb->info, 0, gj + 1);
+    // this thread's row: interchange, scale, then column j + 1 only
+    lr_l = fzero;
+    if (t < cnt) {
+      const int gr = base + t;
+      if (prw != gj) {
+        if (gr == prw)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = dgr[c];
+        else if (gr == gj)
+          for (int c = 0; c < w; ++c) tile[(size_t)c * rpc + t] = prow[c];
+      }
+      if (gr > gj) {
+        Ffc l = tile[(size_t)j * rpc + t];
+        if (!zero) {
+          l = ffc_mul(l, s_inv);
+          tile[(size_t)j * rpc + t] = l;
+        }
+        lr_l = l;
+        if (j + 1 < w) tile[(size_t)(j + 1) * rpc + t] = ffc_fms(tile[(size_t)(j + 1) * rpc + t], l, prow[j + 1]);
+      }
+    }
+    if (j + 1 < w) {
+      __syncthreads();  // column j + 1 of every row is current
+      publish(j + 1);
+      // the rest of this thread's row while the cluster meets
+      if (t < cnt && base + t > gj)
+        for (int c = j + 2; c < w; ++c) tile[(size_t)c * rpc + t] = ffc_fms(tile[(size_t)c * rpc + t], lr_l, prow[c]);
+    }
+  }
+  // no CTA leaves while another may still read its shared memory
+  cluster_sync_all();
+  if (t < cnt)
+    for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + base + t] = ffc_dbl(tile[(size_t)c * rpc + t]);
 }
 
 // ------------------------------------------- conjugate-transpose trsv ----
@@ -1978,6 +2186,18 @@ struct PanelLaunch {
   size_t smem = 0;
 };
 
+__global__ void panel_cluster_la_ff_kernel(double2* __restrict__ A, long long lda, int n, int j0, int w, int rpc,
+                                           int* __restrict__ ipiv, GridBarrier* __restrict__ gb,
+                                           long long astride);
+
+// The second tier's panels in float-float arithmetic (panel_cluster_la_ff_kernel);
+// WMOM_FF_PANEL=0 keeps them in FP64 (read at every panel, so that a test can
+// compare both in one process).
+bool ff_panels() {
+  const char* e = std::getenv("WMOM_FF_PANEL");
+  return !(e && e[0] == '0');
+}
+
 // Largest cluster size this device schedules for panel_cluster_kernel (8 is the
 // portable limit; 16 where the device allows it), probed once per device.
 int max_cluster_size(const DeviceLimits& lim) {
@@ -1998,7 +2218,7 @@ int max_cluster_size(const DeviceLimits& lim) {
       prepare((const void*)panel_cluster_kernel<double2, 1>) &&
       prepare((const void*)panel_cluster_la_kernel<float2, 1>) &&
       prepare((const void*)panel_cluster_la_kernel<float2, 2>) &&
-      prepare((const void*)panel_cluster_la_kernel<double2, 1>)) {
+      prepare((const void*)panel_cluster_la_kernel<double2, 1>) && prepare((const void*)panel_cluster_la_ff_kernel)) {
     for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs, 1, 1);
@@ -2158,6 +2378,13 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
+        if constexpr (std::is_same<C, double2>::value) {
+          if (la && pl.rpt == 1 && gemm_hook != nullptr && ff_panels()) {
+            ce = allow_dynamic_smem((const void*)panel_cluster_la_ff_kernel, pl.smem);
+            if (ce != cudaSuccess) return ce;
+            return cudaLaunchKernelEx(&cfg, panel_cluster_la_ff_kernel, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
+          }
+        }
         if (la)
           return pl.rpt == 2 ? cudaLaunchKernelEx(&cfg, panel_cluster_la_kernel<C, 2>, A, lda, n, jp, w, pl.rpc, ipiv,
                                                   gb, astride)

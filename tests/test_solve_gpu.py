@@ -233,19 +233,21 @@ def test_krylov_step_forced_on(cuda, wmom):
 
 
 def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
-    # the second tier's FP64 LU (cluster panels) with and without the panel's
-    # one-column look-ahead: the same currents bit for bit
+    # the second tier's LU with FP64 cluster panels (WMOM_FF_PANEL=0) with and
+    # without the panel's one-column look-ahead: the same currents bit for bit
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
     freqs = np.array([0.01], np.float32)
     out = {}
     for la in ("1", "0"):
         os.environ["WMOM_PANEL_LOOKAHEAD"] = la
+        os.environ["WMOM_FF_PANEL"] = "0"
         try:
             plan = wmom.Plan(topo)
             out[la] = plan.solve(freqs, 1000, mode=1)
             plan.close()
         finally:
             del os.environ["WMOM_PANEL_LOOKAHEAD"]
+            del os.environ["WMOM_FF_PANEL"]
     assert out["1"][2][0]["tier"] == 2
     assert np.array_equal(out["1"][0], out["0"][0])
 
@@ -312,3 +314,28 @@ def test_second_tier_prediction(cuda, wmom):
     # the lowest frequencies sit in groups after a fully fallen-back one
     assert predicted >= 2, [(r["tier"], r["iterations"]) for r in r1]
     assert st1["tc_gemm"]["launches"] < st0["tc_gemm"]["launches"]
+
+
+def test_float_float_second_tier_panels(cuda, wmom):
+    """The second tier's panels in float-float arithmetic (the default) against the
+    FP64 panels: on the ill-conditioned junction grid both refine to solutions within
+    8 kappa_1 eps of the plain FP64 solve, with the same tiers."""
+    w = wmom
+    topo = w.Topology(w.geometry.precision_grid(2048))
+    freqs = np.array([0.003, 0.03, 0.3], np.float32)
+    plan = w.Plan(topo)
+    out = {}
+    try:
+        for ff in ("1", "0"):
+            os.environ["WMOM_FF_PANEL"] = ff
+            out[ff] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True)
+    finally:
+        os.environ.pop("WMOM_FF_PANEL", None)
+    c64, _, _ = plan.solve(freqs, 1000, mode=w.MODE_FP64)
+    plan.close()
+    for ff in ("1", "0"):
+        cur, _, rep = out[ff]
+        for k in range(len(freqs)):
+            assert rep[k]["status"] == 0 and rep[k]["tier"] == 2, (ff, k, rep[k])
+            bound = max(1e-9, 8 * rep[k]["cond1"] * 2.0 ** -53)
+            assert _rel(cur[k], c64[k]) <= bound, (ff, float(freqs[k]), rep[k])
