@@ -1655,7 +1655,9 @@ __global__ void merge_ff_kernel(double2* a, size_t count) {
 // the second tier's factorisation error (about 2^-45).  The pivot of a column is the
 // row with the largest |re| + |im| of the heads (within 2^-24 of the FP64 choice; on
 // a near tie either row is a valid partial pivot); its reciprocal is computed once
-// per CTA in FP64.
+// per CTA in FP64.  FFS: the matrix itself holds float-float values (float4 hi.re,
+// hi.im, lo.re, lo.im per entry, LuWorkspace::ff_storage), read and written as they
+// are; else complex128, converted on the way in and out.
 struct ClusterPubFf {
   float val;
   int row;
@@ -1676,6 +1678,7 @@ __device__ __forceinline__ Ffc ld_cluster_ffc(uint32_t a) {
 
 __device__ __forceinline__ float ffc_abs1(const Ffc& a) { return fabsf(a.re.h) + fabsf(a.im.h); }
 
+template <bool FFS>
 __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_ff_kernel(double2* __restrict__ A,
                                                                                  long long lda, int n, int j0,
                                                                                  int w, int rpc,
@@ -1711,7 +1714,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_ff_kernel
         if (c0 + u < w) v[u] = A[(size_t)(j0 + c0 + u) * lda + gr];
 #pragma unroll
       for (int u = 0; u < 16; ++u)
-        if (c0 + u < w) tile[(size_t)(c0 + u) * rpc + t] = ffc_of(v[u]);
+        if (c0 + u < w) {
+          if constexpr (FFS) {
+            const float4 f = *reinterpret_cast<const float4*>(&v[u]);
+            tile[(size_t)(c0 + u) * rpc + t] = Ffc{Ff{f.x, f.z}, Ff{f.y, f.w}};
+          } else {
+            tile[(size_t)(c0 + u) * rpc + t] = ffc_of(v[u]);
+          }
+        }
     }
   }
   __syncthreads();
@@ -1850,7 +1860,61 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_ff_kernel
   // no CTA leaves while another may still read its shared memory
   cluster_sync_all();
   if (t < cnt)
-    for (int c = 0; c < w; ++c) A[(size_t)(j0 + c) * lda + base + t] = ffc_dbl(tile[(size_t)c * rpc + t]);
+    for (int c = 0; c < w; ++c) {
+      const Ffc v = tile[(size_t)c * rpc + t];
+      double2* dst = &A[(size_t)(j0 + c) * lda + base + t];
+      if constexpr (FFS)
+        *reinterpret_cast<float4*>(dst) = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+      else
+        *dst = ffc_dbl(v);
+    }
+}
+
+template __global__ void panel_cluster_la_ff_kernel<false>(double2*, long long, int, int, int, int, int*,
+                                                           GridBarrier*, long long);
+template __global__ void panel_cluster_la_ff_kernel<true>(double2*, long long, int, int, int, int, int*,
+                                                          GridBarrier*, long long);
+
+// Unit-lower block solve of the second tier with float-float storage, B <- L^-1 B for
+// an nb x nb unit lower L (nb <= 32): trsm_kernel's structure (L and 16 columns of B
+// in shared memory, the block's elements updated in parallel, one barrier per row of
+// the triangle, each element's updates in increasing k) in float-float arithmetic.
+// A float-float update is a long dependent chain of FP32 operations, so the work of a
+// row step is spread over the block's threads; one column per thread of one warp,
+// tried first, left every chain's latency exposed (227 us per 24-column solve).
+__global__ void __launch_bounds__(256) trsm_lower_ff_kernel(const float4* __restrict__ T, long long ldt,
+                                                            float4* __restrict__ B, long long ldb, int nb,
+                                                            int ncols, long long tstride, long long bstride) {
+  extern __shared__ __align__(16) unsigned char trsm_ff_smem[];
+  T += (size_t)blockIdx.y * tstride;
+  B += (size_t)blockIdx.y * bstride;
+  Ffc* Ts = reinterpret_cast<Ffc*>(trsm_ff_smem);  // nb x nb, column-major
+  Ffc* Bs = Ts + (size_t)nb * nb;                   // nb x kTrsmCols, column-major
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * kTrsmCols;
+  const int nc = min(kTrsmCols, ncols - c0);
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int c = idx / nb, r = idx - c * nb;
+    Ts[idx] = ffc_ld(T, (size_t)c * ldt + r);
+  }
+  for (int idx = tid; idx < nb * nc; idx += blockDim.x) {
+    const int c = idx / nb, r = idx - c * nb;
+    Bs[idx] = ffc_ld(B, (size_t)(c0 + c) * ldb + r);
+  }
+  __syncthreads();
+  const int total = nb * nc;
+  for (int k = 0; k < nb - 1; ++k) {
+    for (int idx = tid; idx < total; idx += blockDim.x) {
+      const int c = idx / nb, r = idx - c * nb;
+      if (r > k) Bs[c * nb + r] = ffc_fms(Bs[c * nb + r], Ts[(size_t)k * nb + r], Bs[c * nb + k]);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < total; idx += blockDim.x) {
+    const int c = idx / nb, r = idx - c * nb;
+    const Ffc v = Bs[idx];
+    B[(size_t)(c0 + c) * ldb + r] = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+  }
 }
 
 // ------------------------------------------- conjugate-transpose trsv ----
@@ -2186,6 +2250,7 @@ struct PanelLaunch {
   size_t smem = 0;
 };
 
+template <bool FFS>
 __global__ void panel_cluster_la_ff_kernel(double2* __restrict__ A, long long lda, int n, int j0, int w, int rpc,
                                            int* __restrict__ ipiv, GridBarrier* __restrict__ gb,
                                            long long astride);
@@ -2218,7 +2283,8 @@ int max_cluster_size(const DeviceLimits& lim) {
       prepare((const void*)panel_cluster_kernel<double2, 1>) &&
       prepare((const void*)panel_cluster_la_kernel<float2, 1>) &&
       prepare((const void*)panel_cluster_la_kernel<float2, 2>) &&
-      prepare((const void*)panel_cluster_la_kernel<double2, 1>) && prepare((const void*)panel_cluster_la_ff_kernel)) {
+      prepare((const void*)panel_cluster_la_kernel<double2, 1>) &&
+      prepare((const void*)panel_cluster_la_ff_kernel<false>) && prepare((const void*)panel_cluster_la_ff_kernel<true>)) {
     for (int cs = kClusterMax; cs >= 1 && !best; cs /= 2) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs, 1, 1);
@@ -2355,6 +2421,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     const int m = n - jp;
     const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w, ws->panel_w64);
     const int P = pl.P;
+    if (ws->ff_storage && !pl.cluster) return cudaErrorInvalidValue;  // see ff_tier2_supported
     {
       if (pl.cluster) {
         if (w > pl.w) return cudaErrorInvalidValue;
@@ -2379,10 +2446,19 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
         cfg.numAttrs = 1;
         stats::Scope sc(stats::kPanel, s, 8.0 * m * (double)w * w / 2.0 * batch);
         if constexpr (std::is_same<C, double2>::value) {
-          if (la && pl.rpt == 1 && gemm_hook != nullptr && ff_panels()) {
-            ce = allow_dynamic_smem((const void*)panel_cluster_la_ff_kernel, pl.smem);
+          if (ws->ff_storage) {
+            // float-float storage is only set up for these panels (ff_tier2_supported)
+            if (!(la && pl.rpt == 1 && gemm_hook != nullptr)) return cudaErrorInvalidValue;
+            ce = allow_dynamic_smem((const void*)panel_cluster_la_ff_kernel<true>, pl.smem);
             if (ce != cudaSuccess) return ce;
-            return cudaLaunchKernelEx(&cfg, panel_cluster_la_ff_kernel, A, lda, n, jp, w, pl.rpc, ipiv, gb, astride);
+            return cudaLaunchKernelEx(&cfg, panel_cluster_la_ff_kernel<true>, A, lda, n, jp, w, pl.rpc, ipiv, gb,
+                                      astride);
+          }
+          if (la && pl.rpt == 1 && gemm_hook != nullptr && ff_panels()) {
+            ce = allow_dynamic_smem((const void*)panel_cluster_la_ff_kernel<false>, pl.smem);
+            if (ce != cudaSuccess) return ce;
+            return cudaLaunchKernelEx(&cfg, panel_cluster_la_ff_kernel<false>, A, lda, n, jp, w, pl.rpc, ipiv, gb,
+                                      astride);
           }
         }
         if (la)
@@ -2442,6 +2518,16 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       trsm_lower_cols_kernel<C><<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads,
                                   tsmem, s>>>(T, lda, Bb, lda, w, nc, astride, astride);
     } else {
+      if (ws->ff_storage) {
+        // float-float storage (the second tier): the warp-per-32-columns kernel in
+        // float-float arithmetic, for every width up to 32
+        if (w > 32) return cudaErrorInvalidValue;
+        const size_t fsmem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(Ffc);
+        stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
+        trsm_lower_ff_kernel<<<dim3((nc + kTrsmCols - 1) / kTrsmCols, batch), 256, fsmem, s>>>(
+            reinterpret_cast<const float4*>(T), lda, reinterpret_cast<float4*>(Bb), lda, w, nc, astride, astride);
+        return cudaGetLastError();
+      }
       // FP64: the work is bound by the SMs' FP64 pipes.  Panels of 8 .. 32 columns
       // (the second tier's) take the one-warp, column-in-registers kernel when their
       // columns give every SM at least two warps; narrower right-hand sides (the
@@ -2747,6 +2833,17 @@ int lu_max_batch(int n, bool fp64_cluster) {
   std::lock_guard<std::mutex> lk(mu);
   cache[key] = best;
   return best;
+}
+
+// Whether the second tier's LU of order n can hold its matrix in float-float form:
+// every panel must be a one-row-per-thread look-ahead cluster panel (the panels that
+// read and write that form), i.e. cluster panels on, look-ahead on, and the tallest
+// panel (n rows) within one cluster.
+bool ff_tier2_supported(int n, int panel_w64) {
+  if (cluster_panels_disabled() || !panel_lookahead()) return false;
+  const DeviceLimits lim = device_limits();
+  const PanelLaunch pl = panel_launch<double2>(n, lim, true, 0, panel_w64);
+  return pl.cluster && pl.rpt == 1;
 }
 
 template int lu_max_batch<double2>(int, bool);

@@ -145,6 +145,26 @@ __device__ __forceinline__ double f32_scaled(float x, int k) {
   return __hiloint2double((int)(mag ? hi : sign), (int)(mag ? (u << 29) : 0u));
 }
 
+// 2^k x for a float x that is zero or normal, by an integer add to its exponent field;
+// ok when the result is zero or a normal float as well.
+__device__ __forceinline__ bool f32_scale_ok(float x, int k) {
+  const int e = (int)((__float_as_uint(x) >> 23) & 255u);
+  return x == 0.f || (e > 0 && e + k >= 1 && e + k <= 254);
+}
+__device__ __forceinline__ float f32_scale(float x, int k) {
+  return x == 0.f ? x : __uint_as_float(__float_as_uint(x) + ((unsigned)k << 23));
+}
+
+// c - (s + e) for a float-float c = (ch, cl) and the unnormalised float pair (s, e):
+// one error-free sum of the heads and the tails added, about 2^-48 relative
+__device__ __forceinline__ void ff_sub_pair(float& ch, float& cl, float s, float e) {
+  float h, t;
+  two_sum(ch, -s, h, t);
+  t = __fadd_rn(t, __fsub_rn(cl, e));
+  ch = __fadd_rn(h, t);
+  cl = __fsub_rn(t, __fsub_rn(ch, h));
+}
+
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<const uint32_t*>(&v);
@@ -155,6 +175,19 @@ __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
 // zero beyond 2K) and the row exponents ea.  A block of 4 warps covers 32 rows:
 // lane = row (coalesced column reads), warp = a quarter of the K2p/2 complex
 // columns; the quarters' row maxima meet in shared memory.
+// An entry of an operand held as complex128, or (FFS) as float-float (float4: hi.re,
+// hi.im, lo.re, lo.im in the same 16 bytes; hi + lo is exact in FP64).
+template <bool FFS>
+__device__ __forceinline__ double2 ld_operand(const double2* p) {
+  if constexpr (FFS) {
+    const float4 f = *reinterpret_cast<const float4*>(p);
+    return make_double2((double)f.x + (double)f.z, (double)f.y + (double)f.w);
+  } else {
+    return *p;
+  }
+}
+
+template <bool FFS>
 __global__ void __launch_bounds__(128) emul_pack_a_kernel(const double2* __restrict__ A, long long lda, int M, int K,
                                                          int K2p, __nv_bfloat16* __restrict__ planes,
                                                          size_t plane_elems, int* __restrict__ ea,
@@ -169,7 +202,7 @@ __global__ void __launch_bounds__(128) emul_pack_a_kernel(const double2* __restr
   double mx = 0.0;
   if (m < M)
     for (int k = k0; k < min(K, k0 + kq); ++k) {
-      const double2 v = A[(size_t)k * lda + m];
+      const double2 v = ld_operand<FFS>(&A[(size_t)k * lda + m]);
       mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
     }
   smax[part][lane] = mx;
@@ -186,7 +219,7 @@ __global__ void __launch_bounds__(128) emul_pack_a_kernel(const double2* __restr
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       double2 v = make_double2(0.0, 0.0);
-      if (kc + u < K) v = A[(size_t)(kc + u) * lda + m];
+      if (kc + u < K) v = ld_operand<FFS>(&A[(size_t)(kc + u) * lda + m]);
       digit_planes(v.x, sc48, pr[u]);
       digit_planes(v.y, sc48, pi[u]);
     }
@@ -204,6 +237,7 @@ __global__ void __launch_bounds__(128) emul_pack_a_kernel(const double2* __restr
 
 // B (K x N complex, column-major) -> NS planes of B'^T (row-major 2N x K2p bf16)
 // and the column exponents eb.  One warp per column (lanes along K).
+template <bool FFS>
 __global__ void emul_pack_b_kernel(const double2* __restrict__ B, long long ldb, int K, int N, int K2p,
                                    __nv_bfloat16* __restrict__ planes, size_t plane_elems,
                                    int* __restrict__ eb, long long bstride) {
@@ -214,7 +248,7 @@ __global__ void emul_pack_b_kernel(const double2* __restrict__ B, long long ldb,
   B += (size_t)b * bstride + (size_t)n * ldb;
   double mx = 0.0;
   for (int k = lane; k < K; k += 32) {
-    const double2 v = B[k];
+    const double2 v = ld_operand<FFS>(&B[k]);
     mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
   }
 #pragma unroll
@@ -227,7 +261,7 @@ __global__ void emul_pack_b_kernel(const double2* __restrict__ B, long long ldb,
   __nv_bfloat16* r1 = r0 + K2p;
   for (int k = lane; k < K2p / 2; k += 32) {
     double2 v = make_double2(0.0, 0.0);
-    if (k < K) v = B[k];
+    if (k < K) v = ld_operand<FFS>(&B[k]);
     float pr[NS], pi[NS];
     digit_planes(v.x, sc48, pr);
     digit_planes(v.y, sc48, pi);
@@ -252,6 +286,10 @@ __device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n)
   return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
 }
 
+// FFS: C holds float-float values (float4 hi.re, hi.im, lo.re, lo.im per entry), which
+// the epilogue updates in float-float arithmetic on the FP32 pipe; else complex128,
+// updated with two FP64 additions per real entry.
+template <bool FFS>
 __global__ void __launch_bounds__(NTHREADS, 1)
     zgemm_sub_emul_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                           const int* __restrict__ ea, const int* __restrict__ eb, double2* __restrict__ C,
@@ -438,6 +476,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               // and integer work)
               const int k = erow + ebm[n];
               double2 v = cv[cc * 8 + j];
+              if constexpr (FFS) {
+                const float s0 = sp[2 * j], e0 = ep[2 * j], s1 = sp[2 * j + 1], e1 = ep[2 * j + 1];
+                float4 f = *reinterpret_cast<const float4*>(&v);  // hi.re, hi.im, lo.re, lo.im
+                if (f32_scale_ok(s0, k) && f32_scale_ok(e0, k) && f32_scale_ok(s1, k) && f32_scale_ok(e1, k)) {
+                  ff_sub_pair(f.x, f.z, f32_scale(s0, k), f32_scale(e0, k));
+                  ff_sub_pair(f.y, f.w, f32_scale(s1, k), f32_scale(e1, k));
+                } else {
+                  // out of FP32's exponent range after scaling: through FP64
+                  const double sc = pow2(k);
+                  const double re = ((double)f.x + (double)f.z - (double)s0 * sc) - (double)e0 * sc;
+                  const double im = ((double)f.y + (double)f.w - (double)s1 * sc) - (double)e1 * sc;
+                  const float rh = __double2float_rn(re), ih = __double2float_rn(im);
+                  f = make_float4(rh, ih, __double2float_rn(re - (double)rh), __double2float_rn(im - (double)ih));
+                }
+                *reinterpret_cast<float4*>(&Cm[(size_t)n * ldc + row]) = f;
+                continue;
+              }
               if (k >= -900 && k <= 900) {
                 v.x = __dsub_rn(__dsub_rn(v.x, f32_scaled(sp[2 * j], k)), f32_scaled(ep[2 * j], k));
                 v.y = __dsub_rn(__dsub_rn(v.y, f32_scaled(sp[2 * j + 1], k)), f32_scaled(ep[2 * j + 1], k));
@@ -515,12 +570,19 @@ cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, con
   int* ea = reinterpret_cast<int*>(pb + NS * b_pl);
   int* eb = ea + (size_t)M * batch;
   stats::count(stats::kMisc, 2);
-  emul_pack_a_kernel<<<dim3((M + 31) / 32, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
-  emul_pack_b_kernel<<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
+  const bool ffs = ws->ff_storage;
+  if (ffs) {
+    emul_pack_a_kernel<true><<<dim3((M + 31) / 32, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
+    emul_pack_b_kernel<true><<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
+  } else {
+    emul_pack_a_kernel<false><<<dim3((M + 31) / 32, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
+    emul_pack_b_kernel<false><<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
+  }
   CUtensorMap ma, mb;
   if (!make_map(&ma, pa, M, K2p, batch, BM) || !make_map(&mb, pb, 2 * N, K2p, batch, BN))
     return cudaErrorInvalidValue;
-  e = allow_dynamic_smem((const void*)zgemm_sub_emul_kernel, SMEM_BYTES);
+  const void* kern = ffs ? (const void*)zgemm_sub_emul_kernel<true> : (const void*)zgemm_sub_emul_kernel<false>;
+  e = allow_dynamic_smem(kern, SMEM_BYTES);
   if (e != cudaSuccess) return e;
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
   const long long ntiles = (long long)tiles_m * tiles_n * batch;
@@ -534,8 +596,12 @@ cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, con
   }
   const int grid = (int)std::min<long long>(ntiles, nsm);
   stats::Scope sc(stats::kEmulGemm, s, 8.0 * M * (double)N * K * batch);
-  zgemm_sub_emul_kernel<<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m, tiles_n,
-                                                           (int)ntiles, ws->tc_err, bstride);
+  if (ffs)
+    zgemm_sub_emul_kernel<true><<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m,
+                                                                   tiles_n, (int)ntiles, ws->tc_err, bstride);
+  else
+    zgemm_sub_emul_kernel<false><<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m,
+                                                                    tiles_n, (int)ntiles, ws->tc_err, bstride);
   return cudaGetLastError();
 }
 

@@ -53,6 +53,10 @@ struct LuWorkspace {
   int panel_w = 0;
   // widest FP64 cluster panel of the precision form's second tier (0 = 32)
   int panel_w64 = 0;
+  // the matrix being factored holds float-float values (float4: hi.re, hi.im,
+  // lo.re, lo.im in place of each complex128; the second tier's storage): panels,
+  // block solves and the digit-plane updates read and write that form
+  bool ff_storage = false;
 };
 
 size_t lu_workspace_bytes(int elem_bytes);  // one matrix: barrier + staging
@@ -96,6 +100,9 @@ cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B
 // refinement.
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
                         cudaStream_t s, int batch = 1, long long astride = 0, const int* sel = nullptr);
+// Whether the second tier's LU of order n (FP64 cluster panels of at most panel_w64
+// columns) can keep its matrix in float-float form (LuWorkspace::ff_storage).
+bool ff_tier2_supported(int n, int panel_w64);
 // `count` complex128 values to float-float in place (hi = fp32(v), lo = fp32(v - hi)),
 // and back (exact).
 cudaError_t split_ff_inplace(double2* a, size_t count, cudaStream_t s);

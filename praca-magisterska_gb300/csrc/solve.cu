@@ -741,7 +741,7 @@ namespace {
 // In-place FP64 LU of the bg matrices in lu64 (n*n apart) whose trailing updates
 // run through `hook` (the digit-plane tensor-core GEMM): the second tier's factors.
 wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws, cudaStream_t s, int* info,
-                        GemmHook<double2> hook) {
+                        GemmHook<double2> hook, bool ff) {
   SWEEP_TRY(lu_workspace_reset_barrier(ws, s));
   // Shape: span panels per tensor-core update, of at most w columns, K = span w <= 96
   // (the most one launch of the digit-plane GEMM takes).  Measured per 12-frequency
@@ -756,9 +756,11 @@ wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws
   const int es = env_int("WMOM_EMUL_SPAN", 1, kMaxSpan);
   const int saved_w64 = ws->panel_w64;
   ws->panel_w64 = large ? 24 : 32;
+  ws->ff_storage = ff;  // lu64 holds float-float values (split_ff_inplace) when set
   const cudaError_t fe =
       lu_factor_t<double2>(lu64, n, n, ipiv, ws, s, hook, bg, (long long)n * n, es ? es : (large ? 4 : 3));
   ws->panel_w64 = saved_w64;
+  ws->ff_storage = false;
   if (fe != cudaSuccess) return wmom_fail_cuda(fe, "lu_factor_t (tier 2)");
   int err = lu_workspace_read_status(ws, info, s, bg);
   err |= tc::read_and_clear_error(ws, s);
@@ -1059,13 +1061,25 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         SWEEP_TRY(cudaMemcpyAsync(flu + (size_t)j * nn, Z64 + (size_t)fb[c0 + j] * nn, sizeof(double2) * nn,
                                   cudaMemcpyDeviceToDevice, s));
       int inf[kMaxLuBatch] = {};
-      const wmom_status fst = factor_emul(n, flu, cn, fpiv, ws, s, inf, emul);
+      // With WMOM_FF_TIER2=1 the second tier factors in float-float form where its
+      // panels allow (ff_tier2_supported): the matrices are split in place first, and
+      // panels, block solves and the digit-plane updates' C work on that form on the
+      // FP32 pipe.  Measured per step (N = 8192 grid / 256-frequency N = 2048 grid):
+      // 888 / 896 ms against 869 / 904 ms with complex128 storage and float-float
+      // panels, the default.  The panels and block solves gain 21 ms, but the
+      // digit-plane packs then convert every entry back to FP64 (+43 ms), and the
+      // update's epilogue does not speed up (its bound is the tcgen05 instruction
+      // path).  By default the factors are split after the factorisation.  Either way
+      // the solves below run in compensated FP32 (lu_solve_ff: about 2^-48 per
+      // operation, below the factors' own error), with every right-hand side scaled
+      // by a power of two to a norm near 1, inside FP32's range.  The condition
+      // estimate merges them back to FP64 first.
+      const char* ffe = std::getenv("WMOM_FF_TIER2");
+      const bool ff = ffe && ffe[0] == '1' && ff_tier2_supported(n, n > 4096 ? 24 : 32);
+      if (ff) SWEEP_TRY(split_ff_inplace(flu, nn * cn, s));
+      const wmom_status fst = factor_emul(n, flu, cn, fpiv, ws, s, inf, emul, ff);
       if (fst != WMOM_OK) return fst;
-      // The solves run in compensated FP32 on these factors split to float-float in
-      // place (lu_solve_ff: about 2^-48 per operation, below the factors' own error),
-      // with every right-hand side scaled by a power of two to a norm near 1, inside
-      // FP32's range.  The condition estimate merges them back to FP64 first.
-      SWEEP_TRY(split_ff_inplace(flu, nn * cn, s));
+      if (!ff) SWEEP_TRY(split_ff_inplace(flu, nn * cn, s));
       const float4* fff = reinterpret_cast<const float4*>(flu);
       double* dscale = g.scal.as<double>();
       auto scale_slots = [&](double2* v, const double* norm, int cnt) -> wmom_status {

@@ -233,14 +233,16 @@ def test_krylov_step_forced_on(cuda, wmom):
 
 
 def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
-    # the second tier's LU with FP64 cluster panels (WMOM_FF_PANEL=0) with and
-    # without the panel's one-column look-ahead: the same currents bit for bit
+    # the second tier's LU with complex128 storage and FP64 cluster panels
+    # (WMOM_FF_TIER2=0, WMOM_FF_PANEL=0) with and without the panel's one-column
+    # look-ahead: the same currents bit for bit
     topo = wmom.Topology(wmom.geometry.precision_grid(2048))
     freqs = np.array([0.01], np.float32)
     out = {}
     for la in ("1", "0"):
         os.environ["WMOM_PANEL_LOOKAHEAD"] = la
         os.environ["WMOM_FF_PANEL"] = "0"
+        os.environ["WMOM_FF_TIER2"] = "0"
         try:
             plan = wmom.Plan(topo)
             out[la] = plan.solve(freqs, 1000, mode=1)
@@ -248,6 +250,7 @@ def test_fp64_cluster_panel_lookahead_is_bit_identical(cuda, wmom):
         finally:
             del os.environ["WMOM_PANEL_LOOKAHEAD"]
             del os.environ["WMOM_FF_PANEL"]
+            del os.environ["WMOM_FF_TIER2"]
     assert out["1"][2][0]["tier"] == 2
     assert np.array_equal(out["1"][0], out["0"][0])
 
@@ -316,24 +319,30 @@ def test_second_tier_prediction(cuda, wmom):
     assert st1["tc_gemm"]["launches"] < st0["tc_gemm"]["launches"]
 
 
-def test_float_float_second_tier_panels(cuda, wmom):
-    """The second tier's panels in float-float arithmetic (the default) against the
-    FP64 panels: on the ill-conditioned junction grid both refine to solutions within
-    8 kappa_1 eps of the plain FP64 solve, with the same tiers."""
+def test_float_float_second_tier(cuda, wmom):
+    """The second tier's LU with complex128 storage and float-float panels (the
+    default), with its matrix in float-float form (WMOM_FF_TIER2=1: panels, block
+    solves and the digit-plane updates on the FP32 pipe), and with FP64 panels
+    (WMOM_FF_PANEL=0): on the ill-conditioned junction grid each refines to solutions
+    within 8 kappa_1 eps of the plain FP64 solve, all in tier 2."""
     w = wmom
     topo = w.Topology(w.geometry.precision_grid(2048))
     freqs = np.array([0.003, 0.03, 0.3], np.float32)
     plan = w.Plan(topo)
     out = {}
+    cases = {"ff_panels": {}, "ff": {"WMOM_FF_TIER2": "1"}, "fp64": {"WMOM_FF_TIER2": "0", "WMOM_FF_PANEL": "0"}}
     try:
-        for ff in ("1", "0"):
-            os.environ["WMOM_FF_PANEL"] = ff
-            out[ff] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True)
+        for name, env in cases.items():
+            for k in ("WMOM_FF_TIER2", "WMOM_FF_PANEL"):
+                os.environ.pop(k, None)
+            os.environ.update(env)
+            out[name] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True)
     finally:
-        os.environ.pop("WMOM_FF_PANEL", None)
+        for k in ("WMOM_FF_TIER2", "WMOM_FF_PANEL"):
+            os.environ.pop(k, None)
     c64, _, _ = plan.solve(freqs, 1000, mode=w.MODE_FP64)
     plan.close()
-    for ff in ("1", "0"):
+    for ff in cases:
         cur, _, rep = out[ff]
         for k in range(len(freqs)):
             assert rep[k]["status"] == 0 and rep[k]["tier"] == 2, (ff, k, rep[k])
