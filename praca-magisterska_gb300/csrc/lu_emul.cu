@@ -19,24 +19,26 @@
 //   * the product of planes i and j has weight 2^(-8(i+j)) ("level" i + j); the
 //     levels 0, 1 and 2 each go to their own TMEM accumulator, where their sums
 //     are exact in FP32 as long as 2K <= 192 (|level-2 sum| <= 192 (2*256*128 +
-//     128^2) 2^-16 < 2^24 2^-16); levels 3..NS-1 share a fourth accumulator,
-//     whose FP32 rounding is below 2^-48 of the leading term;
-//   * the epilogue adds the four accumulators error-free in FP32 (a float pair),
-//     scales the pair by 2^(ea + eb - 16) with integer operations on the exponent
-//     and subtracts it from C with two FP64 additions.
+//     128^2) 2^-16 < 2^24 2^-16); levels 3..NS-1 go to further accumulators (one
+//     shared, or one each, by tile shape), whose FP32 rounding is below 2^-48 of
+//     the leading term;
+//   * the epilogue adds the levels beyond 2 in FP32 and then levels 2, 1 and 0
+//     error-free (a float pair), scales the pair by 2^(ea + eb - 16) with integer
+//     operations on the exponent and subtracts it from C with two FP64 additions.
 // Dropped levels (i + j >= NS) and the digit remainder are about 2^-45 of
 // K * max|A| * max|B|, so the factorisation this update serves is FP64-grade
 // (backward error near FP64 LU's); the FP64 refinement checks every solution.
 //
-// Kernel: persistent, one CTA (10 warps) per SM, 128 x 64 real output tiles
-// (32 complex columns).  A producer thread streams K in chunks of 32 bf16 (one
-// 64-byte swizzle row) of all 2 x NS planes with 4-D TMA into a 3-stage ring; an
-// MMA thread issues the 21 plane products (2 K-steps each) of a chunk into the four
-// accumulators of one of two accumulator sets (2 x 4 x 64 columns fill TMEM);
-// eight epilogue warps (two per TMEM lane quarter) prefetch their 16 entries of C
-// while the tile is multiplied, then read the accumulators with tcgen05.ld and
-// update C while the next tile is multiplied.  Every wait is bounded; on timeout
-// the kernel records an error, skips the rest and still frees its TMEM.
+// Kernel: persistent, one CTA (10 warps) per SM, 128 x BN real output tiles
+// (BN / 2 complex columns; BN = 64 or 32).  A producer thread streams K in chunks of
+// 32 bf16 (one 64-byte swizzle row) of all 2 x NS planes with 4-D TMA into a 3-stage
+// ring; an MMA thread issues the 21 plane products (2 K-steps each) of a chunk into
+// the NLEV accumulators of one of two accumulator sets, products of consecutive
+// levels merged into one wide MMA (EmulShape); eight epilogue warps (two per TMEM
+// lane quarter) prefetch their entries of C while the tile is multiplied, then read
+// the accumulators with tcgen05.ld and update C while the next tile is multiplied.
+// Every wait is bounded; on timeout the kernel records an error, skips the rest and
+// still frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -58,34 +60,57 @@ namespace emul {
 using namespace tc;
 
 constexpr int BM = 128;                             // accumulator lanes = rows of C per tile
-constexpr int BN = 64;                              // real columns = 32 complex columns of C
 constexpr int KC = 32;                              // bf16 of K per chunk (64 bytes)
 constexpr int NS = 6;                               // digit planes per operand
-constexpr int NLEV = 4;                             // accumulators: levels 0, 1, 2, then 3..NS-1
 constexpr int NBUF = 2;                             // accumulator sets (tile i's epilogue || i+1's MMAs)
 constexpr int STAGES = 3;
 constexpr int A_TILE = BM * KC * 2;                 // one plane's tile of A' (8 KB)
-constexpr int B_TILE = BN * KC * 2;                 // one plane's tile of B'^T (4 KB)
-constexpr int STAGE_BYTES = NS * (A_TILE + B_TILE);  // 72 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
 constexpr int EPI_WARPS = 8;                        // two per TMEM lane quarter, one column half each
 constexpr int NTHREADS = 64 + 32 * EPI_WARPS;       // producer warp, MMA warp, epilogue warps
-constexpr int TMEM_COLS = NBUF * NLEV * BN;         // 512: all of TMEM
 constexpr int kMaxK = 96;                           // complex K per launch (2K <= 192)
 
 static_assert(NS * (NS + 1) / 2 == 21, "plane products per chunk");
-static_assert(TMEM_COLS == 512, "accumulators fill TMEM");
 
-// Instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// Tile shape: BN real columns of C per tile and NLEV accumulators per tile (levels
+// 0 .. NLEV-2 each in its own, levels NLEV-1 .. NS-1 sharing the last).  The NLEV
+// accumulators of one set lie side by side in TMEM (level L at column L * BN), and the
+// NS planes of B'^T side by side in shared memory (plane j at row j * BN), so that
+// the products of A plane i with B planes 0 .. NLEV-1-i, whose levels i .. NLEV-1
+// are consecutive accumulators, are ONE MMA of N = (NLEV - i) * BN; only products
+// whose level lies beyond the last accumulator are issued one plane at a time.
+//   64 x 4: 15 MMAs per K step (N = 256, 192, 128, 64 and eleven of 64) instead of the
+//           21 plane products; two sets fill TMEM.
+//   32 x 6: every level in its own accumulator, 6 MMAs per K step (N = 192 .. 32)
+//           for a tile half as wide; A is streamed twice as often per output.
+template <int BN_, int NLEV_>
+struct EmulShape {
+  static constexpr int BN = BN_;
+  static constexpr int NLEV = NLEV_;
+  static constexpr int B_TILE = BN * KC * 2;                    // one plane's tile of B'^T
+  static constexpr int STAGE_BYTES = NS * (A_TILE + B_TILE);
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 128;
+  static constexpr int TMEM_USED = NBUF * NLEV * BN;
+  static constexpr int TMEM_COLS = TMEM_USED <= 256 ? 256 : 512;  // a power of two
+  static_assert(BN % 32 == 0 && NLEV * BN <= 256 && TMEM_USED <= 512, "tile shape");
+  static_assert(NLEV >= 4 && NLEV <= NS, "levels 0, 1, 2 stay exact in their own accumulators");
+  static_assert(STAGE_BYTES % 1024 == 0 && B_TILE % 512 == 0, "swizzle atoms stay aligned");
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+};
+using ShapeWide = EmulShape<64, 4>;
+using ShapeNarrow = EmulShape<32, 6>;
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+// Instruction descriptor: D = F32, A = B = BF16, both K-major, M = BM, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -278,18 +303,18 @@ struct TileCoord {
   int mat, m0, j0;
 };
 
-__device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n) {
+__device__ __forceinline__ TileCoord tile_coord(int t, int tiles_m, int tiles_n, int bn) {
   const int per_mat = tiles_m * tiles_n;
   const int mat = t / per_mat;
   const int r = t - mat * per_mat;
   const int tn = r / tiles_m;
-  return TileCoord{mat, (r - tn * tiles_m) * BM, tn * BN};
+  return TileCoord{mat, (r - tn * tiles_m) * BM, tn * bn};
 }
 
 // FFS: C holds float-float values (float4 hi.re, hi.im, lo.re, lo.im per entry), which
 // the epilogue updates in float-float arithmetic on the FP32 pipe; else complex128,
-// updated with two FP64 additions per real entry.
-template <bool FFS>
+// updated with two FP64 additions per real entry.  SH: the tile shape (EmulShape).
+template <bool FFS, class SH>
 __global__ void __launch_bounds__(NTHREADS, 1)
     zgemm_sub_emul_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                           const int* __restrict__ ea, const int* __restrict__ eb, double2* __restrict__ C,
@@ -298,6 +323,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  constexpr int BN = SH::BN, NLEV = SH::NLEV, B_TILE = SH::B_TILE, STAGE_BYTES = SH::STAGE_BYTES;
+  constexpr int TMEM_COLS = SH::TMEM_COLS;
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
   // bars: full[STAGES], empty[STAGES], tfull[NBUF], tempty[NBUF]
   __shared__ uint32_t tmem_base;
@@ -338,7 +365,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int it = 0;
       bool ok = !s_fail;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+        const TileCoord tc = tile_coord(t, tiles_m, tiles_n, BN);
         for (int c = 0; c < nchunks; ++c) {
           const int s = it % STAGES, use = it / STAGES;
           if (use > 0 && !(ok = role_wait(empty_bar(s), (use - 1) & 1, err, &s_fail))) break;
@@ -379,18 +406,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t a0 = smem_u32(base + s * STAGE_BYTES);
           const uint32_t b0 = a0 + NS * A_TILE;
 #pragma unroll
-          for (int L = 0; L < NS; ++L) {
-            const uint32_t acc = accb + (uint32_t)(min(L, NLEV - 1) * BN);
+          for (int kk = 0; kk < KC / 16; ++kk) {
+            const uint64_t bd0 = sdesc_sw<64>(b0 + kk * 32);  // B planes 0, 1, ... side by side
 #pragma unroll
-            for (int i = 0; i <= L; ++i) {
-              const int j = L - i;
+            for (int i = 0; i < NS; ++i) {
+              const uint64_t ad = sdesc_sw<64>(a0 + i * A_TILE + kk * 32);
+              // B planes 0 .. NLEV-1-i: levels i .. NLEV-1, consecutive accumulators,
+              // one MMA; the tile's first one (i = 0, all NLEV accumulators) overwrites
+              if (i < NLEV)
+                mma_bf16(accb + (uint32_t)(i * BN), ad, bd0, idesc_bf16((NLEV - i) * BN),
+                         (c == 0 && kk == 0 && i == 0) ? 0u : 1u);
+              // B planes whose level lies beyond the last accumulator: into it, one each
 #pragma unroll
-              for (int kk = 0; kk < KC / 16; ++kk) {
-                // the first product into accumulators 0..NLEV-1 of a tile overwrites
-                const uint32_t accum = (c == 0 && i == 0 && kk == 0 && L < NLEV) ? 0u : 1u;
-                mma_bf16(acc, sdesc_sw<64>(a0 + i * A_TILE + kk * 32), sdesc_sw<64>(b0 + j * B_TILE + kk * 32),
-                         accum);
-              }
+              for (int j = (i < NLEV ? NLEV - i : 0); j <= NS - 1 - i; ++j)
+                mma_bf16(accb + (uint32_t)((NLEV - 1) * BN), ad, sdesc_sw<64>(b0 + j * B_TILE + kk * 32),
+                         idesc_bf16(BN), 1u);
             }
           }
           mma_commit(empty_bar(s));
@@ -412,21 +442,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else {
     // ----------------------------------------------------------- epilogue
     // warp w >= 2: TMEM lanes 32 (w % 4) .. +31 (the quarter it may read), complex
-    // columns h*16 .. h*16+15 of the tile
+    // columns h*CW .. h*CW+CW-1 of the tile (CW = BN / 4)
+    constexpr int CW = BN / 4;
     const int q = warp & 3, h = (warp - 2) >> 2;
     int tl = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
-      const TileCoord tc = tile_coord(t, tiles_m, tiles_n);
+      const TileCoord tc = tile_coord(t, tiles_m, tiles_n, BN);
       double2* Cm = C + (size_t)tc.mat * cstride;
       const int* ebm = eb + (size_t)tc.mat * N;
       const int row = tc.m0 + q * 32 + lane;
       const bool row_ok = row < M;
       const int erow = row_ok ? ea[(size_t)tc.mat * M + row] - 16 : 0;
-      const int n0 = (tc.j0 >> 1) + h * 16;
-      // this thread's 16 entries of C, in flight while the tile is multiplied
-      double2 cv[16];
+      const int n0 = (tc.j0 >> 1) + h * CW;
+      // this thread's CW entries of C, in flight while the tile is multiplied
+      double2 cv[CW];
 #pragma unroll
-      for (int j = 0; j < 16; ++j)
+      for (int j = 0; j < CW; ++j)
         cv[j] = (row_ok && n0 + j < N) ? Cm[(size_t)(n0 + j) * ldc + row] : make_double2(0.0, 0.0);
       const int b = tl % NBUF, use = tl / NBUF;
       int ok = 0;
@@ -440,19 +471,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NLEV * BN + h * 32);
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NLEV * BN + h * (BN / 2));
 #pragma unroll
-      for (int cc = 0; cc < 2; ++cc) {
-        // the four levels of 16 real entries (8 complex) summed error-free into float
-        // pairs (s, e), highest level first, one accumulator read at a time
+      for (int cc = 0; cc < BN / 32; ++cc) {
+        // the levels of 16 real entries (8 complex) summed into float pairs (s, e),
+        // highest level first, one accumulator read at a time: the accumulators beyond
+        // level 2 (2^-24 and less of the leading term) in plain FP32, then levels 2, 1
+        // and 0 error-free
         float sp[16], ep[16];
         {
-          uint32_t r3[16], r2[16];
-          tmem_ld16(taddr + (uint32_t)(3 * BN + cc * 16), r3);
+          uint32_t rt[16], r2[16];
+          tmem_ld16(taddr + (uint32_t)((NLEV - 1) * BN + cc * 16), rt);
           tmem_ld16(taddr + (uint32_t)(2 * BN + cc * 16), r2);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          float tail[16];
 #pragma unroll
-          for (int x = 0; x < 16; ++x) two_sum(__uint_as_float(r2[x]), __uint_as_float(r3[x]), sp[x], ep[x]);
+          for (int x = 0; x < 16; ++x) tail[x] = __uint_as_float(rt[x]);
+#pragma unroll
+          for (int L = NLEV - 2; L >= 3; --L) {
+            tmem_ld16(taddr + (uint32_t)(L * BN + cc * 16), rt);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int x = 0; x < 16; ++x) tail[x] = __fadd_rn(tail[x], __uint_as_float(rt[x]));
+          }
+#pragma unroll
+          for (int x = 0; x < 16; ++x) two_sum(__uint_as_float(r2[x]), tail[x], sp[x], ep[x]);
         }
 #pragma unroll
         for (int L = 1; L >= 0; --L) {
@@ -542,6 +585,40 @@ bool make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int k2p, int
 std::mutex g_mu;
 std::vector<LuWorkspace> g_ws;
 
+// Tile width of the update: 32 (ShapeNarrow) unless WMOM_EMUL_TILE=64 (ShapeWide).
+// Measured on 8192 x 8192 x 96: 1.04 ms per call narrow, 1.09 ms wide; both shapes
+// keep the tensor pipe near 45% busy, and the narrow tile's shorter epilogue hides
+// better behind its MMAs.  The shape changes only the FP32 rounding of the levels
+// beyond 2, about 2^-48 of the leading term.
+int emul_tile() {
+  const char* v = std::getenv("WMOM_EMUL_TILE");
+  return (v && std::atoi(v) == 64) ? 64 : 32;
+}
+
+template <class SH>
+cudaError_t launch_gemm(bool ffs, const __nv_bfloat16* pa, const __nv_bfloat16* pb, const int* ea, const int* eb,
+                        double2* C, long long ldc, int M, int N, int K2p, int batch, long long bstride, int* err,
+                        int nsm, cudaStream_t s) {
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, pa, M, K2p, batch, BM) || !make_map(&mb, pb, 2 * N, K2p, batch, SH::BN))
+    return cudaErrorInvalidValue;
+  const void* kern =
+      ffs ? (const void*)zgemm_sub_emul_kernel<true, SH> : (const void*)zgemm_sub_emul_kernel<false, SH>;
+  cudaError_t e = allow_dynamic_smem(kern, SH::SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + SH::BN - 1) / SH::BN;
+  const long long ntiles = (long long)tiles_m * tiles_n * batch;
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const int grid = (int)std::min<long long>(ntiles, nsm);
+  if (ffs)
+    zgemm_sub_emul_kernel<true, SH><<<grid, NTHREADS, SH::SMEM_BYTES, s>>>(
+        ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m, tiles_n, (int)ntiles, err, bstride);
+  else
+    zgemm_sub_emul_kernel<false, SH><<<grid, NTHREADS, SH::SMEM_BYTES, s>>>(
+        ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m, tiles_n, (int)ntiles, err, bstride);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, const double2* B, long long ldb,
@@ -578,15 +655,6 @@ cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, con
     emul_pack_a_kernel<false><<<dim3((M + 31) / 32, batch), 128, 0, s>>>(A, lda, M, K, K2p, pa, a_pl, ea, bstride);
     emul_pack_b_kernel<false><<<dim3((N + 7) / 8, batch), 256, 0, s>>>(B, ldb, K, N, K2p, pb, b_pl, eb, bstride);
   }
-  CUtensorMap ma, mb;
-  if (!make_map(&ma, pa, M, K2p, batch, BM) || !make_map(&mb, pb, 2 * N, K2p, batch, BN))
-    return cudaErrorInvalidValue;
-  const void* kern = ffs ? (const void*)zgemm_sub_emul_kernel<true> : (const void*)zgemm_sub_emul_kernel<false>;
-  e = allow_dynamic_smem(kern, SMEM_BYTES);
-  if (e != cudaSuccess) return e;
-  const int tiles_m = (M + BM - 1) / BM, tiles_n = (2 * N + BN - 1) / BN;
-  const long long ntiles = (long long)tiles_m * tiles_n * batch;
-  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
@@ -594,15 +662,10 @@ cudaError_t zgemm_sub_emul(LuWorkspace* ws, const double2* A, long long lda, con
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
   }
-  const int grid = (int)std::min<long long>(ntiles, nsm);
   stats::Scope sc(stats::kEmulGemm, s, 8.0 * M * (double)N * K * batch);
-  if (ffs)
-    zgemm_sub_emul_kernel<true><<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m,
-                                                                   tiles_n, (int)ntiles, ws->tc_err, bstride);
-  else
-    zgemm_sub_emul_kernel<false><<<grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, ea, eb, C, ldc, M, N, K2p / KC, tiles_m,
-                                                                    tiles_n, (int)ntiles, ws->tc_err, bstride);
-  return cudaGetLastError();
+  if (emul_tile() == 32)
+    return launch_gemm<ShapeNarrow>(ffs, pa, pb, ea, eb, C, ldc, M, N, K2p, batch, bstride, ws->tc_err, nsm, s);
+  return launch_gemm<ShapeWide>(ffs, pa, pb, ea, eb, C, ldc, M, N, K2p, batch, bstride, ws->tc_err, nsm, s);
 }
 
 }  // namespace emul
