@@ -1875,15 +1875,28 @@ template __global__ void panel_cluster_la_ff_kernel<false>(double2*, long long, 
 template __global__ void panel_cluster_la_ff_kernel<true>(double2*, long long, int, int, int, int, int*,
                                                           GridBarrier*, long long);
 
-// Unit-lower block solve of the second tier with float-float storage, B <- L^-1 B for
+// Unit-lower block solve of the second tier in float-float arithmetic, B <- L^-1 B for
 // an nb x nb unit lower L (nb <= 32): trsm_kernel's structure (L and 16 columns of B
 // in shared memory, the block's elements updated in parallel, one barrier per row of
-// the triangle, each element's updates in increasing k) in float-float arithmetic.
-// A float-float update is a long dependent chain of FP32 operations, so the work of a
-// row step is spread over the block's threads; one column per thread of one warp,
-// tried first, left every chain's latency exposed (227 us per 24-column solve).
-__global__ void __launch_bounds__(256) trsm_lower_ff_kernel(const float4* __restrict__ T, long long ldt,
-                                                            float4* __restrict__ B, long long ldb, int nb,
+// the triangle, each element's updates in increasing k) on the FP32 pipe.
+// FFS: the factors are held as float-float (float4 hi.re, hi.im, lo.re, lo.im); else
+// as complex128, split into float-float on load and rounded back to FP64 on store.
+// The result carries about 2^-48 relative error per operation, below the second
+// tier's digit-plane updates' 2^-45.  A float-float update is a long dependent chain
+// of FP32 operations, so the work of a row step is spread over the block's threads;
+// one column per thread of one warp, tried first, left every chain's latency exposed
+// (227 us per 24-column solve).
+template <bool FFS>
+__device__ __forceinline__ Ffc ffc_load(const void* p, size_t i) {
+  if constexpr (FFS)
+    return ffc_ld(reinterpret_cast<const float4*>(p), i);
+  else
+    return ffc_of(reinterpret_cast<const double2*>(p)[i]);
+}
+
+template <bool FFS>
+__global__ void __launch_bounds__(256) trsm_lower_ff_kernel(const double2* __restrict__ T, long long ldt,
+                                                            double2* __restrict__ B, long long ldb, int nb,
                                                             int ncols, long long tstride, long long bstride) {
   extern __shared__ __align__(16) unsigned char trsm_ff_smem[];
   T += (size_t)blockIdx.y * tstride;
@@ -1895,11 +1908,12 @@ __global__ void __launch_bounds__(256) trsm_lower_ff_kernel(const float4* __rest
   const int nc = min(kTrsmCols, ncols - c0);
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
     const int c = idx / nb, r = idx - c * nb;
-    Ts[idx] = ffc_ld(T, (size_t)c * ldt + r);
+    // the unit diagonal and the upper part are never read
+    Ts[idx] = r > c ? ffc_load<FFS>(T, (size_t)c * ldt + r) : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
   }
   for (int idx = tid; idx < nb * nc; idx += blockDim.x) {
     const int c = idx / nb, r = idx - c * nb;
-    Bs[idx] = ffc_ld(B, (size_t)(c0 + c) * ldb + r);
+    Bs[idx] = ffc_load<FFS>(B, (size_t)(c0 + c) * ldb + r);
   }
   __syncthreads();
   const int total = nb * nc;
@@ -1913,7 +1927,10 @@ __global__ void __launch_bounds__(256) trsm_lower_ff_kernel(const float4* __rest
   for (int idx = tid; idx < total; idx += blockDim.x) {
     const int c = idx / nb, r = idx - c * nb;
     const Ffc v = Bs[idx];
-    B[(size_t)(c0 + c) * ldb + r] = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+    if constexpr (FFS)
+      reinterpret_cast<float4*>(B)[(size_t)(c0 + c) * ldb + r] = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+    else
+      B[(size_t)(c0 + c) * ldb + r] = ffc_dbl(v);
   }
 }
 
@@ -2263,6 +2280,13 @@ bool ff_panels() {
   return !(e && e[0] == '0');
 }
 
+// With float-float panels, the second tier's block solves in float-float arithmetic as
+// well (trsm_lower_ff_kernel<false>); WMOM_FF_TRSM=0 keeps them in FP64.
+bool ff_trsm() {
+  const char* e = std::getenv("WMOM_FF_TRSM");
+  return ff_panels() && !(e && e[0] == '0');
+}
+
 // Largest cluster size this device schedules for panel_cluster_kernel (8 is the
 // portable limit; 16 where the device allows it), probed once per device.
 int max_cluster_size(const DeviceLimits& lim) {
@@ -2518,14 +2542,20 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
       trsm_lower_cols_kernel<C><<<dim3((nc + kTrsmColThreads - 1) / kTrsmColThreads, batch), kTrsmColThreads,
                                   tsmem, s>>>(T, lda, Bb, lda, w, nc, astride, astride);
     } else {
-      if (ws->ff_storage) {
-        // float-float storage (the second tier): the warp-per-32-columns kernel in
-        // float-float arithmetic, for every width up to 32
+      if (ws->ff_storage || (gemm_hook != nullptr && w <= 32 && ff_trsm())) {
+        // the second tier: float-float arithmetic on the FP32 pipe, on float-float
+        // storage or on complex128 (split on load, rounded back on store), for every
+        // width up to 32.  Against the FP64 kernels below: N = 8192 grid, 9 second-tier
+        // matrices, 51 ms per step in FP64; 256-frequency N = 2048 grid 145 ms.
         if (w > 32) return cudaErrorInvalidValue;
         const size_t fsmem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(Ffc);
         stats::Scope sc(stats::kTrsm, s, 4.0 * w * (double)w * nc * batch);
-        trsm_lower_ff_kernel<<<dim3((nc + kTrsmCols - 1) / kTrsmCols, batch), 256, fsmem, s>>>(
-            reinterpret_cast<const float4*>(T), lda, reinterpret_cast<float4*>(Bb), lda, w, nc, astride, astride);
+        if (ws->ff_storage)
+          trsm_lower_ff_kernel<true><<<dim3((nc + kTrsmCols - 1) / kTrsmCols, batch), 256, fsmem, s>>>(
+              T, lda, Bb, lda, w, nc, astride, astride);
+        else
+          trsm_lower_ff_kernel<false><<<dim3((nc + kTrsmCols - 1) / kTrsmCols, batch), 256, fsmem, s>>>(
+              T, lda, Bb, lda, w, nc, astride, astride);
         return cudaGetLastError();
       }
       // FP64: the work is bound by the SMs' FP64 pipes.  Panels of 8 .. 32 columns
