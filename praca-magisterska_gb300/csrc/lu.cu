@@ -1853,8 +1853,22 @@ __global__ void __launch_bounds__(kClusterThreads, 1) panel_cluster_la_ff_kernel
       __syncthreads();  // column j + 1 of every row is current
       publish(j + 1);
       // the rest of this thread's row while the cluster meets
-      if (t < cnt && base + t > gj)
-        for (int c = j + 2; c < w; ++c) tile[(size_t)c * rpc + t] = ffc_fms(tile[(size_t)c * rpc + t], lr_l, prow[c]);
+      // (four columns per step, loaded before any is stored: their float-float chains
+      // are independent, so the scheduler interleaves them)
+      if (t < cnt && base + t > gj) {
+        int c = j + 2;
+        for (; c + 3 < w; c += 4) {
+          Ffc a[4], p[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            a[u] = tile[(size_t)(c + u) * rpc + t];
+            p[u] = prow[c + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) tile[(size_t)(c + u) * rpc + t] = ffc_fms(a[u], lr_l, p[u]);
+        }
+        for (; c < w; ++c) tile[(size_t)c * rpc + t] = ffc_fms(tile[(size_t)c * rpc + t], lr_l, prow[c]);
+      }
     }
   }
   // no CTA leaves while another may still read its shared memory
@@ -2383,11 +2397,18 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
     if (sizeof(R) == 4) {
       if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
     } else {
-      static const int target = [] {
+      // rows per CTA: 256 for the FP64 panel (its rank-1 updates want the SMs); the
+      // float-float panel, whose updates run on the FP32 pipe, takes 512 where the
+      // whole panel width fits at that height (fewer CTAs meet at each column's
+      // cluster barrier; N = 8192 grid, 24-column panels: 835 -> 830 ms per step)
+      static const int env_target = [] {
         const char* e = std::getenv("WMOM_FP64_PANEL_ROWS");
         const int v = e ? std::atoi(e) : 0;
-        return v >= 16 && v <= 512 ? v : 256;
+        return v >= 16 && v <= 512 ? v : 0;
       }();
+      const int target = env_target ? env_target
+                         : (ff_panels() && (size_t)kClusterThreads * wcap * sizeof(C) + head <= cap) ? 512
+                                                                                                   : 256;
       int cs0 = 1;
       while (cs0 < kClusterMax && (m + cs0 - 1) / cs0 > target) cs0 *= 2;
       if (try_shape(1, cs0, kClusterMax, 16)) return pl;
