@@ -64,3 +64,28 @@ def test_emul_matches_complex128(cuda, wmom, m, n, k):
     scale = k * amax * bmax
     err = np.abs(out - ref) / scale
     assert np.max(err) < 2.0 ** -40, np.max(err)
+
+
+@pytest.mark.parametrize("tile", ["32", "64"])
+def test_emul_tile_shapes(cuda, wmom, monkeypatch, tile):
+    """Both tile shapes of the update (128 x 32 with one accumulator per level, the
+    default; 128 x 64 with levels 3-5 sharing one) meet the same bound, on ragged
+    edges and several tiles per CTA, and agree with each other to within the FP32
+    rounding of levels 3-5 (2^-45 of the scale)."""
+    monkeypatch.setenv("WMOM_EMUL_TILE", tile)
+    m, n, k = 700, 333, 96
+    rng = np.random.default_rng(7)
+    rs = np.exp2(rng.uniform(-20, 20, (m, 1)))
+    cs = np.exp2(rng.uniform(-20, 20, (1, n)))
+    a = (rng.normal(size=(m, k)) + 1j * rng.normal(size=(m, k))) * rs
+    b = (rng.normal(size=(k, n)) + 1j * rng.normal(size=(k, n))) * cs
+    c = (rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))) * rs * cs
+    out = _emul(wmom, cuda, a, b, c)
+    ref = c - a @ b
+    amax = np.max(np.maximum(np.abs(a.real), np.abs(a.imag)), axis=1, keepdims=True)
+    bmax = np.max(np.maximum(np.abs(b.real), np.abs(b.imag)), axis=0, keepdims=True)
+    scale = k * amax * bmax
+    assert np.max(np.abs(out - ref) / scale) < 2.0 ** -40
+    monkeypatch.setenv("WMOM_EMUL_TILE", "64" if tile == "32" else "32")
+    other = _emul(wmom, cuda, a, b, c)
+    assert np.max(np.abs(out - other) / scale) < 2.0 ** -45

@@ -320,25 +320,29 @@ def test_second_tier_prediction(cuda, wmom):
 
 
 def test_float_float_second_tier(cuda, wmom):
-    """The second tier's LU with complex128 storage and float-float panels (the
-    default), with its matrix in float-float form (WMOM_FF_TIER2=1: panels, block
-    solves and the digit-plane updates on the FP32 pipe), and with FP64 panels
-    (WMOM_FF_PANEL=0): on the ill-conditioned junction grid each refines to solutions
-    within 8 kappa_1 eps of the plain FP64 solve, all in tier 2."""
+    """The second tier's LU with complex128 storage and float-float panels and block
+    solves (the default), with FP64 block solves (WMOM_FF_TRSM=0), with its matrix in
+    float-float form (WMOM_FF_TIER2=1: panels, block solves and the digit-plane
+    updates on the FP32 pipe), with FP64 panels (WMOM_FF_PANEL=0), and with the
+    digit-plane update on 128 x 64 tiles (WMOM_EMUL_TILE=64): on the ill-conditioned
+    junction grid each refines to solutions within 8 kappa_1 eps of the plain FP64
+    solve, all in tier 2."""
     w = wmom
     topo = w.Topology(w.geometry.precision_grid(2048))
     freqs = np.array([0.003, 0.03, 0.3], np.float32)
     plan = w.Plan(topo)
     out = {}
-    cases = {"ff_panels": {}, "ff": {"WMOM_FF_TIER2": "1"}, "fp64": {"WMOM_FF_TIER2": "0", "WMOM_FF_PANEL": "0"}}
+    cases = {"ff_panels": {}, "fp64_trsm": {"WMOM_FF_TRSM": "0"}, "ff": {"WMOM_FF_TIER2": "1"},
+             "fp64": {"WMOM_FF_TIER2": "0", "WMOM_FF_PANEL": "0"}, "wide_tile": {"WMOM_EMUL_TILE": "64"}}
+    keys = ("WMOM_FF_TIER2", "WMOM_FF_PANEL", "WMOM_FF_TRSM", "WMOM_EMUL_TILE")
     try:
         for name, env in cases.items():
-            for k in ("WMOM_FF_TIER2", "WMOM_FF_PANEL"):
+            for k in keys:
                 os.environ.pop(k, None)
             os.environ.update(env)
             out[name] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True)
     finally:
-        for k in ("WMOM_FF_TIER2", "WMOM_FF_PANEL"):
+        for k in keys:
             os.environ.pop(k, None)
     c64, _, _ = plan.solve(freqs, 1000, mode=w.MODE_FP64)
     plan.close()
