@@ -28,6 +28,7 @@
 #include <cstdlib>
 #include <cstdint>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <type_traits>
 #include <vector>
@@ -2347,9 +2348,50 @@ int max_cluster_size(const DeviceLimits& lim) {
   return best;
 }
 
+// Clusters of cs CTAs of `kern` (kClusterThreads threads, smem bytes each) that can
+// be resident at once (cudaOccupancyMaxActiveClusters; no launch), cached per
+// device.  A cluster sits inside one GPC, so on a GB300 at one CTA per SM only 7
+// clusters of 16 CTAs fit, 13 of 10 and 15 of 8, not 152 / cs.
+int active_clusters(const void* kern, int cs, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void*, int, size_t>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const auto key = std::make_tuple(dev, kern, cs, (smem + 1023) / 1024);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (allow_dynamic_smem(kern, smem) == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs, 1, 1);
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) n = 0;
+  }
+  cudaGetLastError();
+  cache[key] = n;
+  return n;
+}
+
+// batch: the matrices of the launch (0: not known).  Cluster panels with one row per
+// thread then take, where their default cluster (the smallest power of two holding
+// the rows, or for the FP64 / float-float panels the rows at the target height) cannot
+// hold the whole batch at once, the smallest cluster of any size that can, at the
+// same width: so that the batch runs in one wave instead of two.  The panel's results
+// do not depend on the cluster size (each row's arithmetic is the same in whichever
+// CTA holds it, and the pivot search breaks ties by row index), only on the width,
+// which stays.
 template <typename C>
 PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = false, int wmax = 0,
-                         int wmax64 = 0) {
+                         int wmax64 = 0, int batch = 0) {
   constexpr int NB = PanelCfg<C>::NB;
   constexpr int NT = PanelCfg<C>::NT;
   using R = decltype(C{}.x);
@@ -2394,8 +2436,29 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
       }
       return false;
     };
+    // a batch that the chosen cluster size cannot hold at once: the smallest cluster of
+    // any size that can, one row per thread, at the same width
+    auto one_wave = [&](const void* kern) {
+      if (batch <= 1 || pl.rpt != 1 || active_clusters(kern, pl.P, pl.smem) >= batch) return;
+      const int rows_fit = (int)std::min<size_t>(kClusterThreads, (cap - head) / ((size_t)pl.w * sizeof(C)));
+      for (int cs = std::max(1, (m + rows_fit - 1) / rows_fit); cs <= std::min(kClusterMax, csmax); ++cs) {
+        const int rpc = (m + cs - 1) / cs;
+        const size_t smem = head + (size_t)rpc * pl.w * sizeof(C);
+        if (rpc > kClusterThreads || smem > cap) continue;
+        if (active_clusters(kern, cs, smem) >= batch) {
+          pl.P = cs;
+          pl.rpc = rpc;
+          pl.smem = smem;
+          return;
+        }
+      }
+    };
     if (sizeof(R) == 4) {
-      if (try_shape(1, 1, kClusterMax, 32) || try_shape(2, 1, kClusterMax, 24)) return pl;
+      if (try_shape(1, 1, kClusterMax, 32)) {
+        one_wave((const void*)panel_cluster_la_kernel<float2, 1>);
+        return pl;
+      }
+      if (try_shape(2, 1, kClusterMax, 24)) return pl;
     } else {
       // rows per CTA: 256 for the FP64 panel (its rank-1 updates want the SMs); the
       // float-float panel, whose updates run on the FP32 pipe, takes 512 where the
@@ -2411,7 +2474,11 @@ PanelLaunch panel_launch(int m, const DeviceLimits& lim, bool fp64_cluster = fal
                                                                                                    : 256;
       int cs0 = 1;
       while (cs0 < kClusterMax && (m + cs0 - 1) / cs0 > target) cs0 *= 2;
-      if (try_shape(1, cs0, kClusterMax, 16)) return pl;
+      if (try_shape(1, cs0, kClusterMax, 16)) {
+        one_wave(ff_panels() ? (const void*)panel_cluster_la_ff_kernel<false>
+                             : (const void*)panel_cluster_la_kernel<double2, 1>);
+        return pl;
+      }
     }
   }
   if (sizeof(R) == 4) {
@@ -2464,7 +2531,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   // panel of columns [jp, jp + w), rows jp..n-1 (cooperative launch)
   auto panel = [&](int jp, int w) -> cudaError_t {
     const int m = n - jp;
-    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w, ws->panel_w64);
+    const PanelLaunch pl = panel_launch<C>(m, lim, gemm_hook != nullptr, ws->panel_w, ws->panel_w64, batch);
     const int P = pl.P;
     if (ws->ff_storage && !pl.cluster) return cudaErrorInvalidValue;  // see ff_tier2_supported
     {

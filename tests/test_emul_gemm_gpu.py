@@ -70,8 +70,9 @@ def test_emul_matches_complex128(cuda, wmom, m, n, k):
 def test_emul_tile_shapes(cuda, wmom, monkeypatch, tile):
     """Both tile shapes of the update (128 x 32 with one accumulator per level, the
     default; 128 x 64 with levels 3-5 sharing one) meet the same bound, on ragged
-    edges and several tiles per CTA, and agree with each other to within the FP32
-    rounding of levels 3-5 (2^-45 of the scale)."""
+    edges and several tiles per CTA.  Each is within about 2^-45 of the scale of the
+    exact product (dropped levels, digit remainder, FP32 rounding of levels 3-5), so
+    the two agree to within twice that (measured 2^-44.1); the test allows 2^-43."""
     monkeypatch.setenv("WMOM_EMUL_TILE", tile)
     m, n, k = 700, 333, 96
     rng = np.random.default_rng(7)
@@ -88,4 +89,4 @@ def test_emul_tile_shapes(cuda, wmom, monkeypatch, tile):
     assert np.max(np.abs(out - ref) / scale) < 2.0 ** -40
     monkeypatch.setenv("WMOM_EMUL_TILE", "64" if tile == "32" else "32")
     other = _emul(wmom, cuda, a, b, c)
-    assert np.max(np.abs(out - other) / scale) < 2.0 ** -45
+    assert np.max(np.abs(out - other) / scale) < 2.0 ** -43
