@@ -1492,11 +1492,16 @@ __device__ __forceinline__ Ffc ffc_ld(const float4* a, size_t i) {
   return Ffc{Ff{v.x, v.z}, Ff{v.y, v.w}};
 }
 
+// inv (optional): the inverses of the factors' kTrsvB x kTrsvB diagonal blocks
+// (ff_block_inverses); the block's solution is then one parallel product with the
+// inverse instead of a kTrsvB-step substitution by one warp, which was the chain's
+// critical path.
 template <bool UPPER>
 __global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__ A, long long lda, int n,
                                                       double2* x, int* flags,
                                                       unsigned int* ticket, int epoch, int* err, long long astride,
-                                                      int flag_stride, const int* __restrict__ sel) {
+                                                      int flag_stride, const int* __restrict__ sel,
+                                                      const float4* __restrict__ inv) {
   __shared__ Ffc xs[kTrsvB];
   __shared__ Ffc part[4][kTrsvB];
   __shared__ Ffc dinv[kTrsvB];  // 1 / u_cc (back substitution)
@@ -1525,12 +1530,16 @@ __global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__
   // its diagonal, in FP64 once per entry, before the waits
   extern __shared__ __align__(16) unsigned char trsv_ff_smem[];
   Ffc* Ds = reinterpret_cast<Ffc*>(trsv_ff_smem);  // kTrsvB x kTrsvB, column-major
+  const float4* Ib = inv ? inv + (((size_t)mat * nblk + b) * 2 + (UPPER ? 1 : 0)) * kTrsvB * kTrsvB : nullptr;
   for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
     const int c = idx / kTrsvB, q = idx - c * kTrsvB;
-    Ds[idx] = (c < rows && q < rows) ? ffc_ld(A, (size_t)(r0 + c) * lda + r0 + q)
-                                     : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+    if (Ib)
+      Ds[idx] = ffc_ld(Ib, idx);
+    else
+      Ds[idx] = (c < rows && q < rows) ? ffc_ld(A, (size_t)(r0 + c) * lda + r0 + q)
+                                       : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
   }
-  if (UPPER && tid < kTrsvB) {
+  if (UPPER && !Ib && tid < kTrsvB) {
     const int c = tid;
     double2 d = make_double2(1.0, 0.0);
     if (c < rows) {
@@ -1586,6 +1595,28 @@ __global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__
   }
   part[g][r] = acc;
   __syncthreads();
+  if (Ib) {
+    // s = x_blk - sum(T x) in xs, then x_blk = Inv s: thread (r, g) sums the columns
+    // g + 4i of row r, the four partial sums meet in part[]
+    if (tid < kTrsvB)
+      xs[tid] = tid < rows ? ffc_add(ffc_add(ffc_of(x[r0 + tid]), ffc_add(part[0][tid], part[1][tid])),
+                                     ffc_add(part[2][tid], part[3][tid]))
+                           : Ffc{Ff{0.f, 0.f}, Ff{0.f, 0.f}};
+    __syncthreads();
+    Ffc y{Ff{0.f, 0.f}, Ff{0.f, 0.f}};  // -sum(Inv s)
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) y = ffc_fms(y, Ds[(size_t)(g + 4 * i) * kTrsvB + r], xs[g + 4 * i]);
+    part[g][r] = y;
+    __syncthreads();
+    if (tid < rows) {
+      const Ffc v = ffc_add(ffc_add(part[0][tid], part[1][tid]), ffc_add(part[2][tid], part[3][tid]));
+      x[r0 + tid] = make_double2(-ff_dbl(v.re), -ff_dbl(v.im));
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_i32(&flags[b], epoch);
+    return;
+  }
   if (tid < 32) {
     // lane l holds rows l and l + 32 of the block; part[] holds -sum(T x) per group
     Ffc s0{Ff{0.f, 0.f}, Ff{0.f, 0.f}}, s1 = s0;
@@ -1627,6 +1658,67 @@ __global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__
   }
   __syncthreads();
   if (tid == 0) st_release_i32(&flags[b], epoch);
+}
+
+// The inverses of the float-float factors' kTrsvB x kTrsvB diagonal blocks, for
+// trsv_ff_kernel: grid (blocks, matrices, 2), z = 0 the unit lower L block, z = 1 the
+// upper U block; inv holds per matrix and block the two inverses, column-major, with
+// an identity beyond the last block's rows.  Thread c computes column c by
+// substitution on e_c in float-float arithmetic (columns of L^-1 by forward, of U^-1
+// by back substitution with the diagonal reciprocals taken in FP64), the block and the
+// columns in shared memory (columns row-major with a padded row, so that the threads'
+// accesses to their own columns are consecutive and the final column-major write
+// reads rows without bank conflicts).
+constexpr int kInvLd = kTrsvB + 1;
+constexpr size_t kTriInvSmem = sizeof(Ffc) * ((size_t)kTrsvB * kTrsvB + (size_t)kTrsvB * kInvLd);
+__global__ void __launch_bounds__(kTrsvB) tri_inv_ff_kernel(const float4* __restrict__ A, long long lda, int n,
+                                                            long long astride, float4* __restrict__ inv) {
+  extern __shared__ __align__(16) unsigned char tri_inv_smem[];
+  Ffc* T = reinterpret_cast<Ffc*>(tri_inv_smem);  // the block, column-major
+  Ffc* Y = T + kTrsvB * kTrsvB;                     // Y[i * kInvLd + c]: row i of column c
+  __shared__ Ffc dinv[kTrsvB];
+  const int b = blockIdx.x, mat = blockIdx.y;
+  const bool upper = blockIdx.z == 1;
+  const int nblk = gridDim.x;
+  const int r0 = b * kTrsvB;
+  const int rows = min(kTrsvB, n - r0);
+  const int c = threadIdx.x;
+  A += (size_t)mat * astride;
+  const Ffc zero{Ff{0.f, 0.f}, Ff{0.f, 0.f}}, one{Ff{1.f, 0.f}, Ff{0.f, 0.f}};
+  for (int k = 0; k < kTrsvB; ++k) {
+    T[(size_t)k * kTrsvB + c] = (k < rows && c < rows) ? ffc_ld(A, (size_t)(r0 + k) * lda + r0 + c) : zero;
+    Y[(size_t)k * kInvLd + c] = k == c ? one : zero;
+  }
+  if (upper) {
+    double2 d = make_double2(1.0, 0.0);
+    if (c < rows) d = ffc_dbl(T[(size_t)c * kTrsvB + c]);
+    dinv[c] = ffc_of(crecip(d));
+  }
+  __syncthreads();
+  if (c < rows) {
+    if (!upper) {
+      for (int k = c; k < rows; ++k) {
+        const Ffc yk = Y[(size_t)k * kInvLd + c];
+        for (int i = k + 1; i < rows; ++i)
+          Y[(size_t)i * kInvLd + c] = ffc_fms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
+      }
+    } else {
+      for (int k = c; k >= 0; --k) {
+        const Ffc yk = ffc_mul(Y[(size_t)k * kInvLd + c], dinv[k]);
+        Y[(size_t)k * kInvLd + c] = yk;
+        for (int i = 0; i < k; ++i)
+          Y[(size_t)i * kInvLd + c] = ffc_fms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
+      }
+    }
+  }
+  __syncthreads();
+  float4* out = inv + (((size_t)mat * nblk + b) * 2 + (upper ? 1 : 0)) * kTrsvB * kTrsvB;
+  for (int idx = c; idx < kTrsvB * kTrsvB; idx += kTrsvB) {
+    // entry (i, j) of the inverse at j * kTrsvB + i (consecutive threads, consecutive i)
+    const int j = idx / kTrsvB, i = idx - j * kTrsvB;
+    const Ffc v = Y[(size_t)i * kInvLd + j];
+    out[idx] = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+  }
 }
 
 // Complex128 entries to float-float in place, (re, im) -> (hi.re, hi.im, lo.re,
@@ -2819,8 +2911,23 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
   return cudaGetLastError();
 }
 
+cudaError_t ff_block_inverses(const float4* A, long long lda, int n, int batch, long long astride, float4* inv,
+                              cudaStream_t s) {
+  if (n <= 0 || batch < 1 || batch > 65535 || !inv) return cudaErrorInvalidValue;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  cudaError_t e = allow_dynamic_smem((const void*)tri_inv_ff_kernel, kTriInvSmem);
+  if (e != cudaSuccess) return e;
+  stats::count(stats::kMisc);
+  tri_inv_ff_kernel<<<dim3(nblk, batch, 2), kTrsvB, kTriInvSmem, s>>>(A, lda, n, astride, inv);
+  return cudaGetLastError();
+}
+
+size_t ff_block_inverse_bytes(int n, int batch) {
+  return (size_t)batch * ((n + kTrsvB - 1) / kTrsvB) * 2 * kTrsvB * kTrsvB * sizeof(float4);
+}
+
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
-                        cudaStream_t s, int batch, long long astride, const int* sel) {
+                        cudaStream_t s, int batch, long long astride, const int* sel, const float4* inv) {
   if (batch < 1 || batch > ws->max_batch || !ws->flags || n > ws->perm_cap) return cudaErrorInvalidValue;
   if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
   if ((size_t)n * batch * sizeof(double2) > ws->rhs_bytes) return cudaErrorInvalidValue;
@@ -2852,10 +2959,10 @@ cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, 
     if (e != cudaSuccess) return e;
     if (pass == 0)
       trsv_ff_kernel<false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                             &ws->barrier->err, astride, ws->flag_cap, sel);
+                                                             &ws->barrier->err, astride, ws->flag_cap, sel, inv);
     else
       trsv_ff_kernel<true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                            &ws->barrier->err, astride, ws->flag_cap, sel);
+                                                            &ws->barrier->err, astride, ws->flag_cap, sel, inv);
   }
   return cudaGetLastError();
 }

@@ -98,8 +98,17 @@ cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B
 // place of each complex128 entry, same layout), in compensated FP32 arithmetic
 // (about 2^-48 relative per operation): the second tier's solves inside its FP64
 // refinement.
+// inv (optional): the inverses of the factors' 64 x 64 diagonal blocks
+// (ff_block_inverses), which turn each block's substitution into one parallel product.
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
-                        cudaStream_t s, int batch = 1, long long astride = 0, const int* sel = nullptr);
+                        cudaStream_t s, int batch = 1, long long astride = 0, const int* sel = nullptr,
+                        const float4* inv = nullptr);
+// The inverses of the 64 x 64 diagonal blocks of the float-float factors (unit lower L
+// and upper U) of `batch` matrices astride apart, into inv (ff_block_inverse_bytes),
+// in float-float arithmetic: for lu_solve_ff.
+cudaError_t ff_block_inverses(const float4* A, long long lda, int n, int batch, long long astride, float4* inv,
+                              cudaStream_t s);
+size_t ff_block_inverse_bytes(int n, int batch);
 // Whether the second tier's LU of order n (FP64 cluster panels of at most panel_w64
 // columns) can keep its matrix in float-float form (LuWorkspace::ff_storage).
 bool ff_tier2_supported(int n, int panel_w64);

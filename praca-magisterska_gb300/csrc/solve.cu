@@ -1081,6 +1081,19 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       if (fst != WMOM_OK) return fst;
       if (!ff) SWEEP_TRY(split_ff_inplace(flu, nn * cn, s));
       const float4* fff = reinterpret_cast<const float4*>(flu);
+      // the inverses of the factors' 64 x 64 diagonal blocks, once per factorisation:
+      // every solve below then takes each block in one parallel product instead of a
+      // 64-step substitution by one warp (WMOM_FF_TRSV_INV=0 keeps the substitution)
+      DevBuf finv;
+      const float4* finvp = nullptr;
+      {
+        const char* ie = std::getenv("WMOM_FF_TRSV_INV");
+        if (!(ie && ie[0] == '0')) {
+          SWEEP_TRY(finv.alloc(ff_block_inverse_bytes(n, cn), s));
+          SWEEP_TRY(ff_block_inverses(fff, n, n, cn, (long long)nn, finv.as<float4>(), s));
+          finvp = finv.as<float4>();
+        }
+      }
       double* dscale = g.scal.as<double>();
       auto scale_slots = [&](double2* v, const double* norm, int cnt) -> wmom_status {
         for (int j = 0; j < kMaxLuBatch; ++j) {
@@ -1109,7 +1122,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         std::vector<double> vn(kMaxLuBatch, g.vnorm);
         wmom_status ss = scale_slots(fx, vn.data(), cn);
         if (ss != WMOM_OK) return ss;
-        SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, fx, ws, s, cn, (long long)nn));
+        SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, fx, ws, s, cn, (long long)nn, nullptr, finvp));
         ss = unscale_slots(fx, cn);
         if (ss != WMOM_OK) return ss;
       }
@@ -1198,7 +1211,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
           wmom_status ss = scale_slots(frr, rn.data(), cn);
           if (ss != WMOM_OK) return ss;
           SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, frr, ws, s, nsa, (long long)nn,
-                                nsa == cn ? nullptr : g.sel.as<int>()));
+                                nsa == cn ? nullptr : g.sel.as<int>(), finvp));
           ss = unscale_slots(frr, cn);
           if (ss != WMOM_OK) return ss;
         }
