@@ -1663,16 +1663,17 @@ __global__ void __launch_bounds__(256) trsv_ff_kernel(const float4* __restrict__
 // The inverses of the float-float factors' kTrsvB x kTrsvB diagonal blocks, for
 // trsv_ff_kernel: grid (blocks, matrices, 2), z = 0 the unit lower L block, z = 1 the
 // upper U block; inv holds per matrix and block the two inverses, column-major, with
-// an identity beyond the last block's rows.  Thread c computes column c by
-// substitution on e_c in float-float arithmetic (columns of L^-1 by forward, of U^-1
-// by back substitution with the diagonal reciprocals taken in FP64), the block and the
-// columns in shared memory (columns row-major with a padded row, so that the threads'
-// accesses to their own columns are consecutive and the final column-major write
-// reads rows without bank conflicts).
+// an identity beyond the last block's rows.  Four threads of one warp compute column c
+// by substitution on e_c in float-float arithmetic, each on every fourth row (columns
+// of L^-1 by forward, of U^-1 by back substitution with the diagonal reciprocals
+// taken in FP64), the block and the columns in shared memory (columns row-major with
+// a padded row, so that the final column-major write reads rows without bank
+// conflicts).  With one thread per column, the first columns' chains (2016 updates
+// for column 0) made it 220 us per CTA.
 constexpr int kInvLd = kTrsvB + 1;
 constexpr size_t kTriInvSmem = sizeof(Ffc) * ((size_t)kTrsvB * kTrsvB + (size_t)kTrsvB * kInvLd);
-__global__ void __launch_bounds__(kTrsvB) tri_inv_ff_kernel(const float4* __restrict__ A, long long lda, int n,
-                                                            long long astride, float4* __restrict__ inv) {
+__global__ void __launch_bounds__(4 * kTrsvB) tri_inv_ff_kernel(const float4* __restrict__ A, long long lda, int n,
+                                                                long long astride, float4* __restrict__ inv) {
   extern __shared__ __align__(16) unsigned char tri_inv_smem[];
   Ffc* T = reinterpret_cast<Ffc*>(tri_inv_smem);  // the block, column-major
   Ffc* Y = T + kTrsvB * kTrsvB;                     // Y[i * kInvLd + c]: row i of column c
@@ -1682,38 +1683,49 @@ __global__ void __launch_bounds__(kTrsvB) tri_inv_ff_kernel(const float4* __rest
   const int nblk = gridDim.x;
   const int r0 = b * kTrsvB;
   const int rows = min(kTrsvB, n - r0);
-  const int c = threadIdx.x;
+  const int tid = threadIdx.x;
+  // column c of the inverse by the four threads (c, q) of one warp, rows q + 4 i each
+  const int c = tid >> 2, q = tid & 3;
   A += (size_t)mat * astride;
   const Ffc zero{Ff{0.f, 0.f}, Ff{0.f, 0.f}}, one{Ff{1.f, 0.f}, Ff{0.f, 0.f}};
-  for (int k = 0; k < kTrsvB; ++k) {
-    T[(size_t)k * kTrsvB + c] = (k < rows && c < rows) ? ffc_ld(A, (size_t)(r0 + k) * lda + r0 + c) : zero;
-    Y[(size_t)k * kInvLd + c] = k == c ? one : zero;
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int j = idx / kTrsvB, i = idx - j * kTrsvB;
+    T[idx] = (i < rows && j < rows) ? ffc_ld(A, (size_t)(r0 + j) * lda + r0 + i) : zero;
+    Y[(size_t)i * kInvLd + j] = i == j ? one : zero;
   }
-  if (upper) {
+  if (upper && tid < kTrsvB) {
     double2 d = make_double2(1.0, 0.0);
-    if (c < rows) d = ffc_dbl(T[(size_t)c * kTrsvB + c]);
-    dinv[c] = ffc_of(crecip(d));
+    if (tid < rows) d = ffc_dbl(ffc_ld(A, (size_t)(r0 + tid) * lda + r0 + tid));
+    dinv[tid] = ffc_of(crecip(d));
   }
   __syncthreads();
-  if (c < rows) {
-    if (!upper) {
-      for (int k = c; k < rows; ++k) {
+  if (!upper) {
+    // forward substitution on e_c: row k is final after step k - 1
+    for (int k = 0; k + 1 < rows; ++k) {
+      __syncwarp();
+      if (c <= k && c < rows) {
         const Ffc yk = Y[(size_t)k * kInvLd + c];
-        for (int i = k + 1; i < rows; ++i)
-          Y[(size_t)i * kInvLd + c] = ffc_fms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
+        for (int i = q; i < rows; i += 4)
+          if (i > k) Y[(size_t)i * kInvLd + c] = ffc_fms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
       }
-    } else {
-      for (int k = c; k >= 0; --k) {
-        const Ffc yk = ffc_mul(Y[(size_t)k * kInvLd + c], dinv[k]);
-        Y[(size_t)k * kInvLd + c] = yk;
-        for (int i = 0; i < k; ++i)
+    }
+  } else {
+    // back substitution on e_c: row k is scaled by 1 / u_kk, then taken off the rows above
+    for (int k = rows - 1; k >= 0; --k) {
+      __syncwarp();
+      Ffc yk = zero;
+      if (c >= k && c < rows) yk = ffc_mul(Y[(size_t)k * kInvLd + c], dinv[k]);
+      __syncwarp();  // every thread of the column has read row k before its owner writes it
+      if (c >= k && c < rows) {
+        if ((k & 3) == q) Y[(size_t)k * kInvLd + c] = yk;
+        for (int i = q; i < k; i += 4)
           Y[(size_t)i * kInvLd + c] = ffc_fms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
       }
     }
   }
   __syncthreads();
   float4* out = inv + (((size_t)mat * nblk + b) * 2 + (upper ? 1 : 0)) * kTrsvB * kTrsvB;
-  for (int idx = c; idx < kTrsvB * kTrsvB; idx += kTrsvB) {
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
     // entry (i, j) of the inverse at j * kTrsvB + i (consecutive threads, consecutive i)
     const int j = idx / kTrsvB, i = idx - j * kTrsvB;
     const Ffc v = Y[(size_t)i * kInvLd + j];
@@ -2918,7 +2930,7 @@ cudaError_t ff_block_inverses(const float4* A, long long lda, int n, int batch, 
   cudaError_t e = allow_dynamic_smem((const void*)tri_inv_ff_kernel, kTriInvSmem);
   if (e != cudaSuccess) return e;
   stats::count(stats::kMisc);
-  tri_inv_ff_kernel<<<dim3(nblk, batch, 2), kTrsvB, kTriInvSmem, s>>>(A, lda, n, astride, inv);
+  tri_inv_ff_kernel<<<dim3(nblk, batch, 2), 4 * kTrsvB, kTriInvSmem, s>>>(A, lda, n, astride, inv);
   return cudaGetLastError();
 }
 
