@@ -799,6 +799,35 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     for (size_t q = 0; q < slots.size(); ++q) rep[mats[q]].cond1 = hs.anorm[mats[q]] * est[q];
     return WMOM_OK;
   };
+  // Componentwise backward errors max_i |r_i| / (|Z||x| + |V|)_i (LAPACK zgerfs'
+  // measure, |z| = |re| + |im|) of the solutions in vector slots slot[q] of x and r,
+  // matrix mat[q] of Zb, read back into hs.berr[slot[q]].  A refined solution whose
+  // backward error is at most 4 sqrt(n) eps (eps = 2^-53) is as good as an FP64 LU's:
+  // it solves a system within that relative distance of Z, entry by entry.
+  const double eps64 = 0x1p-53;
+  const double berr_ok = 4.0 * std::sqrt((double)n) * eps64;
+  auto backward_errors = [&](const double2* Zb, const double2* x, const double2* r, const int* slot, const int* mat,
+                             int cnt) -> wmom_status {
+    if (cnt == 0) return WMOM_OK;
+    const int nch = (n + kGemvChunk - 1) / kGemvChunk;
+    double* part = reinterpret_cast<double*>(g.part.p);
+    for (int q = 0; q < cnt; ++q) {
+      stats::count(stats::kMisc, 2);
+      absgemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nch), kGemvRows, 0, s>>>(
+          Zb + (size_t)mat[q] * nn, n, x + (size_t)slot[q] * n, n, part);
+      berr_finish_kernel<<<1, 1024, 0, s>>>(r + (size_t)slot[q] * n, g.vrep.as<double2>(), part, nch, n,
+                                            &dsc->berr[slot[q]]);
+      SWEEP_TRY(cudaGetLastError());
+    }
+    SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
+    SWEEP_TRY(cudaStreamSynchronize(s));
+    return WMOM_OK;
+  };
+  // WMOM_TRACE_REFINE=1: one line per refinement step and matrix on stderr
+  const char* trace_env = std::getenv("WMOM_TRACE_REFINE");
+  const bool trace = trace_env && trace_env[0] == '1';
+  const char* t1_env = std::getenv("WMOM_T1_BERR");
+  const bool t1_berr = !(t1_env && t1_env[0] == '0');
   if (mode == WMOM_MODE_FP64) {
     SWEEP_TRY(cudaMemcpyAsync(g.x64.p, g.vrep.p, sizeof(double2) * n * bg, cudaMemcpyDeviceToDevice, s));
     SWEEP_TRY(lu_solve_t<double2>(lu64, n, n, ipiv, g.x64.as<double2>(), n, 1, ws, s, bg, (long long)nn));
@@ -858,7 +887,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         SWEEP_TRY(cudaMemcpyAsync(&hs, dscr, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
         SWEEP_TRY(cudaStreamSynchronize(s));
       }
-      int nact = 0;
+      int nact = 0, nleave = 0, leave[kMaxLuBatch];
       for (int b = 0; b < bg; ++b) {
         if (!active[b]) continue;
         const double rel = std::sqrt(hs.rnorm2[b]) / g.vnorm;
@@ -868,28 +897,45 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         if (rel < rel_best[b]) rel_best[b] = rel;
         // converged: the target is met, or the last correction no longer changes the
         // solution at FP64 resolution (systems whose FP64 residual floor lies above
-        // the target); stalled or diverged: FP64 fallback
+        // the target); diverged: FP64 fallback; stalled, out of steps or converging
+        // too slowly: FP64 fallback unless the solution is already backward stable
         const double corr = it > 0 ? std::sqrt(hs.dnorm2[b] / hs.xnorm2[b]) : HUGE_VAL;
+        if (trace)
+          std::fprintf(stderr, "wmom refine: tier 1 matrix %d step %d rel %.3e corr %.3e\n", b, it, rel, corr);
         if (!(rel == rel)) {
           fallback[b] = true;
           active[b] = false;
         } else if (rel <= tol || corr <= 0x1p-48) {
           active[b] = false;
-        } else if (rel > 0.5 * prev[b] && ++stall[b] >= 2) {
-          fallback[b] = true;
+        } else if ((rel > 0.5 * prev[b] && ++stall[b] >= 2) || it >= max_it ||
+                   (tier2 && it >= 3 && rel < last[b] &&
+                    std::log(tol / rel) / std::log(rel / last[b]) > step_budget)) {
           active[b] = false;
-        } else if (it >= max_it) {
-          fallback[b] = true;
-          active[b] = false;
-        } else if (tier2 && it >= 3 && rel < last[b] &&
-                   std::log(tol / rel) / std::log(rel / last[b]) > step_budget) {
-          fallback[b] = true;
-          active[b] = false;
+          leave[nleave++] = b;
         } else {
           if (rel <= 0.5 * prev[b]) stall[b] = 0;
           prev[b] = std::min(prev[b], rel);
           last[b] = rel;
           ++nact;
+        }
+      }
+      // A matrix whose refinement stopped at the FP64 residual floor of its system
+      // (above tol when kappa is large) keeps its tier-1 solution if that solution is
+      // backward stable at FP64 level, the test the second tier accepts by; the FP64-
+      // grade factorisation would only reach the same floor.
+      // (WMOM_T1_BERR=0 turns this off: every such matrix then falls back.)
+      if (!t1_berr)
+        for (int q = 0; q < nleave; ++q) fallback[leave[q]] = true;
+      if (nleave > 0 && t1_berr) {
+        const wmom_status bs =
+            backward_errors(Z64, g.x64.as<double2>(), g.r64.as<double2>(), leave, leave, nleave);
+        if (bs != WMOM_OK) return bs;
+        for (int q = 0; q < nleave; ++q) {
+          const int b = leave[q];
+          fallback[b] = !(hs.berr[b] <= berr_ok);
+          if (trace)
+            std::fprintf(stderr, "wmom refine: tier 1 matrix %d leaves at step %d, backward error %.3e -> %s\n", b,
+                         it, hs.berr[b], fallback[b] ? "fallback" : "accepted");
         }
       }
       if (nact == 0) break;
@@ -1048,7 +1094,6 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   double2* fx = g.fb_x.as<double2>();
   double2* frr = g.fb_r.as<double2>();
   int* fpiv = g.fb_ipiv.as<int>();
-  const double eps64 = 0x1p-53;
   for (int c0 = 0; c0 < nfb; c0 += g.fb_cap) {
     const int cn = std::min(g.fb_cap, nfb - c0);
     bool plain[kMaxLuBatch];
@@ -1153,8 +1198,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         SWEEP_TRY(sumsq_fp64(fx, n, dsc->xnorm2, cn, s));
         SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
         SWEEP_TRY(cudaStreamSynchronize(s));
-        int nact = 0;
-        bool stalled[kMaxLuBatch] = {};
+        int nact = 0, ncheck = 0, cslot[kMaxLuBatch], cmat[kMaxLuBatch];
+        bool stalled[kMaxLuBatch] = {}, check[kMaxLuBatch] = {};
         for (int j = 0; j < cn; ++j) {
           if (!act[j]) continue;
           const int b = fb[c0 + j];
@@ -1162,6 +1207,8 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
           const double rel = std::sqrt(hs.rnorm2[j]) / g.vnorm;
           const double corr = it > 0 && xn > 0 ? std::sqrt(hs.dnorm2[j]) / xn : HUGE_VAL;
           rep[b].iterations += it > 0 ? 1 : 0;
+          if (trace)
+            std::fprintf(stderr, "wmom refine: tier 2 matrix %d step %d rel %.3e corr %.3e\n", b, it, rel, corr);
           if (!(rel == rel)) {
             act[j] = false;
           } else if (rel <= tol || corr <= 0x1p-48) {
@@ -1171,30 +1218,38 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
             act[j] = false;
             stalled[j] = true;
           } else {
+            // a step that did not halve the residual: the solution may already sit at
+            // the FP64 residual floor, where further steps only move it by rounding
+            check[j] = rel > 0.5 * prev2[j];
             if (rel <= 0.5 * prev2[j]) stall2[j] = 0;
             prev2[j] = std::min(prev2[j], rel);
             ++nact;
           }
+          if (stalled[j] || check[j]) {
+            cslot[ncheck] = j;
+            cmat[ncheck++] = b;
+          }
         }
-        // stalled: accepted at FP64 level of the componentwise backward error
-        bool any_stalled = false;
-        for (int j = 0; j < cn; ++j) {
-          if (!stalled[j]) continue;
-          any_stalled = true;
-          const int nch = (n + kGemvChunk - 1) / kGemvChunk;
-          double* part = reinterpret_cast<double*>(g.part.p);
-          stats::count(stats::kMisc, 2);
-          absgemv_partial_kernel<<<dim3((n + kGemvRows - 1) / kGemvRows, nch), kGemvRows, 0, s>>>(
-              Z64 + (size_t)fb[c0 + j] * nn, n, fx + (size_t)j * n, n, part);
-          berr_finish_kernel<<<1, 1024, 0, s>>>(frr + (size_t)j * n, g.vrep.as<double2>(), part, nch, n,
-                                                &dsc->berr[j]);
-          SWEEP_TRY(cudaGetLastError());
-        }
-        if (any_stalled) {
-          SWEEP_TRY(cudaMemcpyAsync(&hs, dsc, sizeof(GroupScalars), cudaMemcpyDeviceToHost, s));
-          SWEEP_TRY(cudaStreamSynchronize(s));
-          for (int j = 0; j < cn; ++j)
-            if (stalled[j] && hs.berr[j] <= 4.0 * std::sqrt((double)n) * eps64) plain[j] = false;
+        // stalled or at the floor: accepted at FP64 level of the componentwise
+        // backward error (a stalled matrix that fails it goes to tier 3; one at a
+        // non-halving step that fails it keeps refining)
+        if (ncheck > 0) {
+          const wmom_status bs = backward_errors(Z64, fx, frr, cslot, cmat, ncheck);
+          if (bs != WMOM_OK) return bs;
+          for (int q = 0; q < ncheck; ++q) {
+            const int j = cslot[q];
+            const bool ok = hs.berr[j] <= berr_ok;
+            if (trace)
+              std::fprintf(stderr, "wmom refine: tier 2 matrix %d %s at step %d, backward error %.3e -> %s\n",
+                           cmat[q], stalled[j] ? "stalls" : "did not halve", it, hs.berr[j],
+                           ok ? "accepted" : (stalled[j] ? "tier 3" : "continues"));
+            if (!ok) continue;
+            plain[j] = false;
+            if (check[j]) {
+              act[j] = false;
+              --nact;
+            }
+          }
         }
         if (nact == 0) break;
         // d = LU^-1 r for the chunk's active matrices; x += d where active
