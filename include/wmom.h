@@ -100,6 +100,12 @@ int wmom_plan_fill_variant(wmom_plan plan);
  * evaluates per frequency (each with a 2-point rule), 0 for the per-entry kernel.
  * Divided by npls^2 it is the pairs per entry; the reference evaluates 4. */
 long long wmom_plan_fill_pairs(wmom_plan plan);
+/* Independent closed current paths of the plan's structure: the cycle rank of the
+ * graph of its segments and nodes, with every node on a PEC ground plane taken as one
+ * (a current returns through the plane); -1 for a null plan.  Structures with loops
+ * are the ones whose conditioning grows as 1/(ka)^2 towards low frequencies (the
+ * precision form's second-tier prediction keys on it).  No reference counterpart. */
+int wmom_plan_loops(wmom_plan plan);
 
 /* Fills nk impedance matrices, one per wave number ka[i] (host array), in FP64.
  * Matrix i starts at z_dev + i*zstride complex elements; ldz >= npls.  The

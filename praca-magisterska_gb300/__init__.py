@@ -86,6 +86,7 @@ _plan_npls = _sig("wmom_plan_npls", ctypes.c_int, [_vp])
 _plan_upload_bytes = _sig("wmom_plan_upload_bytes", ctypes.c_longlong, [_vp])
 _plan_fill_variant = _sig("wmom_plan_fill_variant", ctypes.c_int, [_vp])
 _plan_fill_pairs = _sig("wmom_plan_fill_pairs", ctypes.c_longlong, [_vp])
+_plan_loops = _sig("wmom_plan_loops", ctypes.c_int, [_vp])
 _plan_set_loads = _sig("wmom_plan_set_loads", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp])
 _fill = _sig("wmom_fill", ctypes.c_int, [_vp, _dp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp])
 _fill_geometries = _sig("wmom_fill_geometries", ctypes.c_int,
@@ -284,6 +285,8 @@ class Plan:
         self.multi_frequency_fill = fv == 2
         # pairs the pair-tiled fill evaluates per frequency (0 for the per-entry fill)
         self.fill_pairs = int(_plan_fill_pairs(h))
+        # independent closed current paths (0 for open wires and trees)
+        self.loops = int(_plan_loops(h))
 
     def close(self):
         if self._h:

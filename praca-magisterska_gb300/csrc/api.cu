@@ -359,6 +359,8 @@ long long wmom_plan_fill_pairs(wmom_plan h) {
   return (long long)h->p.pt.rt_ids.size() * (long long)h->p.pt.ct_ids.size();
 }
 
+int wmom_plan_loops(wmom_plan h) { return h ? h->p.loops : -1; }
+
 wmom_status wmom_fill(wmom_plan h, const double* ka, int nk, void* z_dev, long long ldz,
                       long long zstride, void* stream) {
   if (!h || !ka || nk <= 0 || !z_dev || ldz < h->p.npls || (nk > 1 && zstride < ldz * h->p.npls))

@@ -8,8 +8,11 @@
 // geometry ("wersja referencyjna/Zmatrix.cpp":69-84, 154-165, 252-276, 466-490),
 // evaluated once per geometry here instead of once per entry, with the same
 // rounding (this file is compiled without multiply-add contraction).
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <utility>
+#include <vector>
 
 #include "wmom_internal.h"
 
@@ -89,7 +92,42 @@ int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, c
       s.nr = h == 0 ? n1r : n2r;
     }
   }
+  p->loops = wire_loops(p->h_src, nsmax, z, p->ienv == 2);
   return WMOM_OK;
+}
+
+// Independent closed current paths of the structure: the cycle rank E - V + C of the
+// graph whose edges are the segments the basis functions use and whose vertices are
+// their nodes (over a PEC ground, every node on the ground plane is one vertex: a
+// current returns through the plane; the short virtual wires the topology lays in the
+// plane to join a grounded wire to its image are then no edges).  Open wires and
+// trees have none.  Loops are
+// what makes the EFIE's conditioning grow as 1/(ka)^2 towards low frequencies:
+// divergence-free loop currents see only the vector potential, which vanishes with k.
+int wire_loops(const std::vector<SrcHalf>& src, int nsmax, const float* z, bool ground) {
+  std::vector<int> parent(nsmax + 2);
+  for (size_t i = 0; i < parent.size(); ++i) parent[i] = (int)i;
+  const int gnd = nsmax + 1;
+  auto vertex = [&](int k) { return ground && std::fabs(z[k - 1]) < 1.e-6f ? gnd : k; };
+  auto find = [&](int a) {
+    while (parent[a] != a) a = parent[a] = parent[parent[a]];
+    return a;
+  };
+  std::vector<std::pair<int, int>> seg;
+  seg.reserve(src.size());
+  for (const SrcHalf& h : src) seg.emplace_back(std::min(h.nl, h.nr), std::max(h.nl, h.nr));
+  std::sort(seg.begin(), seg.end());
+  seg.erase(std::unique(seg.begin(), seg.end()), seg.end());
+  int loops = 0;
+  for (const auto& e : seg) {
+    if (vertex(e.first) == gnd && vertex(e.second) == gnd) continue;  // lies in the ground plane
+    const int a = find(vertex(e.first)), b = find(vertex(e.second));
+    if (a == b)
+      ++loops;  // this segment closes a path that already joins its nodes
+    else
+      parent[a] = b;
+  }
+  return loops;
 }
 
 }  // namespace wmom

@@ -773,9 +773,19 @@ wmom_status factor_emul(int n, double2* lu64, int bg, int* ipiv, LuWorkspace* ws
 // Solves bg systems Z64[b] x = V with the factors of factor_group; the solutions end
 // in g.x64[0..bg).  Mixed: FP32 solve, FP64 refinement with a per-matrix activity
 // mask, FP64 LU for the matrices that stall.
+//
+// Probe (mixed form, 0 < probe < bg, factor_rest given): the caller has FP32 factors
+// for matrices [0, probe) only, the group's highest frequencies.  Those refine in
+// tier 1 first.  If the lowest of them (matrix probe - 1) needs FP64-grade factors,
+// matrices [probe, bg) -- lower frequencies, worse conditioned -- go straight to the
+// second tier with it; otherwise factor_rest(probe, bg - probe, info + probe) gives
+// them FP32 factors and they refine in tier 1 as well.
 wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float2* lu32, const double2* lu64,
-                        const int* ipiv, const int* info, double tol, LuWorkspace* ws, GroupScratch& g,
-                        wmom_report* rep, bool condest, int nreal, bool direct_t2) {
+                        const int* ipiv, const int* info_in, double tol, LuWorkspace* ws, GroupScratch& g,
+                        wmom_report* rep, bool condest, int nreal, bool direct_t2, int probe = 0,
+                        const std::function<wmom_status(int, int, int*)>* factor_rest = nullptr) {
+  int info[kMaxLuBatch] = {};
+  std::copy(info_in, info_in + bg, info);
   if (nreal <= 0) nreal = n;
   const size_t nn = (size_t)n * n;
   cudaStream_t s = g.s;
@@ -845,9 +855,11 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   bool fallback[kMaxLuBatch] = {}, active[kMaxLuBatch] = {};
   int stall[kMaxLuBatch] = {};
   double prev[kMaxLuBatch], last[kMaxLuBatch], rel_first[kMaxLuBatch], rel_best[kMaxLuBatch];
+  const bool probing = mode == WMOM_MODE_MIXED && !direct_t2 && probe > 0 && probe < bg && factor_rest;
+  const int t1_end = probing ? probe : bg;
   for (int b = 0; b < bg; ++b) {
     fallback[b] = direct_t2 || info[b] != 0;
-    active[b] = !fallback[b];
+    active[b] = !fallback[b] && b < t1_end;
     prev[b] = last[b] = rel_first[b] = rel_best[b] = HUGE_VAL;
   }
   // With the tensor-core second tier, a matrix whose refinement contracts slowly
@@ -863,20 +875,28 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   const int max_it = 40;
   // direct_t2: the caller predicts that no matrix of the group is served by its FP32
   // factors (none were computed); the group goes straight to the second tier
-  if (!direct_t2) {
-    // initial solve in FP32
-    stats::count(stats::kMisc, 2);
-    convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
-    SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
-    widen_vec_kernel<<<vgrid, 256, 0, s>>>(g.d32.as<float2>(), g.x64.as<double2>(), (size_t)n * bg);
-    SWEEP_TRY(cudaGetLastError());
+  // Tier 1 for matrices [b0, b1): FP32 solve, then FP64 refinement of the active ones.
+  auto tier1 = [&](int b0, int b1) -> wmom_status {
     // the matrices still refining: residuals and corrections are computed for these
     // only (one slowly converging matrix no longer keeps its whole batch busy)
     std::vector<int> hsel(kMaxLuBatch, 0);
     int nsel = 0;
-    for (int b = 0; b < bg; ++b)
+    for (int b = b0; b < b1; ++b)
       if (active[b]) hsel[nsel++] = b;
     SWEEP_TRY(cudaMemcpyAsync(g.sel.p, hsel.data(), sizeof(int) * kMaxLuBatch, cudaMemcpyHostToDevice, s));
+    // initial solve in FP32
+    stats::count(stats::kMisc, 2);
+    convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
+    if (b0 == 0 && b1 == bg) {
+      SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+    } else if (nsel > 0) {
+      SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
+                                   g.sel.as<int>()));
+    }
+    const size_t wcount = (size_t)n * (b1 - b0);
+    widen_vec_kernel<<<(unsigned)((wcount + 255) / 256), 256, 0, s>>>(g.d32.as<float2>() + (size_t)b0 * n,
+                                                                     g.x64.as<double2>() + (size_t)b0 * n, wcount);
+    SWEEP_TRY(cudaGetLastError());
     for (int it = 0;; ++it) {
       if (nsel == 0) break;
       {
@@ -973,7 +993,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     // factors are still a usable preconditioner.  The others -- refinement diverged or
     // barely moved, i.e. kappa * u_fp32 >> 1 -- go straight to the FP64 LU.
     constexpr double kKrylovEntry = 1e-3;
-    for (int b = 0; b < bg; ++b) {
+    for (int b = b0; b < b1; ++b) {
       if (!krylov_enabled()) break;
       if (!fallback[b] || info[b] != 0) continue;
       if (!(rel_best[b] <= kKrylovEntry * rel_first[b])) continue;
@@ -1031,6 +1051,30 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         SWEEP_TRY(cudaStreamSynchronize(s));
       }
       if (ok) fallback[b] = false;
+    }
+    return WMOM_OK;
+  };
+  if (!direct_t2) {
+    wmom_status ts = tier1(0, t1_end);
+    if (ts != WMOM_OK) return ts;
+    if (probing) {
+      const bool predict_rest = fallback[probe - 1];
+      if (trace)
+        std::fprintf(stderr, "wmom refine: probe of %d of %d matrices: matrices %d..%d %s\n", probe, bg, probe,
+                     bg - 1, predict_rest ? "go to the second tier" : "get FP32 factors");
+      if (predict_rest) {
+        for (int b = probe; b < bg; ++b) fallback[b] = true;
+      } else {
+        ts = (*factor_rest)(probe, bg - probe, info + probe);
+        if (ts != WMOM_OK) return ts;
+        for (int b = probe; b < bg; ++b) {
+          rep[b].info = info[b];
+          fallback[b] = info[b] != 0;
+          active[b] = !fallback[b];
+        }
+        ts = tier1(probe, bg);
+        if (ts != WMOM_OK) return ts;
+      }
     }
     for (int b = 0; b < bg; ++b)
       if (!fallback[b]) {
@@ -1611,19 +1655,35 @@ int pipeline_groups(int nfreq, int batch) {
 // bit, as it would after failing in tier 1; only its reported refinement steps
 // differ.  A wrong prediction (a matrix that tier 1 would have served) costs time,
 // not accuracy.  WMOM_TIER_PREDICT=0 turns it off.
+//
+// Within a group, structures with wire loops (Plan::loops; open wires keep a bounded
+// kappa as the frequency falls) probe: the group's upper half gets FP32 factors and
+// refines first, and if the lowest frequency of that half needs FP64-grade factors,
+// the lower half joins it in the second tier without FP32 factors (solve_group's
+// probe).  A group probes when it is the sweep's only group, or when the group before
+// it had a matrix fall back (the sweep is then crossing into the ill-conditioned
+// band); elsewhere the extra FP32 factorisation of the second half would cost more
+// than a probe saves.
 struct TierPrediction {
   bool on;
-  bool all_fell_back = false;
+  bool all_fell_back = false, any_fell_back = false;
   explicit TierPrediction(int mode) {
     const char* e = std::getenv("WMOM_TIER_PREDICT");
     on = mode == WMOM_MODE_MIXED && !(e && e[0] == '0') && emul_gemm_hook() != nullptr;
   }
   bool direct() const { return on && all_fell_back; }
+  int probe(const Plan& p, int bg, bool only_group) const {
+    if (!on || all_fell_back || p.loops == 0 || bg < 4) return 0;
+    return only_group || any_fell_back ? bg / 2 : 0;
+  }
   void record(const wmom_report* rep, int bg) {
-    bool all = bg > 0;
-    for (int b = 0; b < bg; ++b)
+    bool all = bg > 0, any = false;
+    for (int b = 0; b < bg; ++b) {
       if (rep[b].tier < 2) all = false;
+      if (rep[b].tier >= 2) any = true;
+    }
     all_fell_back = all;
+    any_fell_back = any;
   }
 };
 
@@ -1718,13 +1778,18 @@ wmom_status run_sweep_pipelined(const SweepArgs& a, const LuConfig& cfg, int G) 
     const double2* Zg = zall.as<double2>() + (size_t)f0 * nn;
     int info[kMaxLuBatch] = {};
     const bool direct = predict.direct();
+    const int probe = direct ? 0 : predict.probe(p, bg, ngroups == 1);
+    const std::function<wmom_status(int, int, int*)> rest = [&](int b0, int cnt, int* inf) {
+      return factor_group(a.mode, n, Zg + (size_t)b0 * nn, cnt, lu.as<float2>() + (size_t)b0 * nn, nullptr,
+                          piv.as<int>() + (size_t)b0 * n, a.ws, sp.hi, inf, nullptr, nullptr, cfg.span);
+    };
     if (!direct) {
-      st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, sp.hi, info,
-                        nullptr, &graph, cfg.span);
+      st = factor_group(a.mode, n, Zg, probe ? probe : bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws,
+                        sp.hi, info, nullptr, &graph, cfg.span);
       if (st != WMOM_OK) return st;
     }
     st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                     rep.data(), a.condest, n, direct);
+                     rep.data(), a.condest, n, direct, probe, &rest);
     if (st != WMOM_OK) return st;
     predict.record(rep.data(), bg);
     st = group_results(g, bg, a.ngap, rep.data(), f0, a.currents, a.zin, a.reports, &overall);
@@ -1801,13 +1866,18 @@ wmom_status run_sweep_ordered(const SweepArgs& a) {
       const double2* Zg = zall.as<double2>() + (size_t)g0 * nn;
       int info[kMaxLuBatch] = {};
       const bool direct = predict.direct();
+      const int probe = direct ? 0 : predict.probe(p, bg, a.nfreq <= B);
+      const std::function<wmom_status(int, int, int*)> rest = [&](int b0, int cnt, int* inf) {
+        return factor_group(a.mode, n, Zg + (size_t)b0 * nn, cnt, lu.as<float2>() + (size_t)b0 * nn, nullptr,
+                            piv.as<int>() + (size_t)b0 * n, a.ws, s, inf, nullptr, nullptr, cfg.span);
+      };
       if (!direct) {
-        st = factor_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), a.ws, s, info,
-                          nullptr, &graph, cfg.span);
+        st = factor_group(a.mode, n, Zg, probe ? probe : bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(),
+                          a.ws, s, info, nullptr, &graph, cfg.span);
         if (st != WMOM_OK) return st;
       }
       st = solve_group(a.mode, n, Zg, bg, lu.as<float2>(), lu.as<double2>(), piv.as<int>(), info, a.tol, a.ws, g,
-                       rep.data(), a.condest, n, direct);
+                       rep.data(), a.condest, n, direct, probe, &rest);
       if (st != WMOM_OK) return st;
       predict.record(rep.data(), bg);
       st = group_results(g, bg, a.ngap, rep.data(), f0 + g0, a.currents, a.zin, a.reports, &overall);

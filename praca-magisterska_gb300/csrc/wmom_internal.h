@@ -115,7 +115,10 @@ struct Plan {
   // lumped series loads R + j*2*pi*f[MHz]*L[uH] on diagonal entries (1-based index)
   std::vector<int> load_idx;
   std::vector<double> load_r, load_l_uh;
+  int loops = 0;  // independent closed current paths (wire_loops)
 };
+
+int wire_loops(const std::vector<SrcHalf>& src, int nsmax, const float* z, bool ground);
 
 int plan_build_tables(Plan* p, const float* x, const float* y, const float* z, const float* rad,
                       const int* ipc, const int* ips, const int* ise);

@@ -358,3 +358,63 @@ def test_float_float_second_tier(cuda, wmom):
             assert rep[k]["status"] == 0 and rep[k]["tier"] == 2, (ff, k, rep[k])
             bound = max(1e-9, 8 * rep[k]["cond1"] * 2.0 ** -53)
             assert _rel(cur[k], c64[k]) <= bound, (ff, float(freqs[k]), rep[k])
+
+
+@pytest.mark.parametrize("name,loops", [("dipole1m_512", 0), ("random_1024", 0), ("mixed_junctions", 3),
+                                        ("ground_monopole", 0), ("ground_frame", 1), ("ground_grid", 9)])
+def test_plan_counts_wire_loops(cuda, wmom, name, loops):
+    """Independent closed current paths: none for open wires and for a monopole
+    standing on a PEC ground, one for a frame whose two legs stand on it (the current
+    returns through the plane), one per cell of a grid."""
+    _, geo = _fixture(name)
+    d, _ = _fixture(name)
+    plan = wmom.Plan(wmom.Topology(geo, ienv=int(d["ienv"])))
+    if loops is None:
+        assert plan.loops >= 0
+    else:
+        assert plan.loops == loops, (name, plan.loops)
+    plan.close()
+    g = wmom.geometry
+    for geo, want in ((g.precision_grid(2048), 400),
+                      (g.geo_text([(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)],
+                                  [(1, 2, 1e-3, 5), (2, 3, 1e-3, 5), (3, 4, 1e-3, 5), (4, 1, 1e-3, 5)]), 1)):
+        plan = wmom.Plan(wmom.Topology(geo))
+        assert plan.loops == want
+        plan.close()
+
+
+def test_second_tier_probe(cuda, wmom):
+    """A one-group sweep of a structure with loops factors the upper half of its
+    frequencies in FP32 first; the lowest of them needs the second tier here (10 kHz
+    on the junction grid), so the lower half goes there without FP32 factors.  Each
+    matrix must get the answer it gets without the prediction, bit for bit where both
+    runs end in the same tier, and the predicted matrices skip their tier-1 steps."""
+    w = wmom
+    topo = w.Topology(w.geometry.precision_grid(2048))
+    plan = w.Plan(topo)
+    assert plan.loops > 0
+    freqs = np.array([0.002, 20.0, 0.01, 0.001, 5.0, 0.005, 0.03, 0.003], np.float32)  # not sorted
+    out = {}
+    os.environ["WMOM_LU_BATCH"] = "8"  # the whole sweep is one group
+    try:
+        for pred in ("0", "1"):
+            os.environ["WMOM_TIER_PREDICT"] = pred
+            out[pred] = plan.solve(freqs, 1000, mode=w.MODE_MIXED, condest=True)
+    finally:
+        for k in ("WMOM_LU_BATCH", "WMOM_TIER_PREDICT"):
+            os.environ.pop(k, None)
+    c0, z0, r0 = out["0"]
+    c1, z1, r1 = out["1"]
+    cfp, _, _ = plan.solve(freqs, 1000, mode=w.MODE_FP64)
+    plan.close()
+    skipped = 0
+    for k, f in enumerate(freqs):
+        assert r1[k]["status"] == 0 and r0[k]["status"] == 0
+        if (r0[k]["tier"] >= 2) == (r1[k]["tier"] >= 2):
+            assert np.array_equal(c1[k], c0[k]) and z1[k] == z0[k], float(f)
+        if f < 0.006:  # the lower half of the sorted sweep
+            assert r1[k]["tier"] == 2, (float(f), r1[k])
+            skipped += r1[k]["iterations"] < r0[k]["iterations"]
+        bound = max(1e-9, 8 * r1[k]["cond1"] * 2.0 ** -53)
+        assert _rel(c1[k], cfp[k]) <= bound, (float(f), r1[k])
+    assert skipped == 4, [(r["tier"], r["iterations"]) for r in r1]
