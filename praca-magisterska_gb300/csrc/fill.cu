@@ -148,18 +148,25 @@ __device__ __forceinline__ void gauss_sums(const double r[2], const double ri[2]
                                            const double wd[2], double ka, const double2* tab, Cx* up, Cx* dn,
                                            Cx* pl) {
   // the falling ramp is one minus the rising one, so its sum is the plain sum minus
-  // the rising sum (wd is kept in the signature for the instances' layout)
+  // the rising sum
+  // (wd is kept in the signature for the instances' layout).  The first point starts
+  // the sums: the same values as accumulating onto zero, two FP64 additions fewer.
   (void)wd;
-  Cx su = {0.0, 0.0}, sp = {0.0, 0.0};
+  Cx su, sp;
 #pragma unroll
   for (int g = 0; g < 2; ++g) {
     double sn, cs;
     sincos_tab(mul(ka, r[g]), tab, &sn, &cs);
     const double gre = mul(cs, ri[g]), gim = -mul(sn, ri[g]);
-    su.re = fma(wu[g], gre, su.re);
-    su.im = fma(wu[g], gim, su.im);
-    sp.re = add(sp.re, gre);
-    sp.im = add(sp.im, gim);
+    if (g == 0) {
+      su = Cx{mul(wu[0], gre), mul(wu[0], gim)};
+      sp = Cx{gre, gim};
+    } else {
+      su.re = fma(wu[g], gre, su.re);
+      su.im = fma(wu[g], gim, su.im);
+      sp.re = add(sp.re, gre);
+      sp.im = add(sp.im, gim);
+    }
   }
   *up = su;
   *dn = Cx{sub(sp.re, su.re), sub(sp.im, su.im)};
@@ -433,14 +440,15 @@ __device__ __forceinline__ bool same_segment(const ObsInst& O, const SrcInst& S)
   return (S.nl == O.ml && S.nr == O.mr) || (S.nl == O.mr && S.nr == O.ml);
 }
 
-// Phase A value of a regular pair from its R, 1/R and projection t.
-// The ramped integrals carry k^2 cq (kc), the plain one cq (hc = cq / 2 with the 1/2
-// of the 2-point rule), so that phase B only adds.
-__device__ __forceinline__ PairVal regular_pair_value(const double r[2], const double ri[2], double t,
+// Phase A value of a regular pair from its R, 1/R and ht = (dl/2) t, t the test
+// projection (ht does not depend on the frequency).  The ramped integrals carry
+// k^2 cq (kc), the plain one cq (hc = cq / 2 with the 1/2 of the 2-point rule), so
+// that phase B only adds.
+__device__ __forceinline__ PairVal regular_pair_value(const double r[2], const double ri[2], double ht,
                                                       const SrcInst& S, const FreqParams& f, const double2* tab) {
   Cx su, sd, sp;
   gauss_sums(r, ri, S.w_up, S.w_dn, f.ka, tab, &su, &sd, &sp);
-  const double htk = mul(mul(S.half, t), f.kc);
+  const double htk = mul(ht, f.kc);
   PairVal v;
   v.wu = make_double2(mul(su.re, htk), mul(su.im, htk));
   v.wd = make_double2(mul(sd.re, htk), mul(sd.im, htk));
@@ -543,7 +551,7 @@ __device__ __forceinline__ void pair_tile(const ObsInst* __restrict__ oinst, con
       const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
       double r[2], ri[2];
       gauss_geometry(ex, S.dc, S.an2, S.s, r, ri);
-      pt[p] = regular_pair_value(r, ri, t, S, f, tab);
+      pt[p] = regular_pair_value(r, ri, mul(S.half, t), S, f, tab);
     } else {
       pt[p] = self_pair_value(t, S, f, selfv[L.ct_ids[q0 + q]]);
     }
@@ -625,7 +633,8 @@ __global__ void __launch_bounds__(256, 3) fill_pair_ragged_kernel(const FillJob*
 
 // Frequency-independent values of a pair, kept in shared memory across frequencies.
 struct PairGeo {
-  double r[2], ri[2], t;
+  double r[2], ri[2];
+  double tw;  // regular pair: (dl/2) t, frequency-independent; self pair: t
 };
 
 constexpr int kMultiThreads = 512;
@@ -654,12 +663,14 @@ __global__ void __launch_bounds__(kMultiThreads, 2) fill_pair_multi_kernel(
     const ObsInst& O = oinst[L.rt_ids[o0 + o]];
     const SrcInst& S = sinst[L.ct_ids[q0 + q]];
     PairGeo g;
-    g.t = dot3(S.dc, O.u);
+    const double t = dot3(S.dc, O.u);
     if (!same_segment(O, S)) {
       const double ex[3] = {sub(O.rm[0], S.rs[0]), sub(O.rm[1], S.rs[1]), sub(O.rm[2], S.rs[2])};
       gauss_geometry(ex, S.dc, S.an2, S.s, g.r, g.ri);
+      g.tw = mul(S.half, t);
     } else {
       g.r[0] = -1.0;  // self pair (a regular pair's R is at least the radius)
+      g.tw = t;
     }
     geo[p] = g;
   }
@@ -671,8 +682,8 @@ __global__ void __launch_bounds__(kMultiThreads, 2) fill_pair_multi_kernel(
       const int qg = L.ct_ids[q0 + q];
       const SrcInst& S = sinst[qg];
       const PairGeo& g = geo[p];
-      pt[p] = g.r[0] < 0.0 ? self_pair_value(g.t, S, f, selfv[(size_t)k * nsrc + qg])
-                           : regular_pair_value(g.r, g.ri, g.t, S, f, tab);
+      pt[p] = g.r[0] < 0.0 ? self_pair_value(g.tw, S, f, selfv[(size_t)k * nsrc + qg])
+                           : regular_pair_value(g.r, g.ri, g.tw, S, f, tab);
     }
     __syncthreads();
     assemble_tile(pt, nQ, L, tr, tc, npls, Z + (size_t)k * zstride, ldz);
