@@ -1256,10 +1256,14 @@ __device__ __forceinline__ void st_release_i32(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// inv (optional): the inverses of the factors' kTrsvB x kTrsvB diagonal blocks
+// (lu_block_inverses); each block's solution is then one parallel product with its
+// inverse instead of a kTrsvB-step substitution by one warp, the chain's critical path.
 template <typename C, bool UPPER>
 __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long long lda, int n, C* x,
                                                    int* flags, unsigned int* ticket, int epoch, int* err,
-                                                   long long astride, int flag_stride, const int* __restrict__ sel) {
+                                                   long long astride, int flag_stride, const int* __restrict__ sel,
+                                                   const C* __restrict__ inv) {
   using R = decltype(C{}.x);
   __shared__ C xs[kTrsvB];
   __shared__ C part[4][kTrsvB];
@@ -1292,16 +1296,20 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   // the diagonal block goes to shared memory first: its loads overlap the waits
   extern __shared__ __align__(16) unsigned char trsv_smem[];
   C* Ds = reinterpret_cast<C*>(trsv_smem);  // kTrsvB x kTrsvB, column-major
+  const C* Ib = inv ? inv + (((size_t)mat * nblk + b) * 2 + (UPPER ? 1 : 0)) * kTrsvB * kTrsvB : nullptr;
   for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
     const int c = idx / kTrsvB, q = idx - c * kTrsvB;
-    Ds[idx] = (c < rows && q < rows) ? A[(size_t)(r0 + c) * lda + r0 + q] : cmake<C>(0, 0);
+    if (Ib)
+      Ds[idx] = Ib[idx];
+    else
+      Ds[idx] = (c < rows && q < rows) ? A[(size_t)(r0 + c) * lda + r0 + q] : cmake<C>(0, 0);
   }
   // back substitution divides by the diagonal: Smith's ratio and the reciprocal of
   // its denominator for every diagonal entry, in parallel and before the waits, so
   // that the dependent chain below multiplies instead of dividing
   __shared__ R dg_r[kTrsvB], dg_inv[kTrsvB];
   __shared__ int dg_sw[kTrsvB];
-  if (UPPER && tid < kTrsvB) {
+  if (UPPER && !Ib && tid < kTrsvB) {
     const int c = tid;
     const C d = (c < rows) ? A[(size_t)(r0 + c) * lda + r0 + c] : cmake<C>(1, 0);
     if (fabs(d.x) >= fabs(d.y)) {
@@ -1365,6 +1373,32 @@ __global__ void __launch_bounds__(256) trsv_kernel(const C* __restrict__ A, long
   }
   part[g][r] = acc;
   __syncthreads();
+  if (Ib) {
+    // s = x_blk - sum(T x) in xs, then x_blk = Inv s: thread (r, g) sums the columns
+    // g + 4i of row r, the four partial sums meet in part[]
+    if (tid < kTrsvB) {
+      C v = cmake<C>(0, 0);
+      if (tid < rows) {
+        const C b0 = x[r0 + tid];
+        v = cmake<C>(b0.x + (part[0][tid].x + part[1][tid].x + part[2][tid].x + part[3][tid].x),
+                     b0.y + (part[0][tid].y + part[1][tid].y + part[2][tid].y + part[3][tid].y));
+      }
+      xs[tid] = v;
+    }
+    __syncthreads();
+    C y = cmake<C>(0, 0);  // -sum(Inv s)
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) y = cfms(y, Ds[(size_t)(g + 4 * i) * kTrsvB + r], xs[g + 4 * i]);
+    part[g][r] = y;
+    __syncthreads();
+    if (tid < rows)
+      x[r0 + tid] = cmake<C>(-((part[0][tid].x + part[1][tid].x) + (part[2][tid].x + part[3][tid].x)),
+                             -((part[0][tid].y + part[1][tid].y) + (part[2][tid].y + part[3][tid].y)));
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release_i32(&flags[b], epoch);
+    return;
+  }
   if (tid < 32) {
     // lane l holds rows l and l + 32 of the block; part[] already holds -sum(T x)
     C s0 = cmake<C>(0, 0), s1 = cmake<C>(0, 0);
@@ -1730,6 +1764,72 @@ __global__ void __launch_bounds__(4 * kTrsvB) tri_inv_ff_kernel(const float4* __
     const int j = idx / kTrsvB, i = idx - j * kTrsvB;
     const Ffc v = Y[(size_t)i * kInvLd + j];
     out[idx] = make_float4(v.re.h, v.im.h, v.re.l, v.im.l);
+  }
+}
+
+// The inverses of the factors' kTrsvB x kTrsvB diagonal blocks for trsv_kernel, in
+// the factors' own arithmetic: tri_inv_ff_kernel's grid, layout and four-threads-per-
+// column substitution on e_c (L^-1 by forward substitution, U^-1 by back
+// substitution with the reciprocals of U's diagonal taken in FP64).
+template <typename C>
+__global__ void __launch_bounds__(4 * kTrsvB) tri_inv_kernel(const C* __restrict__ A, long long lda, int n,
+                                                             long long astride, C* __restrict__ inv) {
+  extern __shared__ __align__(16) unsigned char tri_inv_c_smem[];
+  C* T = reinterpret_cast<C*>(tri_inv_c_smem);  // the block, column-major
+  C* Y = T + kTrsvB * kTrsvB;                    // Y[i * kInvLd + c]: row i of column c
+  __shared__ C dinv[kTrsvB];
+  using R = decltype(C{}.x);
+  const int b = blockIdx.x, mat = blockIdx.y;
+  const bool upper = blockIdx.z == 1;
+  const int nblk = gridDim.x;
+  const int r0 = b * kTrsvB;
+  const int rows = min(kTrsvB, n - r0);
+  const int tid = threadIdx.x;
+  const int c = tid >> 2, q = tid & 3;
+  A += (size_t)mat * astride;
+  const C zero = cmake<C>(0, 0), one = cmake<C>(1, 0);
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int j = idx / kTrsvB, i = idx - j * kTrsvB;
+    T[idx] = (i < rows && j < rows) ? A[(size_t)(r0 + j) * lda + r0 + i] : zero;
+    Y[(size_t)i * kInvLd + j] = i == j ? one : zero;
+  }
+  if (upper && tid < kTrsvB) {
+    double2 d = make_double2(1.0, 0.0);
+    if (tid < rows) {
+      const C v = A[(size_t)(r0 + tid) * lda + r0 + tid];
+      d = make_double2((double)v.x, (double)v.y);
+    }
+    const double2 rc = crecip(d);
+    dinv[tid] = cmake<C>((R)rc.x, (R)rc.y);
+  }
+  __syncthreads();
+  if (!upper) {
+    for (int k = 0; k + 1 < rows; ++k) {
+      __syncwarp();
+      if (c <= k && c < rows) {
+        const C yk = Y[(size_t)k * kInvLd + c];
+        for (int i = q; i < rows; i += 4)
+          if (i > k) Y[(size_t)i * kInvLd + c] = cfms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
+      }
+    }
+  } else {
+    for (int k = rows - 1; k >= 0; --k) {
+      __syncwarp();
+      C yk = zero;
+      if (c >= k && c < rows) yk = cmul(Y[(size_t)k * kInvLd + c], dinv[k]);
+      __syncwarp();  // every thread of the column has read row k before its owner writes it
+      if (c >= k && c < rows) {
+        if ((k & 3) == q) Y[(size_t)k * kInvLd + c] = yk;
+        for (int i = q; i < k; i += 4)
+          Y[(size_t)i * kInvLd + c] = cfms(Y[(size_t)i * kInvLd + c], T[(size_t)k * kTrsvB + i], yk);
+      }
+    }
+  }
+  __syncthreads();
+  C* out = inv + (((size_t)mat * nblk + b) * 2 + (upper ? 1 : 0)) * kTrsvB * kTrsvB;
+  for (int idx = tid; idx < kTrsvB * kTrsvB; idx += blockDim.x) {
+    const int j = idx / kTrsvB, i = idx - j * kTrsvB;
+    out[idx] = Y[(size_t)i * kInvLd + j];
   }
 }
 
@@ -2839,7 +2939,8 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
-                       LuWorkspace* ws, cudaStream_t s, int batch, long long astride, const int* sel) {
+                       LuWorkspace* ws, cudaStream_t s, int batch, long long astride, const int* sel,
+                       const C* inv) {
   constexpr int NB = PanelCfg<C>::NB;
   cudaError_t e;
   if (batch < 1 || batch > ws->max_batch || ((batch > 1 || sel) && (nrhs != 1 || ldb != n)))
@@ -2880,10 +2981,10 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
       if (e != cudaSuccess) return e;
       if (pass == 0)
         trsv_kernel<C, false><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                               &ws->barrier->err, astride, ws->flag_cap, sel);
+                                                               &ws->barrier->err, astride, ws->flag_cap, sel, inv);
       else
         trsv_kernel<C, true><<<nblk * batch, 256, dsmem, s>>>(A, lda, n, B, ws->flags, ws->ticket, ep,
-                                                              &ws->barrier->err, astride, ws->flag_cap, sel);
+                                                              &ws->barrier->err, astride, ws->flag_cap, sel, inv);
     }
     return cudaGetLastError();
   }
@@ -2937,6 +3038,27 @@ cudaError_t ff_block_inverses(const float4* A, long long lda, int n, int batch, 
 size_t ff_block_inverse_bytes(int n, int batch) {
   return (size_t)batch * ((n + kTrsvB - 1) / kTrsvB) * 2 * kTrsvB * kTrsvB * sizeof(float4);
 }
+
+template <typename C>
+cudaError_t lu_block_inverses(const C* A, long long lda, int n, int batch, long long astride, C* inv,
+                              cudaStream_t s) {
+  if (n <= 0 || batch < 1 || batch > 65535 || !inv) return cudaErrorInvalidValue;
+  const int nblk = (n + kTrsvB - 1) / kTrsvB;
+  const size_t smem = sizeof(C) * ((size_t)kTrsvB * kTrsvB + (size_t)kTrsvB * kInvLd);
+  cudaError_t e = allow_dynamic_smem((const void*)tri_inv_kernel<C>, smem);
+  if (e != cudaSuccess) return e;
+  stats::count(stats::kMisc);
+  tri_inv_kernel<C><<<dim3(nblk, batch, 2), 4 * kTrsvB, smem, s>>>(A, lda, n, astride, inv);
+  return cudaGetLastError();
+}
+
+template <typename C>
+size_t lu_block_inverse_bytes(int n, int batch) {
+  return (size_t)batch * ((n + kTrsvB - 1) / kTrsvB) * 2 * kTrsvB * kTrsvB * sizeof(C);
+}
+
+template cudaError_t lu_block_inverses<float2>(const float2*, long long, int, int, long long, float2*, cudaStream_t);
+template size_t lu_block_inverse_bytes<float2>(int, int);
 
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
                         cudaStream_t s, int batch, long long astride, const int* sel, const float4* inv) {
@@ -3091,9 +3213,9 @@ template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWork
 template cudaError_t lu_factor_t<float2>(float2*, long long, int, int*, LuWorkspace*, cudaStream_t,
                                          GemmHook<float2>, int, long long, int);
 template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const int*, double2*, long long, int,
-                                         LuWorkspace*, cudaStream_t, int, long long, const int*);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const double2*);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,
-                                         LuWorkspace*, cudaStream_t, int, long long, const int*);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const float2*);
 template cudaError_t lu_solve_h_t<double2>(const double2*, long long, int, const int*, double2*, LuWorkspace*,
                                            cudaStream_t, int, long long, const int*);
 template cudaError_t lu_solve_h_t<float2>(const float2*, long long, int, const int*, float2*, LuWorkspace*,

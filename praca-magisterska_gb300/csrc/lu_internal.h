@@ -81,10 +81,21 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 // Solves with the factors; batch > 1 needs nrhs == 1 and right-hand sides n apart.
 // sel (device, `batch` entries): solve only these matrices of a larger batch (matrix
 // sel[i] at A + sel[i] * astride, its right-hand side at B + sel[i] * n).
+// inv (optional, one right-hand side): the inverses of the factors' 64 x 64 diagonal
+// blocks (lu_block_inverses), which turn each block's substitution into one parallel
+// product.
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
                        LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0,
-                       const int* sel = nullptr);
+                       const int* sel = nullptr, const C* inv = nullptr);
+// The inverses of the 64 x 64 diagonal blocks of the factors (unit lower L and upper
+// U) of `batch` matrices astride apart, into inv (lu_block_inverse_bytes): per matrix
+// and block L^-1 then U^-1, column-major.  Instantiated for complex FP32.
+template <typename C>
+cudaError_t lu_block_inverses(const C* A, long long lda, int n, int batch, long long astride, C* inv,
+                              cudaStream_t s);
+template <typename C>
+size_t lu_block_inverse_bytes(int n, int batch);
 
 // Solves A^H x = b with the factors of lu_factor_t (the condition estimator's second
 // kind of solve), one right-hand side per matrix, vectors n apart; batch and sel as

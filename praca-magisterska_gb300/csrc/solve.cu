@@ -875,8 +875,24 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
   const int max_it = 40;
   // direct_t2: the caller predicts that no matrix of the group is served by its FP32
   // factors (none were computed); the group goes straight to the second tier
+  // The FP32 solves of tier 1 multiply by the inverses of the factors' 64 x 64
+  // diagonal blocks (lu_block_inverses, once per factorisation) instead of
+  // substituting through each block with one warp: most of tier 1's later steps solve
+  // one or two slowly converging matrices, whose solves are that chain of blocks.
+  // WMOM_TRSV_INV=0 keeps the substitution.
+  DevBuf t1inv;
+  const size_t inv_per = lu_block_inverse_bytes<float2>(n, 1) / sizeof(float2);
+  {
+    const char* ie = std::getenv("WMOM_TRSV_INV");
+    if (mode == WMOM_MODE_MIXED && !direct_t2 && !(ie && ie[0] == '0'))
+      SWEEP_TRY(t1inv.alloc(lu_block_inverse_bytes<float2>(n, bg), s));
+  }
+  float2* t1invp = t1inv.p ? t1inv.as<float2>() : nullptr;
   // Tier 1 for matrices [b0, b1): FP32 solve, then FP64 refinement of the active ones.
   auto tier1 = [&](int b0, int b1) -> wmom_status {
+    if (t1invp)
+      SWEEP_TRY(lu_block_inverses<float2>(lu32 + (size_t)b0 * nn, n, n, b1 - b0, (long long)nn,
+                                          t1invp + (size_t)b0 * inv_per, s));
     // the matrices still refining: residuals and corrections are computed for these
     // only (one slowly converging matrix no longer keeps its whole batch busy)
     std::vector<int> hsel(kMaxLuBatch, 0);
@@ -888,10 +904,11 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     stats::count(stats::kMisc, 2);
     convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
     if (b0 == 0 && b1 == bg) {
-      SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn));
+      SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn, nullptr,
+                                   t1invp));
     } else if (nsel > 0) {
       SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
-                                   g.sel.as<int>()));
+                                   g.sel.as<int>(), t1invp));
     }
     const size_t wcount = (size_t)n * (b1 - b0);
     widen_vec_kernel<<<(unsigned)((wcount + 255) / 256), 256, 0, s>>>(g.d32.as<float2>() + (size_t)b0 * n,
@@ -978,7 +995,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       stats::count(stats::kMisc, 4);
       convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
       SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
-                                   nsel == bg ? nullptr : g.sel.as<int>()));
+                                   nsel == bg ? nullptr : g.sel.as<int>(), t1invp));
 
       sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
       sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);

@@ -418,3 +418,32 @@ def test_second_tier_probe(cuda, wmom):
         bound = max(1e-9, 8 * r1[k]["cond1"] * 2.0 ** -53)
         assert _rel(c1[k], cfp[k]) <= bound, (float(f), r1[k])
     assert skipped == 4, [(r["tier"], r["iterations"]) for r in r1]
+
+
+def test_fp32_solves_through_block_inverses(cuda, wmom):
+    """Tier 1's FP32 solves multiply by the inverses of the factors' 64 x 64 diagonal
+    blocks (the default) or substitute through each block (WMOM_TRSV_INV=0): both
+    refine to the contract against the FP64 form, in the same tiers and about as many
+    steps, on random wires and on the junction grid where it stays in tier 1."""
+    w = wmom
+    for geo, freqs in ((w.geometry.random_wires(1024), [0.01, 1.0, 10.0]),
+                       (w.geometry.precision_grid(2048), [2.0, 10.0, 25.0])):
+        plan = w.Plan(w.Topology(geo))
+        ngap = plan.npls // 2
+        freqs = np.array(freqs, np.float32)
+        c64, _, r64 = plan.solve(freqs, ngap, mode=w.MODE_FP64, condest=True)
+        out = {}
+        for inv in ("1", "0"):
+            os.environ["WMOM_TRSV_INV"] = inv
+            try:
+                out[inv] = plan.solve(freqs, ngap, mode=w.MODE_MIXED)
+            finally:
+                del os.environ["WMOM_TRSV_INV"]
+        plan.close()
+        for inv, (c, _, r) in out.items():
+            for k in range(len(freqs)):
+                assert r[k]["status"] == 0, (inv, r[k])
+                assert _rel(c[k], c64[k]) < _bound(TOL_MIXED, r64[k]["cond1"]), (inv, float(freqs[k]), r[k])
+        r1, r0 = out["1"][2], out["0"][2]
+        assert [r["tier"] for r in r1] == [r["tier"] for r in r0]
+        assert all(abs(a["iterations"] - b["iterations"]) <= 2 for a, b in zip(r1, r0)), (r1, r0)
