@@ -2898,9 +2898,9 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
   } while (0)
 
   // With the tensor-core update, `span` panels share one trailing update (K = span
-  // NB): inside the group each panel is first brought up to date, left-looking, by
-  // thin updates from the group's earlier panels, so the large update reads and
-  // writes the trailing matrix 1/span as often.  Without the hook (FP64 SIMT GEMM,
+  // NB): inside the group each panel is brought up to date by thin updates from the
+  // group's earlier panels, so the large update reads and writes the trailing matrix
+  // 1/span as often.  Without the hook (FP64 SIMT GEMM,
   // bound by the FP64 pipe rather than by traffic) span is 1.
   const int S = gemm_hook ? std::max(1, std::min(span > 0 ? span : 2, kMaxSpan)) : 1;
   for (int j0 = 0; j0 < n;) {
@@ -2915,13 +2915,18 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
     }
     const int cr = c[np], rest = n - cr;
     for (int q = 0; q < np; ++q) {
-      // panel q: apply the group's earlier panels to its columns, then factor it
-      for (int p = 0; p < q; ++p) {
-        LU_TRY(trsm(c[p], w[p], c[q], w[q]));
-        LU_TRY(update(c[p + 1], c[q], n - c[p + 1], w[q], c[p], w[p]));
-      }
+      // panel q, then its U rows and its update for all the group's later panels at
+      // once (one solve and one GEMM over columns c[q+1] .. cr instead of one per later
+      // panel).  Every entry of those columns still receives the updates of panels
+      // 0, 1, .. in that order, and both kernels compute each column (the GEMM each
+      // entry) on its own, so the factors are those of one panel at a time, bit for
+      // bit, with fewer and wider launches.
       LU_TRY(panel(c[q], w[q]));
       LU_TRY(laswp(c[q], w[q]));
+      if (q + 1 < np) {
+        LU_TRY(trsm(c[q], w[q], c[q + 1], cr - c[q + 1]));
+        LU_TRY(update(c[q + 1], c[q + 1], n - c[q + 1], cr - c[q + 1], c[q], w[q]));
+      }
     }
     if (rest > 0) {
       // U rows of the group for the trailing columns, then one update with K = c[np] - j0

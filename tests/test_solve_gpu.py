@@ -447,3 +447,30 @@ def test_fp32_solves_through_block_inverses(cuda, wmom):
         r1, r0 = out["1"][2], out["0"][2]
         assert [r["tier"] for r in r1] == [r["tier"] for r in r0]
         assert all(abs(a["iterations"] - b["iterations"]) <= 2 for a, b in zip(r1, r0)), (r1, r0)
+
+
+def test_second_tier_probe_that_passes(cuda, wmom):
+    """The probe's other branch: a one-group sweep of a structure with loops whose upper
+    half all stays in tier 1 gives the lower half its FP32 factors afterwards (a second
+    batched factorisation) and refines it in tier 1 too.  Every answer, tier and step
+    count must equal the unprobed sweep's: factors and solves do not depend on the
+    batch they run in."""
+    w = wmom
+    plan = w.Plan(w.Topology(w.geometry.precision_grid(2048)))
+    assert plan.loops > 0
+    freqs = np.array([3.0, 25.0, 4.0, 20.0, 6.0, 15.0, 8.0, 10.0], np.float32)
+    out = {}
+    os.environ["WMOM_LU_BATCH"] = "8"  # the whole sweep is one group
+    try:
+        for pred in ("0", "1"):
+            os.environ["WMOM_TIER_PREDICT"] = pred
+            out[pred] = plan.solve(freqs, 1000, mode=w.MODE_MIXED)
+    finally:
+        for k in ("WMOM_LU_BATCH", "WMOM_TIER_PREDICT"):
+            os.environ.pop(k, None)
+    plan.close()
+    c0, z0, r0 = out["0"]
+    c1, z1, r1 = out["1"]
+    assert all(r["tier"] == 1 and r["status"] == 0 for r in r1), r1
+    assert np.array_equal(c1, c0) and np.array_equal(z1, z0)
+    assert [r["iterations"] for r in r1] == [r["iterations"] for r in r0]
