@@ -9,7 +9,7 @@
 namespace wmom {
 
 constexpr int kMaxPanelBlocks = 256;
-constexpr int kMaxLuBatch = 16;  // matrices per batched factorisation
+constexpr int kMaxLuBatch = 32;  // matrices per batched factorisation
 
 // Largest batch whose cooperative panel launches all fit co-resident on this device
 // (cluster panels impose no limit).  fp64_cluster: the FP64 factorisation runs with
