@@ -474,3 +474,28 @@ def test_second_tier_probe_that_passes(cuda, wmom):
     assert all(r["tier"] == 1 and r["status"] == 0 for r in r1), r1
     assert np.array_equal(c1, c0) and np.array_equal(z1, z0)
     assert [r["iterations"] for r in r1] == [r["iterations"] for r in r0]
+
+
+def test_tier1_accepts_backward_stable_solutions(cuda, wmom):
+    """A matrix whose FP32-factor refinement stops at the FP64 residual floor, above the
+    requested tolerance, keeps its tier-1 solution when that solution is backward stable
+    at FP64 level (componentwise backward error at most 4 sqrt(n) 2^-53); with the test
+    turned off (WMOM_T1_BERR=0) the same matrix falls back to the second tier.  Both
+    answers are within 8 kappa_1 eps of the plain FP64 solve (0.3 MHz on the N = 2048
+    junction grid)."""
+    w = wmom
+    plan = w.Plan(w.Topology(w.geometry.precision_grid(2048)))
+    freqs = np.array([0.3], np.float32)
+    c64, _, r64 = plan.solve(freqs, 1000, mode=w.MODE_FP64, condest=True)
+    ca, _, ra = plan.solve(freqs, 1000, mode=w.MODE_MIXED)
+    os.environ["WMOM_T1_BERR"] = "0"
+    try:
+        cb, _, rb = plan.solve(freqs, 1000, mode=w.MODE_MIXED)
+    finally:
+        del os.environ["WMOM_T1_BERR"]
+    plan.close()
+    assert ra[0]["status"] == 0 and ra[0]["tier"] == 1 and ra[0]["fell_back"] == 0, ra[0]
+    assert ra[0]["rel_residual"] > 1e-12  # stopped at the floor, not at the tolerance
+    assert rb[0]["status"] == 0 and rb[0]["tier"] == 2, rb[0]
+    bound = _bound(TOL_MIXED, r64[0]["cond1"])
+    assert _rel(ca[0], c64[0]) < bound and _rel(cb[0], c64[0]) < bound
