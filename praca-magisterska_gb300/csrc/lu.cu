@@ -2375,14 +2375,16 @@ __global__ void pivots_to_perm_kernel(const int* __restrict__ ipiv, int n, int* 
 template <typename C>
 __global__ void gather_rows_kernel(const C* __restrict__ src, long long lds, C* __restrict__ dst,
                                    long long ldd, const int* __restrict__ perm, int n, int nrhs,
-                                   int perm_stride, const int* __restrict__ sel) {
+                                   int perm_stride, const int* __restrict__ sel, int perm_by_matrix = 0) {
   // column c: a right-hand side of one matrix (perm_stride 0) or the right-hand
   // side of matrix c of a batch (perm_stride n; with sel, of matrix sel[c], whose
-  // vector is column sel[c] of dst)
+  // vector is column sel[c] of dst).  The permutations are one per column, or with
+  // perm_by_matrix one per matrix of the whole batch (precomputed, lu_pivots_to_perm)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   const int cd = sel ? sel[c] : c;
-  if (i < n && c < nrhs) dst[(size_t)cd * ldd + i] = src[(size_t)c * lds + perm[(size_t)c * perm_stride + i]];
+  const int pc = perm_by_matrix ? cd : c;
+  if (i < n && c < nrhs) dst[(size_t)cd * ldd + i] = src[(size_t)c * lds + perm[(size_t)pc * perm_stride + i]];
 }
 
 // dst[c] = src[sel[c]] for the n-vectors of the selected matrices of a batch
@@ -2945,7 +2947,7 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
                        LuWorkspace* ws, cudaStream_t s, int batch, long long astride, const int* sel,
-                       const C* inv) {
+                       const C* inv, const int* perm_pre) {
   constexpr int NB = PanelCfg<C>::NB;
   cudaError_t e;
   if (batch < 1 || batch > ws->max_batch || ((batch > 1 || sel) && (nrhs != 1 || ldb != n)))
@@ -2956,8 +2958,9 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
   if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
   e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
   if (e != cudaSuccess) return e;
-  stats::count(stats::kMisc, 2);
-  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
+  const bool pre = perm_pre != nullptr;
+  stats::count(stats::kMisc, pre ? 1 : 2);
+  if (!pre) pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
   C* tmp = reinterpret_cast<C*>(ws->rhs);
   const int ncol = (batch > 1 || sel) ? batch : nrhs;  // columns of the gathered block
   if ((size_t)n * ncol * sizeof(C) > ws->rhs_bytes) return cudaErrorInvalidValue;
@@ -2969,8 +2972,12 @@ cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, 
                           cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
-  gather_rows_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(tmp, n, B, ldb, ws->perm, n, ncol,
-                                                                     (batch > 1 || sel) ? n : 0, sel);
+  if (pre)
+    gather_rows_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(tmp, n, B, ldb, perm_pre, n, ncol,
+                                                                       (batch > 1 || sel) ? n : 0, sel, 1);
+  else
+    gather_rows_kernel<C><<<dim3((n + 255) / 256, ncol), 256, 0, s>>>(tmp, n, B, ldb, ws->perm, n, ncol,
+                                                                       (batch > 1 || sel) ? n : 0, sel);
   if (nrhs == 1 && ws->flags) {
     const int nblk = (n + kTrsvB - 1) / kTrsvB;
     if (nblk > ws->flag_cap) return cudaErrorInvalidValue;
@@ -3065,8 +3072,19 @@ size_t lu_block_inverse_bytes(int n, int batch) {
 template cudaError_t lu_block_inverses<float2>(const float2*, long long, int, int, long long, float2*, cudaStream_t);
 template size_t lu_block_inverse_bytes<float2>(int, int);
 
+cudaError_t lu_pivots_to_perm(const int* ipiv, int n, int batch, int* perm, cudaStream_t s) {
+  if (n <= 0 || batch < 1 || batch > 65535 || !perm || (size_t)n * sizeof(int) > 200 * 1024)
+    return cudaErrorInvalidValue;
+  cudaError_t e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
+  if (e != cudaSuccess) return e;
+  stats::count(stats::kMisc);
+  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, perm, nullptr);
+  return cudaGetLastError();
+}
+
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
-                        cudaStream_t s, int batch, long long astride, const int* sel, const float4* inv) {
+                        cudaStream_t s, int batch, long long astride, const int* sel, const float4* inv,
+                        const int* perm_pre) {
   if (batch < 1 || batch > ws->max_batch || !ws->flags || n > ws->perm_cap) return cudaErrorInvalidValue;
   if ((size_t)n * sizeof(int) > 200 * 1024) return cudaErrorInvalidValue;
   if ((size_t)n * batch * sizeof(double2) > ws->rhs_bytes) return cudaErrorInvalidValue;
@@ -3075,8 +3093,8 @@ cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, 
   cudaError_t e = allow_dynamic_smem((const void*)pivots_to_perm_kernel, (n * sizeof(int)));
   if (e != cudaSuccess) return e;
   // B <- P B, as lu_solve_t's single-right-hand-side path
-  stats::count(stats::kMisc, 2);
-  pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
+  stats::count(stats::kMisc, perm_pre ? 1 : 2);
+  if (!perm_pre) pivots_to_perm_kernel<<<batch, 256, n * sizeof(int), s>>>(ipiv, n, ws->perm, sel);
   double2* tmp = reinterpret_cast<double2*>(ws->rhs);
   if (sel) {
     stats::count(stats::kMisc);
@@ -3085,7 +3103,8 @@ cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, 
     e = cudaMemcpyAsync(tmp, B, sizeof(double2) * (size_t)n * batch, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
   }
-  gather_rows_kernel<double2><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(tmp, n, B, n, ws->perm, n, batch, n, sel);
+  gather_rows_kernel<double2><<<dim3((n + 255) / 256, batch), 256, 0, s>>>(
+      tmp, n, B, n, perm_pre ? perm_pre : ws->perm, n, batch, n, sel, perm_pre ? 1 : 0);
   const size_t dsmem = sizeof(Ffc) * kTrsvB * kTrsvB;
   e = allow_dynamic_smem((const void*)trsv_ff_kernel<false>, dsmem);
   if (e != cudaSuccess) return e;
@@ -3218,9 +3237,11 @@ template cudaError_t lu_factor_t<double2>(double2*, long long, int, int*, LuWork
 template cudaError_t lu_factor_t<float2>(float2*, long long, int, int*, LuWorkspace*, cudaStream_t,
                                          GemmHook<float2>, int, long long, int);
 template cudaError_t lu_solve_t<double2>(const double2*, long long, int, const int*, double2*, long long, int,
-                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const double2*);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const double2*,
+                                         const int*);
 template cudaError_t lu_solve_t<float2>(const float2*, long long, int, const int*, float2*, long long, int,
-                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const float2*);
+                                         LuWorkspace*, cudaStream_t, int, long long, const int*, const float2*,
+                                         const int*);
 template cudaError_t lu_solve_h_t<double2>(const double2*, long long, int, const int*, double2*, LuWorkspace*,
                                            cudaStream_t, int, long long, const int*);
 template cudaError_t lu_solve_h_t<float2>(const float2*, long long, int, const int*, float2*, LuWorkspace*,

@@ -84,10 +84,16 @@ cudaError_t lu_factor_t(C* A, long long lda, int n, int* ipiv, LuWorkspace* ws, 
 // inv (optional, one right-hand side): the inverses of the factors' 64 x 64 diagonal
 // blocks (lu_block_inverses), which turn each block's substitution into one parallel
 // product.
+// perm_pre (optional, device, n ints per matrix of the whole batch, matrix i at
+// perm_pre + i * n): the factors' row permutations from lu_pivots_to_perm, computed
+// once per factorisation instead of on every solve.
 template <typename C>
 cudaError_t lu_solve_t(const C* A, long long lda, int n, const int* ipiv, C* B, long long ldb, int nrhs,
                        LuWorkspace* ws, cudaStream_t s, int batch = 1, long long astride = 0,
-                       const int* sel = nullptr, const C* inv = nullptr);
+                       const int* sel = nullptr, const C* inv = nullptr, const int* perm_pre = nullptr);
+// The row permutation of each of `batch` pivot vectors (ipiv, n apart, LAPACK 1-based)
+// into perm (n apart): row i of P B is row perm[i] of B.
+cudaError_t lu_pivots_to_perm(const int* ipiv, int n, int batch, int* perm, cudaStream_t s);
 // The inverses of the 64 x 64 diagonal blocks of the factors (unit lower L and upper
 // U) of `batch` matrices astride apart, into inv (lu_block_inverse_bytes): per matrix
 // and block L^-1 then U^-1, column-major.  Instantiated for complex FP32.
@@ -113,7 +119,7 @@ cudaError_t lu_solve_h_t(const C* A, long long lda, int n, const int* ipiv, C* B
 // (ff_block_inverses), which turn each block's substitution into one parallel product.
 cudaError_t lu_solve_ff(const float4* A, long long lda, int n, const int* ipiv, double2* B, LuWorkspace* ws,
                         cudaStream_t s, int batch = 1, long long astride = 0, const int* sel = nullptr,
-                        const float4* inv = nullptr);
+                        const float4* inv = nullptr, const int* perm_pre = nullptr);
 // The inverses of the 64 x 64 diagonal blocks of the float-float factors (unit lower L
 // and upper U) of `batch` matrices astride apart, into inv (ff_block_inverse_bytes),
 // in float-float arithmetic: for lu_solve_ff.

@@ -888,11 +888,16 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       SWEEP_TRY(t1inv.alloc(lu_block_inverse_bytes<float2>(n, bg), s));
   }
   float2* t1invp = t1inv.p ? t1inv.as<float2>() : nullptr;
+  // the factors' row permutations, once per factorisation (every solve of a matrix
+  // applies the same one)
+  DevBuf t1perm;
+  if (mode == WMOM_MODE_MIXED && !direct_t2) SWEEP_TRY(t1perm.alloc(sizeof(int) * (size_t)n * bg, s));
   // Tier 1 for matrices [b0, b1): FP32 solve, then FP64 refinement of the active ones.
   auto tier1 = [&](int b0, int b1) -> wmom_status {
     if (t1invp)
       SWEEP_TRY(lu_block_inverses<float2>(lu32 + (size_t)b0 * nn, n, n, b1 - b0, (long long)nn,
                                           t1invp + (size_t)b0 * inv_per, s));
+    SWEEP_TRY(lu_pivots_to_perm(ipiv + (size_t)b0 * n, n, b1 - b0, t1perm.as<int>() + (size_t)b0 * n, s));
     // the matrices still refining: residuals and corrections are computed for these
     // only (one slowly converging matrix no longer keeps its whole batch busy)
     std::vector<int> hsel(kMaxLuBatch, 0);
@@ -905,10 +910,10 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
     convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.vrep.as<double2>(), g.d32.as<float2>(), n, bg, nullptr);
     if (b0 == 0 && b1 == bg) {
       SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, bg, (long long)nn, nullptr,
-                                   t1invp));
+                                   t1invp, t1perm.as<int>()));
     } else if (nsel > 0) {
       SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
-                                   g.sel.as<int>(), t1invp));
+                                   g.sel.as<int>(), t1invp, t1perm.as<int>()));
     }
     const size_t wcount = (size_t)n * (b1 - b0);
     widen_vec_kernel<<<(unsigned)((wcount + 255) / 256), 256, 0, s>>>(g.d32.as<float2>() + (size_t)b0 * n,
@@ -995,7 +1000,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
       stats::count(stats::kMisc, 4);
       convert_vec_kernel<<<vgrid, 256, 0, s>>>(g.r64.as<double2>(), g.d32.as<float2>(), n, bg, dscale);
       SWEEP_TRY(lu_solve_t<float2>(lu32, n, n, ipiv, g.d32.as<float2>(), n, 1, ws, s, nsel, (long long)nn,
-                                   nsel == bg ? nullptr : g.sel.as<int>(), t1invp));
+                                   nsel == bg ? nullptr : g.sel.as<int>(), t1invp, t1perm.as<int>()));
 
       sumsq_f32_kernel<<<bg, 1024, 0, s>>>(g.d32.as<float2>(), n, dinv, dsc->dnorm2);
       sumsq_kernel<<<bg, 1024, 0, s>>>(g.x64.as<double2>(), n, dsc->xnorm2);
@@ -1200,6 +1205,10 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
           finvp = finv.as<float4>();
         }
       }
+      // the chunk's row permutations, once for all its solves
+      DevBuf fperm;
+      SWEEP_TRY(fperm.alloc(sizeof(int) * (size_t)n * cn, s));
+      SWEEP_TRY(lu_pivots_to_perm(fpiv, n, cn, fperm.as<int>(), s));
       double* dscale = g.scal.as<double>();
       auto scale_slots = [&](double2* v, const double* norm, int cnt) -> wmom_status {
         for (int j = 0; j < kMaxLuBatch; ++j) {
@@ -1228,7 +1237,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
         std::vector<double> vn(kMaxLuBatch, g.vnorm);
         wmom_status ss = scale_slots(fx, vn.data(), cn);
         if (ss != WMOM_OK) return ss;
-        SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, fx, ws, s, cn, (long long)nn, nullptr, finvp));
+        SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, fx, ws, s, cn, (long long)nn, nullptr, finvp, fperm.as<int>()));
         ss = unscale_slots(fx, cn);
         if (ss != WMOM_OK) return ss;
       }
@@ -1327,7 +1336,7 @@ wmom_status solve_group(int mode, int n, const double2* Z64, int bg, const float
           wmom_status ss = scale_slots(frr, rn.data(), cn);
           if (ss != WMOM_OK) return ss;
           SWEEP_TRY(lu_solve_ff(fff, n, n, fpiv, frr, ws, s, nsa, (long long)nn,
-                                nsa == cn ? nullptr : g.sel.as<int>(), finvp));
+                                nsa == cn ? nullptr : g.sel.as<int>(), finvp, fperm.as<int>()));
           ss = unscale_slots(frr, cn);
           if (ss != WMOM_OK) return ss;
         }
