@@ -143,6 +143,7 @@ int wire_loops(const std::vector<SrcHalf>& src, int nsmax, const float* z, bool 
 #include <array>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <tuple>
 
 namespace wmom {
@@ -159,8 +160,18 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
     r[1] = (double)y[k - 1];
     r[2] = (double)z[k - 1];
   };
-  std::map<std::array<int, 4>, int> okey;
-  std::map<std::tuple<int, int, int, int, uint32_t>, int> qkey;
+  // instance ids in first-seen order (hash maps, reserved once: ordered maps made this
+  // table build several milliseconds of every N = 8192 plan)
+  struct KeyHash {
+    size_t operator()(const std::array<uint32_t, 5>& k) const {
+      uint64_t h = 0x9E3779B97F4A7C15ull;
+      for (uint32_t v : k) h = (h ^ v) * 0xBF58476D1CE4E5B9ull;
+      return (size_t)(h ^ (h >> 31));
+    }
+  };
+  std::unordered_map<std::array<uint32_t, 5>, int, KeyHash> okey, qkey;
+  okey.reserve(2 * (size_t)npls);
+  qkey.reserve(2 * (size_t)npls);
   std::vector<int> obs_of(2 * (size_t)npls), neg_of(2 * (size_t)npls), src_of(2 * (size_t)npls);
   for (int b = 0; b < npls; ++b) {
     const int np = std::abs(ipc[b]);
@@ -170,7 +181,7 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
       const int ml = ise[ms - 1], mr = ise[ms + nsmax - 1];
       const int other = h == 0 ? ise[s1 - 1] : ise[s2 + nsmax - 1];
       const int lo = std::min(np, other), hi = std::max(np, other);
-      const std::array<int, 4> key{ml, mr, lo, hi};
+      const std::array<uint32_t, 5> key{(uint32_t)ml, (uint32_t)mr, (uint32_t)lo, (uint32_t)hi, 0u};
       auto it = okey.find(key);
       int id;
       const ObsHalf& oh = p->h_obs[2 * (size_t)b + h];
@@ -210,7 +221,7 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
       const int e = sg == 0 ? np : ise[s2 + nsmax - 1];
       uint32_t rbits;
       std::memcpy(&rbits, &rad[seg - 1], 4);
-      const auto key = std::make_tuple(a, e, sh.nl, sh.nr, rbits);
+      const std::array<uint32_t, 5> key{(uint32_t)a, (uint32_t)e, (uint32_t)sh.nl, (uint32_t)sh.nr, rbits};
       auto it = qkey.find(key);
       int id;
       if (it == qkey.end()) {
@@ -247,38 +258,27 @@ void plan_build_pair_tiles(Plan* p, const float* x, const float* y, const float*
   t.col_local.assign(2 * (size_t)npls, 0);
   t.rt_off.assign(t.n_tiles + 1, 0);
   t.ct_off.assign(t.n_tiles + 1, 0);
+  // a tile's distinct instances, in first-seen order: at most 2 T of each, so a linear
+  // search of the tile's list
+  auto local_id = [](std::vector<int>& ids, size_t from, int v) -> int {
+    for (size_t i = from; i < ids.size(); ++i)
+      if (ids[i] == v) return (int)(i - from);
+    ids.push_back(v);
+    return (int)(ids.size() - 1 - from);
+  };
   for (int tile = 0; tile < t.n_tiles; ++tile) {
-    std::map<int, int> lo, lq;
+    const size_t ro = t.rt_ids.size(), co = t.ct_ids.size();
     const int b0 = tile * T, b1 = std::min(npls, b0 + T);
     for (int b = b0; b < b1; ++b)
       for (int h = 0; h < 2; ++h) {
-        const int o = obs_of[2 * (size_t)b + h];
-        auto it = lo.find(o);
-        int l;
-        if (it == lo.end()) {
-          l = (int)lo.size();
-          lo.emplace(o, l);
-          t.rt_ids.push_back(o);
-        } else {
-          l = it->second;
-        }
+        const int l = local_id(t.rt_ids, ro, obs_of[2 * (size_t)b + h]);
         t.row_local[2 * (size_t)b + h] = l | (neg_of[2 * (size_t)b + h] ? (1 << 30) : 0);
-        const int q = src_of[2 * (size_t)b + h];
-        auto iq = lq.find(q);
-        int m;
-        if (iq == lq.end()) {
-          m = (int)lq.size();
-          lq.emplace(q, m);
-          t.ct_ids.push_back(q);
-        } else {
-          m = iq->second;
-        }
-        t.col_local[2 * (size_t)b + h] = m;
+        t.col_local[2 * (size_t)b + h] = local_id(t.ct_ids, co, src_of[2 * (size_t)b + h]);
       }
     t.rt_off[tile + 1] = (int)t.rt_ids.size();
     t.ct_off[tile + 1] = (int)t.ct_ids.size();
-    t.max_o = std::max(t.max_o, (int)lo.size());
-    t.max_q = std::max(t.max_q, (int)lq.size());
+    t.max_o = std::max(t.max_o, (int)(t.rt_ids.size() - ro));
+    t.max_q = std::max(t.max_q, (int)(t.ct_ids.size() - co));
   }
   const size_t smem = (size_t)t.max_o * sizeof(ObsInst) + (size_t)t.max_q * sizeof(SrcInst) +
                       (size_t)t.max_o * t.max_q * 48;
